@@ -1,0 +1,198 @@
+/*
+ * ztm_grav.h - C ABI of the GB300 gravity forward model and adjoint.
+ *
+ * This is the in-process boundary that replaces the gravity section of ZTM's
+ * forward model:
+ *   - TFM.cpp:90-94  GPU branch: float32 files in /dev/shm plus popen("./GFM")
+ *   - TFM.cpp:95-99  CPU branch: std::thread lambda, point-mass sum in double
+ *   - GFM_GPU.cu:16-34  the GF kernel and its host main()
+ * The caller (the C++ inversion driver) owns every host array; the library
+ * copies in and out, or, with ZTM_FLAG_DEVICE_PTRS, reads and writes device
+ * pointers in place.  A context owns its device buffers and CUDA stream.
+ * No function throws; every entry point returns an int status (0 = ok) and
+ * ztm_last_error() gives the message.  A non-zero status is the signal on
+ * which the caller falls back to its CPU path, exactly as TFM.cpp:95 does when
+ * the GPU model did not compile (TFM.cpp:207-208).
+ *
+ * Threading: one context per host thread, or serialise calls on a context.
+ * The library keeps no global CUDA state besides the device it was created on.
+ *
+ * Units.  Point-mass mode keeps the reference's grid units (indices, k up,
+ * density in g/cc, gz in mGal with the 66.7 constant of TFM.cpp:98).  Prism
+ * and interface modes use metres (z up), kg/m^3 and mGal; gz is the downward
+ * attraction (positive above excess mass), the sign convention of TFM.cpp:98.
+ */
+#ifndef ZTM_GRAV_H
+#define ZTM_GRAV_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+enum {
+  ZTM_OK = 0,
+  ZTM_ERR_ARG = -1,     /* bad dimensions, null pointers, bad flags */
+  ZTM_ERR_ALLOC = -2,   /* device or pinned-host allocation failed */
+  ZTM_ERR_CUDA = -3,    /* a CUDA runtime call or kernel launch failed */
+  ZTM_ERR_TIMEOUT = -4, /* a bounded device-side wait gave up */
+  ZTM_ERR_NODEV = -5,   /* no CUDA device, or the device id is invalid */
+  ZTM_ERR_RANGE = -6    /* a size exceeds a documented limit */
+};
+
+/* ---- precision / method ----------------------------------------------- */
+enum {
+  ZTM_PREC_FP64 = 0,  /* plain: every pair in double (closed form / pow) */
+  ZTM_PREC_FP32 = 1,  /* every pair in float with compensated sums */
+  ZTM_PREC_MIXED = 2  /* prism modes: far pairs in float (multipole to 4th
+                         order, compensated), near pairs and the final
+                         per-station sums in double */
+};
+
+/* ---- flags ----------------------------------------------------------- */
+enum {
+  ZTM_FLAG_DEVICE_PTRS = 1 /* all array arguments are device pointers */
+};
+
+typedef struct ztm_ctx ztm_ctx;
+
+/* Reference grid of the point-mass model (TFM.cpp:83 and GFM_GPU.cu:24).
+ * Fine grid: ii=(di-1)*fh+1, jj=(dj-1)*fh+1, kk=(dk-1)*fv+1 nodes, flat index
+ * n = i + j*ii + k*ii*jj.  Stations: the di*dj coarse nodes with
+ * bfr <= i0 < di-bfr and bfr <= j0 < dj-bfr, at height surf[i0+j0*di]. */
+typedef struct {
+  int di, dj, dk;   /* coarse grid dimensions */
+  int fh, fv;       /* horizontal / vertical refinement */
+  int bfr;          /* boundary buffer without stations */
+  double threshold; /* nodes with |drho| > threshold contribute (0.001) */
+  double scale;     /* result multiplier: h/10 for spacing h km (1.0) */
+} ztm_grid;
+
+/* Regular prism mesh: nx*ny columns of nz layers, layer 0 at the top.
+ * Prism (ix,iy,l) spans [x0+ix*dx, x0+(ix+1)*dx] x [y0+iy*dy, ...] x
+ * [z_top-(l+1)*dz, z_top-l*dz].  Density index: ix + nx*(iy + ny*l). */
+typedef struct {
+  int nx, ny, nz;
+  double x0, y0, z_top;
+  double dx, dy, dz;
+} ztm_mesh;
+
+/* Interface mesh: nx*ny prism columns.  Column (ix,iy) spans the cell
+ * horizontally and z in [z_base, -depth[ix+nx*iy]] (depth > 0 below z=0). */
+typedef struct {
+  int nx, ny;
+  double x0, y0;
+  double dx, dy;
+  double z_base; /* elevation of the column bases, e.g. -45000 */
+} ztm_imesh;
+
+/* Per-call options.  Zero-initialise and set what you need. */
+typedef struct {
+  int precision;  /* ZTM_PREC_* */
+  int flags;      /* ZTM_FLAG_* */
+  double G;       /* gravitational constant; 0 selects 6.67e-11, the value
+                     that TFM.cpp:98's 66.7 mGal factor bakes in */
+  double near_q;  /* mixed mode: pairs closer than near_q prism half-
+                     diagonals are evaluated in double; 0 selects 6 */
+  int tile;       /* stations per block; 0 = autotuned */
+  int chunk;      /* prism columns per block; 0 = autotuned */
+} ztm_opts;
+
+/* One job of a batched launch: nmodels density models that share one
+ * geometry and one station set.  rho is nmodels x (nx*ny*nz), gz is
+ * nmodels x ns, model-major. */
+typedef struct {
+  ztm_mesh mesh;
+  int nmodels;
+  const double* rho;
+  int ns;
+  const double* sxyz;
+  double* gz;
+} ztm_job;
+
+/* ---- context --------------------------------------------------------- */
+int ztm_version(void);
+/* Creates a context on CUDA device `device` with its own non-blocking
+ * stream.  Replaces the per-call context creation of GFM_GPU.cu:28-30. */
+int ztm_ctx_create(int device, ztm_ctx** out);
+void ztm_ctx_destroy(ztm_ctx* ctx);
+/* Message of the last failed call on this context ("" if none). */
+const char* ztm_last_error(const ztm_ctx* ctx);
+/* Use `stream` (a cudaStream_t) for subsequent calls; NULL restores the
+ * context's own stream.  The caller keeps ownership of the stream. */
+int ztm_ctx_set_stream(ztm_ctx* ctx, void* stream);
+void* ztm_ctx_stream(ztm_ctx* ctx);
+/* Number of kernels this context has launched so far. */
+long long ztm_ctx_launches(const ztm_ctx* ctx);
+/* Waits for the context's stream and reports device-side errors of calls
+ * made with ZTM_FLAG_DEVICE_PTRS (those calls return without waiting). */
+int ztm_ctx_sync(ztm_ctx* ctx);
+
+/* ---- point-mass mode (reference model) ------------------------------- */
+/* Replaces TFM.cpp:90-99 and GFM_GPU.cu:16-34.  drho has ii*jj*kk values
+ * (g/cc), surf di*dj station heights (grid units), G receives di*dj values
+ * in mGal: interior stations get the sum, the rest are set to 0 (as the GPU
+ * branch returns them, TFM.cpp:94).  If nn is non-NULL only the n_nn listed
+ * nodes contribute (the CPU branch's list, TFM.cpp:89,97); otherwise nodes
+ * with |drho| > grid->threshold.  precision: ZTM_PREC_FP64 or _FP32. */
+int ztm_gfm_pointmass(ztm_ctx* ctx, const ztm_grid* grid, const double* drho,
+                      const int* nn, long long n_nn, const double* surf,
+                      double* G, int precision, int flags);
+
+/* ---- prism mode -------------------------------------------------------- */
+/* gz[s] = sum over all prisms of the closed-form attraction of prism p at
+ * station s (sxyz is ns x 3: x, y, z).  No counterpart in the reference code
+ * (it has only the point-mass model); it is the model the gravity path of
+ * TFM.cpp:83-99 approximates. */
+int ztm_gfm_prism(ztm_ctx* ctx, const ztm_mesh* mesh, const double* rho,
+                  int ns, const double* sxyz, double* gz, const ztm_opts* opt);
+
+/* Explicit prism list: geom is np x 6 (x0,x1,y0,y1,z0,z1), rho np values. */
+int ztm_gfm_prism_list(ztm_ctx* ctx, long long np, const double* geom,
+                       const double* rho, int ns, const double* sxyz,
+                       double* gz, const ztm_opts* opt);
+
+/* Adjoint of ztm_gfm_prism: g_rho[p] = sum_s resid[s] * dgz[s]/drho[p],
+ * i.e. d(0.5*|gz-d|^2)/d(rho) for resid = gz-d.  Supersedes the gravity
+ * columns of the finite-difference Jacobian (TFM.cpp:124-135). */
+int ztm_gfm_adjoint(ztm_ctx* ctx, const ztm_mesh* mesh, int ns,
+                    const double* sxyz, const double* resid, double* g_rho,
+                    const ztm_opts* opt);
+
+/* ---- interface mode ---------------------------------------------------- */
+/* Forward of an interface mesh: column c has density rho_col[c] and its top
+ * at depth[c] (m below z=0). */
+int ztm_gfm_interface(ztm_ctx* ctx, const ztm_imesh* mesh,
+                      const double* depth, const double* rho_col, int ns,
+                      const double* sxyz, double* gz, const ztm_opts* opt);
+
+/* Adjoint of ztm_gfm_interface: g_rho[c] = sum_s resid[s]*dgz[s]/drho[c]
+ * and g_depth[c] = sum_s resid[s]*dgz[s]/ddepth[c] (analytic top-face
+ * derivative).  Either output may be NULL. */
+int ztm_gfm_interface_adjoint(ztm_ctx* ctx, const ztm_imesh* mesh,
+                              const double* depth, const double* rho_col,
+                              int ns, const double* sxyz, const double* resid,
+                              double* g_rho, double* g_depth,
+                              const ztm_opts* opt);
+
+/* Forward + misfit + adjoint in one call: gz = F(depth, rho_col),
+ * *misfit = 0.5*sum (gz-data)^2, gradients as ztm_gfm_interface_adjoint.
+ * gz, g_rho, g_depth may be NULL. */
+int ztm_gfm_interface_misfit(ztm_ctx* ctx, const ztm_imesh* mesh,
+                             const double* depth, const double* rho_col,
+                             int ns, const double* sxyz, const double* data,
+                             double* misfit, double* gz, double* g_rho,
+                             double* g_depth, const ztm_opts* opt);
+
+/* ---- batched ----------------------------------------------------------- */
+/* Evaluates every job (trial models of a line search, independent regional
+ * meshes of uneven size) in one persistent launch, replayed from a CUDA
+ * graph cached on the context when the job shapes repeat.  Replaces the
+ * sequential FM evaluations of the damping trials (TFM.cpp:165). */
+int ztm_gfm_batch(ztm_ctx* ctx, const ztm_job* jobs, int njobs,
+                  const ztm_opts* opt);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ZTM_GRAV_H */

@@ -1,0 +1,194 @@
+"""CPU oracle of the gravity path - TEST INFRASTRUCTURE ONLY.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may
+import this package, and only as the checker (or the timed CPU baseline).
+The product library never calls it; there is no CPU fallback.
+
+Contents (oracle.c):
+  pointmass_tfm   restatement of TFM.cpp:95-99 (double)
+  pointmass_gf    restatement of GFM_GPU.cu:16-22 (float)
+  prism_* / face  published closed form (no reference implementation)
+  ref_gf          the reference GF kernel itself (compiled unchanged into
+                  oracle/_ref/gf_ref.cubin) run on a GPU through the driver API
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+_runner = None
+NTHREADS = max(1, os.cpu_count() or 1)
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        lib = ctypes.CDLL(path)
+        D = ctypes.c_double
+        P = ctypes.c_void_p
+        I = ctypes.c_int
+        L = ctypes.c_long
+        lib.ora_pointmass_tfm.argtypes = [I, I, I, I, I, I, P, P, L, P, P, I]
+        lib.ora_pointmass_gf.argtypes = [I, I, I, I, I, I, P, L, P, P]
+        lib.ora_phi.argtypes = [D, D, D]
+        lib.ora_phi.restype = D
+        lib.ora_prism_unit.argtypes = [D] * 9
+        lib.ora_prism_unit.restype = D
+        lib.ora_face_unit.argtypes = [D] * 8
+        lib.ora_face_unit.restype = D
+        lib.ora_prism_mesh.argtypes = [P, P, I, P, D, P, I, I]
+        lib.ora_prism_list.argtypes = [L, P, P, I, P, D, P, I]
+        lib.ora_mesh_adjoint.argtypes = [P, I, P, P, D, P, I]
+        lib.ora_interface_fwd.argtypes = [P, P, P, I, P, D, P, I]
+        lib.ora_interface_adj.argtypes = [P, P, P, I, P, P, D, P, P, I]
+        _lib = lib
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def mesh_params(mesh):
+    return np.array([mesh.nx, mesh.ny, mesh.nz, mesh.x0, mesh.y0, mesh.z_top,
+                     mesh.dx, mesh.dy, mesh.dz], dtype=np.float64)
+
+
+def imesh_params(im):
+    return np.array([im.nx, im.ny, im.x0, im.y0, im.dx, im.dy, im.z_base], dtype=np.float64)
+
+
+def pointmass_tfm(grid, drho, surf, nn=None, nthreads=None):
+    """TFM.cpp:95-99.  nn defaults to the nodes with |drho| > grid.threshold
+    (the list TFM.cpp:89 builds).  Returns G (di*dj); non-interior 0."""
+    lib = _load()
+    drho = _f64(drho)
+    surf = _f64(surf)
+    if nn is None:
+        nn = np.nonzero(np.abs(drho) > grid.threshold)[0]
+    nn = np.ascontiguousarray(nn, dtype=np.int32)
+    G = np.zeros(grid.di * grid.dj)
+    lib.ora_pointmass_tfm(grid.di, grid.dj, grid.dk, grid.fh, grid.fv, grid.bfr, _p(drho), _p(nn),
+                          nn.size, _p(surf), _p(G), nthreads or NTHREADS)
+    return G * grid.scale if grid.scale != 1.0 else G
+
+
+def pointmass_gf(grid, rho32, s32, nthreads_total=None):
+    """GFM_GPU.cu:16-22 in float, summed in thread order."""
+    lib = _load()
+    rho32 = np.ascontiguousarray(rho32, dtype=np.float32)
+    s32 = np.ascontiguousarray(s32, dtype=np.float32)
+    ii = (grid.di - 1) * grid.fh + 1
+    n = nthreads_total if nthreads_total is not None else (rho32.size // ii) * ii
+    g = np.zeros(grid.di * grid.dj, dtype=np.float32)
+    lib.ora_pointmass_gf(grid.bfr, grid.di, grid.dj, grid.dk, grid.fh, grid.fv, _p(rho32), n,
+                         _p(s32), _p(g))
+    return g
+
+
+def phi(x, y, z):
+    return _load().ora_phi(x, y, z)
+
+
+def prism_unit(xs, ys, zs, x0, x1, y0, y1, z0, z1):
+    return _load().ora_prism_unit(xs, ys, zs, x0, x1, y0, y1, z0, z1)
+
+
+def face_unit(xs, ys, zs, x0, x1, y0, y1, zf):
+    return _load().ora_face_unit(xs, ys, zs, x0, x1, y0, y1, zf)
+
+
+def prism_mesh(mesh, rho, stations, G=6.67e-11, nthreads=None, long_double=False):
+    lib = _load()
+    mp = mesh_params(mesh)
+    rho = _f64(rho)
+    st = _f64(stations).reshape(-1, 3)
+    gz = np.zeros(st.shape[0])
+    lib.ora_prism_mesh(_p(mp), _p(rho), st.shape[0], _p(st), G, _p(gz), nthreads or NTHREADS,
+                       1 if long_double else 0)
+    return gz
+
+
+def prism_list(geom, rho, stations, G=6.67e-11, nthreads=None):
+    lib = _load()
+    geom = _f64(geom).reshape(-1, 6)
+    rho = _f64(rho)
+    st = _f64(stations).reshape(-1, 3)
+    gz = np.zeros(st.shape[0])
+    lib.ora_prism_list(geom.shape[0], _p(geom), _p(rho), st.shape[0], _p(st), G, _p(gz),
+                       nthreads or NTHREADS)
+    return gz
+
+
+def mesh_adjoint(mesh, stations, resid, G=6.67e-11, nthreads=None):
+    lib = _load()
+    mp = mesh_params(mesh)
+    st = _f64(stations).reshape(-1, 3)
+    res = _f64(resid)
+    g = np.zeros(mesh.nx * mesh.ny * mesh.nz)
+    lib.ora_mesh_adjoint(_p(mp), st.shape[0], _p(st), _p(res), G, _p(g), nthreads or NTHREADS)
+    return g
+
+
+def interface_fwd(imesh, depth, rho_col, stations, G=6.67e-11, nthreads=None):
+    lib = _load()
+    ip = imesh_params(imesh)
+    depth = _f64(depth)
+    rho_col = _f64(rho_col)
+    st = _f64(stations).reshape(-1, 3)
+    gz = np.zeros(st.shape[0])
+    lib.ora_interface_fwd(_p(ip), _p(depth), _p(rho_col), st.shape[0], _p(st), G, _p(gz),
+                          nthreads or NTHREADS)
+    return gz
+
+
+def interface_adj(imesh, depth, rho_col, stations, resid, G=6.67e-11, nthreads=None):
+    lib = _load()
+    ip = imesh_params(imesh)
+    depth = _f64(depth)
+    rho_col = _f64(rho_col)
+    st = _f64(stations).reshape(-1, 3)
+    res = _f64(resid)
+    nc = imesh.nx * imesh.ny
+    gr = np.zeros(nc)
+    gd = np.zeros(nc)
+    lib.ora_interface_adj(_p(ip), _p(depth), _p(rho_col), st.shape[0], _p(st), _p(res), G,
+                          _p(gr), _p(gd), nthreads or NTHREADS)
+    return gr, gd
+
+
+# ---- the reference GF kernel itself (GPU host only) ----------------------
+def ref_gf_available():
+    return os.path.exists(_build.CUBIN) and os.path.exists(_build.RUNNER)
+
+
+def ref_gf(grid, rho32, s32, reps=1):
+    """Runs the unchanged reference GF kernel; returns (g float32, ms)."""
+    global _runner
+    if _runner is None:
+        _build.build()
+        r = ctypes.CDLL(_build.RUNNER)
+        P = ctypes.c_void_p
+        I = ctypes.c_int
+        r.ref_gf_run.argtypes = [ctypes.c_char_p, I, I, I, I, I, I, P, ctypes.c_longlong, P, P, I,
+                                 ctypes.POINTER(ctypes.c_float)]
+        r.ref_gf_run.restype = I
+        _runner = r
+    rho32 = np.ascontiguousarray(rho32, dtype=np.float32)
+    s32 = np.ascontiguousarray(s32, dtype=np.float32)
+    g = np.zeros(grid.di * grid.dj, dtype=np.float32)
+    ms = ctypes.c_float(0)
+    rc = _runner.ref_gf_run(_build.CUBIN.encode(), grid.bfr, grid.di, grid.dj, grid.dk, grid.fh,
+                            grid.fv, _p(rho32), rho32.size, _p(s32), _p(g), reps,
+                            ctypes.byref(ms))
+    if rc != 0:
+        raise RuntimeError("reference GF run failed with code %d" % rc)
+    return g, ms.value

@@ -1,0 +1,61 @@
+"""Shared inputs and error measures for the parity tests."""
+import numpy as np
+
+
+def rel_err(a, ref):
+    """Normwise relative error max|a-ref| / max|ref| (the tolerance measure
+    used throughout: per-station relative error is meaningless where the
+    field crosses zero)."""
+    a = np.asarray(a, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    scale = np.max(np.abs(ref))
+    if scale == 0:
+        return float(np.max(np.abs(a)))
+    return float(np.max(np.abs(a - ref)) / scale)
+
+
+def tfm_like_inputs(di, dj, dk, fh=1, fv=2, seed=0, sparsity=0.3):
+    """drho on the fine grid, zero outside a selected set (as TFM.cpp:89
+    leaves it), and station heights surf near the top of the grid."""
+    rng = np.random.default_rng(seed)
+    ii = (di - 1) * fh + 1
+    jj = (dj - 1) * fh + 1
+    kk = (dk - 1) * fv + 1
+    drho = rng.normal(0.0, 0.1, ii * jj * kk)
+    drho[rng.random(drho.size) < sparsity] = 0.0
+    drho[np.abs(drho) <= 0.001] = 0.0
+    surf = (dk - 3) + 0.37 + 0.2 * rng.random(di * dj)
+    return drho, surf
+
+
+def small_mesh(nx=12, ny=10, nz=6, seed=0, dx=1000.0, dy=800.0, dz=500.0):
+    import ztm_gb300
+    rng = np.random.default_rng(seed)
+    mesh = ztm_gb300.make_mesh(nx, ny, nz, dx, dy, dz, x0=-3000.0, y0=1500.0, z_top=200.0)
+    rho = rng.normal(0.0, 200.0, nx * ny * nz)
+    rho[rng.random(rho.size) < 0.1] = 0.0
+    return mesh, rho
+
+
+def awkward_stations(mesh, n_random=40, seed=1):
+    """Random stations plus stations on faces, edges and vertices of the
+    mesh, inside it, and outside it."""
+    rng = np.random.default_rng(seed)
+    x0, y0, zt = mesh.x0, mesh.y0, mesh.z_top
+    X1 = x0 + mesh.nx * mesh.dx
+    Y1 = y0 + mesh.ny * mesh.dy
+    Zb = zt - mesh.nz * mesh.dz
+    st = [
+        (x0, y0, zt),                       # mesh vertex
+        (x0 + mesh.dx, y0 + 2 * mesh.dy, zt),  # interior vertex on the top face
+        (x0 + 0.5 * mesh.dx, y0 + 0.5 * mesh.dy, zt),  # top-face centre
+        (x0 + 2 * mesh.dx, y0 + 0.3 * mesh.dy, zt + 50.0),  # above an edge
+        (X1 + 3000.0, Y1 + 100.0, zt + 10.0),  # outside
+        (0.5 * (x0 + X1), 0.5 * (y0 + Y1), 0.5 * (zt + Zb) + 0.25 * mesh.dz),  # inside
+        (x0 - 500.0, y0 + mesh.dy, zt - mesh.dz),  # beside, on a layer plane
+    ]
+    xs = rng.uniform(x0 - 2000.0, X1 + 2000.0, n_random)
+    ys = rng.uniform(y0 - 2000.0, Y1 + 2000.0, n_random)
+    zs = rng.uniform(zt + 1.0, zt + 3000.0, n_random)
+    st += list(zip(xs, ys, zs))
+    return np.array(st, dtype=np.float64)

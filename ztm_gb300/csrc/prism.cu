@@ -1,0 +1,573 @@
+// prism.cu - closed-form rectangular-prism gravity forward on sm_103a.
+//
+// gz(s) = G * 1e5 * sum_p rho_p * U(s, p)   [mGal],
+// U(s, p) = integral over prism p of (z_s - z)/r^3 dV
+//         = sum over the 8 corners of s_x s_y s_z Phi(corner - station)
+// (Nagy 1966; Plouff 1976; Nagy, Papp & Benedek 2000).  The reference has no
+// prism model: its gravity path (TFM.cpp:96-98, GFM_GPU.cu:22) is the
+// point-mass approximation that the first term of the far-field expansion
+// below reproduces.
+//
+// Three methods:
+//   FP64 plain  every pair with the 8-corner closed form in double.  One
+//               thread per station, prisms streamed through shared memory,
+//               per-chunk partials reduced in a fixed order.
+//   MIXED       pairs outside a per-station near box (every prism whose
+//               centre is >= near_q half-diagonals away) use the 4th-order
+//               far-field expansion in float, Kahan-summed per thread; the
+//               near box is summed in double with vertex sharing (one Phi per
+//               box vertex instead of 8 per prism); partials and the final
+//               per-station sum are double.  The density of a block's columns
+//               is staged in shared memory by 1-D TMA bulk copies, double
+//               buffered on mbarriers.
+//   FP32        as MIXED with the near box also in float.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include <algorithm>
+
+#include "prism_common.cuh"
+#include "ztm_internal.cuh"
+
+namespace {
+
+constexpr int FAR_TS = 128;   // stations per block in the far kernel
+constexpr int F64_TS = 64;    // stations per block in the plain double kernel
+constexpr int NEAR_WPB = 4;   // warps (stations) per block in the near kernel
+
+// ---------------------------------------------------------------------------
+__global__ void station_prep_kernel(MeshDesc m, double L0, int ns,
+                                    const double* __restrict__ sxyz,
+                                    float4* __restrict__ sf, int4* __restrict__ si) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= ns) return;
+  double xs = sxyz[3 * s], ys = sxyz[3 * s + 1], zs = sxyz[3 * s + 2];
+  const double lim = 1.0e9;
+  double fx = fmin(fmax(floor((xs - m.x0) / m.dx), -lim), lim);
+  double fy = fmin(fmax(floor((ys - m.y0) / m.dy), -lim), lim);
+  double fz = fmin(fmax(floor((m.zt - zs) / m.dz), -lim), lim);
+  int ix = (int)fx, iy = (int)fy, iz = (int)fz;
+  double ex = (xs - m.x0) - (ix + 0.5) * m.dx;
+  double ey = (ys - m.y0) - (iy + 0.5) * m.dy;
+  double ez = zs - (m.zt - (iz + 0.5) * m.dz);
+  sf[s] = make_float4((float)(ex / L0), (float)(ey / L0), (float)(ez / L0), 0.f);
+  si[s] = make_int4(ix, iy, iz, 0);
+}
+
+__global__ void transpose_kernel(MeshConst k, int nmodels, const double* __restrict__ rho,
+                                 float* __restrict__ rhoT) {
+  long long total = (long long)nmodels * k.ncols * k.nzp;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    long long mdl = t / ((long long)k.ncols * k.nzp);
+    long long r = t - mdl * (long long)k.ncols * k.nzp;
+    int c = (int)(r / k.nzp), l = (int)(r % k.nzp);
+    float v = 0.f;
+    if (l < k.nz) v = (float)rho[mdl * (long long)k.ncols * k.nz + (long long)l * k.ncols + c];
+    rhoT[t] = v;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NEAR_WPB * 32)
+    near_kernel(MeshConst k, MeshDesc m, int ns, const double* __restrict__ sxyz,
+                const int4* __restrict__ si, const double* __restrict__ rho,
+                double* __restrict__ out) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int s = blockIdx.x * NEAR_WPB + warp;
+  if (s >= ns) return;
+  const NearBox b = near_box(si[s], k);
+  const double xs = sxyz[3 * s], ys = sxyz[3 * s + 1], zs = sxyz[3 * s + 2];
+  const int nvx = b.x1 - b.x0 + 2, nvy = b.y1 - b.y0 + 2, nvz = b.l1 - b.l0 + 2;
+  const int nv = nvx * nvy * nvz;
+  const long long plane = (long long)m.nx * m.ny;
+  T acc = T(0);
+  for (int v = lane; v < nv; v += 32) {
+    const int a = b.x0 + v % nvx;
+    const int bb = b.y0 + (v / nvx) % nvy;
+    const int cz = b.l0 + v / (nvx * nvy);
+    // signed triple difference of the box density around vertex (a, bb, cz):
+    // prism ix = a-1 has the vertex as its upper x limit (+), ix = a lower (-);
+    // layer l = cz has it as its upper z limit (+), l = cz-1 lower (-).
+    double D = 0.0;
+#pragma unroll
+    for (int da = 0; da < 2; da++) {
+      const int ix = a - 1 + da;
+      if (ix < b.x0 || ix > b.x1) continue;
+#pragma unroll
+      for (int db = 0; db < 2; db++) {
+        const int iy = bb - 1 + db;
+        if (iy < b.y0 || iy > b.y1) continue;
+#pragma unroll
+        for (int dc = 0; dc < 2; dc++) {
+          const int l = cz - 1 + dc;
+          if (l < b.l0 || l > b.l1) continue;
+          const double r = rho[ix + (long long)m.nx * iy + plane * l];
+          const int neg = (da == 1) ^ (db == 1) ^ (dc == 0);
+          D += neg ? -r : r;
+        }
+      }
+    }
+    if (D != 0.0) {
+      const T x = (T)((m.x0 + a * m.dx) - xs);
+      const T y = (T)((m.y0 + bb * m.dy) - ys);
+      const T z = (T)((m.zt - cz * m.dz) - zs);
+      acc += (T)D * ztm_phi<T>(x, y, z);
+    }
+  }
+  double tot = warp_sum_d((double)acc);
+  if (lane == 0) out[s] = tot;
+}
+
+// ---------------------------------------------------------------------------
+// far field, float, TMA-staged density
+struct FarArgs {
+  MeshConst k;
+  int ns;
+  int chunk_cols;  // columns per block (grid.y slices the mesh)
+  int sc;          // columns per shared-memory stage
+  const float4* sf;
+  const int4* si;
+  const float* rhoT;
+  double* partial;  // [chunk][ns]
+  int* err;
+};
+
+__device__ __forceinline__ float far_pair(float rho, float Z, float rh, float a0, float h0,
+                                          float h1, const FarCoef& f) {
+  const float Z2 = Z * Z;
+  const float rinv = rsqrtf(rh + Z2);
+  const float ri2 = rinv * rinv;
+  const float ri4 = ri2 * ri2;
+  const float n2 = fmaf(f.a1, Z2, a0);
+  const float H = fmaf(fmaf(f.h2, Z2, h1), Z2, h0);
+  const float t = fmaf(H, ri4, n2) * ri4;
+  const float base = Z * rinv * ri2 * rho;
+  return fmaf(base, t, base);
+}
+
+__global__ void __launch_bounds__(FAR_TS) far_kernel(FarArgs a) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
+  float* stage = reinterpret_cast<float*>(smem_raw + 128);
+  __shared__ int s_lm;
+  const MeshConst& k = a.k;
+  const int stage_floats = a.sc * k.nzp;
+
+  const int c0 = blockIdx.y * a.chunk_cols;
+  const int c1 = min(k.ncols, c0 + a.chunk_cols);
+  if (c0 >= c1) return;  // uniform over the block
+  const int nst = (c1 - c0 + a.sc - 1) / a.sc;
+
+  const int s = blockIdx.x * FAR_TS + threadIdx.x;
+  const bool active = s < a.ns;
+  float ex = 0.f, ey = 0.f, ez = 0.f;
+  int ixs = 0, iys = 0, izs = 0;
+  NearBox nb = {1, 0, 1, 0, 1, 0};
+  if (active) {
+    float4 f = a.sf[s];
+    int4 i = a.si[s];
+    ex = f.x; ey = f.y; ez = f.z;
+    ixs = i.x; iys = i.y; izs = i.z;
+    nb = near_box(i, k);
+  }
+  if (threadIdx.x == 0) {
+    s_lm = 0;
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (active) atomicMax(&s_lm, nb.l1 + 1);
+
+  auto issue = [&](int st) {
+    const int buf = st & 1;
+    const int cs = c0 + st * a.sc;
+    const int ncol = min(a.sc, c1 - cs);
+    const uint32_t bytes = (uint32_t)ncol * k.nzp * 4u;
+    mbar_expect_tx(&bar[buf], bytes);
+    bulk_g2s(stage + buf * stage_floats, a.rhoT + (size_t)cs * k.nzp, bytes, &bar[buf]);
+  };
+  if (threadIdx.x == 0) issue(0);
+  __syncthreads();
+  const int Lm = min(s_lm, k.nz);
+  const FarCoef fc = k.fc;
+
+  Kahan acc;
+  int st = 0;
+  bool timed_out = false;
+  for (; st < nst; st++) {
+    if (threadIdx.x == 0 && st + 1 < nst) issue(st + 1);
+    const bool ok = mbar_wait(&bar[st & 1], (st >> 1) & 1);
+    if (__syncthreads_or(!ok)) {
+      timed_out = true;
+      break;
+    }
+    const float* rs = stage + (st & 1) * stage_floats;
+    const int cs = c0 + st * a.sc;
+    const int ncol = min(a.sc, c1 - cs);
+    if (active) {
+      int ix = cs % k.nx, iy = cs / k.nx;
+      for (int q = 0; q < ncol; q++) {
+        const float X = fmaf((float)(ixs - ix), k.dxn, ex);
+        const float Y = fmaf((float)(iys - iy), k.dyn, ey);
+        const float X2 = X * X, Y2 = Y * Y, rh = X2 + Y2;
+        const float a0 = fmaf(X2, fc.cA, Y2 * fc.cB);
+        const float h1 = fmaf(X2, fc.cX1, Y2 * fc.cY1);
+        const float h0 = fmaf(X2, fmaf(X2, fc.cXX, Y2 * fc.cXY), Y2 * Y2 * fc.cYY);
+        const bool ncl = ix >= nb.x0 && ix <= nb.x1 && iy >= nb.y0 && iy <= nb.y1;
+        const int elo = ncl ? nb.l0 : k.nz;
+        const unsigned espan = ncl ? (unsigned)(nb.l1 - nb.l0) : 0u;
+        const float* col = rs + q * k.nzp;
+        float zf = (float)(-izs);  // Z(l) = (l - izs) dz + ez
+        int l = 0;
+        for (; l < Lm; l++, zf += 1.f) {
+          const float v = far_pair(col[l], fmaf(zf, k.dzn, ez), rh, a0, h0, h1, fc);
+          const bool excl = (unsigned)(l - elo) <= espan;
+          acc.add(excl ? 0.f : v);  // select: a NaN at a box prism is dropped
+        }
+#pragma unroll 4
+        for (; l < k.nz; l++, zf += 1.f)
+          acc.add(far_pair(col[l], fmaf(zf, k.dzn, ez), rh, a0, h0, h1, fc));
+        if (++ix == k.nx) {
+          ix = 0;
+          ++iy;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (timed_out) {
+    if (threadIdx.x == 0) {
+      atomicOr(a.err, ZTM_DEVERR_TIMEOUT);
+      // let copies already in flight land before the block's shared memory
+      // is released (bounded as well)
+      mbar_wait(&bar[st & 1], (st >> 1) & 1);
+      if (st + 1 < nst) mbar_wait(&bar[(st + 1) & 1], ((st + 1) >> 1) & 1);
+    }
+    return;
+  }
+  if (active) a.partial[(size_t)blockIdx.y * a.ns + s] = acc.value();
+}
+
+// gz[s] = G5 * (far_scale * sum_c partial[c][s] + near[s])
+__global__ void finalize_kernel(int ns, int nchunks, const double* __restrict__ partial,
+                                double far_scale, const double* __restrict__ near,
+                                double G5, double* __restrict__ gz) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= ns) return;
+  double f = 0.0;
+  for (int c = 0; c < nchunks; c++) f += partial[(size_t)c * ns + s];
+  double g = far_scale * f;
+  if (near) g += near[s];
+  gz[s] = G5 * g;
+}
+
+// ---------------------------------------------------------------------------
+// plain double, every pair with the closed form
+__global__ void __launch_bounds__(F64_TS)
+    mesh_f64_kernel(MeshDesc m, int ns, const double* __restrict__ sxyz,
+                    const double* __restrict__ rho, long long chunk_len,
+                    double* __restrict__ partial) {
+  __shared__ double tile[256];
+  const int s = blockIdx.x * F64_TS + threadIdx.x;
+  const bool active = s < ns;
+  double xs = 0, ys = 0, zs = 0;
+  if (active) {
+    xs = sxyz[3 * s];
+    ys = sxyz[3 * s + 1];
+    zs = sxyz[3 * s + 2];
+  }
+  const long long np = (long long)m.nx * m.ny * m.nz;
+  const long long p0 = (long long)blockIdx.y * chunk_len;
+  const long long p1 = min(np, p0 + chunk_len);
+  const long long plane = (long long)m.nx * m.ny;
+  double acc = 0.0;
+  for (long long t0 = p0; t0 < p1; t0 += 256) {
+    __syncthreads();
+    for (int q = threadIdx.x; q < 256; q += F64_TS) tile[q] = (t0 + q < p1) ? rho[t0 + q] : 0.0;
+    __syncthreads();
+    const int cnt = (int)min(256LL, p1 - t0);
+    if (!active) continue;
+    for (int q = 0; q < cnt; q++) {
+      const double r = tile[q];
+      if (r == 0.0) continue;  // uniform: all lanes read prism q
+      const long long p = t0 + q;
+      const int l = (int)(p / plane);
+      const long long rem = p - (long long)l * plane;
+      const int iy = (int)(rem / m.nx), ix = (int)(rem % m.nx);
+      const double xa = (m.x0 + ix * m.dx) - xs, xb = (m.x0 + (ix + 1) * m.dx) - xs;
+      const double ya = (m.y0 + iy * m.dy) - ys, yb = (m.y0 + (iy + 1) * m.dy) - ys;
+      const double za = (m.zt - (l + 1) * m.dz) - zs, zb = (m.zt - l * m.dz) - zs;
+      acc += r * ztm_prism_unit<double>(xa, xb, ya, yb, za, zb);
+    }
+  }
+  if (active) partial[(size_t)blockIdx.y * ns + s] = acc;
+}
+
+// ---------------------------------------------------------------------------
+// explicit prism lists
+struct ListPrism {
+  float xh, xl, yh, yl, zh, zl;  // centre (units of 1 km), hi + lo
+  float w;                       // rho * volume (km^3)
+  float ell2;                    // (near_q * half diagonal)^2 (km^2)
+  FarCoef fc;
+};
+
+__device__ __forceinline__ void split2(double v, float* h, float* l) {
+  float hi = (float)v;
+  *h = hi;
+  *l = (float)(v - (double)hi);
+}
+
+constexpr double LIST_L0 = 1000.0;
+
+__global__ void list_prep_kernel(long long np, const double* __restrict__ geom,
+                                 const double* __restrict__ rho, double near_q,
+                                 ListPrism* __restrict__ lp) {
+  long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= np) return;
+  const double* g = geom + 6 * q;
+  double dx = fabs(g[1] - g[0]), dy = fabs(g[3] - g[2]), dz = fabs(g[5] - g[4]);
+  // signed volume: reversed bounds flip the sign, as the closed form does
+  double vol = (g[1] - g[0]) * (g[3] - g[2]) * (g[5] - g[4]);
+  ListPrism p;
+  split2(0.5 * (g[0] + g[1]) / LIST_L0, &p.xh, &p.xl);
+  split2(0.5 * (g[2] + g[3]) / LIST_L0, &p.yh, &p.yl);
+  split2(0.5 * (g[4] + g[5]) / LIST_L0, &p.zh, &p.zl);
+  p.w = (float)(rho[q] * vol / (LIST_L0 * LIST_L0 * LIST_L0));
+  double ell = 0.5 * sqrt(dx * dx + dy * dy + dz * dz) / LIST_L0;
+  p.ell2 = (float)(near_q * near_q * ell * ell);
+  p.fc = far_coef(dx / LIST_L0, dy / LIST_L0, dz / LIST_L0);
+  lp[q] = p;
+}
+
+template <bool F64NEAR>
+__global__ void __launch_bounds__(F64_TS)
+    list_kernel(long long np, const double* __restrict__ geom, const double* __restrict__ rho,
+                const ListPrism* __restrict__ lp, int ns, const double* __restrict__ sxyz,
+                long long chunk_len, int method, double* __restrict__ partial) {
+  // method 0: every pair closed form in double; 1: mixed / float split
+  const int s = blockIdx.x * F64_TS + threadIdx.x;
+  if (s >= ns) return;
+  const double xs = sxyz[3 * s], ys = sxyz[3 * s + 1], zs = sxyz[3 * s + 2];
+  float sxh, sxl, syh, syl, szh, szl;
+  split2(xs / LIST_L0, &sxh, &sxl);
+  split2(ys / LIST_L0, &syh, &syl);
+  split2(zs / LIST_L0, &szh, &szl);
+  const long long q0 = (long long)blockIdx.y * chunk_len;
+  const long long q1 = min(np, q0 + chunk_len);
+  double near = 0.0;
+  Kahan far;
+  for (long long q = q0; q < q1; q++) {
+    const double r = rho[q];
+    if (r == 0.0) continue;
+    bool closed = (method == 0);
+    float X = 0.f, Y = 0.f, Z = 0.f, R2 = 0.f;
+    ListPrism p;
+    if (!closed) {
+      p = lp[q];
+      X = (sxh - p.xh) + (sxl - p.xl);
+      Y = (syh - p.yh) + (syl - p.yl);
+      Z = (szh - p.zh) + (szl - p.zl);
+      R2 = X * X + Y * Y + Z * Z;
+      closed = R2 < p.ell2;
+    }
+    if (closed) {
+      const double* g = geom + 6 * q;
+      if (F64NEAR || method == 0) {
+        near += r * ztm_prism_unit<double>(g[0] - xs, g[1] - xs, g[2] - ys, g[3] - ys,
+                                           g[4] - zs, g[5] - zs);
+      } else {
+        near += r * (double)ztm_prism_unit<float>(
+                        (float)(g[0] - xs), (float)(g[1] - xs), (float)(g[2] - ys),
+                        (float)(g[3] - ys), (float)(g[4] - zs), (float)(g[5] - zs));
+      }
+    } else {
+      const float X2 = X * X, Y2 = Y * Y, rh = X2 + Y2;
+      const float a0 = fmaf(X2, p.fc.cA, Y2 * p.fc.cB);
+      const float h1 = fmaf(X2, p.fc.cX1, Y2 * p.fc.cY1);
+      const float h0 = fmaf(X2, fmaf(X2, p.fc.cXX, Y2 * p.fc.cXY), Y2 * Y2 * p.fc.cYY);
+      far.add(far_pair(p.w, Z, rh, a0, h0, h1, p.fc));
+    }
+  }
+  // far sum is in km^3 * km / km^3 = 1/km units -> metres: * (L0 km^2 -> m)
+  partial[(size_t)blockIdx.y * ns + s] = near + LIST_L0 * far.value();
+}
+
+// ---------------------------------------------------------------------------
+struct FarShape {
+  int tiles, chunks, chunk_cols, sc;
+  size_t smem;
+};
+
+FarShape far_shape(const MeshConst& k, int ns, int num_sms, const ztm_opts* o) {
+  FarShape f;
+  f.tiles = std::max(1, (ns + FAR_TS - 1) / FAR_TS);
+  // stage: sc columns of nzp floats, at most 24 KB per stage
+  int sc = std::max(1, (24 * 1024) / (k.nzp * 4));
+  sc = std::min(sc, 64);
+  f.sc = sc;
+  int want_blocks = 8 * std::max(num_sms, 1);
+  int chunks = std::max(1, want_blocks / f.tiles);
+  if (o && o->chunk > 0) chunks = std::max(1, (k.ncols + o->chunk - 1) / o->chunk);
+  chunks = std::min(chunks, std::max(1, k.ncols / sc));
+  chunks = std::min(chunks, 65535);
+  int cc = (k.ncols + chunks - 1) / chunks;
+  cc = ((cc + sc - 1) / sc) * sc;
+  f.chunk_cols = cc;
+  f.chunks = (k.ncols + cc - 1) / cc;
+  f.smem = 128 + 2 * (size_t)sc * k.nzp * 4;
+  return f;
+}
+
+long long f64_chunks(long long np, int tiles, int num_sms, long long* len) {
+  long long want = std::max(1LL, (long long)(8 * std::max(num_sms, 1)) / tiles);
+  long long maxc = std::max(1LL, np / 256);
+  long long ch = std::min(std::min(want, maxc), 65535LL);
+  long long l = (np + ch - 1) / ch;
+  l = ((l + 255) / 256) * 256;
+  *len = l;
+  return (np + l - 1) / l;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// launchers shared with other translation units
+MeshConst make_mesh_const(const MeshDesc& m, double near_q) {
+  MeshConst k;
+  k.nx = m.nx; k.ny = m.ny; k.nz = m.nz;
+  k.nzp = (m.nz + 3) & ~3;
+  k.ncols = m.nx * m.ny;
+  near_widths(m.dx, m.dy, m.dz, near_q, &k.wx, &k.wy, &k.wl);
+  k.L0 = std::max(m.dx, std::max(m.dy, m.dz));
+  k.dxn = (float)(m.dx / k.L0);
+  k.dyn = (float)(m.dy / k.L0);
+  k.dzn = (float)(m.dz / k.L0);
+  k.fc = far_coef(m.dx / k.L0, m.dy / k.L0, m.dz / k.L0);
+  return k;
+}
+
+void launch_mesh_station_prep(ztm_ctx* c, const MeshDesc& m, double L0, int ns,
+                              const double* sxyz, float4* sf, int4* si) {
+  if (ns <= 0) return;
+  station_prep_kernel<<<(ns + 127) / 128, 128, 0, c->stream>>>(m, L0, ns, sxyz, sf, si);
+  c->launches++;
+}
+
+void launch_mesh_transpose(ztm_ctx* c, const MeshConst& k, int nmodels, const double* rho,
+                           float* rhoT) {
+  long long total = (long long)nmodels * k.ncols * k.nzp;
+  int blocks = (int)std::min<long long>((total + 255) / 256, 32LL * std::max(c->num_sms, 1));
+  transpose_kernel<<<std::max(blocks, 1), 256, 0, c->stream>>>(k, nmodels, rho, rhoT);
+  c->launches++;
+}
+
+void launch_mesh_near(ztm_ctx* c, const MeshConst& k, const MeshDesc& m, int ns,
+                      const double* sxyz, const int4* si, const double* rho, double* out,
+                      bool f64) {
+  if (ns <= 0) return;
+  int blocks = (ns + NEAR_WPB - 1) / NEAR_WPB;
+  if (f64)
+    near_kernel<double><<<blocks, NEAR_WPB * 32, 0, c->stream>>>(k, m, ns, sxyz, si, rho, out);
+  else
+    near_kernel<float><<<blocks, NEAR_WPB * 32, 0, c->stream>>>(k, m, ns, sxyz, si, rho, out);
+  c->launches++;
+}
+
+size_t ztm_prism_ws(const MeshDesc& m, int ns, int precision, int num_sms, const ztm_opts* o) {
+  if (precision == ZTM_PREC_FP64) {
+    long long np = (long long)m.nx * m.ny * m.nz, len;
+    int tiles = std::max(1, (ns + F64_TS - 1) / F64_TS);
+    long long ch = f64_chunks(np, tiles, num_sms, &len);
+    return WsCarver::need((size_t)ch * ns * 8);
+  }
+  double nq = (o && o->near_q > 0) ? o->near_q : 6.0;
+  MeshConst k = make_mesh_const(m, nq);
+  FarShape f = far_shape(k, ns, num_sms, o);
+  return WsCarver::need((size_t)k.ncols * k.nzp * 4) + WsCarver::need((size_t)ns * 16) * 2 +
+         WsCarver::need((size_t)ns * 8) + WsCarver::need((size_t)f.chunks * ns * 8);
+}
+
+int ztm_launch_prism(ztm_ctx* c, const MeshDesc& m, const double* d_rho, int ns,
+                     const double* d_sxyz, double* d_gz, double G, int precision,
+                     const ztm_opts* o, WsCarver& wc) {
+  const double G5 = G * 1.0e5;
+  if (precision == ZTM_PREC_FP64) {
+    long long np = (long long)m.nx * m.ny * m.nz, len;
+    int tiles = std::max(1, (ns + F64_TS - 1) / F64_TS);
+    long long ch = f64_chunks(np, tiles, c->num_sms, &len);
+    double* partial = wc.take<double>((size_t)ch * ns);
+    mesh_f64_kernel<<<dim3(tiles, (unsigned)ch), F64_TS, 0, c->stream>>>(m, ns, d_sxyz, d_rho, len,
+                                                                         partial);
+    finalize_kernel<<<(ns + 255) / 256, 256, 0, c->stream>>>(ns, (int)ch, partial, 1.0, nullptr,
+                                                             G5, d_gz);
+    c->launches += 2;
+    return ztm_after_launch(c, "prism FP64 kernels");
+  }
+  const double nq = (o && o->near_q > 0) ? o->near_q : 6.0;
+  MeshConst k = make_mesh_const(m, nq);
+  FarShape f = far_shape(k, ns, c->num_sms, o);
+  float* rhoT = wc.take<float>((size_t)k.ncols * k.nzp);
+  float4* sf = wc.take<float4>(ns);
+  int4* si = wc.take<int4>(ns);
+  double* near = wc.take<double>(ns);
+  double* partial = wc.take<double>((size_t)f.chunks * ns);
+  launch_mesh_transpose(c, k, 1, d_rho, rhoT);
+  launch_mesh_station_prep(c, m, k.L0, ns, d_sxyz, sf, si);
+  launch_mesh_near(c, k, m, ns, d_sxyz, si, d_rho, near, precision == ZTM_PREC_MIXED);
+  FarArgs a;
+  a.k = k; a.ns = ns; a.chunk_cols = f.chunk_cols; a.sc = f.sc;
+  a.sf = sf; a.si = si; a.rhoT = rhoT; a.partial = partial; a.err = c->d_err;
+  cudaFuncSetAttribute(far_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+  far_kernel<<<dim3(f.tiles, f.chunks), FAR_TS, f.smem, c->stream>>>(a);
+  const double far_scale = k.L0 * (double)k.dxn * k.dyn * k.dzn;
+  finalize_kernel<<<(ns + 255) / 256, 256, 0, c->stream>>>(ns, f.chunks, partial, far_scale, near,
+                                                           G5, d_gz);
+  c->launches += 2;
+  return ztm_after_launch(c, "prism mixed kernels");
+}
+
+size_t ztm_prism_list_ws(long long np, int ns, int precision, int num_sms) {
+  int tiles = std::max(1, (ns + F64_TS - 1) / F64_TS);
+  long long len;
+  long long ch = f64_chunks(std::max(np, 1LL), tiles, num_sms, &len);
+  size_t w = WsCarver::need((size_t)ch * ns * 8);
+  if (precision != ZTM_PREC_FP64) w += WsCarver::need((size_t)np * sizeof(ListPrism));
+  return w;
+}
+
+int ztm_launch_prism_list(ztm_ctx* c, long long np, const double* d_geom, const double* d_rho,
+                          int ns, const double* d_sxyz, double* d_gz, double G, int precision,
+                          double near_q, WsCarver& wc) {
+  const double G5 = G * 1.0e5;
+  int tiles = std::max(1, (ns + F64_TS - 1) / F64_TS);
+  long long len;
+  long long ch = f64_chunks(std::max(np, 1LL), tiles, c->num_sms, &len);
+  double* partial = wc.take<double>((size_t)ch * ns);
+  ListPrism* lp = nullptr;
+  if (precision != ZTM_PREC_FP64 && np > 0) {
+    lp = wc.take<ListPrism>(np);
+    list_prep_kernel<<<(unsigned)((np + 255) / 256), 256, 0, c->stream>>>(np, d_geom, d_rho,
+                                                                          near_q, lp);
+    c->launches++;
+  }
+  if (np > 0) {
+    dim3 grid(tiles, (unsigned)ch);
+    int method = precision == ZTM_PREC_FP64 ? 0 : 1;
+    if (precision == ZTM_PREC_FP32)
+      list_kernel<false><<<grid, F64_TS, 0, c->stream>>>(np, d_geom, d_rho, lp, ns, d_sxyz, len,
+                                                         method, partial);
+    else
+      list_kernel<true><<<grid, F64_TS, 0, c->stream>>>(np, d_geom, d_rho, lp, ns, d_sxyz, len,
+                                                        method, partial);
+    c->launches++;
+  } else {
+    ch = 0;
+  }
+  finalize_kernel<<<(ns + 255) / 256, 256, 0, c->stream>>>(ns, (int)ch, partial, 1.0, nullptr, G5,
+                                                           d_gz);
+  c->launches++;
+  return ztm_after_launch(c, "prism list kernels");
+}

@@ -1,0 +1,106 @@
+// prism_common.cuh - geometry preparation and the far-field expansion shared
+// by the forward, adjoint and batched prism kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "ztm_internal.cuh"
+
+// Far-field expansion of one prism's attraction, relative to the point-mass
+// term.  With (X, Y, Z) = station minus prism centre and r = |(X,Y,Z)|:
+//   gz = G rho V Z/r^3 * [1 + t2 + t4],
+//   t2 = (cA X^2 + cB Y^2 + a1 Z^2) / r^4,
+//   t4 = (h0 + h1 Z^2 + h2 Z^4) / r^8,
+//   h1 = cX1 X^2 + cY1 Y^2,  h0 = cXX X^4 + cXY X^2 Y^2 + cYY Y^4.
+// This is the Taylor expansion of Z/r^3 over the prism volume to fourth
+// order (second moments dx^2/12, fourth moments dx^4/80, mixed dx^2 dy^2/144;
+// odd moments vanish by symmetry), with the harmonic identity
+// d_zz = -(d_xx + d_yy) used to fold the z derivatives.  Lengths are in the
+// normalised unit L0 (the largest cell edge) so that float cannot overflow.
+struct FarCoef {
+  float cA, cB, a1;
+  float cX1, cY1, cXX, cXY, cYY, h2;
+};
+
+__host__ __device__ inline FarCoef far_coef(double dx, double dy, double dz) {
+  double x2 = dx * dx, y2 = dy * dy, z2 = dz * dz;
+  double x4 = x2 * x2, y4 = y2 * y2, z4 = z2 * z2;
+  FarCoef f;
+  f.cA = (float)((4 * x2 - y2 - 3 * z2) / 8);
+  f.cB = (float)((4 * y2 - x2 - 3 * z2) / 8);
+  f.a1 = (float)((2 * z2 - x2 - y2) / 8);
+  f.h2 = (float)((9 * x4 + 10 * x2 * y2 - 40 * x2 * z2 + 9 * y4 - 40 * y2 * z2 + 24 * z4) / 384);
+  f.cX1 = (float)(-(54 * x4 + 25 * x2 * y2 - 205 * x2 * z2 - 9 * y4 + 5 * y2 * z2 + 60 * z4) / 192);
+  f.cY1 = (float)(-(-9 * x4 + 25 * x2 * y2 + 5 * x2 * z2 + 54 * y4 - 205 * y2 * z2 + 60 * z4) / 192);
+  f.cXX = (float)((24 * x4 - 20 * x2 * y2 - 60 * x2 * z2 + 3 * y4 + 10 * y2 * z2 + 15 * z4) / 128);
+  f.cXY = (float)((-36 * x4 + 170 * x2 * y2 - 50 * x2 * z2 - 36 * y4 - 50 * y2 * z2 + 30 * z4) / 128);
+  f.cYY = (float)((3 * x4 - 20 * x2 * y2 + 10 * x2 * z2 + 24 * y4 - 60 * y2 * z2 + 15 * z4) / 128);
+  return f;
+}
+
+// Regular-mesh constants for the mixed kernels.
+struct MeshConst {
+  int nx, ny, nz, nzp;  // nzp: layers padded to a multiple of 4
+  int ncols;
+  int wx, wy, wl;       // near-box half widths (columns, columns, layers)
+  float dxn, dyn, dzn;  // cell edges / L0
+  double L0;
+  FarCoef fc;
+};
+
+// Half widths of the near box: every prism outside it has its centre at
+// least near_q * (half diagonal) from the station.  A prism whose index
+// differs from the station's home index by k >= w+1 along an axis is at
+// least (w + 1/2) cells away along that axis.
+inline void near_widths(double dx, double dy, double dz, double near_q, int* wx, int* wy,
+                        int* wl) {
+  double ell = 0.5 * sqrt(dx * dx + dy * dy + dz * dz);
+  double R = near_q * ell;
+  *wx = (int)ceil(R / dx - 0.5);
+  *wy = (int)ceil(R / dy - 0.5);
+  *wl = (int)ceil(R / dz - 0.5);
+  if (*wx < 0) *wx = 0;
+  if (*wy < 0) *wy = 0;
+  if (*wl < 0) *wl = 0;
+}
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) {
+  return v < lo ? lo : (v > hi ? hi : v);
+}
+
+// Near box of a station (inclusive bounds), clamped to the mesh.
+struct NearBox {
+  int x0, x1, y0, y1, l0, l1;
+};
+__device__ __forceinline__ NearBox near_box(int4 si, const MeshConst& k) {
+  NearBox b;
+  int cx = clampi(si.x, 0, k.nx - 1), cy = clampi(si.y, 0, k.ny - 1),
+      cz = clampi(si.z, 0, k.nz - 1);
+  b.x0 = max(0, cx - k.wx);
+  b.x1 = min(k.nx - 1, cx + k.wx);
+  b.y0 = max(0, cy - k.wy);
+  b.y1 = min(k.ny - 1, cy + k.wy);
+  b.l0 = max(0, cz - k.wl);
+  b.l1 = min(k.nz - 1, cz + k.wl);
+  return b;
+}
+
+// ---- host launchers (prism.cu) ------------------------------------------
+MeshConst make_mesh_const(const MeshDesc& m, double near_q);
+// Station-relative integer/float decomposition (computed in double once per
+// station): x_s - x0 = (ixs + 1/2) dx + ex, likewise y, and
+// z_s = z_top - (izs + 1/2) dz + ez, so that station-minus-centre offsets are
+// k*d + e with an exact integer k and a small float e (e in units of L0).
+void launch_mesh_station_prep(ztm_ctx* c, const MeshDesc& m, double L0, int ns,
+                              const double* sxyz, float4* sf, int4* si);
+// Column-major float copy of the density: rhoT[c*nzp + l], c = ix + nx*iy,
+// padded layers zero.  nmodels > 1: model-major blocks of ncols*nzp floats.
+void launch_mesh_transpose(ztm_ctx* c, const MeshConst& k, int nmodels, const double* rho,
+                           float* rhoT);
+// Near box in double (or float) with vertex sharing: for each station, the
+// sum over box vertices of Phi(vertex - station) times the signed triple
+// difference of the density over the (up to 8) box prisms around the vertex.
+// One warp per station.  out[s] = that sum (metres x density, without G).
+void launch_mesh_near(ztm_ctx* c, const MeshConst& k, const MeshDesc& m, int ns,
+                      const double* sxyz, const int4* si, const double* rho, double* out,
+                      bool f64);

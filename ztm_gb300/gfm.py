@@ -1,0 +1,307 @@
+"""Host-side mirror of ZTM's gravity call surface over the C ABI.
+
+The reference's gravity path is the block of FM::FM at TFM.cpp:83-99: it
+takes the fine-grid density perturbation `drho` (built at TFM.cpp:85-89), the
+station heights `surf = topo + sea` and returns the field `G` (mGal) on the
+di x dj grid, either through the GFM process (TFM.cpp:90-94) or the CPU
+lambda (TFM.cpp:95-99).  `GravityContext.pointmass` is that call.  The prism,
+interface, adjoint and batched calls extend it with the closed-form model.
+
+Arrays may be numpy arrays (host memory: the library copies in and out) or
+CUDA torch tensors (device memory: used in place, the call is asynchronous on
+the context's stream).  Every call goes through libztmgrav.so; there is no
+CPU fallback, and a non-zero status raises GravityError.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+
+PRECISIONS = {"fp64": _lib.PREC_FP64, "fp32": _lib.PREC_FP32, "mixed": _lib.PREC_MIXED}
+DEFAULT_G = 6.67e-11  # the constant behind the 66.7 mGal factor of TFM.cpp:98
+
+
+class GravityError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("ztm status %d: %s" % (code, msg))
+        self.code = code
+
+
+def _is_torch_cuda(x):
+    return type(x).__module__.startswith("torch") and getattr(x, "is_cuda", False)
+
+
+class _Args:
+    """Collects array arguments of one call; all host or all device."""
+
+    def __init__(self):
+        self.device = None
+        self.keep = []
+
+    def _kind(self, dev):
+        if self.device is None:
+            self.device = dev
+        elif self.device != dev:
+            raise ValueError("mix of host and device arrays in one call")
+
+    def arr(self, x, n=None, dtype=np.float64, name="array"):
+        if x is None:
+            return None
+        if _is_torch_cuda(x):
+            import torch
+            want = torch.float64 if dtype == np.float64 else torch.int32
+            if x.dtype != want:
+                raise TypeError("%s must be %s" % (name, want))
+            if not x.is_contiguous():
+                raise ValueError("%s must be contiguous" % name)
+            if n is not None and x.numel() != n:
+                raise ValueError("%s has %d elements, expected %d" % (name, x.numel(), n))
+            self._kind(True)
+            self.keep.append(x)
+            return ctypes.c_void_p(x.data_ptr())
+        a = np.ascontiguousarray(x, dtype=dtype)
+        if n is not None and a.size != n:
+            raise ValueError("%s has %d elements, expected %d" % (name, a.size, n))
+        self._kind(False)
+        self.keep.append(a)
+        return a.ctypes.data_as(ctypes.c_void_p)
+
+    def out(self, n, like=None):
+        if self.device:
+            import torch
+            t = torch.empty(n, dtype=torch.float64, device=like.device if like is not None else "cuda")
+            self.keep.append(t)
+            return t, ctypes.c_void_p(t.data_ptr())
+        a = np.empty(n, dtype=np.float64)
+        self.keep.append(a)
+        return a, a.ctypes.data_as(ctypes.c_void_p)
+
+    @property
+    def flags(self):
+        return _lib.FLAG_DEVICE_PTRS if self.device else 0
+
+
+def make_grid(di, dj, dk, fh=1, fv=2, bfr=10, threshold=0.001, scale=1.0):
+    """Reference grid (defaults: GFM_GPU.cu:24 for fh, fv, bfr)."""
+    return _lib.Grid(di, dj, dk, fh, fv, bfr, threshold, scale)
+
+
+def make_mesh(nx, ny, nz, dx, dy, dz, x0=0.0, y0=0.0, z_top=0.0):
+    return _lib.Mesh(nx, ny, nz, x0, y0, z_top, dx, dy, dz)
+
+
+def make_imesh(nx, ny, dx, dy, z_base, x0=0.0, y0=0.0):
+    return _lib.IMesh(nx, ny, x0, y0, dx, dy, z_base)
+
+
+def _opts(precision, flags, G, near_q, tile=0, chunk=0):
+    if isinstance(precision, str):
+        precision = PRECISIONS[precision]
+    return _lib.Opts(precision, flags, G or 0.0, near_q or 0.0, tile, chunk)
+
+
+class GravityContext:
+    """One CUDA device, one stream, one grow-only workspace."""
+
+    def __init__(self, device=0):
+        self._lib = _lib.load()
+        h = ctypes.c_void_p()
+        rc = self._lib.ztm_ctx_create(int(device), ctypes.byref(h))
+        if rc != 0:
+            raise GravityError(rc, "context creation failed on device %d" % device)
+        self._h = h
+        self.device = device
+
+    # -- lifetime ------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.ztm_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc):
+        if rc != 0:
+            msg = self._lib.ztm_last_error(self._h)
+            raise GravityError(rc, msg.decode() if msg else "")
+
+    @property
+    def stream(self):
+        return self._lib.ztm_ctx_stream(self._h)
+
+    def set_stream(self, stream_ptr):
+        self._check(self._lib.ztm_ctx_set_stream(self._h, ctypes.c_void_p(stream_ptr or 0)))
+
+    def launches(self):
+        return int(self._lib.ztm_ctx_launches(self._h))
+
+    def sync(self):
+        self._check(self._lib.ztm_ctx_sync(self._h))
+
+    # -- point mass (TFM.cpp:90-99) -------------------------------------
+    def pointmass(self, grid, drho, surf, nn=None, precision="fp64"):
+        """G (di*dj, mGal) from drho (ii*jj*kk, g/cc) and surf (di*dj)."""
+        ii = (grid.di - 1) * grid.fh + 1
+        jj = (grid.dj - 1) * grid.fh + 1
+        kk = (grid.dk - 1) * grid.fv + 1
+        a = _Args()
+        pd = a.arr(drho, ii * jj * kk, name="drho")
+        ps = a.arr(surf, grid.di * grid.dj, name="surf")
+        pn, n_nn = None, 0
+        if nn is not None:
+            pn = a.arr(nn, None, dtype=np.int32, name="nn")
+            n_nn = int(nn.numel() if _is_torch_cuda(nn) else np.asarray(nn).size)
+        out, po = a.out(grid.di * grid.dj, drho)
+        prec = PRECISIONS[precision] if isinstance(precision, str) else precision
+        self._check(self._lib.ztm_gfm_pointmass(self._h, ctypes.byref(grid), pd, pn, n_nn, ps, po,
+                                                prec, a.flags))
+        return out
+
+    # -- prism mesh -----------------------------------------------------
+    def prism(self, mesh, rho, stations, precision="mixed", G=None, near_q=None, tile=0, chunk=0):
+        np_ = mesh.nx * mesh.ny * mesh.nz
+        a = _Args()
+        pr = a.arr(rho, np_, name="rho")
+        ns = _nstations(stations)
+        px = a.arr(stations, 3 * ns, name="stations")
+        out, po = a.out(ns, rho)
+        o = _opts(precision, a.flags, G, near_q, tile, chunk)
+        self._check(self._lib.ztm_gfm_prism(self._h, ctypes.byref(mesh), pr, ns, px, po,
+                                            ctypes.byref(o)))
+        return out
+
+    def prism_list(self, geom, rho, stations, precision="fp64", G=None, near_q=None):
+        n = _nstations_list(geom)
+        a = _Args()
+        pg = a.arr(geom, 6 * n, name="geom")
+        pr = a.arr(rho, n, name="rho")
+        ns = _nstations(stations)
+        px = a.arr(stations, 3 * ns, name="stations")
+        out, po = a.out(ns, rho)
+        o = _opts(precision, a.flags, G, near_q)
+        self._check(self._lib.ztm_gfm_prism_list(self._h, n, pg, pr, ns, px, po, ctypes.byref(o)))
+        return out
+
+    def adjoint(self, mesh, stations, resid, precision="mixed", G=None, near_q=None):
+        np_ = mesh.nx * mesh.ny * mesh.nz
+        ns = _nstations(stations)
+        a = _Args()
+        px = a.arr(stations, 3 * ns, name="stations")
+        pr = a.arr(resid, ns, name="resid")
+        out, po = a.out(np_, resid)
+        o = _opts(precision, a.flags, G, near_q)
+        self._check(self._lib.ztm_gfm_adjoint(self._h, ctypes.byref(mesh), ns, px, pr, po,
+                                              ctypes.byref(o)))
+        return out
+
+    # -- interface --------------------------------------------------------
+    def interface(self, imesh, depth, rho_col, stations, precision="mixed", G=None, near_q=None):
+        nc = imesh.nx * imesh.ny
+        ns = _nstations(stations)
+        a = _Args()
+        pd = a.arr(depth, nc, name="depth")
+        pr = a.arr(rho_col, nc, name="rho_col")
+        px = a.arr(stations, 3 * ns, name="stations")
+        out, po = a.out(ns, depth)
+        o = _opts(precision, a.flags, G, near_q)
+        self._check(self._lib.ztm_gfm_interface(self._h, ctypes.byref(imesh), pd, pr, ns, px, po,
+                                                ctypes.byref(o)))
+        return out
+
+    def interface_adjoint(self, imesh, depth, rho_col, stations, resid, precision="mixed",
+                          G=None, near_q=None):
+        nc = imesh.nx * imesh.ny
+        ns = _nstations(stations)
+        a = _Args()
+        pd = a.arr(depth, nc, name="depth")
+        pr = a.arr(rho_col, nc, name="rho_col")
+        px = a.arr(stations, 3 * ns, name="stations")
+        pres = a.arr(resid, ns, name="resid")
+        g_rho, pgr = a.out(nc, depth)
+        g_dep, pgd = a.out(nc, depth)
+        o = _opts(precision, a.flags, G, near_q)
+        self._check(self._lib.ztm_gfm_interface_adjoint(self._h, ctypes.byref(imesh), pd, pr, ns,
+                                                        px, pres, pgr, pgd, ctypes.byref(o)))
+        return g_rho, g_dep
+
+    def interface_misfit(self, imesh, depth, rho_col, stations, data, precision="mixed",
+                         G=None, near_q=None):
+        """Returns (misfit, gz, g_rho, g_depth) for misfit 0.5*|gz - data|^2."""
+        nc = imesh.nx * imesh.ny
+        ns = _nstations(stations)
+        a = _Args()
+        pd = a.arr(depth, nc, name="depth")
+        pr = a.arr(rho_col, nc, name="rho_col")
+        px = a.arr(stations, 3 * ns, name="stations")
+        pdat = a.arr(data, ns, name="data")
+        gz, pgz = a.out(ns, depth)
+        g_rho, pgr = a.out(nc, depth)
+        g_dep, pgd = a.out(nc, depth)
+        mis = ctypes.c_double(0.0)
+        if a.device:
+            import torch
+            mt = torch.zeros(1, dtype=torch.float64, device=depth.device)
+            a.keep.append(mt)
+            pmis = ctypes.c_void_p(mt.data_ptr())
+        else:
+            pmis = ctypes.cast(ctypes.pointer(mis), ctypes.c_void_p)
+        o = _opts(precision, a.flags, G, near_q)
+        self._check(self._lib.ztm_gfm_interface_misfit(self._h, ctypes.byref(imesh), pd, pr, ns,
+                                                       px, pdat, pmis, pgz, pgr, pgd,
+                                                       ctypes.byref(o)))
+        misfit = mt if a.device else mis.value
+        return misfit, gz, g_rho, g_dep
+
+    # -- batched ----------------------------------------------------------
+    def batch(self, jobs, precision="mixed", G=None, near_q=None):
+        """jobs: list of (mesh, rho[nmodels, nprisms], stations[ns, 3]).
+        Returns a list of gz arrays [nmodels, ns]."""
+        a = _Args()
+        arr = (_lib.Job * len(jobs))()
+        outs = []
+        for i, (mesh, rho, st) in enumerate(jobs):
+            np_ = mesh.nx * mesh.ny * mesh.nz
+            nm = int(rho.shape[0]) if getattr(rho, "ndim", 1) == 2 else 1
+            ns = _nstations(st)
+            pr = a.arr(rho, nm * np_, name="rho")
+            px = a.arr(st, 3 * ns, name="stations")
+            out, po = a.out(nm * ns, rho)
+            outs.append((out, nm, ns))
+            arr[i].mesh = mesh
+            arr[i].nmodels = nm
+            arr[i].rho = pr
+            arr[i].ns = ns
+            arr[i].sxyz = px
+            arr[i].gz = po
+        o = _opts(precision, a.flags, G, near_q)
+        self._check(self._lib.ztm_gfm_batch(self._h, arr, len(jobs), ctypes.byref(o)))
+        return [out.reshape(nm, ns) for out, nm, ns in outs]
+
+
+def _nstations(st):
+    shape = tuple(st.shape)
+    if len(shape) == 2 and shape[1] == 3:
+        return int(shape[0])
+    if len(shape) == 1 and shape[0] % 3 == 0:
+        return int(shape[0] // 3)
+    raise ValueError("stations must be (ns, 3)")
+
+
+def _nstations_list(geom):
+    shape = tuple(geom.shape)
+    if len(shape) == 2 and shape[1] == 6:
+        return int(shape[0])
+    if len(shape) == 1 and shape[0] % 6 == 0:
+        return int(shape[0] // 6)
+    raise ValueError("geom must be (np, 6)")
