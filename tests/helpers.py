@@ -25,6 +25,10 @@ def tfm_like_inputs(di, dj, dk, fh=1, fv=2, seed=0, sparsity=0.3):
     drho[rng.random(drho.size) < sparsity] = 0.0
     drho[np.abs(drho) <= 0.001] = 0.0
     surf = (dk - 3) + 0.37 + 0.2 * rng.random(di * dj)
+    # TFM.cpp:89 keeps only nodes deeper than 10 km (one grid unit at
+    # h = 10 km) below the surface; masses never sit next to a station
+    k = (np.arange(ii * jj * kk) // (ii * jj)) / fv
+    drho[k > surf.min() - 1.0] = 0.0
     return drho, surf
 
 

@@ -1,0 +1,45 @@
+"""Batched persistent launch vs one-at-a-time calls (same mixed method)."""
+import numpy as np
+import pytest
+
+import ztm_gb300
+from helpers import rel_err, small_mesh
+
+pytestmark = pytest.mark.gpu
+
+
+def test_batch_matches_single_calls(ctx):
+    rng = np.random.default_rng(0)
+    jobs = []
+    for shape in [(40, 32, 12), (17, 23, 5), (64, 48, 10)]:
+        mesh, rho = small_mesh(*shape, seed=sum(shape))
+        nm = 1 + shape[2] % 11
+        models = np.stack([rho * (1 + 0.1 * k) + rng.normal(0, 5, rho.size) for k in range(nm)])
+        ns = 50 + shape[0]
+        st = np.stack([rng.uniform(mesh.x0, mesh.x0 + mesh.nx * mesh.dx, ns),
+                       rng.uniform(mesh.y0, mesh.y0 + mesh.ny * mesh.dy, ns),
+                       rng.uniform(mesh.z_top, mesh.z_top + 2000, ns)], 1)
+        jobs.append((mesh, models, st))
+    outs = ctx.batch(jobs)
+    for (mesh, models, st), out in zip(jobs, outs):
+        for k in range(models.shape[0]):
+            ref = ctx.prism(mesh, models[k], st, precision="mixed")
+            assert rel_err(out[k], ref) <= 1e-6
+    # replay of the cached graph gives bitwise the same result
+    outs2 = ctx.batch(jobs)
+    for a, b in zip(outs, outs2):
+        assert np.array_equal(a, b)
+
+
+def test_batch_line_search_trials(ctx):
+    mesh, rho = small_mesh(48, 40, 16, seed=5)
+    _, p = small_mesh(48, 40, 16, seed=6)
+    alphas = np.linspace(0, 2, 32)
+    trials = rho[None, :] + alphas[:, None] * p[None, :]
+    st = np.stack(np.meshgrid(np.arange(20) * 2000.0 + 500, np.arange(16) * 2000.0 + 1700), -1).reshape(-1, 2)
+    st = np.concatenate([st, np.full((len(st), 1), 300.0)], 1)
+    out = ctx.batch([(mesh, trials, st)])[0]
+    g0 = ctx.prism(mesh, rho, st, precision="fp64")
+    gp = ctx.prism(mesh, p, st, precision="fp64")
+    for k, a in enumerate(alphas):
+        assert rel_err(out[k], g0 + a * gp) <= 1e-6

@@ -18,7 +18,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
                      "-Xcompiler", "-ffp-contract=off"]
 
-SOURCES = ["ztm_capi.cu", "pointmass.cu", "prism.cu", "stubs.cu"]
+SOURCES = ["ztm_capi.cu", "pointmass.cu", "prism.cu", "adjoint.cu", "iface.cu", "batch.cu"]
 HOST_SOURCES = []
 
 
@@ -67,7 +67,7 @@ def build(verbose=False, force=False):
         _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs)
     shim_src = os.path.join(CSRC, "gfm_shim.cpp")
     if os.path.exists(shim_src) and (force or _stale(SHIM, [shim_src, LIB])):
-        _run(["g++", "-O2", "-std=c++17", "-o", SHIM, shim_src,
+        _run(["g++", "-O2", "-std=c++17", "-Wall", "-o", SHIM, shim_src,
               "-I" + os.path.join(ROOT, "include"), "-L" + LIBDIR, "-lztmgrav",
               "-Wl,-rpath,$ORIGIN"])
     return LIB

@@ -1,0 +1,292 @@
+// adjoint.cu - transposed sum of the prism forward (dmisfit/drho).
+//
+// For misfit 0.5*|gz - d|^2 and residual r = gz - d, the density gradient is
+//   g_rho[p] = sum_s r[s] * dgz[s]/drho[p] = G*1e5 * sum_s r[s] * U(s, p),
+// the transpose of the forward sum (prism.cu) with the same pair function.
+// The reference has no adjoint: its optimiser differentiates every gravity
+// parameter by a full forward run (TFM.cpp:124-135); this is what replaces
+// those gravity columns.
+//
+//   FP64 plain  thread per prism, stations streamed through shared memory,
+//               8-corner closed form in double; station chunks reduced in a
+//               fixed order.
+//   MIXED/FP32  far pairs: thread per (column, group of 8 layers), the
+//               column's horizontal offsets computed once per station and the
+//               4th-order far-field expansion per layer in float with Kahan
+//               sums.  Near pairs (prisms in the station's near box): one
+//               warp per station computes Phi once per box vertex in shared
+//               memory, combines the 8 corners of each box prism and adds
+//               r[s]*U to g_rho with double atomics.  The far kernel writes
+//               every g_rho entry first, so the result is complete after the
+//               near kernel; the atomics make the last bits order-dependent.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "prism_common.cuh"
+#include "ztm_internal.cuh"
+
+namespace {
+
+constexpr int ADJ_TS = 128;
+constexpr int ADJ_LG = 8;      // layers per thread in the far kernel
+constexpr int ADJ_STILE = 256; // stations per shared-memory tile
+
+__device__ __forceinline__ float far_pair_unit(float w, float Z, float rh, float a0, float h0,
+                                               float h1, const FarCoef& f) {
+  const float Z2 = Z * Z;
+  const float rinv = rsqrtf(rh + Z2);
+  const float ri2 = rinv * rinv;
+  const float ri4 = ri2 * ri2;
+  const float n2 = fmaf(f.a1, Z2, a0);
+  const float H = fmaf(fmaf(f.h2, Z2, h1), Z2, h0);
+  const float t = fmaf(H, ri4, n2) * ri4;
+  const float base = Z * rinv * ri2 * w;
+  return fmaf(base, t, base);
+}
+
+// grid.x covers ncols * ceil(nz/LG) threads.  g[p] = G5*L0*Vn * sum.
+__global__ void __launch_bounds__(ADJ_TS)
+    adj_far_kernel(MeshConst k, int ns, const float4* __restrict__ sf,
+                   const int4* __restrict__ si, const double* __restrict__ res,
+                   double scale, double* __restrict__ g) {
+  __shared__ float4 s_f[ADJ_STILE];
+  __shared__ int4 s_i[ADJ_STILE];
+  __shared__ float s_r[ADJ_STILE];
+  const int ngroups = (k.nz + ADJ_LG - 1) / ADJ_LG;
+  const long long t = blockIdx.x * (long long)ADJ_TS + threadIdx.x;
+  const bool active = t < (long long)k.ncols * ngroups;
+  int c = 0, lg = 0;
+  if (active) {
+    lg = (int)(t / k.ncols);
+    c = (int)(t % k.ncols);
+  }
+  const int ix = c % k.nx, iy = c / k.nx;
+  const int l0 = lg * ADJ_LG;
+  const FarCoef fc = k.fc;
+  Kahan acc[ADJ_LG];
+  for (int s0 = 0; s0 < ns; s0 += ADJ_STILE) {
+    __syncthreads();
+    for (int q = threadIdx.x; q < ADJ_STILE; q += ADJ_TS) {
+      const int s = s0 + q;
+      if (s < ns) {
+        s_f[q] = sf[s];
+        s_i[q] = si[s];
+        s_r[q] = (float)res[s];
+      } else {
+        s_f[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+        s_i[q] = make_int4(0, 0, 0, 0);
+        s_r[q] = 0.f;
+      }
+    }
+    __syncthreads();
+    if (!active) continue;
+    const int cnt = min(ADJ_STILE, ns - s0);
+    for (int q = 0; q < cnt; q++) {
+      const float4 f = s_f[q];
+      const int4 i = s_i[q];
+      const float w = s_r[q];
+      const float X = fmaf((float)(i.x - ix), k.dxn, f.x);
+      const float Y = fmaf((float)(i.y - iy), k.dyn, f.y);
+      const float X2 = X * X, Y2 = Y * Y, rh = X2 + Y2;
+      const float a0 = fmaf(X2, fc.cA, Y2 * fc.cB);
+      const float h1 = fmaf(X2, fc.cX1, Y2 * fc.cY1);
+      const float h0 = fmaf(X2, fmaf(X2, fc.cXX, Y2 * fc.cXY), Y2 * Y2 * fc.cYY);
+      const NearBox b = near_box(i, k);
+      const bool ncl = ix >= b.x0 && ix <= b.x1 && iy >= b.y0 && iy <= b.y1;
+      const int elo = ncl ? b.l0 : k.nz;
+      const unsigned espan = ncl ? (unsigned)(b.l1 - b.l0) : 0u;
+#pragma unroll
+      for (int j = 0; j < ADJ_LG; j++) {
+        const int l = l0 + j;
+        const float Z = fmaf((float)(l - i.z), k.dzn, f.z);
+        const float v = far_pair_unit(w, Z, rh, a0, h0, h1, fc);
+        const bool excl = ((unsigned)(l - elo) <= espan) || l >= k.nz;
+        acc[j].add(excl ? 0.f : v);
+      }
+    }
+  }
+  if (!active) return;
+  const long long plane = (long long)k.ncols;
+#pragma unroll
+  for (int j = 0; j < ADJ_LG; j++) {
+    const int l = l0 + j;
+    if (l < k.nz) g[c + plane * l] = scale * acc[j].value();
+  }
+}
+
+// Near box, one warp per station: Phi at every box vertex into shared
+// memory, then per box prism the signed 8-corner sum, scaled by r[s], added
+// to g with double atomics.
+template <typename T>
+__global__ void adj_near_kernel(MeshConst k, MeshDesc m, int ns, const double* __restrict__ sxyz,
+                                const int4* __restrict__ si, const double* __restrict__ res,
+                                double G5, int nv_cap, double* __restrict__ g) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  T* phi = reinterpret_cast<T*>(smem) + (size_t)warp * nv_cap;
+  const int s = blockIdx.x * (blockDim.x >> 5) + warp;
+  if (s >= ns) return;
+  const double r = res[s];
+  if (r == 0.0) return;
+  const NearBox b = near_box(si[s], k);
+  const double xs = sxyz[3 * s], ys = sxyz[3 * s + 1], zs = sxyz[3 * s + 2];
+  const int nvx = b.x1 - b.x0 + 2, nvy = b.y1 - b.y0 + 2, nvz = b.l1 - b.l0 + 2;
+  const int nv = nvx * nvy * nvz;
+  if (nv > nv_cap) return;  // host sizes nv_cap for the largest box
+  for (int v = lane; v < nv; v += 32) {
+    const int a = b.x0 + v % nvx;
+    const int bb = b.y0 + (v / nvx) % nvy;
+    const int cz = b.l0 + v / (nvx * nvy);
+    phi[v] = ztm_phi<T>((T)((m.x0 + a * m.dx) - xs), (T)((m.y0 + bb * m.dy) - ys),
+                        (T)((m.zt - cz * m.dz) - zs));
+  }
+  __syncwarp();
+  const int bx = nvx - 1, by = nvy - 1, bz = nvz - 1;
+  const int nb = bx * by * bz;
+  const long long plane = (long long)m.nx * m.ny;
+  for (int q = lane; q < nb; q += 32) {
+    const int qx = q % bx, qy = (q / bx) % by, qz = q / (bx * by);
+    // vertices: x lower qx (-), upper qx+1 (+); z: layer top index qz (+),
+    // bottom qz+1 (-)
+    auto P = [&](int dx_, int dy_, int dz_) {
+      return phi[(qx + dx_) + nvx * ((qy + dy_) + nvy * (qz + dz_))];
+    };
+    T u = P(1, 1, 0) - P(0, 1, 0) - P(1, 0, 0) + P(0, 0, 0) - P(1, 1, 1) + P(0, 1, 1) + P(1, 0, 1) -
+          P(0, 0, 1);
+    const long long p = (b.x0 + qx) + (long long)m.nx * (b.y0 + qy) + plane * (b.l0 + qz);
+    atomicAdd(&g[p], G5 * r * (double)u);
+  }
+}
+
+// ---- plain double ---------------------------------------------------------
+__global__ void __launch_bounds__(ADJ_TS)
+    adj_f64_kernel(MeshDesc m, int ns, const double* __restrict__ sxyz,
+                   const double* __restrict__ res, int chunk_len, double* __restrict__ partial) {
+  __shared__ double s_st[4 * 128];
+  const long long np = (long long)m.nx * m.ny * m.nz;
+  const long long p = blockIdx.x * (long long)ADJ_TS + threadIdx.x;
+  const bool active = p < np;
+  const long long plane = (long long)m.nx * m.ny;
+  int ix = 0, iy = 0, l = 0;
+  if (active) {
+    l = (int)(p / plane);
+    long long rem = p - (long long)l * plane;
+    iy = (int)(rem / m.nx);
+    ix = (int)(rem % m.nx);
+  }
+  const double xa = m.x0 + ix * m.dx, xb = m.x0 + (ix + 1) * m.dx;
+  const double ya = m.y0 + iy * m.dy, yb = m.y0 + (iy + 1) * m.dy;
+  const double za = m.zt - (l + 1) * m.dz, zb = m.zt - l * m.dz;
+  const int s0 = blockIdx.y * chunk_len, s1 = min(ns, s0 + chunk_len);
+  double acc = 0.0;
+  for (int t0 = s0; t0 < s1; t0 += 128) {
+    __syncthreads();
+    for (int q = threadIdx.x; q < 128; q += ADJ_TS) {
+      const int s = t0 + q;
+      const bool ok = s < s1;
+      s_st[4 * q] = ok ? sxyz[3 * s] : 0.0;
+      s_st[4 * q + 1] = ok ? sxyz[3 * s + 1] : 0.0;
+      s_st[4 * q + 2] = ok ? sxyz[3 * s + 2] : 0.0;
+      s_st[4 * q + 3] = ok ? res[s] : 0.0;
+    }
+    __syncthreads();
+    if (!active) continue;
+    const int cnt = min(128, s1 - t0);
+    for (int q = 0; q < cnt; q++) {
+      const double r = s_st[4 * q + 3];
+      if (r == 0.0) continue;
+      const double xs = s_st[4 * q], ys = s_st[4 * q + 1], zs = s_st[4 * q + 2];
+      acc += r * ztm_prism_unit<double>(xa - xs, xb - xs, ya - ys, yb - ys, za - zs, zb - zs);
+    }
+  }
+  if (active) partial[(size_t)blockIdx.y * np + p] = acc;
+}
+
+__global__ void adj_f64_finalize(long long np, int nchunks, const double* __restrict__ partial,
+                                 double G5, double* __restrict__ g) {
+  long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (p >= np) return;
+  double a = 0.0;
+  for (int c = 0; c < nchunks; c++) a += partial[(size_t)c * np + p];
+  g[p] = G5 * a;
+}
+
+int adj_f64_chunks(long long np, int ns, int num_sms, int* len) {
+  long long blocks = (np + ADJ_TS - 1) / ADJ_TS;
+  long long want = std::max(1LL, (8LL * std::max(num_sms, 1)) / std::max(blocks, 1LL));
+  long long ch = std::min<long long>(std::min(want, (long long)std::max(1, ns / 32)), 65535);
+  ch = std::max(1LL, ch);
+  int l = (int)((ns + ch - 1) / ch);
+  *len = std::max(l, 1);
+  return (ns + *len - 1) / *len;
+}
+
+int near_cap(const MeshConst& k) {
+  return (std::min(2 * k.wx + 1, k.nx) + 1) * (std::min(2 * k.wy + 1, k.ny) + 1) *
+         (std::min(2 * k.wl + 1, k.nz) + 1);
+}
+
+}  // namespace
+
+size_t ztm_adjoint_ws(const MeshDesc& m, int ns, int precision, int num_sms) {
+  long long np = (long long)m.nx * m.ny * m.nz;
+  if (precision == ZTM_PREC_FP64) {
+    int len;
+    int ch = adj_f64_chunks(np, std::max(ns, 1), num_sms, &len);
+    return WsCarver::need((size_t)ch * np * 8);
+  }
+  return 2 * WsCarver::need((size_t)std::max(ns, 1) * 16);
+}
+
+int ztm_launch_adjoint(ztm_ctx* c, const MeshDesc& m, int ns, const double* d_sxyz,
+                       const double* d_res, double* d_g, double G, int precision,
+                       const ztm_opts* o, WsCarver& wc) {
+  const double G5 = G * 1.0e5;
+  const long long np = (long long)m.nx * m.ny * m.nz;
+  if (ns == 0) {
+    cudaMemsetAsync(d_g, 0, np * 8, c->stream);
+    return ztm_after_launch(c, "adjoint (no stations)");
+  }
+  if (precision == ZTM_PREC_FP64) {
+    int len;
+    int ch = adj_f64_chunks(np, ns, c->num_sms, &len);
+    double* partial = wc.take<double>((size_t)ch * np);
+    dim3 grid((unsigned)((np + ADJ_TS - 1) / ADJ_TS), ch);
+    adj_f64_kernel<<<grid, ADJ_TS, 0, c->stream>>>(m, ns, d_sxyz, d_res, len, partial);
+    adj_f64_finalize<<<(unsigned)((np + 255) / 256), 256, 0, c->stream>>>(np, ch, partial, G5, d_g);
+    c->launches += 2;
+    return ztm_after_launch(c, "adjoint FP64 kernels");
+  }
+  const double nq = (o && o->near_q > 0) ? o->near_q : 6.0;
+  MeshConst k = make_mesh_const(m, nq);
+  float4* sf = wc.take<float4>(ns);
+  int4* si = wc.take<int4>(ns);
+  launch_mesh_station_prep(c, m, k.L0, ns, d_sxyz, sf, si);
+  const int ngroups = (k.nz + ADJ_LG - 1) / ADJ_LG;
+  const long long threads = (long long)k.ncols * ngroups;
+  const double scale = G5 * k.L0 * (double)k.dxn * k.dyn * k.dzn;
+  adj_far_kernel<<<(unsigned)((threads + ADJ_TS - 1) / ADJ_TS), ADJ_TS, 0, c->stream>>>(
+      k, ns, sf, si, d_res, scale, d_g);
+  c->launches++;
+  const int cap = near_cap(k);
+  const bool f64 = precision == ZTM_PREC_MIXED;
+  const size_t per_warp = (size_t)cap * (f64 ? 8 : 4);
+  if (per_warp > 200 * 1024)
+    return ztm_fail(c, ZTM_ERR_RANGE, "near_q too large for the adjoint's near box");
+  int wpb = (int)std::max<size_t>(1, std::min<size_t>(4, (96 * 1024) / per_warp));
+  size_t smem = per_warp * wpb;
+  if (f64) {
+    cudaFuncSetAttribute(adj_near_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)std::max<size_t>(smem, 48 * 1024));
+    adj_near_kernel<double><<<(ns + wpb - 1) / wpb, wpb * 32, smem, c->stream>>>(
+        k, m, ns, d_sxyz, si, d_res, G5, cap, d_g);
+  } else {
+    cudaFuncSetAttribute(adj_near_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)std::max<size_t>(smem, 48 * 1024));
+    adj_near_kernel<float><<<(ns + wpb - 1) / wpb, wpb * 32, smem, c->stream>>>(
+        k, m, ns, d_sxyz, si, d_res, G5, cap, d_g);
+  }
+  c->launches++;
+  return ztm_after_launch(c, "adjoint mixed kernels");
+}

@@ -1,0 +1,518 @@
+// batch.cu - batched prism forward: many density models and uneven meshes
+// in one persistent launch, replayed from a CUDA graph.
+//
+// The reference evaluates its damping trials one full forward model after
+// another (TFM.cpp:165, each FM call running the GPU process of
+// TFM.cpp:90-94).  Here a job is (mesh, stations, nmodels densities); the
+// trial models of a line search are one job with nmodels > 1 and share every
+// pair's geometry: the far-field kernel value of a (station, prism) pair is
+// computed once and applied to a group of up to 8 models (one Kahan sum per
+// model).  Independent regional meshes are further jobs.
+//
+// Work items, taken from one global counter by a persistent grid of
+// (resident blocks x SMs):
+//   near item  (job, station tile): for each station, Phi at the near-box
+//              vertices in double into shared memory once, then per model
+//              the signed triple difference of that model's density.
+//   far item   (job, station tile, column chunk, model group): the float
+//              far field over the chunk, density staged by 1-D TMA bulk
+//              copies (one per model of the group) on an mbarrier.
+// Every item bumps its tile's completion counter; the block that completes a
+// tile adds the tile's partials in a fixed order and writes gz, so the launch
+// needs no second kernel and the result is deterministic.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "prism_common.cuh"
+#include "ztm_internal.cuh"
+
+namespace {
+
+constexpr int B_TS = 128;   // threads per block = stations per tile
+constexpr int B_MG = 8;     // models per far item
+constexpr int B_WARPS = B_TS / 32;
+
+struct BJob {
+  MeshConst k;
+  MeshDesc m;
+  int nmodels, ns, tiles, chunks, chunk_cols, sc, mgroups, nv_cap;
+  long long near_base, far_base;
+  double far_scale, G5;
+  const float4* sf;
+  const int4* si;
+  const float* rhoT;     // nmodels x ncols x nzp
+  const double* rho;     // nmodels x np (layer-major, as given)
+  const double* sxyz;
+  double* partial;       // [model][chunk][ns]
+  double* near;          // [model][ns]
+  double* gz;            // [model][ns]
+  int* done;             // [tiles]
+};
+
+struct BArgs {
+  const BJob* jobs;
+  int njobs;
+  long long n_near, n_items;
+  int* counter;
+  int* err;
+};
+
+__device__ __forceinline__ float unit_pair(float Z, float rh, float a0, float h0, float h1,
+                                           const FarCoef& f) {
+  const float Z2 = Z * Z;
+  const float rinv = rsqrtf(rh + Z2);
+  const float ri2 = rinv * rinv;
+  const float ri4 = ri2 * ri2;
+  const float n2 = fmaf(f.a1, Z2, a0);
+  const float H = fmaf(fmaf(f.h2, Z2, h1), Z2, h0);
+  const float t = fmaf(H, ri4, n2) * ri4;
+  const float base = Z * rinv * ri2;
+  return fmaf(base, t, base);
+}
+
+// tile completion: the last item of a tile writes gz for its stations
+__device__ void tile_done(const BJob& J, int tile, int expected, int* s_flag) {
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) *s_flag = (atomicAdd(&J.done[tile], 1) == expected - 1);
+  __syncthreads();
+  if (!*s_flag) return;
+  __threadfence();
+  const int s = tile * B_TS + threadIdx.x;
+  if (s >= J.ns) return;
+  for (int md = 0; md < J.nmodels; md++) {
+    const double* pp = J.partial + (size_t)md * J.chunks * J.ns;
+    double f = 0.0;
+    for (int c = 0; c < J.chunks; c++) f += __ldcg(pp + (size_t)c * J.ns + s);
+    const double g = J.far_scale * f + __ldcg(J.near + (size_t)md * J.ns + s);
+    J.gz[(size_t)md * J.ns + s] = J.G5 * g;
+  }
+}
+
+__device__ void near_item(const BJob& J, int tile, double* phi_all) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double* phi = phi_all + (size_t)warp * J.nv_cap;
+  const MeshDesc& m = J.m;
+  const long long plane = (long long)m.nx * m.ny;
+  const long long np = plane * m.nz;
+  for (int j = warp; j < B_TS; j += B_WARPS) {
+    const int s = tile * B_TS + j;
+    if (s >= J.ns) break;
+    const NearBox b = near_box(J.si[s], J.k);
+    const double xs = J.sxyz[3 * s], ys = J.sxyz[3 * s + 1], zs = J.sxyz[3 * s + 2];
+    const int nvx = b.x1 - b.x0 + 2, nvy = b.y1 - b.y0 + 2, nvz = b.l1 - b.l0 + 2;
+    const int nv = min(nvx * nvy * nvz, J.nv_cap);
+    for (int v = lane; v < nv; v += 32) {
+      const int a = b.x0 + v % nvx, bb = b.y0 + (v / nvx) % nvy, cz = b.l0 + v / (nvx * nvy);
+      phi[v] = ztm_phi<double>((m.x0 + a * m.dx) - xs, (m.y0 + bb * m.dy) - ys,
+                               (m.zt - cz * m.dz) - zs);
+    }
+    __syncwarp();
+    for (int md = 0; md < J.nmodels; md++) {
+      const double* rho = J.rho + (size_t)md * np;
+      double acc = 0.0;
+      for (int v = lane; v < nv; v += 32) {
+        const int a = b.x0 + v % nvx, bb = b.y0 + (v / nvx) % nvy, cz = b.l0 + v / (nvx * nvy);
+        double D = 0.0;
+        for (int da = 0; da < 2; da++) {
+          const int ix = a - 1 + da;
+          if (ix < b.x0 || ix > b.x1) continue;
+          for (int db = 0; db < 2; db++) {
+            const int iy = bb - 1 + db;
+            if (iy < b.y0 || iy > b.y1) continue;
+            for (int dc = 0; dc < 2; dc++) {
+              const int l = cz - 1 + dc;
+              if (l < b.l0 || l > b.l1) continue;
+              const double r = rho[ix + (long long)m.nx * iy + plane * l];
+              D += ((da == 1) ^ (db == 1) ^ (dc == 0)) ? -r : r;
+            }
+          }
+        }
+        acc += D * phi[v];
+      }
+      acc = warp_sum_d(acc);
+      if (lane == 0) J.near[(size_t)md * J.ns + s] = acc;
+    }
+    __syncwarp();
+  }
+}
+
+__global__ void __launch_bounds__(B_TS) batch_kernel(BArgs a) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
+  float* stage = reinterpret_cast<float*>(smem_raw + 128);
+  double* phi = reinterpret_cast<double*>(smem_raw + 128);
+  __shared__ long long s_item;
+  __shared__ int s_flag, s_lm;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  unsigned uses0 = 0, uses1 = 0;  // completed phases per buffer (uniform)
+  for (long long guard = 0; guard < a.n_items + 1; guard++) {
+    if (threadIdx.x == 0) s_item = atomicAdd(a.counter, 1);
+    __syncthreads();
+    const long long item = s_item;
+    __syncthreads();
+    if (item >= a.n_items) break;
+    if (item < a.n_near) {
+      int j = 0;
+      while (j + 1 < a.njobs && a.jobs[j + 1].near_base <= item) j++;
+      const BJob& J = a.jobs[j];
+      const int tile = (int)(item - J.near_base);
+      near_item(J, tile, phi);
+      __syncthreads();
+      tile_done(J, tile, J.chunks * J.mgroups + 1, &s_flag);
+      continue;
+    }
+    int j = 0;
+    while (j + 1 < a.njobs && a.jobs[j + 1].far_base <= item) j++;
+    const BJob& J = a.jobs[j];
+    long long r = item - J.far_base;
+    const int tile = (int)(r % J.tiles);
+    r /= J.tiles;
+    const int chunk = (int)(r % J.chunks);
+    const int mg = (int)(r / J.chunks);
+    const MeshConst& k = J.k;
+    const int m0 = mg * B_MG, mcnt = min(B_MG, J.nmodels - m0);
+    const int c0 = chunk * J.chunk_cols, c1 = min(k.ncols, c0 + J.chunk_cols);
+    const int nst = (c1 - c0 + J.sc - 1) / J.sc;
+    const int stage_floats = J.sc * k.nzp * B_MG;
+    const int s = tile * B_TS + threadIdx.x;
+    const bool active = s < J.ns;
+    float ex = 0.f, ey = 0.f, ez = 0.f;
+    int ixs = 0, iys = 0, izs = 0;
+    NearBox nb = {1, 0, 1, 0, 1, 0};
+    if (threadIdx.x == 0) s_lm = 0;
+    __syncthreads();
+    if (active) {
+      const float4 f = J.sf[s];
+      const int4 i = J.si[s];
+      ex = f.x; ey = f.y; ez = f.z;
+      ixs = i.x; iys = i.y; izs = i.z;
+      nb = near_box(i, k);
+      atomicMax(&s_lm, nb.l1 + 1);
+    }
+    auto issue = [&](int st) {
+      const int buf = st & 1;
+      const int cs = c0 + st * J.sc;
+      const int ncol = min(J.sc, c1 - cs);
+      const uint32_t bytes = (uint32_t)ncol * k.nzp * 4u;
+      mbar_expect_tx(&bar[buf], bytes * (uint32_t)mcnt);
+      for (int q = 0; q < mcnt; q++)
+        bulk_g2s(stage + buf * stage_floats + q * J.sc * k.nzp,
+                 J.rhoT + ((size_t)(m0 + q) * k.ncols + cs) * k.nzp, bytes, &bar[buf]);
+    };
+    if (threadIdx.x == 0 && nst > 0) issue(0);
+    __syncthreads();
+    const int Lm = min(s_lm, k.nz);
+    const FarCoef fc = k.fc;
+    Kahan acc[B_MG];
+    bool timed_out = false;
+    for (int st = 0; st < nst; st++) {
+      if (threadIdx.x == 0 && st + 1 < nst) issue(st + 1);
+      const int buf = st & 1;
+      const unsigned par = (buf ? uses1 : uses0) & 1u;
+      const bool ok = mbar_wait(&bar[buf], par);
+      if (buf) uses1++; else uses0++;
+      if (__syncthreads_or(!ok)) {
+        timed_out = true;
+        break;
+      }
+      const float* rs = stage + buf * stage_floats;
+      const int cs = c0 + st * J.sc;
+      const int ncol = min(J.sc, c1 - cs);
+      if (active) {
+        int ix = cs % k.nx, iy = cs / k.nx;
+        for (int q = 0; q < ncol; q++) {
+          const float X = fmaf((float)(ixs - ix), k.dxn, ex);
+          const float Y = fmaf((float)(iys - iy), k.dyn, ey);
+          const float X2 = X * X, Y2 = Y * Y, rh = X2 + Y2;
+          const float a0 = fmaf(X2, fc.cA, Y2 * fc.cB);
+          const float h1 = fmaf(X2, fc.cX1, Y2 * fc.cY1);
+          const float h0 = fmaf(X2, fmaf(X2, fc.cXX, Y2 * fc.cXY), Y2 * Y2 * fc.cYY);
+          const bool ncl = ix >= nb.x0 && ix <= nb.x1 && iy >= nb.y0 && iy <= nb.y1;
+          const int elo = ncl ? nb.l0 : k.nz;
+          const unsigned espan = ncl ? (unsigned)(nb.l1 - nb.l0) : 0u;
+          const float* col = rs + q * k.nzp;
+          const int mstride = J.sc * k.nzp;
+          float zf = (float)(-izs);
+          for (int l = 0; l < k.nz; l++, zf += 1.f) {
+            float K = unit_pair(fmaf(zf, k.dzn, ez), rh, a0, h0, h1, fc);
+            if (l < Lm && (unsigned)(l - elo) <= espan) K = 0.f;
+#pragma unroll
+            for (int md = 0; md < B_MG; md++)
+              if (md < mcnt) acc[md].add(K * col[md * mstride + l]);
+          }
+          if (++ix == k.nx) {
+            ix = 0;
+            ++iy;
+          }
+        }
+      }
+      __syncthreads();
+    }
+    if (timed_out) {
+      if (threadIdx.x == 0) atomicOr(a.err, ZTM_DEVERR_TIMEOUT);
+      return;
+    }
+    if (active) {
+#pragma unroll
+      for (int md = 0; md < B_MG; md++)
+        if (md < mcnt)
+          J.partial[((size_t)(m0 + md) * J.chunks + chunk) * J.ns + s] = acc[md].value();
+    }
+    tile_done(J, tile, J.chunks * J.mgroups + 1, &s_flag);
+  }
+}
+
+struct Plan {
+  std::vector<BJob> jobs;
+  long long n_near = 0, n_items = 0;
+  size_t smem = 128;
+  size_t ws_bytes = 0;
+};
+
+// Shapes only (no pointers): per-job tiles, chunks, stage widths, workspace.
+Plan plan(const ztm_job* jobs, int njobs, double near_q, int num_sms) {
+  Plan p;
+  size_t ws = 0;
+  for (int j = 0; j < njobs; j++) {
+    const ztm_job& q = jobs[j];
+    BJob J;
+    MeshDesc m;
+    m.nx = q.mesh.nx; m.ny = q.mesh.ny; m.nz = q.mesh.nz;
+    m.x0 = q.mesh.x0; m.y0 = q.mesh.y0; m.zt = q.mesh.z_top;
+    m.dx = q.mesh.dx; m.dy = q.mesh.dy; m.dz = q.mesh.dz;
+    J.m = m;
+    J.k = make_mesh_const(m, near_q);
+    J.nmodels = q.nmodels;
+    J.ns = q.ns;
+    J.tiles = std::max(1, (q.ns + B_TS - 1) / B_TS);
+    J.mgroups = (q.nmodels + B_MG - 1) / B_MG;
+    int sc = std::max(1, (24 * 1024) / (J.k.nzp * 4 * B_MG));
+    sc = std::min(sc, 32);
+    J.sc = sc;
+    // aim for ~16 items per SM over the whole batch: split columns so that a
+    // far item holds roughly 2^22 pair-model evaluations at least
+    long long pairs_tile = (long long)B_TS * J.k.ncols * m.nz;
+    long long target = 1LL << 24;
+    int chunks = (int)std::max(1LL, std::min<long long>(pairs_tile / target, J.k.ncols / sc));
+    chunks = std::max(chunks, 1);
+    int cc = (J.k.ncols + chunks - 1) / chunks;
+    cc = ((cc + sc - 1) / sc) * sc;
+    J.chunk_cols = cc;
+    J.chunks = (J.k.ncols + cc - 1) / cc;
+    J.nv_cap = (std::min(2 * J.k.wx + 1, m.nx) + 1) * (std::min(2 * J.k.wy + 1, m.ny) + 1) *
+               (std::min(2 * J.k.wl + 1, m.nz) + 1);
+    J.far_scale = J.k.L0 * (double)J.k.dxn * J.k.dyn * J.k.dzn;
+    p.smem = std::max(p.smem, 128 + (size_t)2 * sc * J.k.nzp * 4 * B_MG);
+    p.smem = std::max(p.smem, 128 + (size_t)B_WARPS * J.nv_cap * 8);
+    ws += WsCarver::need((size_t)q.nmodels * J.k.ncols * J.k.nzp * 4);
+    ws += WsCarver::need((size_t)q.ns * 16) * 2;
+    ws += WsCarver::need((size_t)q.nmodels * J.chunks * q.ns * 8);
+    ws += WsCarver::need((size_t)q.nmodels * q.ns * 8);
+    ws += WsCarver::need((size_t)J.tiles * 4);
+    p.jobs.push_back(J);
+  }
+  for (auto& J : p.jobs) {
+    J.near_base = p.n_near;
+    p.n_near += J.tiles;
+  }
+  long long far = p.n_near;
+  for (auto& J : p.jobs) {
+    J.far_base = far;
+    far += (long long)J.tiles * J.chunks * J.mgroups;
+  }
+  p.n_items = far;
+  ws += WsCarver::need(sizeof(BJob) * njobs) + WsCarver::need(64);
+  p.ws_bytes = ws;
+  (void)num_sms;
+  return p;
+}
+
+void destroy_entry(ZtmGraphEntry& e) {
+  if (e.exec) cudaGraphExecDestroy(e.exec);
+  if (e.graph) cudaGraphDestroy(e.graph);
+  e.exec = nullptr;
+  e.graph = nullptr;
+}
+
+}  // namespace
+
+extern "C" int ztm_gfm_batch(ztm_ctx* c, const ztm_job* jobs, int njobs, const ztm_opts* o) {
+  if (!c) return ZTM_ERR_ARG;
+  c->err.clear();
+  if (njobs < 0 || (njobs > 0 && !jobs)) return ztm_fail(c, ZTM_ERR_ARG, "bad job list");
+  if (njobs == 0) return ZTM_OK;
+  if (njobs > 4096) return ztm_fail(c, ZTM_ERR_RANGE, "more than 4096 jobs");
+  if (o && (o->precision != ZTM_PREC_MIXED || (o->flags & ~ZTM_FLAG_DEVICE_PTRS)))
+    return ztm_fail(c, ZTM_ERR_ARG, "batched launches run the mixed method only");
+  const bool dev = o && (o->flags & ZTM_FLAG_DEVICE_PTRS);
+  const double G = (o && o->G > 0) ? o->G : 6.67e-11;
+  const double nq = (o && o->near_q > 0) ? o->near_q : 6.0;
+  for (int j = 0; j < njobs; j++) {
+    const ztm_job& q = jobs[j];
+    if (q.mesh.nx < 1 || q.mesh.ny < 1 || q.mesh.nz < 1 || !(q.mesh.dx > 0) ||
+        !(q.mesh.dy > 0) || !(q.mesh.dz > 0) || q.nmodels < 1 || q.ns < 1 || !q.rho ||
+        !q.sxyz || !q.gz)
+      return ztm_fail(c, ZTM_ERR_ARG, "bad job " + std::to_string(j));
+    if ((long long)q.mesh.nx * q.mesh.ny * q.mesh.nz * q.nmodels > (1LL << 31) - 1)
+      return ztm_fail(c, ZTM_ERR_RANGE, "job " + std::to_string(j) + " is too large");
+  }
+  int prev = -1;
+  cudaGetDevice(&prev);
+  if (prev != c->device) cudaSetDevice(c->device);
+  struct Restore {
+    int p, d;
+    ~Restore() {
+      if (p >= 0 && p != d) cudaSetDevice(p);
+    }
+  } restore{prev, c->device};
+
+  Plan p = plan(jobs, njobs, nq, c->num_sms);
+  if (p.smem > 200 * 1024) return ztm_fail(c, ZTM_ERR_RANGE, "near box too large for a batch");
+  size_t stage_bytes = 0;
+  if (!dev)
+    for (int j = 0; j < njobs; j++) {
+      const ztm_job& q = jobs[j];
+      long long np = (long long)q.mesh.nx * q.mesh.ny * q.mesh.nz;
+      stage_bytes += WsCarver::need((size_t)q.nmodels * np * 8) +
+                     WsCarver::need((size_t)q.ns * 24) +
+                     WsCarver::need((size_t)q.nmodels * q.ns * 8);
+    }
+  int rc = ztm_ws_reserve(c, p.ws_bytes + stage_bytes + 8192);
+  if (rc) return rc;
+  WsCarver wc(c->ws);
+  int* counter = wc.take<int>(16);
+  BJob* d_jobs = wc.take<BJob>(njobs);
+  std::vector<const double*> rho_d(njobs), xyz_d(njobs);
+  std::vector<double*> gz_d(njobs);
+  for (int j = 0; j < njobs; j++) {
+    const ztm_job& q = jobs[j];
+    long long np = (long long)q.mesh.nx * q.mesh.ny * q.mesh.nz;
+    if (dev) {
+      rho_d[j] = q.rho;
+      xyz_d[j] = q.sxyz;
+      gz_d[j] = q.gz;
+    } else {
+      double* r = wc.take<double>((size_t)q.nmodels * np);
+      double* x = wc.take<double>((size_t)q.ns * 3);
+      double* g = wc.take<double>((size_t)q.nmodels * q.ns);
+      const void* tmp;
+      if ((rc = ztm_stage_in(c, q.rho, (size_t)q.nmodels * np * 8, false, r, &tmp))) return rc;
+      if ((rc = ztm_stage_in(c, q.sxyz, (size_t)q.ns * 24, false, x, &tmp))) return rc;
+      rho_d[j] = r;
+      xyz_d[j] = x;
+      gz_d[j] = g;
+    }
+  }
+  for (int j = 0; j < njobs; j++) {
+    BJob& J = p.jobs[j];
+    J.rho = rho_d[j];
+    J.sxyz = xyz_d[j];
+    J.gz = gz_d[j];
+    J.G5 = G * 1.0e5;
+    float* rhoT = wc.take<float>((size_t)J.nmodels * J.k.ncols * J.k.nzp);
+    J.rhoT = rhoT;
+    float4* sf = wc.take<float4>(J.ns);
+    int4* si = wc.take<int4>(J.ns);
+    J.sf = sf;
+    J.si = si;
+    J.partial = wc.take<double>((size_t)J.nmodels * J.chunks * J.ns);
+    J.near = wc.take<double>((size_t)J.nmodels * J.ns);
+    J.done = wc.take<int>(J.tiles);
+  }
+  // graph key: shapes and every pointer the graph bakes in
+  std::vector<long long> key;
+  key.push_back(njobs);
+  key.push_back((long long)(size_t)c->ws);
+  key.push_back((long long)(size_t)c->stream);
+  key.push_back((long long)(nq * 1e6));
+  for (int j = 0; j < njobs; j++) {
+    const ztm_job& q = jobs[j];
+    key.insert(key.end(), {q.mesh.nx, q.mesh.ny, q.mesh.nz, (long long)(q.mesh.dx * 1e3),
+                           (long long)(q.mesh.dy * 1e3), (long long)(q.mesh.dz * 1e3),
+                           (long long)(q.mesh.x0 * 1e3), (long long)(q.mesh.y0 * 1e3),
+                           (long long)(q.mesh.z_top * 1e3), q.nmodels, q.ns,
+                           (long long)(size_t)rho_d[j], (long long)(size_t)xyz_d[j],
+                           (long long)(size_t)gz_d[j], (long long)(G * 1e20)});
+  }
+  // The job table lives in the shared workspace, which other calls reuse:
+  // upload it on every call, ahead of the graph, in stream order.  The host
+  // copy must outlive the asynchronous copy, so keep it on the context.
+  c->batch_table.assign(reinterpret_cast<const char*>(p.jobs.data()),
+                        reinterpret_cast<const char*>(p.jobs.data()) + sizeof(BJob) * njobs);
+  if ((rc = ztm_cuda_check(c, cudaMemcpyAsync(d_jobs, c->batch_table.data(), sizeof(BJob) * njobs,
+                                              cudaMemcpyHostToDevice, c->stream),
+                           "upload batch table")))
+    return rc;
+  ZtmGraphEntry* entry = nullptr;
+  for (auto& e : c->graphs)
+    if (e.key == key) entry = &e;
+  if (!entry) {
+    if (c->graphs.size() >= 8) {
+      destroy_entry(c->graphs.front());
+      c->graphs.erase(c->graphs.begin());
+    }
+    cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)std::max<size_t>(p.smem, 48 * 1024));
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, B_TS, p.smem);
+    per_sm = std::max(1, per_sm);
+    long long grid = std::min<long long>((long long)per_sm * c->num_sms, p.n_items);
+    BArgs args;
+    args.jobs = d_jobs;
+    args.njobs = njobs;
+    args.n_near = p.n_near;
+    args.n_items = p.n_items;
+    args.counter = counter;
+    args.err = c->d_err;
+    ZtmGraphEntry e;
+    e.key = key;
+    cudaGraph_t g = nullptr;
+    const long long launches_before = c->launches;
+    if ((rc = ztm_cuda_check(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal),
+                             "begin graph capture")))
+      return rc;
+    for (int j = 0; j < njobs; j++) {
+      BJob& J = p.jobs[j];
+      launch_mesh_transpose(c, J.k, J.nmodels, J.rho, const_cast<float*>(J.rhoT));
+      launch_mesh_station_prep(c, J.m, J.k.L0, J.ns, J.sxyz, const_cast<float4*>(J.sf),
+                               const_cast<int4*>(J.si));
+      cudaMemsetAsync(J.done, 0, sizeof(int) * J.tiles, c->stream);
+    }
+    cudaMemsetAsync(counter, 0, sizeof(int) * 16, c->stream);
+    batch_kernel<<<(unsigned)grid, B_TS, p.smem, c->stream>>>(args);
+    cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
+    c->launches = launches_before;  // captured launches are counted per replay
+    if (ce != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return ztm_cuda_check(c, ce, "end graph capture");
+    }
+    e.graph = g;
+    if ((rc = ztm_cuda_check(c, cudaGraphInstantiate(&e.exec, g, 0), "instantiate batch graph"))) {
+      cudaGraphDestroy(g);
+      return rc;
+    }
+    c->graphs.push_back(e);
+    entry = &c->graphs.back();
+  }
+  if ((rc = ztm_cuda_check(c, cudaGraphLaunch(entry->exec, c->stream), "launch batch graph")))
+    return rc;
+  c->launches += 1 + 2LL * njobs;
+  if (dev) return ZTM_OK;
+  for (int j = 0; j < njobs; j++) {
+    const ztm_job& q = jobs[j];
+    if ((rc = ztm_cuda_check(c, cudaMemcpyAsync(q.gz, gz_d[j], (size_t)q.nmodels * q.ns * 8,
+                                                cudaMemcpyDeviceToHost, c->stream),
+                             "copy batch result")))
+      return rc;
+  }
+  if ((rc = ztm_cuda_check(c, cudaStreamSynchronize(c->stream), "batch"))) return rc;
+  return ztm_check_device_error(c);
+}

@@ -1,0 +1,573 @@
+// iface.cu - interface (prism-column) model: forward, adjoint and misfit.
+//
+// Column c = (ix, iy) spans its cell horizontally and z in [z_base, -depth[c]]
+// with density rho[c].  gz(s) = G*1e5 * sum_c rho[c] * U(s, c), U the prism
+// integral of (z_s - z)/r^3.  The adjoint gives
+//   g_rho[c]   = G*1e5 * sum_s r[s] * U(s, c)
+//   g_depth[c] = -G*1e5 * rho[c] * sum_s r[s] * F(s, c),
+// F the integral of (z_s - z_top)/r^3 over the column's top face (the
+// analytic derivative of U with respect to the top, 4-corner atan sum).
+// This is the Moho-interface parameterisation of the reference's density
+// builder (TFM.cpp:85-88), where a column's density contrast switches at the
+// rendered Moho depth; the reference differentiates it only by finite
+// differences of full forward runs (TFM.cpp:124-135).
+//
+// Mixed method.  Far columns: the vertical integral is exact,
+//   1/r_top - 1/r_base = thick (u_t + u_b) / (r_t r_b (r_t + r_b)),
+// written without cancellation, and the horizontal integral over the cell
+// is the 4th-order Taylor expansion of 1/r in (X, Y):
+//   C(u) = (Q2 + Q0 r^2)/r^5 + (P4 + P2 r^2 + P0 r^4)/r^9,
+// with Q2 = (dx^2 X^2 + dy^2 Y^2)/8, Q0 = -(dx^2 + dy^2)/24,
+//      P4 = 7/128 (dx^4 X^4 + dy^4 Y^4) + 35/192 dx^2 dy^2 X^2 Y^2,
+//      P2 = -3/64 (dx^4 X^2 + dy^4 Y^2) - 5/192 dx^2 dy^2 (X^2 + Y^2),
+//      P0 = 3/640 (dx^4 + dy^4) + 1/192 dx^2 dy^2,
+// so U ~ dx dy [1/r_t - 1/r_b + C(u_t) - C(u_b)].  The face term is the 2-D
+// form of the prism far-field expansion (dz = 0).  All in float with Kahan
+// sums.  Near columns (within near_q horizontal half-diagonals of the
+// station's home column) use the closed forms in double.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "prism_common.cuh"
+#include "ztm_internal.cuh"
+
+namespace {
+
+constexpr int IF_TS = 128;
+constexpr int IF_TILE = 256;
+constexpr int IF_NEAR_WPB = 4;
+
+struct IConst {
+  int nx, ny, ncols, w;  // w: near window half width (columns)
+  float dxn, dyn;
+  double L0;
+  float Q0, P0;
+  float q2x, q2y;        // Q2 = q2x X^2 + q2y Y^2
+  float p4x, p4y, p4xy;  // P4
+  float p2x, p2y;        // P2 = p2x X^2 + p2y Y^2
+  FarCoef face;          // 2-D face expansion
+};
+
+IConst make_iconst(const IMeshDesc& m, double near_q) {
+  IConst k;
+  k.nx = m.nx;
+  k.ny = m.ny;
+  k.ncols = m.nx * m.ny;
+  k.L0 = std::max(m.dx, m.dy);
+  double dx = m.dx / k.L0, dy = m.dy / k.L0;
+  k.dxn = (float)dx;
+  k.dyn = (float)dy;
+  double x2 = dx * dx, y2 = dy * dy, x4 = x2 * x2, y4 = y2 * y2;
+  k.q2x = (float)(x2 / 8);
+  k.q2y = (float)(y2 / 8);
+  k.Q0 = (float)(-(x2 + y2) / 24);
+  k.p4x = (float)(7.0 / 128 * x4);
+  k.p4y = (float)(7.0 / 128 * y4);
+  k.p4xy = (float)(35.0 / 192 * x2 * y2);
+  k.p2x = (float)(-3.0 / 64 * x4 - 5.0 / 192 * x2 * y2);
+  k.p2y = (float)(-3.0 / 64 * y4 - 5.0 / 192 * x2 * y2);
+  k.P0 = (float)(3.0 / 640 * (x4 + y4) + 1.0 / 192 * x2 * y2);
+  k.face = far_coef(dx, dy, 0.0);
+  double ellh = 0.5 * sqrt(m.dx * m.dx + m.dy * m.dy);
+  int w = (int)ceil(near_q * ellh / std::min(m.dx, m.dy) - 0.5);
+  k.w = std::max(w, 0);
+  return k;
+}
+
+struct IStation {  // per-station float data
+  float ex, ey, zs, r;
+};
+
+__global__ void iface_station_prep(IMeshDesc m, double L0, int ns, const double* __restrict__ sxyz,
+                                   const double* __restrict__ res, IStation* __restrict__ sf,
+                                   int2* __restrict__ si) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= ns) return;
+  double xs = sxyz[3 * s], ys = sxyz[3 * s + 1], zs = sxyz[3 * s + 2];
+  const double lim = 1.0e9;
+  int ix = (int)fmin(fmax(floor((xs - m.x0) / m.dx), -lim), lim);
+  int iy = (int)fmin(fmax(floor((ys - m.y0) / m.dy), -lim), lim);
+  IStation f;
+  f.ex = (float)(((xs - m.x0) - (ix + 0.5) * m.dx) / L0);
+  f.ey = (float)(((ys - m.y0) - (iy + 0.5) * m.dy) / L0);
+  f.zs = (float)(zs / L0);
+  f.r = res ? (float)res[s] : 0.f;
+  sf[s] = f;
+  si[s] = make_int2(ix, iy);
+}
+
+// per column: (rho, depth/L0, thickness/L0, 0)
+__global__ void iface_col_prep(IMeshDesc m, double L0, const double* __restrict__ depth,
+                               const double* __restrict__ rho, float4* __restrict__ cf) {
+  long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (c >= (long long)m.nx * m.ny) return;
+  double d = depth[c];
+  double thick = (-d - m.zb) / L0;
+  cf[c] = make_float4((float)rho[c], (float)(d / L0), (float)thick, 0.f);
+}
+
+__device__ __forceinline__ bool in_window(int ixs, int iys, int ix, int iy, const IConst& k) {
+  int cx = clampi(ixs, 0, k.nx - 1), cy = clampi(iys, 0, k.ny - 1);
+  return abs(ix - cx) <= k.w && abs(iy - cy) <= k.w;
+}
+
+// Unit column integral (normalised, without dx dy) and, if wanted, the unit
+// face integral, for one far pair.
+__device__ __forceinline__ float col_unit(float X2, float Y2, float rh, float ut, float th,
+                                          float Q2, float P4, float P2, const IConst& k) {
+  const float ub = ut + th;
+  const float rt2 = fmaf(ut, ut, rh), rb2 = fmaf(ub, ub, rh);
+  const float it = rsqrtf(rt2), ib = rsqrtf(rb2);
+  const float itb = it * ib;
+  const float L = th * (ut + ub) * itb * itb / (it + ib);
+  const float it2 = it * it, ib2 = ib * ib;
+  const float ct = it2 * it2 * it * fmaf(k.Q0, rt2, Q2) +
+                   (it2 * it2) * (it2 * it2) * it * fmaf(fmaf(k.P0, rt2, P2), rt2, P4);
+  const float cb = ib2 * ib2 * ib * fmaf(k.Q0, rb2, Q2) +
+                   (ib2 * ib2) * (ib2 * ib2) * ib * fmaf(fmaf(k.P0, rb2, P2), rb2, P4);
+  return L + (ct - cb);
+}
+
+__device__ __forceinline__ float face_unit_far(float X2, float Y2, float rh, float ut,
+                                               const FarCoef& f) {
+  const float Z2 = ut * ut;
+  const float rinv = rsqrtf(rh + Z2);
+  const float ri2 = rinv * rinv, ri4 = ri2 * ri2;
+  const float a0 = fmaf(X2, f.cA, Y2 * f.cB);
+  const float h1 = fmaf(X2, f.cX1, Y2 * f.cY1);
+  const float h0 = fmaf(X2, fmaf(X2, f.cXX, Y2 * f.cXY), Y2 * Y2 * f.cYY);
+  const float n2 = fmaf(f.a1, Z2, a0);
+  const float H = fmaf(fmaf(f.h2, Z2, h1), Z2, h0);
+  const float t = fmaf(H, ri4, n2) * ri4;
+  const float base = ut * rinv * ri2;
+  return fmaf(base, t, base);
+}
+
+// ---- forward, far (thread per station) ------------------------------------
+__global__ void __launch_bounds__(IF_TS)
+    iface_far_fwd(IConst k, int ns, const IStation* __restrict__ sf, const int2* __restrict__ si,
+                  const float4* __restrict__ cf, int chunk_len, double* __restrict__ partial) {
+  __shared__ float4 s_c[IF_TILE];
+  const int s = blockIdx.x * IF_TS + threadIdx.x;
+  const bool active = s < ns;
+  IStation st = {0.f, 0.f, 0.f, 0.f};
+  int2 hi = make_int2(0, 0);
+  if (active) {
+    st = sf[s];
+    hi = si[s];
+  }
+  const int c0 = blockIdx.y * chunk_len, c1 = min(k.ncols, c0 + chunk_len);
+  Kahan acc;
+  for (int t0 = c0; t0 < c1; t0 += IF_TILE) {
+    __syncthreads();
+    for (int q = threadIdx.x; q < IF_TILE; q += IF_TS)
+      s_c[q] = (t0 + q < c1) ? cf[t0 + q] : make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncthreads();
+    if (!active) continue;
+    const int cnt = min(IF_TILE, c1 - t0);
+    int ix = t0 % k.nx, iy = t0 / k.nx;
+    for (int q = 0; q < cnt; q++) {
+      const float4 col = s_c[q];
+      const float X = fmaf((float)(hi.x - ix), k.dxn, st.ex);
+      const float Y = fmaf((float)(hi.y - iy), k.dyn, st.ey);
+      const float X2 = X * X, Y2 = Y * Y, rh = X2 + Y2;
+      const float Q2 = fmaf(k.q2x, X2, k.q2y * Y2);
+      const float P4 = fmaf(k.p4x * X2, X2, fmaf(k.p4y * Y2, Y2, k.p4xy * X2 * Y2));
+      const float P2 = fmaf(k.p2x, X2, k.p2y * Y2);
+      const float v = col.x * col_unit(X2, Y2, rh, st.zs + col.y, col.z, Q2, P4, P2, k);
+      acc.add(in_window(hi.x, hi.y, ix, iy, k) ? 0.f : v);
+      if (++ix == k.nx) {
+        ix = 0;
+        ++iy;
+      }
+    }
+  }
+  if (active) partial[(size_t)blockIdx.y * ns + s] = acc.value();
+}
+
+// ---- forward, near window in double (warp per station) ---------------------
+__global__ void iface_near_fwd(IConst k, IMeshDesc m, int ns, const double* __restrict__ sxyz,
+                               const int2* __restrict__ si, const double* __restrict__ depth,
+                               const double* __restrict__ rho, double* __restrict__ out) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int s = blockIdx.x * IF_NEAR_WPB + warp;
+  if (s >= ns) return;
+  const int2 h = si[s];
+  const int cx = clampi(h.x, 0, k.nx - 1), cy = clampi(h.y, 0, k.ny - 1);
+  const int x0 = max(0, cx - k.w), x1 = min(k.nx - 1, cx + k.w);
+  const int y0 = max(0, cy - k.w), y1 = min(k.ny - 1, cy + k.w);
+  const int wx = x1 - x0 + 1, n = wx * (y1 - y0 + 1);
+  const double xs = sxyz[3 * s], ys = sxyz[3 * s + 1], zs = sxyz[3 * s + 2];
+  double acc = 0.0;
+  for (int q = lane; q < n; q += 32) {
+    const int ix = x0 + q % wx, iy = y0 + q / wx;
+    const long long c = ix + (long long)m.nx * iy;
+    const double r = rho[c];
+    if (r == 0.0) continue;
+    acc += r * ztm_prism_unit<double>((m.x0 + ix * m.dx) - xs, (m.x0 + (ix + 1) * m.dx) - xs,
+                                      (m.y0 + iy * m.dy) - ys, (m.y0 + (iy + 1) * m.dy) - ys,
+                                      m.zb - zs, -depth[c] - zs);
+  }
+  acc = warp_sum_d(acc);
+  if (lane == 0) out[s] = acc;
+}
+
+__global__ void iface_finalize(int ns, int nchunks, const double* __restrict__ partial,
+                               double far_scale, const double* __restrict__ near, double G5,
+                               double* __restrict__ gz) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= ns) return;
+  double f = 0.0;
+  for (int c = 0; c < nchunks; c++) f += partial[(size_t)c * ns + s];
+  double g = far_scale * f;
+  if (near) g += near[s];
+  gz[s] = G5 * g;
+}
+
+// ---- forward, plain double --------------------------------------------------
+__global__ void __launch_bounds__(64)
+    iface_f64_fwd(IMeshDesc m, int ns, const double* __restrict__ sxyz,
+                  const double* __restrict__ depth, const double* __restrict__ rho, int chunk_len,
+                  double* __restrict__ partial) {
+  const int s = blockIdx.x * 64 + threadIdx.x;
+  if (s >= ns) return;
+  const double xs = sxyz[3 * s], ys = sxyz[3 * s + 1], zs = sxyz[3 * s + 2];
+  const int nc = m.nx * m.ny;
+  const int c0 = blockIdx.y * chunk_len, c1 = min(nc, c0 + chunk_len);
+  double acc = 0.0;
+  for (int c = c0; c < c1; c++) {
+    const double r = rho[c];
+    if (r == 0.0) continue;
+    const int ix = c % m.nx, iy = c / m.nx;
+    acc += r * ztm_prism_unit<double>((m.x0 + ix * m.dx) - xs, (m.x0 + (ix + 1) * m.dx) - xs,
+                                      (m.y0 + iy * m.dy) - ys, (m.y0 + (iy + 1) * m.dy) - ys,
+                                      m.zb - zs, -depth[c] - zs);
+  }
+  partial[(size_t)blockIdx.y * ns + s] = acc;
+}
+
+// ---- adjoint, far (thread per column) --------------------------------------
+__global__ void __launch_bounds__(IF_TS)
+    iface_far_adj(IConst k, int ns, const IStation* __restrict__ sf, const int2* __restrict__ si,
+                  const float4* __restrict__ cf, double sc_rho, double sc_dep,
+                  double* __restrict__ g_rho, double* __restrict__ g_dep) {
+  __shared__ IStation s_f[IF_TILE];
+  __shared__ int2 s_i[IF_TILE];
+  const int c = blockIdx.x * IF_TS + threadIdx.x;
+  const bool active = c < k.ncols;
+  const int ix = active ? c % k.nx : 0, iy = active ? c / k.nx : 0;
+  const float4 col = active ? cf[c] : make_float4(0.f, 0.f, 0.f, 0.f);
+  Kahan ar, ad;
+  for (int t0 = 0; t0 < ns; t0 += IF_TILE) {
+    __syncthreads();
+    for (int q = threadIdx.x; q < IF_TILE; q += IF_TS) {
+      const bool ok = t0 + q < ns;
+      IStation z = {0.f, 0.f, 0.f, 0.f};
+      s_f[q] = ok ? sf[t0 + q] : z;
+      s_i[q] = ok ? si[t0 + q] : make_int2(0, 0);
+    }
+    __syncthreads();
+    if (!active) continue;
+    const int cnt = min(IF_TILE, ns - t0);
+    for (int q = 0; q < cnt; q++) {
+      const IStation st = s_f[q];
+      const int2 h = s_i[q];
+      const float X = fmaf((float)(h.x - ix), k.dxn, st.ex);
+      const float Y = fmaf((float)(h.y - iy), k.dyn, st.ey);
+      const float X2 = X * X, Y2 = Y * Y, rh = X2 + Y2;
+      const float Q2 = fmaf(k.q2x, X2, k.q2y * Y2);
+      const float P4 = fmaf(k.p4x * X2, X2, fmaf(k.p4y * Y2, Y2, k.p4xy * X2 * Y2));
+      const float P2 = fmaf(k.p2x, X2, k.p2y * Y2);
+      const float ut = st.zs + col.y;
+      const float u = col_unit(X2, Y2, rh, ut, col.z, Q2, P4, P2, k);
+      const float f = face_unit_far(X2, Y2, rh, ut, k.face);
+      const bool near = in_window(h.x, h.y, ix, iy, k);
+      ar.add(near ? 0.f : st.r * u);
+      ad.add(near ? 0.f : st.r * f);
+    }
+  }
+  if (!active) return;
+  if (g_rho) g_rho[c] = sc_rho * ar.value();
+  if (g_dep) g_dep[c] = -sc_dep * (double)col.x * ad.value();
+}
+
+// ---- adjoint, near window in double (warp per station, atomics) ------------
+__global__ void iface_near_adj(IConst k, IMeshDesc m, int ns, const double* __restrict__ sxyz,
+                               const int2* __restrict__ si, const double* __restrict__ depth,
+                               const double* __restrict__ rho, const double* __restrict__ res,
+                               double G5, double* __restrict__ g_rho,
+                               double* __restrict__ g_dep) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int s = blockIdx.x * IF_NEAR_WPB + warp;
+  if (s >= ns) return;
+  const double r = res[s];
+  if (r == 0.0) return;
+  const int2 h = si[s];
+  const int cx = clampi(h.x, 0, k.nx - 1), cy = clampi(h.y, 0, k.ny - 1);
+  const int x0 = max(0, cx - k.w), x1 = min(k.nx - 1, cx + k.w);
+  const int y0 = max(0, cy - k.w), y1 = min(k.ny - 1, cy + k.w);
+  const int wx = x1 - x0 + 1, n = wx * (y1 - y0 + 1);
+  const double xs = sxyz[3 * s], ys = sxyz[3 * s + 1], zs = sxyz[3 * s + 2];
+  for (int q = lane; q < n; q += 32) {
+    const int ix = x0 + q % wx, iy = y0 + q / wx;
+    const long long c = ix + (long long)m.nx * iy;
+    const double xa = (m.x0 + ix * m.dx) - xs, xb = (m.x0 + (ix + 1) * m.dx) - xs;
+    const double ya = (m.y0 + iy * m.dy) - ys, yb = (m.y0 + (iy + 1) * m.dy) - ys;
+    const double ztop = -depth[c];
+    if (g_rho) {
+      double u = ztm_prism_unit<double>(xa, xb, ya, yb, m.zb - zs, ztop - zs);
+      atomicAdd(&g_rho[c], G5 * r * u);
+    }
+    if (g_dep) {
+      double f = ztm_face_unit(xa, xb, ya, yb, zs - ztop);
+      atomicAdd(&g_dep[c], -G5 * rho[c] * r * f);
+    }
+  }
+}
+
+// ---- adjoint, plain double (thread per column, station chunks) --------------
+__global__ void __launch_bounds__(IF_TS)
+    iface_f64_adj(IMeshDesc m, int ns, const double* __restrict__ sxyz,
+                  const double* __restrict__ depth, const double* __restrict__ res, int chunk_len,
+                  double* __restrict__ pr, double* __restrict__ pd) {
+  const long long nc = (long long)m.nx * m.ny;
+  const long long c = blockIdx.x * (long long)IF_TS + threadIdx.x;
+  if (c >= nc) return;
+  const int ix = (int)(c % m.nx), iy = (int)(c / m.nx);
+  const double ztop = -depth[c];
+  const int s0 = blockIdx.y * chunk_len, s1 = min(ns, s0 + chunk_len);
+  double ar = 0.0, ad = 0.0;
+  for (int s = s0; s < s1; s++) {
+    const double r = res[s];
+    if (r == 0.0) continue;
+    const double xs = sxyz[3 * s], ys = sxyz[3 * s + 1], zs = sxyz[3 * s + 2];
+    const double xa = (m.x0 + ix * m.dx) - xs, xb = (m.x0 + (ix + 1) * m.dx) - xs;
+    const double ya = (m.y0 + iy * m.dy) - ys, yb = (m.y0 + (iy + 1) * m.dy) - ys;
+    if (pr) ar += r * ztm_prism_unit<double>(xa, xb, ya, yb, m.zb - zs, ztop - zs);
+    if (pd) ad += r * ztm_face_unit(xa, xb, ya, yb, zs - ztop);
+  }
+  if (pr) pr[(size_t)blockIdx.y * nc + c] = ar;
+  if (pd) pd[(size_t)blockIdx.y * nc + c] = ad;
+}
+
+__global__ void iface_f64_adj_finalize(long long nc, int nchunks, const double* __restrict__ pr,
+                                       const double* __restrict__ pd,
+                                       const double* __restrict__ rho, double G5,
+                                       double* __restrict__ g_rho, double* __restrict__ g_dep) {
+  long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  double a = 0.0, b = 0.0;
+  for (int k = 0; k < nchunks; k++) {
+    if (pr) a += pr[(size_t)k * nc + c];
+    if (pd) b += pd[(size_t)k * nc + c];
+  }
+  if (g_rho) g_rho[c] = G5 * a;
+  if (g_dep) g_dep[c] = -G5 * rho[c] * b;
+}
+
+// residual and misfit: r = gz - data, misfit = 0.5 * sum r^2 (one block,
+// fixed reduction order).
+__global__ void residual_kernel(int ns, const double* __restrict__ gz,
+                                const double* __restrict__ data, double* __restrict__ r,
+                                double* __restrict__ misfit) {
+  __shared__ double red[1024];
+  double a = 0.0;
+  for (int s = threadIdx.x; s < ns; s += blockDim.x) {
+    double v = gz[s] - data[s];
+    r[s] = v;
+    a += v * v;
+  }
+  red[threadIdx.x] = a;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *misfit = 0.5 * red[0];
+}
+
+int chunks_for(long long units, int tiles, int num_sms, int minlen, int* len) {
+  long long want = std::max(1LL, (8LL * std::max(num_sms, 1)) / std::max(tiles, 1));
+  long long ch = std::min<long long>(want, std::max(1LL, units / minlen));
+  ch = std::max(1LL, std::min(ch, 65535LL));
+  *len = (int)((units + ch - 1) / ch);
+  if (*len < 1) *len = 1;
+  return (int)((units + *len - 1) / *len);
+}
+
+}  // namespace
+
+size_t ztm_iface_ws(const IMeshDesc& m, int ns, int precision, int num_sms) {
+  long long nc = (long long)m.nx * m.ny;
+  int len;
+  int tiles = std::max(1, (ns + 63) / 64);
+  int ch = chunks_for(nc, tiles, num_sms, 64, &len);
+  int cha = chunks_for(std::max(ns, 1), (int)((nc + IF_TS - 1) / IF_TS), num_sms, 32, &len);
+  size_t w = WsCarver::need((size_t)ch * std::max(ns, 1) * 8) * 2;  // forward partials (x2 slack)
+  w += WsCarver::need((size_t)cha * nc * 8) * 2;                    // double adjoint partials
+  w += WsCarver::need((size_t)nc * 16) + WsCarver::need((size_t)std::max(ns, 1) * 16) +
+       WsCarver::need((size_t)std::max(ns, 1) * 8) * 4;
+  (void)precision;
+  return w;
+}
+
+static int iface_forward_impl(ztm_ctx* c, const IMeshDesc& m, const double* d_depth,
+                              const double* d_rho, int ns, const double* d_sxyz, double* d_gz,
+                              double G, int precision, const ztm_opts* o, WsCarver& wc) {
+  const double G5 = G * 1.0e5;
+  const long long nc = (long long)m.nx * m.ny;
+  if (precision == ZTM_PREC_FP64) {
+    int tiles = std::max(1, (ns + 63) / 64), len;
+    int ch = chunks_for(nc, tiles, c->num_sms, 64, &len);
+    double* partial = wc.take<double>((size_t)ch * ns);
+    iface_f64_fwd<<<dim3(tiles, ch), 64, 0, c->stream>>>(m, ns, d_sxyz, d_depth, d_rho, len,
+                                                         partial);
+    iface_finalize<<<(ns + 255) / 256, 256, 0, c->stream>>>(ns, ch, partial, 1.0, nullptr, G5,
+                                                            d_gz);
+    c->launches += 2;
+    return ztm_after_launch(c, "interface FP64 forward");
+  }
+  const double nq = (o && o->near_q > 0) ? o->near_q : 6.0;
+  IConst k = make_iconst(m, nq);
+  IStation* sf = wc.take<IStation>(ns);
+  int2* si = wc.take<int2>(ns);
+  float4* cf = wc.take<float4>(nc);
+  double* near = wc.take<double>(ns);
+  iface_station_prep<<<(ns + 127) / 128, 128, 0, c->stream>>>(m, k.L0, ns, d_sxyz, nullptr, sf,
+                                                              si);
+  iface_col_prep<<<(unsigned)((nc + 255) / 256), 256, 0, c->stream>>>(m, k.L0, d_depth, d_rho, cf);
+  iface_near_fwd<<<(ns + IF_NEAR_WPB - 1) / IF_NEAR_WPB, IF_NEAR_WPB * 32, 0, c->stream>>>(
+      k, m, ns, d_sxyz, si, d_depth, d_rho, near);
+  int tiles = std::max(1, (ns + IF_TS - 1) / IF_TS), len;
+  int ch = chunks_for(nc, tiles, c->num_sms, IF_TILE, &len);
+  double* partial = wc.take<double>((size_t)ch * ns);
+  iface_far_fwd<<<dim3(tiles, ch), IF_TS, 0, c->stream>>>(k, ns, sf, si, cf, len, partial);
+  iface_finalize<<<(ns + 255) / 256, 256, 0, c->stream>>>(ns, ch, partial,
+                                                          k.L0 * (double)k.dxn * k.dyn, near, G5,
+                                                          d_gz);
+  c->launches += 5;
+  return ztm_after_launch(c, "interface mixed forward");
+}
+
+int ztm_launch_iface_fwd(ztm_ctx* c, const IMeshDesc& m, const double* d_depth,
+                         const double* d_rho, int ns, const double* d_sxyz, double* d_gz,
+                         double G, int precision, const ztm_opts* o, WsCarver& wc) {
+  return iface_forward_impl(c, m, d_depth, d_rho, ns, d_sxyz, d_gz, G, precision, o, wc);
+}
+
+int ztm_launch_iface_adj(ztm_ctx* c, const IMeshDesc& m, const double* d_depth,
+                         const double* d_rho, int ns, const double* d_sxyz, const double* d_res,
+                         double* d_grho, double* d_gdep, double G, int precision,
+                         const ztm_opts* o, WsCarver& wc) {
+  const double G5 = G * 1.0e5;
+  const long long nc = (long long)m.nx * m.ny;
+  if (ns == 0) {
+    if (d_grho) cudaMemsetAsync(d_grho, 0, nc * 8, c->stream);
+    if (d_gdep) cudaMemsetAsync(d_gdep, 0, nc * 8, c->stream);
+    return ztm_after_launch(c, "interface adjoint (no stations)");
+  }
+  if (precision == ZTM_PREC_FP64) {
+    int len;
+    int ch = chunks_for(ns, (int)((nc + IF_TS - 1) / IF_TS), c->num_sms, 32, &len);
+    double* pr = d_grho ? wc.take<double>((size_t)ch * nc) : nullptr;
+    double* pd = d_gdep ? wc.take<double>((size_t)ch * nc) : nullptr;
+    iface_f64_adj<<<dim3((unsigned)((nc + IF_TS - 1) / IF_TS), ch), IF_TS, 0, c->stream>>>(
+        m, ns, d_sxyz, d_depth, d_res, len, pr, pd);
+    iface_f64_adj_finalize<<<(unsigned)((nc + 255) / 256), 256, 0, c->stream>>>(
+        nc, ch, pr, pd, d_rho, G5, d_grho, d_gdep);
+    c->launches += 2;
+    return ztm_after_launch(c, "interface FP64 adjoint");
+  }
+  const double nq = (o && o->near_q > 0) ? o->near_q : 6.0;
+  IConst k = make_iconst(m, nq);
+  IStation* sf = wc.take<IStation>(ns);
+  int2* si = wc.take<int2>(ns);
+  float4* cf = wc.take<float4>(nc);
+  iface_station_prep<<<(ns + 127) / 128, 128, 0, c->stream>>>(m, k.L0, ns, d_sxyz, d_res, sf, si);
+  iface_col_prep<<<(unsigned)((nc + 255) / 256), 256, 0, c->stream>>>(m, k.L0, d_depth, d_rho, cf);
+  // face integral is dimensionless: dx dy / L0^2 * (u / r^3 in 1/L0^2 units)
+  const double sc_rho = G5 * k.L0 * (double)k.dxn * k.dyn;
+  const double sc_dep = G5 * (double)k.dxn * k.dyn;
+  iface_far_adj<<<(unsigned)((nc + IF_TS - 1) / IF_TS), IF_TS, 0, c->stream>>>(
+      k, ns, sf, si, cf, sc_rho, sc_dep, d_grho, d_gdep);
+  iface_near_adj<<<(ns + IF_NEAR_WPB - 1) / IF_NEAR_WPB, IF_NEAR_WPB * 32, 0, c->stream>>>(
+      k, m, ns, d_sxyz, si, d_depth, d_rho, d_res, G5, d_grho, d_gdep);
+  c->launches += 4;
+  return ztm_after_launch(c, "interface mixed adjoint");
+}
+
+// ---------------------------------------------------------------------------
+// forward + misfit + adjoint (C ABI)
+extern "C" int ztm_gfm_interface_misfit(ztm_ctx* c, const ztm_imesh* mesh, const double* depth,
+                                        const double* rho_col, int ns, const double* sxyz,
+                                        const double* data, double* misfit, double* gz,
+                                        double* g_rho, double* g_depth, const ztm_opts* o) {
+  if (!c) return ZTM_ERR_ARG;
+  c->err.clear();
+  if (!mesh || !depth || !rho_col || !sxyz || !data || !misfit)
+    return ztm_fail(c, ZTM_ERR_ARG, "null argument");
+  if (mesh->nx < 1 || mesh->ny < 1 || !(mesh->dx > 0) || !(mesh->dy > 0))
+    return ztm_fail(c, ZTM_ERR_ARG, "bad interface mesh");
+  if (ns < 1) return ztm_fail(c, ZTM_ERR_ARG, "ns must be >= 1");
+  if (o && (o->precision < 0 || o->precision > 2 || (o->flags & ~ZTM_FLAG_DEVICE_PTRS)))
+    return ztm_fail(c, ZTM_ERR_ARG, "bad options");
+  const int prec = o ? o->precision : ZTM_PREC_FP64;
+  const bool dev = o && (o->flags & ZTM_FLAG_DEVICE_PTRS);
+  const double G = (o && o->G > 0) ? o->G : 6.67e-11;
+  IMeshDesc m;
+  m.nx = mesh->nx; m.ny = mesh->ny; m.x0 = mesh->x0; m.y0 = mesh->y0;
+  m.dx = mesh->dx; m.dy = mesh->dy; m.zb = mesh->z_base;
+  const long long nc = (long long)m.nx * m.ny;
+  int prev = -1;
+  cudaGetDevice(&prev);
+  if (prev != c->device) cudaSetDevice(c->device);
+  struct Restore {
+    int p, d;
+    ~Restore() {
+      if (p >= 0 && p != d) cudaSetDevice(p);
+    }
+  } restore{prev, c->device};
+  size_t need = 2 * WsCarver::need(nc * 8) + WsCarver::need((size_t)ns * 24) +
+                4 * WsCarver::need((size_t)ns * 8) + 2 * WsCarver::need(nc * 8) + 256 +
+                ztm_iface_ws(m, ns, prec, c->num_sms) + 4096;
+  int rc = ztm_ws_reserve(c, need);
+  if (rc) return rc;
+  WsCarver wc(c->ws);
+  double* s_dep = wc.take<double>(nc);
+  double* s_rho = wc.take<double>(nc);
+  double* s_xyz = wc.take<double>((size_t)ns * 3);
+  double* s_dat = wc.take<double>(ns);
+  double* s_gz = wc.take<double>(ns);
+  double* s_r = wc.take<double>(ns);
+  double* s_mis = wc.take<double>(1);
+  double* s_gr = wc.take<double>(nc);
+  double* s_gd = wc.take<double>(nc);
+  const void *pd, *pr, *px, *pdat;
+  if ((rc = ztm_stage_in(c, depth, nc * 8, dev, s_dep, &pd))) return rc;
+  if ((rc = ztm_stage_in(c, rho_col, nc * 8, dev, s_rho, &pr))) return rc;
+  if ((rc = ztm_stage_in(c, sxyz, (size_t)ns * 24, dev, s_xyz, &px))) return rc;
+  if ((rc = ztm_stage_in(c, data, (size_t)ns * 8, dev, s_dat, &pdat))) return rc;
+  double* ogz = (dev && gz) ? gz : s_gz;
+  rc = iface_forward_impl(c, m, (const double*)pd, (const double*)pr, ns, (const double*)px, ogz,
+                          G, prec, o, wc);
+  if (rc) return rc;
+  double* omis = dev ? misfit : s_mis;
+  residual_kernel<<<1, 1024, 0, c->stream>>>(ns, ogz, (const double*)pdat, s_r, omis);
+  c->launches++;
+  double* ogr = g_rho ? (dev ? g_rho : s_gr) : nullptr;
+  double* ogd = g_depth ? (dev ? g_depth : s_gd) : nullptr;
+  if (ogr || ogd) {
+    rc = ztm_launch_iface_adj(c, m, (const double*)pd, (const double*)pr, ns, (const double*)px,
+                              s_r, ogr, ogd, G, prec, o, wc);
+    if (rc) return rc;
+  }
+  if ((rc = ztm_cuda_check(c, cudaGetLastError(), "interface misfit kernels"))) return rc;
+  if (dev) return ZTM_OK;
+  cudaMemcpyAsync(misfit, s_mis, 8, cudaMemcpyDeviceToHost, c->stream);
+  if (gz) cudaMemcpyAsync(gz, s_gz, (size_t)ns * 8, cudaMemcpyDeviceToHost, c->stream);
+  if (g_rho) cudaMemcpyAsync(g_rho, s_gr, nc * 8, cudaMemcpyDeviceToHost, c->stream);
+  if (g_depth) cudaMemcpyAsync(g_depth, s_gd, nc * 8, cudaMemcpyDeviceToHost, c->stream);
+  if ((rc = ztm_cuda_check(c, cudaStreamSynchronize(c->stream), "interface misfit"))) return rc;
+  return ztm_check_device_error(c);
+}

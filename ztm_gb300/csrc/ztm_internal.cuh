@@ -36,8 +36,9 @@ struct ztm_ctx {
   size_t ws_size = 0;
   // device error word written by bounded waits / bounds checks
   int* d_err = nullptr;
-  // batched-launch graph cache
+  // batched-launch graph cache and the host copy of the last job table
   std::vector<ZtmGraphEntry> graphs;
+  std::vector<char> batch_table;
 };
 
 // ---------------------------------------------------------------------------

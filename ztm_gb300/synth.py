@@ -25,7 +25,7 @@ def gaussian_field(shape, spacing, corr, rng):
     k2 = sum(g * g for g in grids)
     sig = corr / 2.0
     f *= np.exp(-0.5 * k2 * sig * sig)
-    out = np.fft.irfftn(f, s=shape)
+    out = np.fft.irfftn(f, s=shape, axes=tuple(range(len(shape))))
     out -= out.mean()
     sd = out.std()
     return out / sd if sd > 0 else out
