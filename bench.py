@@ -1,0 +1,373 @@
+#!/usr/bin/env python
+"""Benchmark of the gravity forward path (prism model, mixed precision).
+
+Workload: the mixed-precision forward of a 256x256x64 prism mesh
+(1 x 1 x 0.5 km cells, seeded Gaussian density +- 300 kg/m^3 plus 20 box
+anomalies) at 128x128 stations draped on seeded fractal topography
+(0-3 km): 6.87e10 (station, prism) pairs per step.  A step is one full
+forward (all pairs) with the inputs resident in HBM.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Our arm prints value = pairs/s over all ranks (weak scaling: every rank
+runs the full workload; no collective on the data path), e2e = the same
+through the public API with pinned host buffers (H2D of density and
+stations and D2H of gz inside the timed region), the roofline of the
+dominant kernel against the measured FP32 FMA issue peak, and the CPU
+baseline (the double-precision oracle on the host cores, bounded sample).
+The reference arm times the reference's own gravity algorithm
+(TFM.cpp:95-99, point mass in double, restated in oracle/) on the host
+cores, on the same geometry, on a bounded station sample.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "prism·station gz evals/s and gradient evals/s; mixed vs FP64 at ≤1e-6 rel err"
+UNIT = "evals/s"
+WORKLOAD = ("mixed-precision prism forward, 256x256x64 prisms (1x1x0.5 km), 128x128 stations "
+            "draped on fractal topography 0-3 km")
+# executed float flops per (station, prism) pair in the far-field kernel
+# (FMA = 2): layer counter 1, Z 2, Z^2 1, r^2 1, rsqrt^2 1, ^4 1, t2 poly 2,
+# t4 poly 4, combine 3, base 3, final FMA 2, Kahan 4 -> 25 (+1 MUFU rsqrt)
+FLOPS_PER_PAIR = 25
+L2_BYTES = 129 * 2 ** 20
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")),
+            int(os.environ.get("WORLD_SIZE", "1")))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    def __init__(self, index):
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.proc = None
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax = float(p[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def read_traffic():
+    """DRAM bytes per far-kernel launch from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "prism_far_config2.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1])
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_baseline_prism(mesh, rho, st, nsample=48):
+    import numpy as np
+    import oracle
+    idx = np.linspace(0, len(st) - 1, nsample).astype(int)
+    t0 = time.perf_counter()
+    oracle.prism_mesh(mesh, rho, st[idx])
+    dt = time.perf_counter() - t0
+    pairs = nsample * mesh.nx * mesh.ny * mesh.nz
+    return {"value": pairs / dt, "unit": UNIT, "cores": oracle.NTHREADS, "kind": "port",
+            "sample": "%d of %d stations x all %d prisms, closed form in double (oracle/oracle.c)"
+                      % (nsample, len(st), mesh.nx * mesh.ny * mesh.nz), "seconds": dt}
+
+
+def pointmass_mapping(mesh, rho, st):
+    """Config-2 geometry on the reference's point-mass grid: node-centred
+    cells, h = 1 km horizontally, fv = 2 (0.5 km layers), g/cc, grid units;
+    the 66.7 constant assumes h = 10 km, so scale = h/10."""
+    import numpy as np
+    import ztm_gb300
+    nx, ny, nz = mesh.nx, mesh.ny, mesh.nz
+    kk = nz + 1 if nz % 2 == 0 else nz  # (dk-1)*fv+1 must hold every layer
+    dk = (kk - 1) // 2 + 1
+    g = ztm_gb300.make_grid(nx, ny, dk, 1, 2, 0, threshold=0.001, scale=mesh.dx / 10000.0)
+    drho = np.zeros(nx * ny * kk)
+    r = rho.reshape(nz, ny, nx) / 1000.0  # layer 0 on top -> highest k
+    for l in range(nz):
+        K = (kk - 1) - l - (kk - nz)
+        drho[K * nx * ny:(K + 1) * nx * ny] = r[l].ravel()
+    # node k (grid units of h) of the top layer centre: (kk-1-(kk-nz))/2
+    ktop = ((kk - 1) - (kk - nz)) / 2.0
+    surf = np.full(nx * ny, ktop + 0.25 + 1.0)
+    for x, y, z in st:
+        i, j = int(x // mesh.dx), int(y // mesh.dy)
+        surf[i + nx * j] = ktop + (z / 1000.0 + 0.25) / (mesh.dx / 1000.0)
+    return g, drho, surf
+
+
+def run_reference(args, rank):
+    """The reference's CPU algorithm (TFM.cpp:95-99) on the host cores."""
+    if rank != 0:
+        return 0
+    import numpy as np
+    import oracle
+    from ztm_gb300 import synth
+    mesh, rho, st = synth.config2()
+    g, drho, surf = pointmass_mapping(mesh, rho, st)
+    ns_sample = int(os.environ.get("ZTM_REF_SAMPLE", "128"))
+    nn = np.nonzero(np.abs(drho) > g.threshold)[0].astype(np.int32)
+    times = []
+    for it in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        oracle.pointmass_tfm_sample(g, drho, surf, 0, ns_sample, nn=nn)
+        dt = time.perf_counter() - t0
+        if it >= args.warmup:
+            times.append(dt)
+    pairs = ns_sample * nn.size
+    value = pairs * len(times) / sum(times)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_dict(args.gpus),
+            "algorithm": "point mass in double, TFM.cpp:95-99 (the reference's CPU gravity path), "
+                         "restated in oracle/oracle.c; same geometry as our arm, node-centred",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": oracle.NTHREADS, "kind": "port",
+                             "sample": "%d of %d stations x %d nodes per step"
+                                       % (ns_sample, mesh.nx * mesh.ny, nn.size)},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def config_dict(n):
+    return {"workload": WORKLOAD, "prisms": [256, 256, 64], "cell_m": [1000, 1000, 500],
+            "stations": [128, 128], "pairs_per_step": 256 * 256 * 64 * 128 * 128,
+            "precision": "mixed: far pairs float (4th-order expansion, Kahan), near box and "
+                         "per-station sums double", "near_q": 6,
+            "l2": "flushed between timed steps (256 MiB write)",
+            "parallelism": "replica per GPU" if n > 1 else "single GPU"}
+
+
+def run_ours(args, rank, local_rank, world):
+    import numpy as np
+    import torch
+    import ztm_gb300
+    from ztm_gb300 import synth
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    ctx = ztm_gb300.GravityContext(local_rank)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    mesh, rho, st = synth.config2()
+    np_ = mesh.nx * mesh.ny * mesh.nz
+    pairs = np_ * len(st)
+    d_rho = torch.tensor(rho, device="cuda")
+    d_st = torch.tensor(st, device="cuda")
+    flush = torch.empty(256 * 2 ** 20 // 4, dtype=torch.float32, device="cuda")
+
+    def step():
+        return ctx.prism(mesh, d_rho, d_st, precision="mixed")
+
+    for _ in range(args.warmup):
+        step()
+    ctx.sync()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    clocks = ClockSampler(local_rank) if rank == 0 else None
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = ctx.launches()
+    ctx.profile(True)
+    for i in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()  # L2 flush, outside the step's events
+        ev[i][0].record(stream)
+        out = step()
+        ev[i][1].record(stream)
+    ctx.sync()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop() if clocks else None
+    launches = ctx.launches() - launches0
+    far_ms, far_n = ctx.profile_read("prism_far")
+    near_ms, near_n = ctx.profile_read("prism_near")
+    ctx.profile(False)
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_s = sum(step_ms) / 1e3
+    if dist:
+        t = torch.tensor([total_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+    value = world * pairs * args.steps / total_s
+    ms_per_step = 1e3 * total_s / args.steps
+    gz = out.cpu().numpy()
+    if not np.all(np.isfinite(gz)):
+        raise RuntimeError("non-finite gz")
+
+    # end to end through the public API: pinned host buffers, H2D+D2H inside
+    h_rho = torch.empty(np_, dtype=torch.float64, pin_memory=True).numpy()
+    h_rho[:] = rho
+    h_st = torch.empty(st.size, dtype=torch.float64, pin_memory=True).numpy().reshape(-1, 3)
+    h_st[:] = st
+    e2e_steps = max(1, min(args.steps, 5))
+    ctx.prism(mesh, h_rho, h_st, precision="mixed")
+    e2e_t = []
+    for _ in range(e2e_steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        ctx.sync()
+        t0 = time.perf_counter()
+        g_host = ctx.prism(mesh, h_rho, h_st, precision="mixed")
+        e2e_t.append(time.perf_counter() - t0)
+    if dist:
+        t = torch.tensor([sum(e2e_t)], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_total = float(t.item())
+    else:
+        e2e_total = sum(e2e_t)
+    e2e = {"value": world * pairs * e2e_steps / e2e_total, "unit": UNIT,
+           "h2d_bytes_per_step": int(h_rho.nbytes + h_st.nbytes),
+           "d2h_bytes_per_step": int(g_host.nbytes)}
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return 0
+
+    peak32 = ctx.measure_peak("fp32")
+    far_avg = far_ms / max(far_n, 1)
+    achieved = FLOPS_PER_PAIR * pairs / (far_avg * 1e-3) / 1e12
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": config_dict(world), "clocks": clk, "e2e": e2e,
+            "gpu_launches": launches,
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak32,
+                         "unit": "TFLOP/s", "frac": achieved / peak32 if peak32 else None,
+                         "traffic": read_traffic(),
+                         "kernel": "prism far field (far_kernel)",
+                         "flops_per_pair": FLOPS_PER_PAIR, "pairs_per_launch": pairs,
+                         "kernel_ms": far_avg,
+                         "peak_source": "measured FP32 FMA issue rate on this GPU "
+                                        "(ztm_measure_peak; MEASURED_PEAKS.json has only HBM "
+                                        "and bf16 tensor peaks, neither bounds this kernel)"},
+            "kernels_ms": {"prism_far": far_avg, "prism_near": near_ms / max(near_n, 1),
+                           "step": ms_per_step}}
+    if not args.quick:
+        line.update(extras(ctx, mesh, rho, st, d_rho, d_st, gz))
+        if world == 1:
+            line["cpu_baseline"] = cpu_baseline_prism(mesh, rho, st)
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def extras(ctx, mesh, rho, st, d_rho, d_st, gz_mixed):
+    """Side measurements: plain FP64 kernel rate and the mixed error on a
+    station subset, gradient evals/s, and the reference GF kernel on the
+    same geometry."""
+    import numpy as np
+    import torch
+    import oracle
+    out = {}
+    np_ = mesh.nx * mesh.ny * mesh.nz
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    sub = np.arange(0, len(st), len(st) // 64)[:64]
+    ds = torch.tensor(st[sub], device="cuda")
+    ctx.prism(mesh, d_rho, ds, precision="fp64")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    ref = ctx.prism(mesh, d_rho, ds, precision="fp64")
+    e1.record(stream)
+    ctx.sync()
+    ms64 = e0.elapsed_time(e1)
+    r = ref.cpu().numpy()
+    m = gz_mixed[sub]
+    out["fp64_plain"] = {"value": np_ * len(sub) / (ms64 * 1e-3), "unit": UNIT,
+                         "sample": "%d stations x all prisms" % len(sub)}
+    out["accuracy"] = {"normwise_rel_err_vs_fp64": float(np.max(np.abs(m - r)) / np.max(np.abs(r))),
+                       "max_station_rel_err": float(np.max(np.abs(m - r) / np.abs(r))),
+                       "stations_checked": len(sub)}
+    # gradient evals/s: adjoint of the same forward (d misfit / d rho)
+    res = torch.tensor(np.random.default_rng(0).normal(0, 1, len(st)), device="cuda")
+    ctx.adjoint(mesh, d_st, res, precision="mixed")
+    e0.record(stream)
+    ctx.adjoint(mesh, d_st, res, precision="mixed")
+    e1.record(stream)
+    ctx.sync()
+    msa = e0.elapsed_time(e1)
+    out["gradient"] = {"value": np_ * len(st) / (msa * 1e-3), "unit": "gradient evals/s",
+                       "ms": msa, "what": "d misfit / d rho, all pairs, mixed"}
+    if oracle.ref_gf_available():
+        g, drho, surf = pointmass_mapping(mesh, rho, st)
+        gf, ms = oracle.ref_gf(g, drho.astype(np.float32), surf.astype(np.float32), reps=3)
+        nodes = int(np.count_nonzero(np.abs(drho.astype(np.float32)) > 0.001))
+        out["reference_gf_gpu"] = {
+            "value": nodes * mesh.nx * mesh.ny / (ms * 1e-3), "unit": "point-mass pairs/s",
+            "ms": ms, "what": "reference GF kernel (GFM_GPU.cu:16-22) compiled unchanged for "
+                              "sm_103a, same geometry on its grid (%d stations x %d nodes)"
+                              % (mesh.nx * mesh.ny, nodes)}
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--quick", action="store_true", help="skip side measurements")
+    args = ap.parse_args()
+    rank, local_rank, world = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, rank)
+    return run_ours(args, rank, local_rank, world)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

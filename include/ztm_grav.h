@@ -128,6 +128,22 @@ long long ztm_ctx_launches(const ztm_ctx* ctx);
  * made with ZTM_FLAG_DEVICE_PTRS (those calls return without waiting). */
 int ztm_ctx_sync(ztm_ctx* ctx);
 
+/* ---- tracing ----------------------------------------------------------- */
+/* While enabled, the context brackets each of its compute kernels with CUDA
+ * events on its stream.  ztm_ctx_profile_read waits for the stream, returns
+ * the summed device time (ms) and launch count of the kernels whose name
+ * contains `name` ("" = all), and clears the records.  Kernel names:
+ * pointmass, prism_far, prism_near, prism_f64, prism_list, adjoint_far,
+ * adjoint_near, adjoint_f64, iface_far, iface_near, iface_f64, batch.
+ * The reference's only timer is a host clock (zmath.cpp:265-268). */
+int ztm_ctx_profile(ztm_ctx* ctx, int enable);
+int ztm_ctx_profile_read(ztm_ctx* ctx, const char* name, double* ms,
+                         long long* count);
+/* Issue-rate micro-benchmarks of the device, the denominators of the
+ * compute roofline: kind 0 = FP32 FMA (TFLOP/s, 2 flops per FMA), 1 = FP64
+ * FMA (TFLOP/s), 2 = float rsqrt on the special-function unit (Gop/s). */
+int ztm_measure_peak(ztm_ctx* ctx, int kind, double* value);
+
 /* ---- point-mass mode (reference model) ------------------------------- */
 /* Replaces TFM.cpp:90-99 and GFM_GPU.cu:16-34.  drho has ii*jj*kk values
  * (g/cc), surf di*dj station heights (grid units), G receives di*dj values

@@ -33,6 +33,7 @@ def _load():
         I = ctypes.c_int
         L = ctypes.c_long
         lib.ora_pointmass_tfm.argtypes = [I, I, I, I, I, I, P, P, L, P, P, I]
+        lib.ora_pointmass_tfm_range.argtypes = [I, I, I, I, I, I, P, P, L, P, P, L, L, I]
         lib.ora_pointmass_gf.argtypes = [I, I, I, I, I, I, P, L, P, P]
         lib.ora_phi.argtypes = [D, D, D]
         lib.ora_phi.restype = D
@@ -79,6 +80,22 @@ def pointmass_tfm(grid, drho, surf, nn=None, nthreads=None):
     lib.ora_pointmass_tfm(grid.di, grid.dj, grid.dk, grid.fh, grid.fv, grid.bfr, _p(drho), _p(nn),
                           nn.size, _p(surf), _p(G), nthreads or NTHREADS)
     return G * grid.scale if grid.scale != 1.0 else G
+
+
+def pointmass_tfm_sample(grid, drho, surf, s_lo, s_hi, nn=None, nthreads=None):
+    """TFM.cpp:95-99 for interior stations s_lo..s_hi only (a bounded
+    sample for timing).  Returns G (di*dj) with the sampled entries set."""
+    lib = _load()
+    drho = _f64(drho)
+    surf = _f64(surf)
+    if nn is None:
+        nn = np.nonzero(np.abs(drho) > grid.threshold)[0]
+    nn = np.ascontiguousarray(nn, dtype=np.int32)
+    G = np.zeros(grid.di * grid.dj)
+    lib.ora_pointmass_tfm_range(grid.di, grid.dj, grid.dk, grid.fh, grid.fv, grid.bfr, _p(drho),
+                                _p(nn), nn.size, _p(surf), _p(G), s_lo, s_hi,
+                                nthreads or NTHREADS)
+    return G, nn.size
 
 
 def pointmass_gf(grid, rho32, s32, nthreads_total=None):

@@ -7,7 +7,11 @@
  *   ora_pointmass_tfm  restates the CPU gravity lambda of TFM.cpp:95-99 with
  *                      its index maps (TFM.cpp:85,97), its bfr interior
  *                      (TFM.cpp:96,99), pow(.,1.5) in double, summation in
- *                      nn order and the per-term division by fh*fh*fv.
+ *                      nn order and the per-term division by fh*fh*fv.  The
+ *                      reference gives each station row a thread; here the
+ *                      threads split the stations evenly (same arithmetic per
+ *                      station), so that a bounded sample of stations still
+ *                      uses every core.
  *   ora_pointmass_gf   restates the GF kernel of GFM_GPU.cu:16-22 in float,
  *                      with the kernel's own index math (ii=di*fh, :17) and a
  *                      sequential (thread-order) summation in place of the
@@ -83,7 +87,8 @@ static void parallel_for(long n, int nthreads, range_fn fn, void* arg) {
 /* ---------------------------------------------------------------------- */
 /* point-mass model                                                        */
 typedef struct {
-  int di, dj, dk, fh, fv, bfr, ii, jj;
+  int di, dj, dk, fh, fv, bfr, ii, jj, ni;
+  long s_lo;
   const double* drho;
   const int* nn;
   long n_nn;
@@ -91,41 +96,52 @@ typedef struct {
   double* G;
 } pm_args;
 
-/* One station row j0, as one std::thread of TFM.cpp:95-99 does. */
-static void pm_rows(long lo, long hi, void* p) {
+/* Interior stations s_lo+lo .. s_lo+hi (row-major over (i0, j0)); each
+ * station is the body of the GFM lambda of TFM.cpp:96-98 for one i0. */
+static void pm_stations(long lo, long hi, void* p) {
   pm_args* a = (pm_args*)p;
   const int fh = a->fh, fv = a->fv, ii = a->ii, jj = a->jj;
-  for (long jr = lo; jr < hi; jr++) {
-    int j0 = (int)jr + a->bfr;
-    for (int i0 = a->bfr; i0 < a->di - a->bfr; i0 += 1) {
-      int m = i0 + j0 * a->di;
-      double k0 = a->surf[m];
-      double g = 0;
-      for (long t = 0; t < a->n_nn; t++) {
-        int n = a->nn[t];
-        double i = (n % ii) / (1. * fh), j = ((n / ii) % jj) / (1. * fh),
-               k = (n / (ii * jj)) / (1. * fv);
-        g += (66.7 * a->drho[n] * (k0 - k) /
-              pow((i0 - i) * (i0 - i) + (j0 - j) * (j0 - j) + (k0 - k) * (k0 - k),
-                  1.5)) /
-             (fh * fh * fv);
-      }
-      a->G[m] = g;
+  for (long t = lo; t < hi; t++) {
+    long sidx = a->s_lo + t;
+    int i0 = a->bfr + (int)(sidx % a->ni), j0 = a->bfr + (int)(sidx / a->ni);
+    int m = i0 + j0 * a->di;
+    double k0 = a->surf[m];
+    double g = 0;
+    for (long q = 0; q < a->n_nn; q++) {
+      int n = a->nn[q];
+      double i = (n % ii) / (1. * fh), j = ((n / ii) % jj) / (1. * fh),
+             k = (n / (ii * jj)) / (1. * fv);
+      g += (66.7 * a->drho[n] * (k0 - k) /
+            pow((i0 - i) * (i0 - i) + (j0 - j) * (j0 - j) + (k0 - k) * (k0 - k), 1.5)) /
+           (fh * fh * fv);
     }
+    a->G[m] = g;
   }
+}
+
+void ora_pointmass_tfm_range(int di, int dj, int dk, int fh, int fv, int bfr,
+                             const double* drho, const int* nn, long n_nn,
+                             const double* surf, double* G, long s_lo, long s_hi,
+                             int nthreads) {
+  pm_args a;
+  a.di = di; a.dj = dj; a.dk = dk; a.fh = fh; a.fv = fv; a.bfr = bfr;
+  a.ii = (di - 1) * fh + 1;
+  a.jj = (dj - 1) * fh + 1;
+  a.ni = di - 2 * bfr;
+  a.drho = drho; a.nn = nn; a.n_nn = n_nn; a.surf = surf; a.G = G;
+  long ns = (long)(di - 2 * bfr) * (dj - 2 * bfr);
+  if (di - 2 * bfr <= 0 || dj - 2 * bfr <= 0) return;
+  if (s_hi < 0 || s_hi > ns) s_hi = ns;
+  if (s_lo < 0) s_lo = 0;
+  if (s_hi <= s_lo) return;
+  a.s_lo = s_lo;
+  parallel_for(s_hi - s_lo, nthreads, pm_stations, &a);
 }
 
 void ora_pointmass_tfm(int di, int dj, int dk, int fh, int fv, int bfr,
                        const double* drho, const int* nn, long n_nn,
                        const double* surf, double* G, int nthreads) {
-  pm_args a;
-  a.di = di; a.dj = dj; a.dk = dk; a.fh = fh; a.fv = fv; a.bfr = bfr;
-  a.ii = (di - 1) * fh + 1;
-  a.jj = (dj - 1) * fh + 1;
-  a.drho = drho; a.nn = nn; a.n_nn = n_nn; a.surf = surf; a.G = G;
-  long rows = dj - 2 * bfr;
-  if (rows <= 0) return;
-  parallel_for(rows, nthreads, pm_rows, &a);
+  ora_pointmass_tfm_range(di, dj, dk, fh, fv, bfr, drho, nn, n_nn, surf, G, 0, -1, nthreads);
 }
 
 void ora_pointmass_gf(int bfr, int di, int dj, int dk, int fh, int fv,

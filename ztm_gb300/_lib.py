@@ -29,7 +29,7 @@ EXPORTS = (
     "ztm_ctx_set_stream", "ztm_ctx_stream", "ztm_ctx_launches", "ztm_ctx_sync",
     "ztm_gfm_pointmass", "ztm_gfm_prism", "ztm_gfm_prism_list", "ztm_gfm_adjoint",
     "ztm_gfm_interface", "ztm_gfm_interface_adjoint", "ztm_gfm_interface_misfit",
-    "ztm_gfm_batch",
+    "ztm_gfm_batch", "ztm_ctx_profile", "ztm_ctx_profile_read", "ztm_measure_peak",
 )
 
 
@@ -87,6 +87,10 @@ _SIGS = {
     "ztm_gfm_interface_misfit": (_I, [_P, ctypes.POINTER(IMesh), _P, _P, _I, _P, _P, _P, _P,
                                       _P, _P, ctypes.POINTER(Opts)]),
     "ztm_gfm_batch": (_I, [_P, ctypes.POINTER(Job), _I, ctypes.POINTER(Opts)]),
+    "ztm_ctx_profile": (_I, [_P, _I]),
+    "ztm_ctx_profile_read": (_I, [_P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double),
+                                  ctypes.POINTER(_LL)]),
+    "ztm_measure_peak": (_I, [_P, _I, ctypes.POINTER(ctypes.c_double)]),
 }
 
 _lib = None

@@ -253,7 +253,10 @@ int ztm_launch_adjoint(ztm_ctx* c, const MeshDesc& m, int ns, const double* d_sx
     int ch = adj_f64_chunks(np, ns, c->num_sms, &len);
     double* partial = wc.take<double>((size_t)ch * np);
     dim3 grid((unsigned)((np + ADJ_TS - 1) / ADJ_TS), ch);
-    adj_f64_kernel<<<grid, ADJ_TS, 0, c->stream>>>(m, ns, d_sxyz, d_res, len, partial);
+    {
+      ZtmProf prof_(c, "adjoint_f64");
+      adj_f64_kernel<<<grid, ADJ_TS, 0, c->stream>>>(m, ns, d_sxyz, d_res, len, partial);
+    }
     adj_f64_finalize<<<(unsigned)((np + 255) / 256), 256, 0, c->stream>>>(np, ch, partial, G5, d_g);
     c->launches += 2;
     return ztm_after_launch(c, "adjoint FP64 kernels");
@@ -266,8 +269,11 @@ int ztm_launch_adjoint(ztm_ctx* c, const MeshDesc& m, int ns, const double* d_sx
   const int ngroups = (k.nz + ADJ_LG - 1) / ADJ_LG;
   const long long threads = (long long)k.ncols * ngroups;
   const double scale = G5 * k.L0 * (double)k.dxn * k.dyn * k.dzn;
-  adj_far_kernel<<<(unsigned)((threads + ADJ_TS - 1) / ADJ_TS), ADJ_TS, 0, c->stream>>>(
-      k, ns, sf, si, d_res, scale, d_g);
+  {
+    ZtmProf prof_(c, "adjoint_far");
+    adj_far_kernel<<<(unsigned)((threads + ADJ_TS - 1) / ADJ_TS), ADJ_TS, 0, c->stream>>>(
+        k, ns, sf, si, d_res, scale, d_g);
+  }
   c->launches++;
   const int cap = near_cap(k);
   const bool f64 = precision == ZTM_PREC_MIXED;
@@ -279,13 +285,19 @@ int ztm_launch_adjoint(ztm_ctx* c, const MeshDesc& m, int ns, const double* d_sx
   if (f64) {
     cudaFuncSetAttribute(adj_near_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)std::max<size_t>(smem, 48 * 1024));
-    adj_near_kernel<double><<<(ns + wpb - 1) / wpb, wpb * 32, smem, c->stream>>>(
-        k, m, ns, d_sxyz, si, d_res, G5, cap, d_g);
+    {
+      ZtmProf prof_(c, "adjoint_near");
+      adj_near_kernel<double><<<(ns + wpb - 1) / wpb, wpb * 32, smem, c->stream>>>(
+          k, m, ns, d_sxyz, si, d_res, G5, cap, d_g);
+    }
   } else {
     cudaFuncSetAttribute(adj_near_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)std::max<size_t>(smem, 48 * 1024));
-    adj_near_kernel<float><<<(ns + wpb - 1) / wpb, wpb * 32, smem, c->stream>>>(
-        k, m, ns, d_sxyz, si, d_res, G5, cap, d_g);
+    {
+      ZtmProf prof_(c, "adjoint_near");
+      adj_near_kernel<float><<<(ns + wpb - 1) / wpb, wpb * 32, smem, c->stream>>>(
+          k, m, ns, d_sxyz, si, d_res, G5, cap, d_g);
+    }
   }
   c->launches++;
   return ztm_after_launch(c, "adjoint mixed kernels");

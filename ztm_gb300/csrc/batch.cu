@@ -502,8 +502,11 @@ extern "C" int ztm_gfm_batch(ztm_ctx* c, const ztm_job* jobs, int njobs, const z
     c->graphs.push_back(e);
     entry = &c->graphs.back();
   }
-  if ((rc = ztm_cuda_check(c, cudaGraphLaunch(entry->exec, c->stream), "launch batch graph")))
-    return rc;
+  {
+    ZtmProf prof_(c, "batch");
+    rc = ztm_cuda_check(c, cudaGraphLaunch(entry->exec, c->stream), "launch batch graph");
+  }
+  if (rc) return rc;
   c->launches += 1 + 2LL * njobs;
   if (dev) return ZTM_OK;
   for (int j = 0; j < njobs; j++) {

@@ -421,8 +421,11 @@ static int iface_forward_impl(ztm_ctx* c, const IMeshDesc& m, const double* d_de
     int tiles = std::max(1, (ns + 63) / 64), len;
     int ch = chunks_for(nc, tiles, c->num_sms, 64, &len);
     double* partial = wc.take<double>((size_t)ch * ns);
-    iface_f64_fwd<<<dim3(tiles, ch), 64, 0, c->stream>>>(m, ns, d_sxyz, d_depth, d_rho, len,
-                                                         partial);
+    {
+      ZtmProf prof_(c, "iface_f64");
+      iface_f64_fwd<<<dim3(tiles, ch), 64, 0, c->stream>>>(m, ns, d_sxyz, d_depth, d_rho, len,
+                                                           partial);
+    }
     iface_finalize<<<(ns + 255) / 256, 256, 0, c->stream>>>(ns, ch, partial, 1.0, nullptr, G5,
                                                             d_gz);
     c->launches += 2;
@@ -437,12 +440,18 @@ static int iface_forward_impl(ztm_ctx* c, const IMeshDesc& m, const double* d_de
   iface_station_prep<<<(ns + 127) / 128, 128, 0, c->stream>>>(m, k.L0, ns, d_sxyz, nullptr, sf,
                                                               si);
   iface_col_prep<<<(unsigned)((nc + 255) / 256), 256, 0, c->stream>>>(m, k.L0, d_depth, d_rho, cf);
-  iface_near_fwd<<<(ns + IF_NEAR_WPB - 1) / IF_NEAR_WPB, IF_NEAR_WPB * 32, 0, c->stream>>>(
-      k, m, ns, d_sxyz, si, d_depth, d_rho, near);
+  {
+    ZtmProf prof_(c, "iface_near");
+    iface_near_fwd<<<(ns + IF_NEAR_WPB - 1) / IF_NEAR_WPB, IF_NEAR_WPB * 32, 0, c->stream>>>(
+        k, m, ns, d_sxyz, si, d_depth, d_rho, near);
+  }
   int tiles = std::max(1, (ns + IF_TS - 1) / IF_TS), len;
   int ch = chunks_for(nc, tiles, c->num_sms, IF_TILE, &len);
   double* partial = wc.take<double>((size_t)ch * ns);
-  iface_far_fwd<<<dim3(tiles, ch), IF_TS, 0, c->stream>>>(k, ns, sf, si, cf, len, partial);
+  {
+    ZtmProf prof_(c, "iface_far");
+    iface_far_fwd<<<dim3(tiles, ch), IF_TS, 0, c->stream>>>(k, ns, sf, si, cf, len, partial);
+  }
   iface_finalize<<<(ns + 255) / 256, 256, 0, c->stream>>>(ns, ch, partial,
                                                           k.L0 * (double)k.dxn * k.dyn, near, G5,
                                                           d_gz);
@@ -472,8 +481,11 @@ int ztm_launch_iface_adj(ztm_ctx* c, const IMeshDesc& m, const double* d_depth,
     int ch = chunks_for(ns, (int)((nc + IF_TS - 1) / IF_TS), c->num_sms, 32, &len);
     double* pr = d_grho ? wc.take<double>((size_t)ch * nc) : nullptr;
     double* pd = d_gdep ? wc.take<double>((size_t)ch * nc) : nullptr;
-    iface_f64_adj<<<dim3((unsigned)((nc + IF_TS - 1) / IF_TS), ch), IF_TS, 0, c->stream>>>(
-        m, ns, d_sxyz, d_depth, d_res, len, pr, pd);
+    {
+      ZtmProf prof_(c, "iface_f64");
+      iface_f64_adj<<<dim3((unsigned)((nc + IF_TS - 1) / IF_TS), ch), IF_TS, 0, c->stream>>>(
+          m, ns, d_sxyz, d_depth, d_res, len, pr, pd);
+    }
     iface_f64_adj_finalize<<<(unsigned)((nc + 255) / 256), 256, 0, c->stream>>>(
         nc, ch, pr, pd, d_rho, G5, d_grho, d_gdep);
     c->launches += 2;
@@ -489,10 +501,16 @@ int ztm_launch_iface_adj(ztm_ctx* c, const IMeshDesc& m, const double* d_depth,
   // face integral is dimensionless: dx dy / L0^2 * (u / r^3 in 1/L0^2 units)
   const double sc_rho = G5 * k.L0 * (double)k.dxn * k.dyn;
   const double sc_dep = G5 * (double)k.dxn * k.dyn;
-  iface_far_adj<<<(unsigned)((nc + IF_TS - 1) / IF_TS), IF_TS, 0, c->stream>>>(
-      k, ns, sf, si, cf, sc_rho, sc_dep, d_grho, d_gdep);
-  iface_near_adj<<<(ns + IF_NEAR_WPB - 1) / IF_NEAR_WPB, IF_NEAR_WPB * 32, 0, c->stream>>>(
-      k, m, ns, d_sxyz, si, d_depth, d_rho, d_res, G5, d_grho, d_gdep);
+  {
+    ZtmProf prof_(c, "iface_far");
+    iface_far_adj<<<(unsigned)((nc + IF_TS - 1) / IF_TS), IF_TS, 0, c->stream>>>(
+        k, ns, sf, si, cf, sc_rho, sc_dep, d_grho, d_gdep);
+  }
+  {
+    ZtmProf prof_(c, "iface_near");
+    iface_near_adj<<<(ns + IF_NEAR_WPB - 1) / IF_NEAR_WPB, IF_NEAR_WPB * 32, 0, c->stream>>>(
+        k, m, ns, d_sxyz, si, d_depth, d_rho, d_res, G5, d_grho, d_gdep);
+  }
   c->launches += 4;
   return ztm_after_launch(c, "interface mixed adjoint");
 }

@@ -167,9 +167,15 @@ int ztm_launch_pointmass(ztm_ctx* c, const PmParams& p, const double* d_drho,
   if (p.ns > 0 && p.nnodes > 0) {
     dim3 grid(tiles, chunks);
     if (precision == ZTM_PREC_FP64)
-      pm_gather_kernel<true><<<grid, PM_TS, 0, c->stream>>>(p, d_drho, d_nn, d_surf, len, partial, c->d_err);
+      {
+        ZtmProf prof_(c, "pointmass");
+        pm_gather_kernel<true><<<grid, PM_TS, 0, c->stream>>>(p, d_drho, d_nn, d_surf, len, partial, c->d_err);
+      }
     else
-      pm_gather_kernel<false><<<grid, PM_TS, 0, c->stream>>>(p, d_drho, d_nn, d_surf, len, partial, c->d_err);
+      {
+        ZtmProf prof_(c, "pointmass");
+        pm_gather_kernel<false><<<grid, PM_TS, 0, c->stream>>>(p, d_drho, d_nn, d_surf, len, partial, c->d_err);
+      }
     c->launches++;
   } else {
     chunks = 0;

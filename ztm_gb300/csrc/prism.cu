@@ -470,9 +470,15 @@ void launch_mesh_near(ztm_ctx* c, const MeshConst& k, const MeshDesc& m, int ns,
   if (ns <= 0) return;
   int blocks = (ns + NEAR_WPB - 1) / NEAR_WPB;
   if (f64)
-    near_kernel<double><<<blocks, NEAR_WPB * 32, 0, c->stream>>>(k, m, ns, sxyz, si, rho, out);
+    {
+      ZtmProf prof_(c, "prism_near");
+      near_kernel<double><<<blocks, NEAR_WPB * 32, 0, c->stream>>>(k, m, ns, sxyz, si, rho, out);
+    }
   else
-    near_kernel<float><<<blocks, NEAR_WPB * 32, 0, c->stream>>>(k, m, ns, sxyz, si, rho, out);
+    {
+      ZtmProf prof_(c, "prism_near");
+      near_kernel<float><<<blocks, NEAR_WPB * 32, 0, c->stream>>>(k, m, ns, sxyz, si, rho, out);
+    }
   c->launches++;
 }
 
@@ -499,8 +505,11 @@ int ztm_launch_prism(ztm_ctx* c, const MeshDesc& m, const double* d_rho, int ns,
     int tiles = std::max(1, (ns + F64_TS - 1) / F64_TS);
     long long ch = f64_chunks(np, tiles, c->num_sms, &len);
     double* partial = wc.take<double>((size_t)ch * ns);
-    mesh_f64_kernel<<<dim3(tiles, (unsigned)ch), F64_TS, 0, c->stream>>>(m, ns, d_sxyz, d_rho, len,
-                                                                         partial);
+    {
+      ZtmProf prof_(c, "prism_f64");
+      mesh_f64_kernel<<<dim3(tiles, (unsigned)ch), F64_TS, 0, c->stream>>>(m, ns, d_sxyz, d_rho, len,
+                                                                           partial);
+    }
     finalize_kernel<<<(ns + 255) / 256, 256, 0, c->stream>>>(ns, (int)ch, partial, 1.0, nullptr,
                                                              G5, d_gz);
     c->launches += 2;
@@ -521,7 +530,10 @@ int ztm_launch_prism(ztm_ctx* c, const MeshDesc& m, const double* d_rho, int ns,
   a.k = k; a.ns = ns; a.chunk_cols = f.chunk_cols; a.sc = f.sc;
   a.sf = sf; a.si = si; a.rhoT = rhoT; a.partial = partial; a.err = c->d_err;
   cudaFuncSetAttribute(far_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-  far_kernel<<<dim3(f.tiles, f.chunks), FAR_TS, f.smem, c->stream>>>(a);
+  {
+    ZtmProf prof_(c, "prism_far");
+    far_kernel<<<dim3(f.tiles, f.chunks), FAR_TS, f.smem, c->stream>>>(a);
+  }
   const double far_scale = k.L0 * (double)k.dxn * k.dyn * k.dzn;
   finalize_kernel<<<(ns + 255) / 256, 256, 0, c->stream>>>(ns, f.chunks, partial, far_scale, near,
                                                            G5, d_gz);
@@ -557,11 +569,17 @@ int ztm_launch_prism_list(ztm_ctx* c, long long np, const double* d_geom, const 
     dim3 grid(tiles, (unsigned)ch);
     int method = precision == ZTM_PREC_FP64 ? 0 : 1;
     if (precision == ZTM_PREC_FP32)
-      list_kernel<false><<<grid, F64_TS, 0, c->stream>>>(np, d_geom, d_rho, lp, ns, d_sxyz, len,
-                                                         method, partial);
+      {
+        ZtmProf prof_(c, "prism_list");
+        list_kernel<false><<<grid, F64_TS, 0, c->stream>>>(np, d_geom, d_rho, lp, ns, d_sxyz, len,
+                                                           method, partial);
+      }
     else
-      list_kernel<true><<<grid, F64_TS, 0, c->stream>>>(np, d_geom, d_rho, lp, ns, d_sxyz, len,
-                                                        method, partial);
+      {
+        ZtmProf prof_(c, "prism_list");
+        list_kernel<true><<<grid, F64_TS, 0, c->stream>>>(np, d_geom, d_rho, lp, ns, d_sxyz, len,
+                                                          method, partial);
+      }
     c->launches++;
   } else {
     ch = 0;

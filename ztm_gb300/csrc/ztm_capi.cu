@@ -225,6 +225,11 @@ void ztm_ctx_destroy(ztm_ctx* c) {
     if (e.exec) cudaGraphExecDestroy(e.exec);
     if (e.graph) cudaGraphDestroy(e.graph);
   }
+  for (auto& r : c->prof_recs) {
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  for (auto e : c->prof_pool) cudaEventDestroy(e);
   if (c->ws) cudaFree(c->ws);
   if (c->d_err) cudaFree(c->d_err);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);

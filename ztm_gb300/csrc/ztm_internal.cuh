@@ -24,6 +24,11 @@ struct ZtmGraphEntry {
   cudaGraphExec_t exec = nullptr;
 };
 
+struct ZtmProfRec {
+  const char* name;
+  cudaEvent_t a, b;
+};
+
 struct ztm_ctx {
   int device = 0;
   int num_sms = 0;
@@ -39,6 +44,18 @@ struct ztm_ctx {
   // batched-launch graph cache and the host copy of the last job table
   std::vector<ZtmGraphEntry> graphs;
   std::vector<char> batch_table;
+  // tracing: events around compute kernels while enabled
+  bool prof = false;
+  std::vector<ZtmProfRec> prof_recs;
+  std::vector<cudaEvent_t> prof_pool;
+};
+
+// Brackets one kernel launch with events when tracing is enabled.
+struct ZtmProf {
+  ztm_ctx* c;
+  cudaEvent_t b = nullptr;
+  ZtmProf(ztm_ctx* ctx, const char* name);
+  ~ZtmProf();
 };
 
 // ---------------------------------------------------------------------------

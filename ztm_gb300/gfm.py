@@ -149,6 +149,27 @@ class GravityContext:
     def sync(self):
         self._check(self._lib.ztm_ctx_sync(self._h))
 
+    # -- tracing ----------------------------------------------------------
+    def profile(self, enable=True):
+        """Bracket the context's compute kernels with CUDA events."""
+        self._check(self._lib.ztm_ctx_profile(self._h, 1 if enable else 0))
+
+    def profile_read(self, name=""):
+        """(total device ms, launches) of traced kernels matching `name`;
+        clears the records."""
+        ms = ctypes.c_double(0.0)
+        n = ctypes.c_longlong(0)
+        self._check(self._lib.ztm_ctx_profile_read(self._h, name.encode(), ctypes.byref(ms),
+                                                   ctypes.byref(n)))
+        return ms.value, n.value
+
+    def measure_peak(self, kind):
+        """kind 'fp32' / 'fp64' (TFLOP/s of FMA) or 'rsqrt' (Gop/s)."""
+        k = {"fp32": 0, "fp64": 1, "rsqrt": 2}[kind]
+        v = ctypes.c_double(0.0)
+        self._check(self._lib.ztm_measure_peak(self._h, k, ctypes.byref(v)))
+        return v.value
+
     # -- point mass (TFM.cpp:90-99) -------------------------------------
     def pointmass(self, grid, drho, surf, nn=None, precision="fp64"):
         """G (di*dj, mGal) from drho (ii*jj*kk, g/cc) and surf (di*dj)."""
