@@ -200,6 +200,20 @@ int ztm_gfm_interface_misfit(ztm_ctx* ctx, const ztm_imesh* mesh,
                              double* misfit, double* gz, double* g_rho,
                              double* g_depth, const ztm_opts* opt);
 
+/* Nonlinear inversion of the column tops: minimises
+ *   0.5*|gz(depth) - data|^2 + 0.5*lambda*sum_neighbours (m_i - m_j)^2,
+ * m = depth in km, by L-BFGS with an Armijo line search, one forward and one
+ * adjoint (ztm_gfm_interface_misfit) per evaluation.  depth (m) is the
+ * start model on entry and the result on return.  history (iterations+1
+ * values, may be NULL) receives the data misfit 0.5*|r|^2 before each
+ * iteration and at the end; *n_done the iterations taken.  Host arrays
+ * only.  Replaces the damped Gauss-Newton loop of LMA::fit (TFM.cpp:155-167)
+ * for the gravity interface, whose Jacobian came from finite differences. */
+int ztm_invert_interface(ztm_ctx* ctx, const ztm_imesh* mesh, double* depth,
+                         const double* rho_col, int ns, const double* sxyz,
+                         const double* data, double lambda, int iterations,
+                         const ztm_opts* opt, double* history, int* n_done);
+
 /* ---- batched ----------------------------------------------------------- */
 /* Evaluates every job (trial models of a line search, independent regional
  * meshes of uneven size) in one persistent launch, replayed from a CUDA

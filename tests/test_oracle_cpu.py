@@ -21,8 +21,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 # ---- point-mass model (TFM.cpp:95-99, GFM_GPU.cu:16-22) --------------------
 # The reference GF kernel accumulates in float without compensation, in the
 # order its atomics land; with mixed-sign densities the sums cancel, so its
-# outputs carry ~1e-4 normwise error.  TOL_GF bounds that.
-TOL_GF = 1e-3
+# outputs carry up to ~1e-5 normwise error (measured 1e-6..1e-5 on the
+# golden cases).  TOL_GF bounds that.
+TOL_GF = 5e-5
 
 
 def test_tfm_and_gf_restatements_agree():

@@ -79,7 +79,7 @@ def test_reference_gf_kernel_agrees(ctx):
     drho, surf = tfm_like_inputs(61, 61, 33, seed=8)
     ref = oracle.pointmass_tfm(g, drho, surf)
     gf, _ = oracle.ref_gf(g, drho.astype(np.float32), surf.astype(np.float32))
-    # the reference accumulates in float in atomic order: ~1e-4 normwise
-    assert rel_err(gf, ref) <= 1e-3
+    # the reference accumulates in float in atomic order: ~1e-5 normwise
+    assert rel_err(gf, ref) <= 5e-5
     ours = ctx.pointmass(g, drho, surf, precision="fp32")
     assert rel_err(ours, ref) <= TOL32

@@ -19,7 +19,7 @@ NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
                      "-Xcompiler", "-ffp-contract=off"]
 
 SOURCES = ["ztm_capi.cu", "pointmass.cu", "prism.cu", "adjoint.cu", "iface.cu", "batch.cu", "trace.cu"]
-HOST_SOURCES = []
+HOST_SOURCES = ["invert.cpp"]
 
 
 def _nvcc():
@@ -57,7 +57,8 @@ def build(verbose=False, force=False):
         op = os.path.join(OBJDIR, src.rsplit(".", 1)[0] + ".o")
         objs.append(op)
         if force or _stale(op, [sp] + headers):
-            jobs.append([nvcc] + NVCC_FLAGS + ["-c", sp, "-o", op])
+            flags = NVCC_FLAGS + (["-I" + os.path.join(ROOT, "include")] if src.endswith(".cpp") else [])
+            jobs.append([nvcc] + flags + ["-c", sp, "-o", op])
     if jobs:
         with ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
             for out in ex.map(_run, jobs):

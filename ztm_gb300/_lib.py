@@ -30,6 +30,7 @@ EXPORTS = (
     "ztm_gfm_pointmass", "ztm_gfm_prism", "ztm_gfm_prism_list", "ztm_gfm_adjoint",
     "ztm_gfm_interface", "ztm_gfm_interface_adjoint", "ztm_gfm_interface_misfit",
     "ztm_gfm_batch", "ztm_ctx_profile", "ztm_ctx_profile_read", "ztm_measure_peak",
+    "ztm_invert_interface",
 )
 
 
@@ -91,6 +92,8 @@ _SIGS = {
     "ztm_ctx_profile_read": (_I, [_P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double),
                                   ctypes.POINTER(_LL)]),
     "ztm_measure_peak": (_I, [_P, _I, ctypes.POINTER(ctypes.c_double)]),
+    "ztm_invert_interface": (_I, [_P, ctypes.POINTER(IMesh), _P, _P, _I, _P, _P, ctypes.c_double, _I,
+                                  ctypes.POINTER(Opts), _P, ctypes.POINTER(_I)]),
 }
 
 _lib = None

@@ -32,19 +32,6 @@ constexpr int ADJ_TS = 128;
 constexpr int ADJ_LG = 8;      // layers per thread in the far kernel
 constexpr int ADJ_STILE = 256; // stations per shared-memory tile
 
-__device__ __forceinline__ float far_pair_unit(float w, float Z, float rh, float a0, float h0,
-                                               float h1, const FarCoef& f) {
-  const float Z2 = Z * Z;
-  const float rinv = rsqrtf(rh + Z2);
-  const float ri2 = rinv * rinv;
-  const float ri4 = ri2 * ri2;
-  const float n2 = fmaf(f.a1, Z2, a0);
-  const float H = fmaf(fmaf(f.h2, Z2, h1), Z2, h0);
-  const float t = fmaf(H, ri4, n2) * ri4;
-  const float base = Z * rinv * ri2 * w;
-  return fmaf(base, t, base);
-}
-
 // grid.x covers ncols * ceil(nz/LG) threads.  g[p] = G5*L0*Vn * sum.
 __global__ void __launch_bounds__(ADJ_TS)
     adj_far_kernel(MeshConst k, int ns, const float4* __restrict__ sf,
@@ -88,21 +75,24 @@ __global__ void __launch_bounds__(ADJ_TS)
       const float w = s_r[q];
       const float X = fmaf((float)(i.x - ix), k.dxn, f.x);
       const float Y = fmaf((float)(i.y - iy), k.dyn, f.y);
-      const float X2 = X * X, Y2 = Y * Y, rh = X2 + Y2;
-      const float a0 = fmaf(X2, fc.cA, Y2 * fc.cB);
-      const float h1 = fmaf(X2, fc.cX1, Y2 * fc.cY1);
-      const float h0 = fmaf(X2, fmaf(X2, fc.cXX, Y2 * fc.cXY), Y2 * Y2 * fc.cYY);
+      const ColPoly cp = col_poly(X, Y, fc);
       const NearBox b = near_box(i, k);
       const bool ncl = ix >= b.x0 && ix <= b.x1 && iy >= b.y0 && iy <= b.y1;
       const int elo = ncl ? b.l0 : k.nz;
       const unsigned espan = ncl ? (unsigned)(b.l1 - b.l0) : 0u;
+      const float Zg = fmaf((float)(l0 - i.z), k.dzn, f.z);
+      if (ncl || l0 + ADJ_LG > k.nz) {
 #pragma unroll
-      for (int j = 0; j < ADJ_LG; j++) {
-        const int l = l0 + j;
-        const float Z = fmaf((float)(l - i.z), k.dzn, f.z);
-        const float v = far_pair_unit(w, Z, rh, a0, h0, h1, fc);
-        const bool excl = ((unsigned)(l - elo) <= espan) || l >= k.nz;
-        acc[j].add(excl ? 0.f : v);
+        for (int j = 0; j < ADJ_LG; j++) {
+          const int l = l0 + j;
+          const float v = far_unit(fmaf((float)j, k.dzn, Zg), cp, fc.a1);
+          const bool excl = ((unsigned)(l - elo) <= espan) || l >= k.nz;
+          acc[j].add(w * (excl ? 0.f : v));
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < ADJ_LG; j++)
+          acc[j].add(w * far_unit(fmaf((float)j, k.dzn, Zg), cp, fc.a1));
       }
     }
   }

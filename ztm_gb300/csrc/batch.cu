@@ -59,19 +59,6 @@ struct BArgs {
   int* err;
 };
 
-__device__ __forceinline__ float unit_pair(float Z, float rh, float a0, float h0, float h1,
-                                           const FarCoef& f) {
-  const float Z2 = Z * Z;
-  const float rinv = rsqrtf(rh + Z2);
-  const float ri2 = rinv * rinv;
-  const float ri4 = ri2 * ri2;
-  const float n2 = fmaf(f.a1, Z2, a0);
-  const float H = fmaf(fmaf(f.h2, Z2, h1), Z2, h0);
-  const float t = fmaf(H, ri4, n2) * ri4;
-  const float base = Z * rinv * ri2;
-  return fmaf(base, t, base);
-}
-
 // tile completion: the last item of a tile writes gz for its stations
 __device__ void tile_done(const BJob& J, int tile, int expected, int* s_flag) {
   __threadfence();
@@ -231,18 +218,15 @@ __global__ void __launch_bounds__(B_TS) batch_kernel(BArgs a) {
         for (int q = 0; q < ncol; q++) {
           const float X = fmaf((float)(ixs - ix), k.dxn, ex);
           const float Y = fmaf((float)(iys - iy), k.dyn, ey);
-          const float X2 = X * X, Y2 = Y * Y, rh = X2 + Y2;
-          const float a0 = fmaf(X2, fc.cA, Y2 * fc.cB);
-          const float h1 = fmaf(X2, fc.cX1, Y2 * fc.cY1);
-          const float h0 = fmaf(X2, fmaf(X2, fc.cXX, Y2 * fc.cXY), Y2 * Y2 * fc.cYY);
+          const ColPoly cp = col_poly(X, Y, fc);
           const bool ncl = ix >= nb.x0 && ix <= nb.x1 && iy >= nb.y0 && iy <= nb.y1;
           const int elo = ncl ? nb.l0 : k.nz;
           const unsigned espan = ncl ? (unsigned)(nb.l1 - nb.l0) : 0u;
           const float* col = rs + q * k.nzp;
           const int mstride = J.sc * k.nzp;
-          float zf = (float)(-izs);
-          for (int l = 0; l < k.nz; l++, zf += 1.f) {
-            float K = unit_pair(fmaf(zf, k.dzn, ez), rh, a0, h0, h1, fc);
+          const float zb = fmaf((float)(-izs), k.dzn, ez);
+          for (int l = 0; l < k.nz; l++) {
+            float K = far_unit(fmaf((float)l, k.dzn, zb), cp, fc.a1);
             if (l < Lm && (unsigned)(l - elo) <= espan) K = 0.f;
 #pragma unroll
             for (int md = 0; md < B_MG; md++)

@@ -211,24 +211,31 @@ __global__ void __launch_bounds__(FAR_TS) far_kernel(FarArgs a) {
       for (int q = 0; q < ncol; q++) {
         const float X = fmaf((float)(ixs - ix), k.dxn, ex);
         const float Y = fmaf((float)(iys - iy), k.dyn, ey);
-        const float X2 = X * X, Y2 = Y * Y, rh = X2 + Y2;
-        const float a0 = fmaf(X2, fc.cA, Y2 * fc.cB);
-        const float h1 = fmaf(X2, fc.cX1, Y2 * fc.cY1);
-        const float h0 = fmaf(X2, fmaf(X2, fc.cXX, Y2 * fc.cXY), Y2 * Y2 * fc.cYY);
+        const ColPoly cp = col_poly(X, Y, fc);
         const bool ncl = ix >= nb.x0 && ix <= nb.x1 && iy >= nb.y0 && iy <= nb.y1;
         const int elo = ncl ? nb.l0 : k.nz;
         const unsigned espan = ncl ? (unsigned)(nb.l1 - nb.l0) : 0u;
         const float* col = rs + q * k.nzp;
-        float zf = (float)(-izs);  // Z(l) = (l - izs) dz + ez
-        int l = 0;
-        for (; l < Lm; l++, zf += 1.f) {
-          const float v = far_pair(col[l], fmaf(zf, k.dzn, ez), rh, a0, h0, h1, fc);
-          const bool excl = (unsigned)(l - elo) <= espan;
-          acc.add(excl ? 0.f : v);  // select: a NaN at a box prism is dropped
+        for (int l0 = 0; l0 < k.nz; l0 += 4) {
+          const float4 r4 = *reinterpret_cast<const float4*>(col + l0);
+          const float Zg = fmaf((float)(l0 - izs), k.dzn, ez);  // Z(l) = (l - izs) dz + ez
+          const float rr[4] = {r4.x, r4.y, r4.z, r4.w};
+          float g = 0.f;
+          if (l0 < Lm || l0 + 4 > k.nz) {  // uniform: near-box layers or the ragged last group
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+              const int l = l0 + j;
+              const float v = far_unit(fmaf((float)j, k.dzn, Zg), cp, fc.a1);
+              const bool excl = ((unsigned)(l - elo) <= espan) || l >= k.nz;
+              g = fmaf(rr[j], excl ? 0.f : v, g);  // select first: a NaN is dropped
+            }
+          } else {
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+              g = fmaf(rr[j], far_unit(fmaf((float)j, k.dzn, Zg), cp, fc.a1), g);
+          }
+          acc.add(g);
         }
-#pragma unroll 4
-        for (; l < k.nz; l++, zf += 1.f)
-          acc.add(far_pair(col[l], fmaf(zf, k.dzn, ez), rh, a0, h0, h1, fc));
         if (++ix == k.nx) {
           ix = 0;
           ++iy;
@@ -408,7 +415,8 @@ FarShape far_shape(const MeshConst& k, int ns, int num_sms, const ztm_opts* o) {
   int sc = std::max(1, (24 * 1024) / (k.nzp * 4));
   sc = std::min(sc, 64);
   f.sc = sc;
-  int want_blocks = 8 * std::max(num_sms, 1);
+  // one full wave: 12 blocks of 4 warps per SM at <= 40 registers
+  int want_blocks = 12 * std::max(num_sms, 1);
   int chunks = std::max(1, want_blocks / f.tiles);
   if (o && o->chunk > 0) chunks = std::max(1, (k.ncols + o->chunk - 1) / o->chunk);
   chunks = std::min(chunks, std::max(1, k.ncols / sc));
@@ -466,18 +474,19 @@ void launch_mesh_transpose(ztm_ctx* c, const MeshConst& k, int nmodels, const do
 
 void launch_mesh_near(ztm_ctx* c, const MeshConst& k, const MeshDesc& m, int ns,
                       const double* sxyz, const int4* si, const double* rho, double* out,
-                      bool f64) {
+                      bool f64, cudaStream_t stream) {
   if (ns <= 0) return;
+  if (!stream) stream = c->stream;
   int blocks = (ns + NEAR_WPB - 1) / NEAR_WPB;
   if (f64)
     {
-      ZtmProf prof_(c, "prism_near");
-      near_kernel<double><<<blocks, NEAR_WPB * 32, 0, c->stream>>>(k, m, ns, sxyz, si, rho, out);
+      ZtmProf prof_(c, "prism_near", stream);
+      near_kernel<double><<<blocks, NEAR_WPB * 32, 0, stream>>>(k, m, ns, sxyz, si, rho, out);
     }
   else
     {
-      ZtmProf prof_(c, "prism_near");
-      near_kernel<float><<<blocks, NEAR_WPB * 32, 0, c->stream>>>(k, m, ns, sxyz, si, rho, out);
+      ZtmProf prof_(c, "prism_near", stream);
+      near_kernel<float><<<blocks, NEAR_WPB * 32, 0, stream>>>(k, m, ns, sxyz, si, rho, out);
     }
   c->launches++;
 }
@@ -525,7 +534,10 @@ int ztm_launch_prism(ztm_ctx* c, const MeshDesc& m, const double* d_rho, int ns,
   double* partial = wc.take<double>((size_t)f.chunks * ns);
   launch_mesh_transpose(c, k, 1, d_rho, rhoT);
   launch_mesh_station_prep(c, m, k.L0, ns, d_sxyz, sf, si);
-  launch_mesh_near(c, k, m, ns, d_sxyz, si, d_rho, near, precision == ZTM_PREC_MIXED);
+  // the double near box runs on the side stream, concurrently with the float
+  // far field (different pipes: FP64 vs FMA/MUFU)
+  ztm_fork(c);
+  launch_mesh_near(c, k, m, ns, d_sxyz, si, d_rho, near, precision == ZTM_PREC_MIXED, c->aux);
   FarArgs a;
   a.k = k; a.ns = ns; a.chunk_cols = f.chunk_cols; a.sc = f.sc;
   a.sf = sf; a.si = si; a.rhoT = rhoT; a.partial = partial; a.err = c->d_err;
@@ -534,6 +546,7 @@ int ztm_launch_prism(ztm_ctx* c, const MeshDesc& m, const double* d_rho, int ns,
     ZtmProf prof_(c, "prism_far");
     far_kernel<<<dim3(f.tiles, f.chunks), FAR_TS, f.smem, c->stream>>>(a);
   }
+  ztm_join(c);
   const double far_scale = k.L0 * (double)k.dxn * k.dyn * k.dzn;
   finalize_kernel<<<(ns + 255) / 256, 256, 0, c->stream>>>(ns, f.chunks, partial, far_scale, near,
                                                            G5, d_gz);

@@ -38,6 +38,40 @@ __host__ __device__ inline FarCoef far_coef(double dx, double dy, double dz) {
   return f;
 }
 
+// Per-(station, column) coefficients of the far-field correction written
+// as a polynomial in u = 1/r^2: substituting Z^2 = r^2 - rh (rh = X^2+Y^2)
+// into t2 + t4 gives
+//   1 + t2 + t4 = 1 + u (a1 + u (C2 + u (C3 + u C4))),
+//   C2 = a0 - a1 rh + h2,  C3 = h1 - 2 h2 rh,  C4 = h0 - h1 rh + h2 rh^2,
+// so a pair costs one rsqrt and a 4-term Horner chain, with no Z^2 terms.
+struct ColPoly {
+  float rh, C2, C3, C4;
+};
+
+__device__ __forceinline__ ColPoly col_poly(float X, float Y, const FarCoef& f) {
+  const float X2 = X * X, Y2 = Y * Y, rh = X2 + Y2;
+  const float a0 = fmaf(X2, f.cA, Y2 * f.cB);
+  const float h1 = fmaf(X2, f.cX1, Y2 * f.cY1);
+  const float h0 = fmaf(X2, fmaf(X2, f.cXX, Y2 * f.cXY), Y2 * Y2 * f.cYY);
+  ColPoly c;
+  c.rh = rh;
+  c.C2 = fmaf(-f.a1, rh, a0) + f.h2;
+  c.C3 = fmaf(-2.f * f.h2, rh, h1);
+  c.C4 = fmaf(fmaf(f.h2, rh, -h1), rh, h0);
+  return c;
+}
+
+// Z/r^3 * (1 + t2 + t4) for one pair (unit density, normalised units).
+__device__ __forceinline__ float far_unit(float Z, const ColPoly& c, float a1) {
+  const float rinv = rsqrtf(fmaf(Z, Z, c.rh));
+  const float u = rinv * rinv;
+  float p = fmaf(c.C4, u, c.C3);
+  p = fmaf(p, u, c.C2);
+  p = fmaf(p, u, a1);
+  const float s = fmaf(p, u, 1.f);
+  return (Z * s) * (rinv * u);
+}
+
 // Regular-mesh constants for the mixed kernels.
 struct MeshConst {
   int nx, ny, nz, nzp;  // nzp: layers padded to a multiple of 4
@@ -103,4 +137,4 @@ void launch_mesh_transpose(ztm_ctx* c, const MeshConst& k, int nmodels, const do
 // One warp per station.  out[s] = that sum (metres x density, without G).
 void launch_mesh_near(ztm_ctx* c, const MeshConst& k, const MeshDesc& m, int ns,
                       const double* sxyz, const int4* si, const double* rho, double* out,
-                      bool f64);
+                      bool f64, cudaStream_t stream = nullptr);

@@ -4,6 +4,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <vector>
 
 #include "ztm_internal.cuh"
 
@@ -18,22 +19,23 @@ static cudaEvent_t prof_event(ztm_ctx* c) {
   return e;
 }
 
-ZtmProf::ZtmProf(ztm_ctx* ctx, const char* name) : c(ctx) {
+ZtmProf::ZtmProf(ztm_ctx* ctx, const char* name, cudaStream_t stream)
+    : c(ctx), s(stream ? stream : ctx->stream) {
   if (!c->prof) return;
   cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
-  cudaStreamIsCapturing(c->stream, &st);
+  cudaStreamIsCapturing(s, &st);
   if (st != cudaStreamCaptureStatusNone) return;  // no events inside a graph capture
   ZtmProfRec r;
   r.name = name;
   r.a = prof_event(c);
   r.b = prof_event(c);
-  cudaEventRecord(r.a, c->stream);
+  cudaEventRecord(r.a, s);
   b = r.b;
   c->prof_recs.push_back(r);
 }
 
 ZtmProf::~ZtmProf() {
-  if (b) cudaEventRecord(b, c->stream);
+  if (b) cudaEventRecord(b, s);
 }
 
 namespace {
@@ -84,20 +86,23 @@ extern "C" int ztm_ctx_profile_read(ztm_ctx* c, const char* name, double* ms, lo
   int rc = ztm_cuda_check(c, cudaStreamSynchronize(c->stream), "profile read");
   double tot = 0.0;
   long long n = 0;
+  std::vector<ZtmProfRec> keep;
   for (auto& r : c->prof_recs) {
-    if (!rc && (!name || !*name || strstr(r.name, name))) {
+    if (!name || !*name || strstr(r.name, name)) {
       float t = 0.f;
-      if (cudaEventElapsedTime(&t, r.a, r.b) == cudaSuccess) {
+      if (!rc && cudaEventElapsedTime(&t, r.a, r.b) == cudaSuccess) {
         tot += t;
         n++;
       } else {
         cudaGetLastError();
       }
+      c->prof_pool.push_back(r.a);
+      c->prof_pool.push_back(r.b);
+    } else {
+      keep.push_back(r);
     }
-    c->prof_pool.push_back(r.a);
-    c->prof_pool.push_back(r.b);
   }
-  c->prof_recs.clear();
+  c->prof_recs.swap(keep);
   *ms = tot;
   *count = n;
   if (prev >= 0 && prev != c->device) cudaSetDevice(prev);

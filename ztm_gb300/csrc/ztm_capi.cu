@@ -149,6 +149,16 @@ int ztm_ws_reserve(ztm_ctx* c, size_t bytes) {
   return ZTM_OK;
 }
 
+void ztm_fork(ztm_ctx* c) {
+  cudaEventRecord(c->ev_fork, c->stream);
+  cudaStreamWaitEvent(c->aux, c->ev_fork, 0);
+}
+
+void ztm_join(ztm_ctx* c) {
+  cudaEventRecord(c->ev_join, c->aux);
+  cudaStreamWaitEvent(c->stream, c->ev_join, 0);
+}
+
 int ztm_after_launch(ztm_ctx* c, const char* what) {
   return ztm_cuda_check(c, cudaGetLastError(), what);
 }
@@ -204,10 +214,16 @@ int ztm_ctx_create(int device, ztm_ctx** out) {
   if (cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device) !=
           cudaSuccess ||
       cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
       cudaMalloc((void**)&c->d_err, sizeof(int)) != cudaSuccess ||
       cudaMemset(c->d_err, 0, sizeof(int)) != cudaSuccess) {
     cudaGetLastError();
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
+    if (c->aux) cudaStreamDestroy(c->aux);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
     if (c->d_err) cudaFree(c->d_err);
     delete c;
     return ZTM_ERR_CUDA;
@@ -232,6 +248,12 @@ void ztm_ctx_destroy(ztm_ctx* c) {
   for (auto e : c->prof_pool) cudaEventDestroy(e);
   if (c->ws) cudaFree(c->ws);
   if (c->d_err) cudaFree(c->d_err);
+  if (c->aux) {
+    cudaStreamSynchronize(c->aux);
+    cudaStreamDestroy(c->aux);
+  }
+  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+  if (c->ev_join) cudaEventDestroy(c->ev_join);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;
 }

@@ -34,6 +34,8 @@ struct ztm_ctx {
   int num_sms = 0;
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
+  cudaStream_t aux = nullptr;  // side stream for concurrent kernels
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   std::string err;
   long long launches = 0;
   // grow-only device workspace; carved per call
@@ -53,10 +55,17 @@ struct ztm_ctx {
 // Brackets one kernel launch with events when tracing is enabled.
 struct ZtmProf {
   ztm_ctx* c;
+  cudaStream_t s;
   cudaEvent_t b = nullptr;
-  ZtmProf(ztm_ctx* ctx, const char* name);
+  ZtmProf(ztm_ctx* ctx, const char* name, cudaStream_t stream = nullptr);
   ~ZtmProf();
 };
+
+// Fork/join of the context's side stream: work launched on c->aux between
+// ztm_fork and ztm_join runs concurrently with the main stream's work and is
+// ordered before everything the main stream does after the join.
+void ztm_fork(ztm_ctx* c);
+void ztm_join(ztm_ctx* c);
 
 // ---------------------------------------------------------------------------
 // host helpers

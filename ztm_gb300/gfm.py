@@ -284,6 +284,31 @@ class GravityContext:
         misfit = mt if a.device else mis.value
         return misfit, gz, g_rho, g_dep
 
+    def invert_interface(self, imesh, depth0, rho_col, stations, data, lam=1e-2, iterations=20,
+                         precision="mixed", G=None, near_q=None):
+        """L-BFGS inversion of the column tops (host arrays).  Returns
+        (depth, data-misfit history, iterations taken)."""
+        nc = imesh.nx * imesh.ny
+        ns = _nstations(stations)
+        a = _Args()
+        depth = np.array(depth0, dtype=np.float64, copy=True)
+        if depth.size != nc:
+            raise ValueError("depth0 has %d values, expected %d" % (depth.size, nc))
+        pd = depth.ctypes.data_as(ctypes.c_void_p)
+        pr = a.arr(rho_col, nc, name="rho_col")
+        px = a.arr(stations, 3 * ns, name="stations")
+        pdat = a.arr(data, ns, name="data")
+        if a.device:
+            raise ValueError("invert_interface takes host arrays")
+        hist = np.zeros(iterations + 1)
+        done = ctypes.c_int(0)
+        o = _opts(precision, 0, G, near_q)
+        self._check(self._lib.ztm_invert_interface(self._h, ctypes.byref(imesh), pd, pr, ns, px, pdat,
+                                                   float(lam), int(iterations), ctypes.byref(o),
+                                                   hist.ctypes.data_as(ctypes.c_void_p),
+                                                   ctypes.byref(done)))
+        return depth, hist[:done.value + 1], done.value
+
     # -- batched ----------------------------------------------------------
     def batch(self, jobs, precision="mixed", G=None, near_q=None):
         """jobs: list of (mesh, rho[nmodels, nprisms], stations[ns, 3]).
