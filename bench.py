@@ -36,9 +36,10 @@ UNIT = "evals/s"
 WORKLOAD = ("mixed-precision prism forward, 256x256x64 prisms (1x1x0.5 km), 128x128 stations "
             "draped on fractal topography 0-3 km")
 # executed float flops per (station, prism) pair in the far-field kernel
-# (FMA = 2): layer counter 1, Z 2, Z^2 1, r^2 1, rsqrt^2 1, ^4 1, t2 poly 2,
-# t4 poly 4, combine 3, base 3, final FMA 2, Kahan 4 -> 25 (+1 MUFU rsqrt)
-FLOPS_PER_PAIR = 25
+# (FMA = 2; the rsqrt on the special-function unit is not counted): Z 2,
+# r^2 2, 1/r^2 1, Horner in 1/r^2 8, Z*s 1, 1/r^3 1, product 1, density FMA 2,
+# and per 8-layer group 7 (group Z, layer counter, Kahan add) -> 19
+FLOPS_PER_PAIR = 19
 L2_BYTES = 129 * 2 ** 20
 
 

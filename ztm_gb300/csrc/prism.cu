@@ -146,7 +146,7 @@ __device__ __forceinline__ float far_pair(float rho, float Z, float rh, float a0
   return fmaf(base, t, base);
 }
 
-__global__ void __launch_bounds__(FAR_TS) far_kernel(FarArgs a) {
+__global__ void __launch_bounds__(FAR_TS, 12) far_kernel(FarArgs a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
   float* stage = reinterpret_cast<float*>(smem_raw + 128);
@@ -216,14 +216,16 @@ __global__ void __launch_bounds__(FAR_TS) far_kernel(FarArgs a) {
         const int elo = ncl ? nb.l0 : k.nz;
         const unsigned espan = ncl ? (unsigned)(nb.l1 - nb.l0) : 0u;
         const float* col = rs + q * k.nzp;
-        for (int l0 = 0; l0 < k.nz; l0 += 4) {
-          const float4 r4 = *reinterpret_cast<const float4*>(col + l0);
-          const float Zg = fmaf((float)(l0 - izs), k.dzn, ez);  // Z(l) = (l - izs) dz + ez
-          const float rr[4] = {r4.x, r4.y, r4.z, r4.w};
+        float zf = (float)(-izs);  // (l0 - izs), exact in float, stepped by 8
+        for (int l0 = 0; l0 < k.nz; l0 += 8, zf += 8.f) {
+          const float4 ra = *reinterpret_cast<const float4*>(col + l0);
+          const float4 rb = *reinterpret_cast<const float4*>(col + l0 + 4);
+          const float rr[8] = {ra.x, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z, rb.w};
+          const float Zg = fmaf(zf, k.dzn, ez);  // Z(l) = (l - izs) dz + ez
           float g = 0.f;
-          if (l0 < Lm || l0 + 4 > k.nz) {  // uniform: near-box layers or the ragged last group
+          if (l0 < Lm || l0 + 8 > k.nz) {  // uniform: near-box layers or the ragged last group
 #pragma unroll
-            for (int j = 0; j < 4; j++) {
+            for (int j = 0; j < 8; j++) {
               const int l = l0 + j;
               const float v = far_unit(fmaf((float)j, k.dzn, Zg), cp, fc.a1);
               const bool excl = ((unsigned)(l - elo) <= espan) || l >= k.nz;
@@ -231,7 +233,7 @@ __global__ void __launch_bounds__(FAR_TS) far_kernel(FarArgs a) {
             }
           } else {
 #pragma unroll
-            for (int j = 0; j < 4; j++)
+            for (int j = 0; j < 8; j++)
               g = fmaf(rr[j], far_unit(fmaf((float)j, k.dzn, Zg), cp, fc.a1), g);
           }
           acc.add(g);
@@ -446,7 +448,7 @@ long long f64_chunks(long long np, int tiles, int num_sms, long long* len) {
 MeshConst make_mesh_const(const MeshDesc& m, double near_q) {
   MeshConst k;
   k.nx = m.nx; k.ny = m.ny; k.nz = m.nz;
-  k.nzp = (m.nz + 3) & ~3;
+  k.nzp = (m.nz + 7) & ~7;
   k.ncols = m.nx * m.ny;
   near_widths(m.dx, m.dy, m.dz, near_q, &k.wx, &k.wy, &k.wl);
   k.L0 = std::max(m.dx, std::max(m.dy, m.dz));

@@ -61,9 +61,18 @@ __device__ __forceinline__ ColPoly col_poly(float X, float Y, const FarCoef& f) 
   return c;
 }
 
+// Reciprocal square root on the special-function unit, subnormals flushed
+// (PTX rsqrt.approx.ftz.f32): far-field distances are never subnormal, and
+// the flush spares the scaling steps an IEEE-subnormal-safe rsqrtf needs.
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 // Z/r^3 * (1 + t2 + t4) for one pair (unit density, normalised units).
 __device__ __forceinline__ float far_unit(float Z, const ColPoly& c, float a1) {
-  const float rinv = rsqrtf(fmaf(Z, Z, c.rh));
+  const float rinv = rsqrt_ftz(fmaf(Z, Z, c.rh));
   const float u = rinv * rinv;
   float p = fmaf(c.C4, u, c.C3);
   p = fmaf(p, u, c.C2);
@@ -74,7 +83,7 @@ __device__ __forceinline__ float far_unit(float Z, const ColPoly& c, float a1) {
 
 // Regular-mesh constants for the mixed kernels.
 struct MeshConst {
-  int nx, ny, nz, nzp;  // nzp: layers padded to a multiple of 4
+  int nx, ny, nz, nzp;  // nzp: layers padded to a multiple of 8
   int ncols;
   int wx, wy, wl;       // near-box half widths (columns, columns, layers)
   float dxn, dyn, dzn;  // cell edges / L0
