@@ -155,6 +155,25 @@ int ztm_gfm_pointmass(ztm_ctx* ctx, const ztm_grid* grid, const double* drho,
                       const int* nn, long long n_nn, const double* surf,
                       double* G, int precision, int flags);
 
+/* Allocation-free point-mass forward.  No counterpart in the reference.
+ * For callers that cannot allocate device memory at the time of the call
+ * (a host that fixes the GPU memory budget up front, work issued while a
+ * stream is being captured, a real-time loop that must not allocate): the
+ * same sum as ztm_gfm_pointmass with drho, surf and G as DEVICE pointers on
+ * the current device, launched on `stream` (a cudaStream_t; NULL = the
+ * legacy default stream) and not waited for.  No context, no staging, no
+ * cudaMalloc/cudaFree: the scratch is a fixed 4 MiB array reserved in each
+ * GPU that loads the library.  Limits: at most 524,256 interior stations
+ * (ZTM_ERR_RANGE beyond); all nodes with |drho| > grid->threshold contribute
+ * (no nn list).  Every call on a device shares that array, so calls that can
+ * overlap on one GPU race: serialise them on one stream.  The first call on
+ * each device looks the array up (cudaGetSymbolAddress); make it before any
+ * stream capture starts.  Returns ZTM_OK, ZTM_ERR_ARG, ZTM_ERR_RANGE,
+ * ZTM_ERR_NODEV or ZTM_ERR_CUDA. */
+int ztm_gfm_pointmass_noalloc(const ztm_grid* grid, const double* drho,
+                              const double* surf, double* G, int precision,
+                              void* stream);
+
 /* ---- prism mode -------------------------------------------------------- */
 /* gz[s] = sum over all prisms of the closed-form attraction of prism p at
  * station s (sxyz is ns x 3: x, y, z).  No counterpart in the reference code

@@ -30,7 +30,7 @@ EXPORTS = (
     "ztm_gfm_pointmass", "ztm_gfm_prism", "ztm_gfm_prism_list", "ztm_gfm_adjoint",
     "ztm_gfm_interface", "ztm_gfm_interface_adjoint", "ztm_gfm_interface_misfit",
     "ztm_gfm_batch", "ztm_ctx_profile", "ztm_ctx_profile_read", "ztm_measure_peak",
-    "ztm_invert_interface",
+    "ztm_invert_interface", "ztm_gfm_pointmass_noalloc",
 )
 
 
@@ -78,6 +78,7 @@ _SIGS = {
     "ztm_ctx_launches": (_LL, [_P]),
     "ztm_ctx_sync": (_I, [_P]),
     "ztm_gfm_pointmass": (_I, [_P, ctypes.POINTER(Grid), _P, _P, _LL, _P, _P, _I, _I]),
+    "ztm_gfm_pointmass_noalloc": (_I, [ctypes.POINTER(Grid), _P, _P, _P, _I, _P]),
     "ztm_gfm_prism": (_I, [_P, ctypes.POINTER(Mesh), _P, _I, _P, _P, ctypes.POINTER(Opts)]),
     "ztm_gfm_prism_list": (_I, [_P, _LL, _P, _P, _I, _P, _P, ctypes.POINTER(Opts)]),
     "ztm_gfm_adjoint": (_I, [_P, ctypes.POINTER(Mesh), _I, _P, _P, _P, ctypes.POINTER(Opts)]),

@@ -13,8 +13,10 @@
 // partials that a second kernel adds in a fixed order.  No atomics, so the
 // result is bitwise reproducible.
 #include <cuda_runtime.h>
+#include <math.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "ztm_internal.cuh"
 
@@ -185,4 +187,123 @@ int ztm_launch_pointmass(ztm_ctx* c, const PmParams& p, const double* d_drho,
   pm_finalize_kernel<<<(M + 255) / 256, 256, 0, c->stream>>>(p, chunks, partial, factor, d_G);
   c->launches++;
   return ztm_after_launch(c, "point-mass kernels");
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of the point-mass forward.
+//
+// Some callers cannot allocate device memory when they need a forward: a host
+// application that hands the GPU to this code with a fixed memory budget set
+// up front (and treats any later cudaMalloc as a failure), code that runs
+// while a stream is being captured into a CUDA graph (cudaMalloc is not
+// allowed there), or a real-time inversion loop that must not pay for, or
+// risk, an allocation inside its iterations.  For them
+// ztm_gfm_pointmass_noalloc runs the same gather kernels as
+// ztm_gfm_pointmass with all of its scratch (the per-chunk partial sums and
+// the error word) in the fixed array below.  It needs no context, does no
+// host<->device staging, and calls no cudaMalloc, cudaFree or allocating
+// library routine.
+//
+// Limits and sharing:
+//   * ZTM_NOALLOC_SCRATCH_BYTES (4 MiB) per GPU, reserved in every GPU that
+//     loads the library for as long as the library stays loaded;
+//   * at most (4 MiB - 256) / 8 = 524,256 interior stations (fewer node
+//     chunks are used when the stations fill the array);
+//   * every call on a device writes the same array: calls that may overlap
+//     on that GPU (different streams, or threads without ordering) race and
+//     give wrong results; serialise them on one stream;
+//   * the first call on each device looks up the array's device address
+//     (cudaGetSymbolAddress, which may load the module onto the device); make
+//     that first call before any stream capture begins.
+#define ZTM_NOALLOC_SCRATCH_BYTES (4u << 20)
+static __device__ __align__(256) unsigned char g_pm_scratch[ZTM_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[NOALLOC_MAX_DEVICES] = {};
+}  // namespace
+
+extern "C" int ztm_gfm_pointmass_noalloc(const ztm_grid* g, const double* drho,
+                                         const double* surf, double* G, int precision,
+                                         void* stream) {
+  if (!g || !drho || !surf || !G) return ZTM_ERR_ARG;
+  if (precision != ZTM_PREC_FP64 && precision != ZTM_PREC_FP32) return ZTM_ERR_ARG;
+  if (g->di < 1 || g->dj < 1 || g->dk < 1 || g->fh < 1 || g->fv < 1 || g->bfr < 0 ||
+      !(g->threshold >= 0) || !isfinite(g->scale))
+    return ZTM_ERR_ARG;
+  int dev = -1, nsm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) {
+    cudaGetLastError();
+    return ZTM_ERR_NODEV;
+  }
+  if (dev >= NOALLOC_MAX_DEVICES) return ZTM_ERR_RANGE;
+  if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return ZTM_ERR_CUDA;
+  }
+  PmParams p;
+  p.di = g->di; p.dj = g->dj; p.fh = g->fh; p.fv = g->fv; p.bfr = g->bfr;
+  p.ii = (g->di - 1) * g->fh + 1;
+  p.jj = (g->dj - 1) * g->fh + 1;
+  p.kk = (g->dk - 1) * g->fv + 1;
+  const long long N = (long long)p.ii * p.jj * p.kk;
+  if (N > (1LL << 31) - 1) return ZTM_ERR_RANGE;
+  p.ni = std::max(0, g->di - 2 * g->bfr);
+  p.nj = std::max(0, g->dj - 2 * g->bfr);
+  p.ns = p.ni * p.nj;
+  p.thr = g->threshold;
+  p.nnodes = N;
+  p.N = N;
+  const long long cap = (ZTM_NOALLOC_SCRATCH_BYTES - 256) / sizeof(double);
+  if (p.ns > cap) return ZTM_ERR_RANGE;  // more interior stations than the array holds
+
+  // one-time set-up per device: the host-side name of the array is not a
+  // device address; ask the runtime for the address on this device
+  void* base = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+      void* a = nullptr;
+      if (cudaGetSymbolAddress(&a, g_pm_scratch) != cudaSuccess || !a) {
+        cudaGetLastError();
+        return ZTM_ERR_CUDA;
+      }
+      g_noalloc_addr[dev] = a;
+    }
+    base = g_noalloc_addr[dev];
+  }
+  int* err = reinterpret_cast<int*>(base);
+  double* partial = reinterpret_cast<double*>(static_cast<char*>(base) + 256);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+
+  int tiles, chunks;
+  long long len;
+  pm_shape(p, nsm, &tiles, &chunks, &len);
+  if (p.ns > 0 && (long long)chunks * p.ns > cap) {  // fewer, longer node chunks
+    chunks = (int)std::max(1LL, cap / p.ns);
+    len = (p.nnodes + chunks - 1) / chunks;
+    len = ((len + PM_TILE - 1) / PM_TILE) * PM_TILE;
+    chunks = (int)((p.nnodes + len - 1) / len);
+  }
+  // every (chunk, station) partial is rewritten below; only the error word
+  // has to start at zero
+  if (cudaMemsetAsync(err, 0, sizeof(int), s) != cudaSuccess) {
+    cudaGetLastError();
+    return ZTM_ERR_CUDA;
+  }
+  if (p.ns > 0 && p.nnodes > 0) {
+    dim3 grid(tiles, chunks);
+    if (precision == ZTM_PREC_FP64)
+      pm_gather_kernel<true><<<grid, PM_TS, 0, s>>>(p, drho, nullptr, surf, len, partial, err);
+    else
+      pm_gather_kernel<false><<<grid, PM_TS, 0, s>>>(p, drho, nullptr, surf, len, partial, err);
+  } else {
+    chunks = 0;
+  }
+  const double factor = g->scale * 66.7 / ((double)p.fh * p.fh * p.fv);
+  const int M = p.di * p.dj;
+  pm_finalize_kernel<<<(M + 255) / 256, 256, 0, s>>>(p, chunks, partial, factor, G);
+  if (cudaGetLastError() != cudaSuccess) return ZTM_ERR_CUDA;
+  return ZTM_OK;
 }
