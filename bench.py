@@ -302,6 +302,7 @@ def run_ours(args, rank, local_rank, world):
         line.update(extras(ctx, mesh, rho, st, d_rho, d_st, gz))
         if world == 1:
             line["cpu_baseline"] = cpu_baseline_prism(mesh, rho, st)
+            line["other_configs"] = other_configs(ctx)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -354,6 +355,75 @@ def extras(ctx, mesh, rho, st, d_rho, d_st, gz_mixed):
                               "sm_103a, same geometry on its grid (%d stations x %d nodes)"
                               % (mesh.nx * mesh.ny, nodes)}
     return out
+
+
+def _timed(ctx, fn, reps=1):
+    import torch
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    fn()
+    ctx.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        out = fn()
+    e1.record(stream)
+    ctx.sync()
+    return e0.elapsed_time(e1) / reps, out
+
+
+def other_configs(ctx):
+    """The other BASELINE workloads, once each (not the headline)."""
+    import numpy as np
+    import torch
+    from ztm_gb300 import synth
+    res = {}
+    # adjoint workload: 256x256 interface columns, 128x128 stations
+    im, depth, rho, st, start = synth.config3()
+    rng = np.random.default_rng(3)
+    d = lambda a: torch.tensor(a, device="cuda")
+    dd, dr, ds, d0 = d(depth), d(rho), d(st), d(start)
+    data = ctx.interface(im, dd, dr, ds, precision="fp64")
+    ctx.sync()
+    data = data + d(rng.normal(0, 0.05, len(st)))
+    ms_m, out_m = _timed(ctx, lambda: ctx.interface_misfit(im, d0, dr, ds, data, precision="mixed"), 3)
+    ms_d, out_d = _timed(ctx, lambda: ctx.interface_misfit(im, d0, dr, ds, data, precision="fp64"))
+    pairs = im.nx * im.ny * len(st)
+    err = lambda a, b: float((a - b).abs().max() / b.abs().max())
+    res["adjoint_interface_256x256"] = {
+        "pairs": pairs, "mixed_ms_forward_plus_adjoint": ms_m, "fp64_ms_forward_plus_adjoint": ms_d,
+        "speedup_vs_fp64": ms_d / ms_m,
+        "mixed_gz_evals_plus_gradient_evals_per_s": 2 * pairs / (ms_m * 1e-3),
+        "rel_err_vs_fp64": {"misfit": float(abs(out_m[0] - out_d[0]) / out_d[0]),
+                            "gz": err(out_m[1], out_d[1]), "g_rho": err(out_m[2], out_d[2]),
+                            "g_depth": err(out_m[3], out_d[3])}}
+    # batched workload: 32 line-search trials + 16 uneven regional meshes
+    jobs, alphas = synth.config4()
+    djobs = [(m_, d(r_.reshape(r_.shape[0], -1) if r_.ndim == 2 else r_), d(s_)) for m_, r_, s_ in jobs]
+    ctx.batch(djobs)  # builds and caches the graph
+    ctx.sync()
+    ms_b, outs = _timed(ctx, lambda: ctx.batch(djobs), 2)
+    mp = sum(int(r_.shape[0]) * m_.nx * m_.ny * m_.nz * len(s_) for m_, r_, s_ in jobs)
+    one = ctx.prism(jobs[0][0], djobs[0][1][5], djobs[0][2], precision="mixed")
+    ctx.sync()
+    res["batched_32_trials_plus_16_meshes"] = {
+        "model_pairs": mp, "ms": ms_b, "model_pair_evals_per_s": mp / (ms_b * 1e-3),
+        "launches_per_call": "1 graph: 2 prep kernels per job + 1 persistent kernel",
+        "rel_err_trial5_vs_single_call": err(outs[0][5], one)}
+    # inversion workload: 512x512 columns, 256x256 stations, 20 L-BFGS iterations
+    im5, dep5, rho5, st5, start5 = synth.config5()
+    data5 = ctx.interface(im5, d(dep5), d(rho5), d(st5), precision="mixed")
+    ctx.sync()
+    data5 = data5.cpu().numpy() + np.random.default_rng(5).normal(0, 0.05, len(st5))
+    t0 = time.perf_counter()
+    dep_out, hist, nit = ctx.invert_interface(im5, start5, rho5, st5, data5, lam=1e-2, iterations=20,
+                                              precision="mixed")
+    dt = time.perf_counter() - t0
+    res["inversion_512x512_20_iterations"] = {
+        "seconds": dt, "iterations": nit, "misfit_start": float(hist[0]),
+        "misfit_end": float(hist[-1]), "pairs_per_forward": im5.nx * im5.ny * len(st5),
+        "mean_abs_depth_error_m": {"start": float(np.abs(start5 - dep5).mean()),
+                                   "end": float(np.abs(dep_out - dep5).mean())}}
+    return res
 
 
 def main():

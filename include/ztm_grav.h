@@ -51,7 +51,11 @@ enum {
 
 /* ---- flags ----------------------------------------------------------- */
 enum {
-  ZTM_FLAG_DEVICE_PTRS = 1 /* all array arguments are device pointers */
+  ZTM_FLAG_DEVICE_PTRS = 1, /* all array arguments are device pointers */
+  ZTM_FLAG_AUTOTUNE = 2     /* prism forward: on the first call for a mesh
+                               shape and station count, time the candidate
+                               launch shapes (blocks per SM x columns per
+                               stage) and keep the fastest on the context */
 };
 
 typedef struct ztm_ctx ztm_ctx;
@@ -94,8 +98,9 @@ typedef struct {
                      that TFM.cpp:98's 66.7 mGal factor bakes in */
   double near_q;  /* mixed mode: pairs closer than near_q prism half-
                      diagonals are evaluated in double; 0 selects 6 */
-  int tile;       /* stations per block; 0 = autotuned */
-  int chunk;      /* prism columns per block; 0 = autotuned */
+  int tile;       /* reserved, 0 */
+  int chunk;      /* prism columns per block; 0 = chosen by the library
+                     (from the autotuner's cache when ZTM_FLAG_AUTOTUNE) */
 } ztm_opts;
 
 /* One job of a batched launch: nmodels density models that share one

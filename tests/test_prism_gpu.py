@@ -122,3 +122,13 @@ def test_config2_mixed_vs_fp64_subset(ctx):
     idx = {tuple(r): i for i, r in enumerate(st)}
     pick = [idx[tuple(r)] for r in sub]
     assert rel_err(full[pick], out) <= 1e-7  # chunking differs with the station count
+
+
+def test_autotuned_shape_gives_the_same_field(ctx):
+    mesh, rho = small_mesh(96, 80, 16, seed=11)
+    st = awkward_stations(mesh, n_random=300)
+    ref = ctx.prism(mesh, rho, st, precision="mixed")
+    a = ctx.prism(mesh, rho, st, precision="mixed", autotune=True)  # tunes and caches
+    b = ctx.prism(mesh, rho, st, precision="mixed", autotune=True)  # cached shape
+    assert np.array_equal(a, b)
+    assert rel_err(a, ref) <= 1e-7  # only the summation grouping differs

@@ -224,13 +224,35 @@ __global__ void __launch_bounds__(B_TS) batch_kernel(BArgs a) {
           const unsigned espan = ncl ? (unsigned)(nb.l1 - nb.l0) : 0u;
           const float* col = rs + q * k.nzp;
           const int mstride = J.sc * k.nzp;
-          const float zb = fmaf((float)(-izs), k.dzn, ez);
-          for (int l = 0; l < k.nz; l++) {
-            float K = far_unit(fmaf((float)l, k.dzn, zb), cp, fc.a1);
-            if (l < Lm && (unsigned)(l - elo) <= espan) K = 0.f;
+          float zf = (float)(-izs);  // (l0 - izs), exact, stepped by 8
+          for (int l0 = 0; l0 < k.nz; l0 += 8, zf += 8.f) {
+            const float Zg = fmaf(zf, k.dzn, ez);
+            float K[8];
 #pragma unroll
-            for (int md = 0; md < B_MG; md++)
-              if (md < mcnt) acc[md].add(K * col[md * mstride + l]);
+            for (int j = 0; j < 8; j++) {
+              const int l = l0 + j;
+              const float v = far_unit(fmaf((float)j, k.dzn, Zg), cp, fc.a1);
+              const bool excl = (l < Lm && (unsigned)(l - elo) <= espan) || l >= k.nz;
+              K[j] = excl ? 0.f : v;  // select: a NaN at a box prism is dropped
+            }
+            // one kernel value per pair, applied to every model of the group;
+            // plain sums over 8 layers, compensated across groups
+#pragma unroll
+            for (int md = 0; md < B_MG; md++) {
+              if (md < mcnt) {
+                const float4 ra = *reinterpret_cast<const float4*>(col + md * mstride + l0);
+                const float4 rb = *reinterpret_cast<const float4*>(col + md * mstride + l0 + 4);
+                float g = K[0] * ra.x;
+                g = fmaf(K[1], ra.y, g);
+                g = fmaf(K[2], ra.z, g);
+                g = fmaf(K[3], ra.w, g);
+                g = fmaf(K[4], rb.x, g);
+                g = fmaf(K[5], rb.y, g);
+                g = fmaf(K[6], rb.z, g);
+                g = fmaf(K[7], rb.w, g);
+                acc[md].add(g);
+              }
+            }
           }
           if (++ix == k.nx) {
             ix = 0;

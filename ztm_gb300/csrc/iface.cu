@@ -118,9 +118,9 @@ __device__ __forceinline__ float col_unit(float X2, float Y2, float rh, float ut
                                           float Q2, float P4, float P2, const IConst& k) {
   const float ub = ut + th;
   const float rt2 = fmaf(ut, ut, rh), rb2 = fmaf(ub, ub, rh);
-  const float it = rsqrtf(rt2), ib = rsqrtf(rb2);
+  const float it = rsqrt_ftz(rt2), ib = rsqrt_ftz(rb2);
   const float itb = it * ib;
-  const float L = th * (ut + ub) * itb * itb / (it + ib);
+  const float L = __fdividef(th * (ut + ub) * itb * itb, it + ib);
   const float it2 = it * it, ib2 = ib * ib;
   const float ct = it2 * it2 * it * fmaf(k.Q0, rt2, Q2) +
                    (it2 * it2) * (it2 * it2) * it * fmaf(fmaf(k.P0, rt2, P2), rt2, P4);
@@ -132,7 +132,7 @@ __device__ __forceinline__ float col_unit(float X2, float Y2, float rh, float ut
 __device__ __forceinline__ float face_unit_far(float X2, float Y2, float rh, float ut,
                                                const FarCoef& f) {
   const float Z2 = ut * ut;
-  const float rinv = rsqrtf(rh + Z2);
+  const float rinv = rsqrt_ftz(rh + Z2);
   const float ri2 = rinv * rinv, ri4 = ri2 * ri2;
   const float a0 = fmaf(X2, f.cA, Y2 * f.cB);
   const float h1 = fmaf(X2, f.cX1, Y2 * f.cY1);

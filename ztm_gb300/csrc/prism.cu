@@ -410,15 +410,18 @@ struct FarShape {
   size_t smem;
 };
 
-FarShape far_shape(const MeshConst& k, int ns, int num_sms, const ztm_opts* o) {
+// Launch shape of the far kernel: bps blocks per SM wanted (a full wave is
+// 12 at 40 registers), sc columns per shared-memory stage (0 = as many as fit
+// 24 KB).
+FarShape far_shape(const MeshConst& k, int ns, int num_sms, const ztm_opts* o, int bps = 12,
+                   int sc_want = 0) {
   FarShape f;
   f.tiles = std::max(1, (ns + FAR_TS - 1) / FAR_TS);
-  // stage: sc columns of nzp floats, at most 24 KB per stage
   int sc = std::max(1, (24 * 1024) / (k.nzp * 4));
   sc = std::min(sc, 64);
+  if (sc_want > 0) sc = std::max(1, std::min(sc, sc_want));
   f.sc = sc;
-  // one full wave: 12 blocks of 4 warps per SM at <= 40 registers
-  int want_blocks = 12 * std::max(num_sms, 1);
+  int want_blocks = bps * std::max(num_sms, 1);
   int chunks = std::max(1, want_blocks / f.tiles);
   if (o && o->chunk > 0) chunks = std::max(1, (k.ncols + o->chunk - 1) / o->chunk);
   chunks = std::min(chunks, std::max(1, k.ncols / sc));
@@ -429,6 +432,10 @@ FarShape far_shape(const MeshConst& k, int ns, int num_sms, const ztm_opts* o) {
   f.chunks = (k.ncols + cc - 1) / cc;
   f.smem = 128 + 2 * (size_t)sc * k.nzp * 4;
   return f;
+}
+
+std::vector<long long> tune_key(const MeshConst& k, int ns) {
+  return {1, k.nx, k.ny, k.nz, ns};
 }
 
 long long f64_chunks(long long np, int tiles, int num_sms, long long* len) {
@@ -502,9 +509,11 @@ size_t ztm_prism_ws(const MeshDesc& m, int ns, int precision, int num_sms, const
   }
   double nq = (o && o->near_q > 0) ? o->near_q : 6.0;
   MeshConst k = make_mesh_const(m, nq);
-  FarShape f = far_shape(k, ns, num_sms, o);
+  int chunks = 0;
+  for (int bps : {6, 12, 24}) chunks = std::max(chunks, far_shape(k, ns, num_sms, o, bps, 8).chunks);
+  chunks = std::max(chunks, far_shape(k, ns, num_sms, o).chunks);
   return WsCarver::need((size_t)k.ncols * k.nzp * 4) + WsCarver::need((size_t)ns * 16) * 2 +
-         WsCarver::need((size_t)ns * 8) + WsCarver::need((size_t)f.chunks * ns * 8);
+         WsCarver::need((size_t)ns * 8) + WsCarver::need((size_t)chunks * ns * 8);
 }
 
 int ztm_launch_prism(ztm_ctx* c, const MeshDesc& m, const double* d_rho, int ns,
@@ -528,22 +537,60 @@ int ztm_launch_prism(ztm_ctx* c, const MeshDesc& m, const double* d_rho, int ns,
   }
   const double nq = (o && o->near_q > 0) ? o->near_q : 6.0;
   MeshConst k = make_mesh_const(m, nq);
-  FarShape f = far_shape(k, ns, c->num_sms, o);
+  int bps = 12, scw = 0;
+  auto it = c->tuned.find(tune_key(k, ns));
+  if (it != c->tuned.end()) {
+    bps = it->second[0];
+    scw = it->second[1];
+  }
   float* rhoT = wc.take<float>((size_t)k.ncols * k.nzp);
   float4* sf = wc.take<float4>(ns);
   int4* si = wc.take<int4>(ns);
   double* near = wc.take<double>(ns);
-  double* partial = wc.take<double>((size_t)f.chunks * ns);
+  int max_chunks = 0;
+  for (int b : {6, 12, 24}) max_chunks = std::max(max_chunks, far_shape(k, ns, c->num_sms, o, b, 8).chunks);
+  max_chunks = std::max(max_chunks, far_shape(k, ns, c->num_sms, o).chunks);
+  double* partial = wc.take<double>((size_t)max_chunks * ns);
   launch_mesh_transpose(c, k, 1, d_rho, rhoT);
   launch_mesh_station_prep(c, m, k.L0, ns, d_sxyz, sf, si);
+  cudaFuncSetAttribute(far_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+  FarArgs a;
+  a.k = k; a.ns = ns; a.sf = sf; a.si = si; a.rhoT = rhoT; a.partial = partial; a.err = c->d_err;
+  if (o && (o->flags & ZTM_FLAG_AUTOTUNE) && !(o->chunk > 0) && it == c->tuned.end()) {
+    // time each candidate once (after one untimed launch) and keep the fastest
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    for (int b : {6, 12, 24})
+      for (int w : {8, 16, 0}) {
+        FarShape t = far_shape(k, ns, c->num_sms, o, b, w);
+        a.chunk_cols = t.chunk_cols;
+        a.sc = t.sc;
+        far_kernel<<<dim3(t.tiles, t.chunks), FAR_TS, t.smem, c->stream>>>(a);
+        cudaEventRecord(e0, c->stream);
+        far_kernel<<<dim3(t.tiles, t.chunks), FAR_TS, t.smem, c->stream>>>(a);
+        cudaEventRecord(e1, c->stream);
+        c->launches += 2;
+        float ms = 0.f;
+        if (cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) ==
+                                                           cudaSuccess && ms < best) {
+          best = ms;
+          bps = b;
+          scw = w;
+        }
+      }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    c->tuned[tune_key(k, ns)] = {bps, scw};
+  }
+  FarShape f = far_shape(k, ns, c->num_sms, o, bps, scw);
+  a.chunk_cols = f.chunk_cols;
+  a.sc = f.sc;
   // the double near box runs on the side stream, concurrently with the float
   // far field (different pipes: FP64 vs FMA/MUFU)
   ztm_fork(c);
   launch_mesh_near(c, k, m, ns, d_sxyz, si, d_rho, near, precision == ZTM_PREC_MIXED, c->aux);
-  FarArgs a;
-  a.k = k; a.ns = ns; a.chunk_cols = f.chunk_cols; a.sc = f.sc;
-  a.sf = sf; a.si = si; a.rhoT = rhoT; a.partial = partial; a.err = c->d_err;
-  cudaFuncSetAttribute(far_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
   {
     ZtmProf prof_(c, "prism_far");
     far_kernel<<<dim3(f.tiles, f.chunks), FAR_TS, f.smem, c->stream>>>(a);

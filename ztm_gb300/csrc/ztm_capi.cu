@@ -42,7 +42,7 @@ int check_opts(ztm_ctx* c, const ztm_opts* o) {
   if (!o) return ZTM_OK;
   if (o->precision < ZTM_PREC_FP64 || o->precision > ZTM_PREC_MIXED)
     return ztm_fail(c, ZTM_ERR_ARG, "opts.precision must be 0, 1 or 2");
-  if (o->flags & ~ZTM_FLAG_DEVICE_PTRS)
+  if (o->flags & ~(ZTM_FLAG_DEVICE_PTRS | ZTM_FLAG_AUTOTUNE))
     return ztm_fail(c, ZTM_ERR_ARG, "unknown bit in opts.flags");
   if (!(o->G >= 0) || !(o->near_q >= 0) || o->tile < 0 || o->chunk < 0)
     return ztm_fail(c, ZTM_ERR_ARG, "negative or NaN option value");

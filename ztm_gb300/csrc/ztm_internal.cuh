@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <map>
 #include <string>
 #include <vector>
 
@@ -46,6 +47,8 @@ struct ztm_ctx {
   // batched-launch graph cache and the host copy of the last job table
   std::vector<ZtmGraphEntry> graphs;
   std::vector<char> batch_table;
+  // launch shapes chosen by the autotuner, keyed by workload shape
+  std::map<std::vector<long long>, std::vector<int>> tuned;
   // tracing: events around compute kernels while enabled
   bool prof = false;
   std::vector<ZtmProfRec> prof_recs;

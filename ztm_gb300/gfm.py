@@ -20,6 +20,7 @@ from . import _lib
 
 PRECISIONS = {"fp64": _lib.PREC_FP64, "fp32": _lib.PREC_FP32, "mixed": _lib.PREC_MIXED}
 DEFAULT_G = 6.67e-11  # the constant behind the 66.7 mGal factor of TFM.cpp:98
+AUTOTUNE = 2  # ZTM_FLAG_AUTOTUNE
 
 
 class GravityError(RuntimeError):
@@ -190,14 +191,15 @@ class GravityContext:
         return out
 
     # -- prism mesh -----------------------------------------------------
-    def prism(self, mesh, rho, stations, precision="mixed", G=None, near_q=None, tile=0, chunk=0):
+    def prism(self, mesh, rho, stations, precision="mixed", G=None, near_q=None, tile=0, chunk=0,
+              autotune=False):
         np_ = mesh.nx * mesh.ny * mesh.nz
         a = _Args()
         pr = a.arr(rho, np_, name="rho")
         ns = _nstations(stations)
         px = a.arr(stations, 3 * ns, name="stations")
         out, po = a.out(ns, rho)
-        o = _opts(precision, a.flags, G, near_q, tile, chunk)
+        o = _opts(precision, a.flags | (AUTOTUNE if autotune else 0), G, near_q, tile, chunk)
         self._check(self._lib.ztm_gfm_prism(self._h, ctypes.byref(mesh), pr, ns, px, po,
                                             ctypes.byref(o)))
         return out
