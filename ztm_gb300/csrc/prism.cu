@@ -146,7 +146,7 @@ __device__ __forceinline__ float far_pair(float rho, float Z, float rh, float a0
   return fmaf(base, t, base);
 }
 
-__global__ void __launch_bounds__(FAR_TS, 12) far_kernel(FarArgs a) {
+__global__ void __launch_bounds__(FAR_TS, 10) far_kernel(FarArgs a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
   float* stage = reinterpret_cast<float*>(smem_raw + 128);
@@ -192,6 +192,7 @@ __global__ void __launch_bounds__(FAR_TS, 12) far_kernel(FarArgs a) {
   __syncthreads();
   const int Lm = min(s_lm, k.nz);
   const FarCoef fc = k.fc;
+  const float2 dz2 = make_float2(k.dzn, k.dzn);
 
   Kahan acc;
   int st = 0;
@@ -206,7 +207,7 @@ __global__ void __launch_bounds__(FAR_TS, 12) far_kernel(FarArgs a) {
     const float* rs = stage + (st & 1) * stage_floats;
     const int cs = c0 + st * a.sc;
     const int ncol = min(a.sc, c1 - cs);
-    if (active) {
+    {  // every lane runs the loop (inactive lanes on dummy data) for the warp vote
       int ix = cs % k.nx, iy = cs / k.nx;
       for (int q = 0; q < ncol; q++) {
         const float X = fmaf((float)(ixs - ix), k.dxn, ex);
@@ -216,27 +217,37 @@ __global__ void __launch_bounds__(FAR_TS, 12) far_kernel(FarArgs a) {
         const int elo = ncl ? nb.l0 : k.nz;
         const unsigned espan = ncl ? (unsigned)(nb.l1 - nb.l0) : 0u;
         const float* col = rs + q * k.nzp;
+        const ColPoly2 cp2 = col_poly2(cp, fc.a1);
+        // a column lies in some lane's near box only near the warp's
+        // stations: test that once per column for the whole warp
+        const bool warp_near = __any_sync(0xffffffffu, ncl);
         float zf = (float)(-izs);  // (l0 - izs), exact in float, stepped by 8
         for (int l0 = 0; l0 < k.nz; l0 += 8, zf += 8.f) {
           const float4 ra = *reinterpret_cast<const float4*>(col + l0);
           const float4 rb = *reinterpret_cast<const float4*>(col + l0 + 4);
-          const float rr[8] = {ra.x, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z, rb.w};
           const float Zg = fmaf(zf, k.dzn, ez);  // Z(l) = (l - izs) dz + ez
-          float g = 0.f;
-          if (l0 < Lm || l0 + 8 > k.nz) {  // uniform: near-box layers or the ragged last group
+          const float2 zg2 = make_float2(Zg, Zg);
+          float2 Zj[4];
 #pragma unroll
-            for (int j = 0; j < 8; j++) {
-              const int l = l0 + j;
-              const float v = far_unit(fmaf((float)j, k.dzn, Zg), cp, fc.a1);
-              const bool excl = ((unsigned)(l - elo) <= espan) || l >= k.nz;
-              g = fmaf(rr[j], excl ? 0.f : v, g);  // select first: a NaN is dropped
+          for (int j = 0; j < 4; j++)
+            Zj[j] = __ffma2_rn(make_float2((float)(2 * j), (float)(2 * j + 1)), dz2, zg2);
+          float2 v[4];
+#pragma unroll
+          for (int j = 0; j < 4; j++) v[j] = far_unit2(Zj[j], cp2);
+          if ((warp_near && l0 < Lm) || l0 + 8 > k.nz) {  // warp-uniform
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+              const int la = l0 + 2 * j, lb = la + 1;
+              // select, not multiply: a NaN at a box prism is dropped
+              if (((unsigned)(la - elo) <= espan) || la >= k.nz) v[j].x = 0.f;
+              if (((unsigned)(lb - elo) <= espan) || lb >= k.nz) v[j].y = 0.f;
             }
-          } else {
-#pragma unroll
-            for (int j = 0; j < 8; j++)
-              g = fmaf(rr[j], far_unit(fmaf((float)j, k.dzn, Zg), cp, fc.a1), g);
           }
-          acc.add(g);
+          float2 g = __fmul2_rn(make_float2(ra.x, ra.y), v[0]);
+          g = __ffma2_rn(make_float2(ra.z, ra.w), v[1], g);
+          g = __ffma2_rn(make_float2(rb.x, rb.y), v[2], g);
+          g = __ffma2_rn(make_float2(rb.z, rb.w), v[3], g);
+          acc.add(g.x + g.y);
         }
         if (++ix == k.nx) {
           ix = 0;
@@ -411,9 +422,9 @@ struct FarShape {
 };
 
 // Launch shape of the far kernel: bps blocks per SM wanted (a full wave is
-// 12 at 40 registers), sc columns per shared-memory stage (0 = as many as fit
+// 10 at 47 registers), sc columns per shared-memory stage (0 = as many as fit
 // 24 KB).
-FarShape far_shape(const MeshConst& k, int ns, int num_sms, const ztm_opts* o, int bps = 12,
+FarShape far_shape(const MeshConst& k, int ns, int num_sms, const ztm_opts* o, int bps = 10,
                    int sc_want = 0) {
   FarShape f;
   f.tiles = std::max(1, (ns + FAR_TS - 1) / FAR_TS);
@@ -510,7 +521,7 @@ size_t ztm_prism_ws(const MeshDesc& m, int ns, int precision, int num_sms, const
   double nq = (o && o->near_q > 0) ? o->near_q : 6.0;
   MeshConst k = make_mesh_const(m, nq);
   int chunks = 0;
-  for (int bps : {6, 12, 24}) chunks = std::max(chunks, far_shape(k, ns, num_sms, o, bps, 8).chunks);
+  for (int bps : {5, 10, 20}) chunks = std::max(chunks, far_shape(k, ns, num_sms, o, bps, 8).chunks);
   chunks = std::max(chunks, far_shape(k, ns, num_sms, o).chunks);
   return WsCarver::need((size_t)k.ncols * k.nzp * 4) + WsCarver::need((size_t)ns * 16) * 2 +
          WsCarver::need((size_t)ns * 8) + WsCarver::need((size_t)chunks * ns * 8);
@@ -537,7 +548,7 @@ int ztm_launch_prism(ztm_ctx* c, const MeshDesc& m, const double* d_rho, int ns,
   }
   const double nq = (o && o->near_q > 0) ? o->near_q : 6.0;
   MeshConst k = make_mesh_const(m, nq);
-  int bps = 12, scw = 0;
+  int bps = 10, scw = 0;
   auto it = c->tuned.find(tune_key(k, ns));
   if (it != c->tuned.end()) {
     bps = it->second[0];
@@ -548,7 +559,7 @@ int ztm_launch_prism(ztm_ctx* c, const MeshDesc& m, const double* d_rho, int ns,
   int4* si = wc.take<int4>(ns);
   double* near = wc.take<double>(ns);
   int max_chunks = 0;
-  for (int b : {6, 12, 24}) max_chunks = std::max(max_chunks, far_shape(k, ns, c->num_sms, o, b, 8).chunks);
+  for (int b : {5, 10, 20}) max_chunks = std::max(max_chunks, far_shape(k, ns, c->num_sms, o, b, 8).chunks);
   max_chunks = std::max(max_chunks, far_shape(k, ns, c->num_sms, o).chunks);
   double* partial = wc.take<double>((size_t)max_chunks * ns);
   launch_mesh_transpose(c, k, 1, d_rho, rhoT);
@@ -562,7 +573,7 @@ int ztm_launch_prism(ztm_ctx* c, const MeshDesc& m, const double* d_rho, int ns,
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     float best = 1e30f;
-    for (int b : {6, 12, 24})
+    for (int b : {5, 10, 20})
       for (int w : {8, 16, 0}) {
         FarShape t = far_shape(k, ns, c->num_sms, o, b, w);
         a.chunk_cols = t.chunk_cols;

@@ -81,6 +81,35 @@ __device__ __forceinline__ float far_unit(float Z, const ColPoly& c, float a1) {
   return (Z * s) * (rinv * u);
 }
 
+// Two layers at once on the packed FP32 path (Blackwell FFMA2/FMUL2: one
+// issue slot for two float FMAs with the same rounding as two FFMAs); the
+// two rsqrts stay scalar on the special-function unit.  Returns
+// (Z/r^3 (1+t2+t4)) for Z = Zv.x and Zv.y.
+struct ColPoly2 {
+  float2 rh, C2, C3, C4, a1;
+};
+
+__device__ __forceinline__ ColPoly2 col_poly2(const ColPoly& c, float a1) {
+  ColPoly2 d;
+  d.rh = make_float2(c.rh, c.rh);
+  d.C2 = make_float2(c.C2, c.C2);
+  d.C3 = make_float2(c.C3, c.C3);
+  d.C4 = make_float2(c.C4, c.C4);
+  d.a1 = make_float2(a1, a1);
+  return d;
+}
+
+__device__ __forceinline__ float2 far_unit2(float2 Z, const ColPoly2& c) {
+  const float2 r2 = __ffma2_rn(Z, Z, c.rh);
+  const float2 rinv = make_float2(rsqrt_ftz(r2.x), rsqrt_ftz(r2.y));
+  const float2 u = __fmul2_rn(rinv, rinv);
+  float2 p = __ffma2_rn(c.C4, u, c.C3);
+  p = __ffma2_rn(p, u, c.C2);
+  p = __ffma2_rn(p, u, c.a1);
+  const float2 s = __ffma2_rn(p, u, make_float2(1.f, 1.f));
+  return __fmul2_rn(__fmul2_rn(Z, s), __fmul2_rn(rinv, u));
+}
+
 // Regular-mesh constants for the mixed kernels.
 struct MeshConst {
   int nx, ny, nz, nzp;  // nzp: layers padded to a multiple of 8
