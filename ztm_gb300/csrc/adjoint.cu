@@ -69,30 +69,47 @@ __global__ void __launch_bounds__(ADJ_TS)
     __syncthreads();
     if (!active) continue;
     const int cnt = min(ADJ_STILE, ns - s0);
-    for (int q = 0; q < cnt; q++) {
-      const float4 f = s_f[q];
-      const int4 i = s_i[q];
-      const float w = s_r[q];
-      const float X = fmaf((float)(i.x - ix), k.dxn, f.x);
-      const float Y = fmaf((float)(i.y - iy), k.dyn, f.y);
-      const ColPoly cp = col_poly(X, Y, fc);
-      const NearBox b = near_box(i, k);
-      const bool ncl = ix >= b.x0 && ix <= b.x1 && iy >= b.y0 && iy <= b.y1;
-      const int elo = ncl ? b.l0 : k.nz;
-      const unsigned espan = ncl ? (unsigned)(b.l1 - b.l0) : 0u;
-      const float Zg = fmaf((float)(l0 - i.z), k.dzn, f.z);
-      if (ncl || l0 + ADJ_LG > k.nz) {
+    // plain float sums over 16 stations, compensated across the groups
+    for (int q0 = 0; q0 < cnt; q0 += 16) {
+      float2 gs[ADJ_LG / 2];
 #pragma unroll
-        for (int j = 0; j < ADJ_LG; j++) {
-          const int l = l0 + j;
-          const float v = far_unit(fmaf((float)j, k.dzn, Zg), cp, fc.a1);
-          const bool excl = ((unsigned)(l - elo) <= espan) || l >= k.nz;
-          acc[j].add(w * (excl ? 0.f : v));
+      for (int j = 0; j < ADJ_LG / 2; j++) gs[j] = make_float2(0.f, 0.f);
+      const int q1 = min(cnt, q0 + 16);
+      for (int q = q0; q < q1; q++) {
+        const float4 f = s_f[q];
+        const int4 i = s_i[q];
+        const float w = s_r[q];
+        const float X = fmaf((float)(i.x - ix), k.dxn, f.x);
+        const float Y = fmaf((float)(i.y - iy), k.dyn, f.y);
+        const ColPoly cp = col_poly(X, Y, fc);
+        const NearBox b = near_box(i, k);
+        const bool ncl = ix >= b.x0 && ix <= b.x1 && iy >= b.y0 && iy <= b.y1;
+        const int elo = ncl ? b.l0 : k.nz;
+        const unsigned espan = ncl ? (unsigned)(b.l1 - b.l0) : 0u;
+        const float Zg = fmaf((float)(l0 - i.z), k.dzn, f.z);
+        const ColPoly2 cp2 = col_poly2(cp, fc.a1);
+        const float2 zg2 = make_float2(Zg, Zg), dz2 = make_float2(k.dzn, k.dzn);
+        float2 v[ADJ_LG / 2];
+#pragma unroll
+        for (int j = 0; j < ADJ_LG / 2; j++)
+          v[j] = far_unit2(__ffma2_rn(make_float2((float)(2 * j), (float)(2 * j + 1)), dz2, zg2),
+                           cp2);
+        if (ncl || l0 + ADJ_LG > k.nz) {
+#pragma unroll
+          for (int j = 0; j < ADJ_LG / 2; j++) {
+            const int la = l0 + 2 * j, lb = la + 1;
+            if (((unsigned)(la - elo) <= espan) || la >= k.nz) v[j].x = 0.f;
+            if (((unsigned)(lb - elo) <= espan) || lb >= k.nz) v[j].y = 0.f;
+          }
         }
-      } else {
+        const float2 w2 = make_float2(w, w);
 #pragma unroll
-        for (int j = 0; j < ADJ_LG; j++)
-          acc[j].add(w * far_unit(fmaf((float)j, k.dzn, Zg), cp, fc.a1));
+        for (int j = 0; j < ADJ_LG / 2; j++) gs[j] = __ffma2_rn(w2, v[j], gs[j]);
+      }
+#pragma unroll
+      for (int j = 0; j < ADJ_LG / 2; j++) {
+        acc[2 * j].add(gs[j].x);
+        acc[2 * j + 1].add(gs[j].y);
       }
     }
   }
