@@ -426,6 +426,59 @@ def other_configs(ctx):
     return res
 
 
+def run_workload(args, local_rank):
+    """The other workloads as the timed step (side measurements and ncu
+    targets; the default forward workload is the headline)."""
+    import numpy as np
+    import torch
+    import ztm_gb300
+    from ztm_gb300 import synth
+    torch.cuda.set_device(local_rank)
+    ctx = ztm_gb300.GravityContext(local_rank)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    d = lambda a: torch.tensor(np.ascontiguousarray(a), device="cuda")
+    if args.workload == "adjoint":
+        mesh, rho, st = synth.config2()
+        ds = d(st)
+        res = d(np.random.default_rng(0).normal(0, 1, len(st)))
+        units = mesh.nx * mesh.ny * mesh.nz * len(st)
+        what = "d misfit/d rho of the 256x256x64 mesh at 128x128 stations (gradient evals)"
+        step = lambda: ctx.adjoint(mesh, ds, res, precision="mixed")
+    elif args.workload == "interface":
+        im, depth, rho, st, start = synth.config3()
+        dd, dr, dst, d0 = d(depth), d(rho), d(st), d(start)
+        data = ctx.interface(im, dd, dr, dst, precision="fp64")
+        ctx.sync()
+        units = 2 * im.nx * im.ny * len(st)
+        what = ("forward + adjoint (misfit, d/drho, d/ddepth) of 256x256 Moho columns at "
+                "128x128 stations (gz evals + gradient evals)")
+        step = lambda: ctx.interface_misfit(im, d0, dr, dst, data, precision="mixed")
+    elif args.workload == "batch":
+        jobs, _ = synth.config4()
+        djobs = [(m_, d(r_), d(s_)) for m_, r_, s_ in jobs]
+        units = sum(int(r_.shape[0]) * m_.nx * m_.ny * m_.nz * len(s_) for m_, r_, s_ in jobs)
+        what = ("32 line-search trials on the 256x256x64 mesh + 16 regional meshes, one "
+                "graph-captured persistent launch (model-pair evals)")
+        step = lambda: ctx.batch(djobs)
+    else:
+        raise SystemExit("unknown workload " + args.workload)
+    for _ in range(args.warmup):
+        step()
+    ctx.sync()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    for i in range(args.steps):
+        ev[i][0].record(stream)
+        step()
+        ev[i][1].record(stream)
+    ctx.sync()
+    ms = sum(a.elapsed_time(b) for a, b in ev) / args.steps
+    print(json.dumps({"workload": args.workload, "what": what, "value": units / (ms * 1e-3),
+                      "unit": "evals/s", "ms_per_step": ms, "steps": args.steps,
+                      "warmup": args.warmup, "evals_per_step": units}), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -433,10 +486,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quick", action="store_true", help="skip side measurements")
+    ap.add_argument("--workload", default="forward",
+                    choices=["forward", "adjoint", "interface", "batch"],
+                    help="forward (the headline) or another workload as the timed step")
     args = ap.parse_args()
     rank, local_rank, world = dist_env()
     if args.impl == "reference":
         return run_reference(args, rank)
+    if args.workload != "forward":
+        return run_workload(args, local_rank)
     return run_ours(args, rank, local_rank, world)
 
 

@@ -40,6 +40,8 @@ constexpr int IF_NEAR_WPB = 4;
 
 struct IConst {
   int nx, ny, ncols, w;  // w: near window half width (columns)
+  int words;             // 32-bit mask words per station ((2w+1)^2 bits)
+  double near_h;         // near_q * horizontal half diagonal (m)
   float dxn, dyn;
   double L0;
   float Q0, P0;
@@ -72,6 +74,8 @@ IConst make_iconst(const IMeshDesc& m, double near_q) {
   double ellh = 0.5 * sqrt(m.dx * m.dx + m.dy * m.dy);
   int w = (int)ceil(near_q * ellh / std::min(m.dx, m.dy) - 0.5);
   k.w = std::max(w, 0);
+  k.words = ((2 * k.w + 1) * (2 * k.w + 1) + 31) / 32;
+  k.near_h = near_q * ellh;
   return k;
 }
 
@@ -107,9 +111,51 @@ __global__ void iface_col_prep(IMeshDesc m, double L0, const double* __restrict_
   cf[c] = make_float4((float)rho[c], (float)(d / L0), (float)thick, 0.f);
 }
 
-__device__ __forceinline__ bool in_window(int ixs, int iys, int ix, int iy, const IConst& k) {
-  int cx = clampi(ixs, 0, k.nx - 1), cy = clampi(iys, 0, k.ny - 1);
-  return abs(ix - cx) <= k.w && abs(iy - cy) <= k.w;
+// Near columns of a station: inside the (2w+1)^2 window around its home
+// column (clamped to the mesh) AND with the station less than near_h above
+// the column's top.  Outside the window the horizontal distance alone is
+// >= near_q half-diagonals; inside it, a station that high above the top is
+// as far from every point of the column.  The window slot of (ix, iy):
+__device__ __forceinline__ bool window_slot(int ixs, int iys, int ix, int iy, const IConst& k,
+                                            int* slot) {
+  const int cx = clampi(ixs, 0, k.nx - 1), cy = clampi(iys, 0, k.ny - 1);
+  if (abs(ix - cx) > k.w || abs(iy - cy) > k.w) return false;
+  const int x0 = max(0, cx - k.w), x1 = min(k.nx - 1, cx + k.w), y0 = max(0, cy - k.w);
+  *slot = (ix - x0) + (x1 - x0 + 1) * (iy - y0);
+  return true;
+}
+
+// The near bit of (station, column), from the mask the mask kernel wrote.
+__device__ __forceinline__ bool is_near(const uint32_t* __restrict__ mask, int s, int ixs, int iys,
+                                        int ix, int iy, const IConst& k) {
+  int slot;
+  if (!window_slot(ixs, iys, ix, iy, k, &slot)) return false;
+  return (__ldg(mask + (size_t)s * k.words + (slot >> 5)) >> (slot & 31)) & 1u;
+}
+
+// One warp per station: the near bit of every window column, in double.
+__global__ void iface_near_mask(IConst k, int ns, const double* __restrict__ sxyz,
+                                const int2* __restrict__ si, const double* __restrict__ depth,
+                                uint32_t* __restrict__ mask) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int s = blockIdx.x * 4 + warp;
+  if (s >= ns) return;
+  const int2 h = si[s];
+  const int cx = clampi(h.x, 0, k.nx - 1), cy = clampi(h.y, 0, k.ny - 1);
+  const int x0 = max(0, cx - k.w), x1 = min(k.nx - 1, cx + k.w);
+  const int y0 = max(0, cy - k.w), y1 = min(k.ny - 1, cy + k.w);
+  const int wx = x1 - x0 + 1, n = wx * (y1 - y0 + 1);
+  const double zs = sxyz[3 * s + 2];
+  for (int wd = 0; wd < k.words; wd++) {
+    const int q = wd * 32 + lane;
+    bool nb = false;
+    if (q < n) {
+      const int ix = x0 + q % wx, iy = y0 + q / wx;
+      nb = zs + depth[ix + (long long)k.nx * iy] < k.near_h;  // zs - z_top < near_h
+    }
+    const uint32_t bits = __ballot_sync(0xffffffffu, nb);
+    if (lane == 0) mask[(size_t)s * k.words + wd] = bits;
+  }
 }
 
 // Unit column integral (normalised, without dx dy) and, if wanted, the unit
@@ -147,7 +193,8 @@ __device__ __forceinline__ float face_unit_far(float X2, float Y2, float rh, flo
 // ---- forward, far (thread per station) ------------------------------------
 __global__ void __launch_bounds__(IF_TS)
     iface_far_fwd(IConst k, int ns, const IStation* __restrict__ sf, const int2* __restrict__ si,
-                  const float4* __restrict__ cf, int chunk_len, double* __restrict__ partial) {
+                  const float4* __restrict__ cf, const uint32_t* __restrict__ mask, int chunk_len,
+                  double* __restrict__ partial) {
   __shared__ float4 s_c[IF_TILE];
   const int s = blockIdx.x * IF_TS + threadIdx.x;
   const bool active = s < ns;
@@ -167,6 +214,7 @@ __global__ void __launch_bounds__(IF_TS)
     if (!active) continue;
     const int cnt = min(IF_TILE, c1 - t0);
     int ix = t0 % k.nx, iy = t0 / k.nx;
+    float g = 0.f;  // plain sum over 8 columns, compensated across groups
     for (int q = 0; q < cnt; q++) {
       const float4 col = s_c[q];
       const float X = fmaf((float)(hi.x - ix), k.dxn, st.ex);
@@ -176,12 +224,17 @@ __global__ void __launch_bounds__(IF_TS)
       const float P4 = fmaf(k.p4x * X2, X2, fmaf(k.p4y * Y2, Y2, k.p4xy * X2 * Y2));
       const float P2 = fmaf(k.p2x, X2, k.p2y * Y2);
       const float v = col.x * col_unit(X2, Y2, rh, st.zs + col.y, col.z, Q2, P4, P2, k);
-      acc.add(in_window(hi.x, hi.y, ix, iy, k) ? 0.f : v);
+      g += is_near(mask, s, hi.x, hi.y, ix, iy, k) ? 0.f : v;  // select drops a NaN
+      if ((q & 7) == 7) {
+        acc.add(g);
+        g = 0.f;
+      }
       if (++ix == k.nx) {
         ix = 0;
         ++iy;
       }
     }
+    acc.add(g);
   }
   if (active) partial[(size_t)blockIdx.y * ns + s] = acc.value();
 }
@@ -189,7 +242,8 @@ __global__ void __launch_bounds__(IF_TS)
 // ---- forward, near window in double (warp per station) ---------------------
 __global__ void iface_near_fwd(IConst k, IMeshDesc m, int ns, const double* __restrict__ sxyz,
                                const int2* __restrict__ si, const double* __restrict__ depth,
-                               const double* __restrict__ rho, double* __restrict__ out) {
+                               const double* __restrict__ rho, const uint32_t* __restrict__ mask,
+                               double* __restrict__ out) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int s = blockIdx.x * IF_NEAR_WPB + warp;
   if (s >= ns) return;
@@ -201,6 +255,7 @@ __global__ void iface_near_fwd(IConst k, IMeshDesc m, int ns, const double* __re
   const double xs = sxyz[3 * s], ys = sxyz[3 * s + 1], zs = sxyz[3 * s + 2];
   double acc = 0.0;
   for (int q = lane; q < n; q += 32) {
+    if (!((mask[(size_t)s * k.words + (q >> 5)] >> (q & 31)) & 1u)) continue;
     const int ix = x0 + q % wx, iy = y0 + q / wx;
     const long long c = ix + (long long)m.nx * iy;
     const double r = rho[c];
@@ -250,7 +305,8 @@ __global__ void __launch_bounds__(64)
 // ---- adjoint, far (thread per column) --------------------------------------
 __global__ void __launch_bounds__(IF_TS)
     iface_far_adj(IConst k, int ns, const IStation* __restrict__ sf, const int2* __restrict__ si,
-                  const float4* __restrict__ cf, double sc_rho, double sc_dep,
+                  const float4* __restrict__ cf, const uint32_t* __restrict__ mask, double sc_rho,
+                  double sc_dep,
                   double* __restrict__ g_rho, double* __restrict__ g_dep) {
   __shared__ IStation s_f[IF_TILE];
   __shared__ int2 s_i[IF_TILE];
@@ -282,7 +338,7 @@ __global__ void __launch_bounds__(IF_TS)
       const float ut = st.zs + col.y;
       const float u = col_unit(X2, Y2, rh, ut, col.z, Q2, P4, P2, k);
       const float f = face_unit_far(X2, Y2, rh, ut, k.face);
-      const bool near = in_window(h.x, h.y, ix, iy, k);
+      const bool near = is_near(mask, t0 + q, h.x, h.y, ix, iy, k);
       ar.add(near ? 0.f : st.r * u);
       ad.add(near ? 0.f : st.r * f);
     }
@@ -296,8 +352,8 @@ __global__ void __launch_bounds__(IF_TS)
 __global__ void iface_near_adj(IConst k, IMeshDesc m, int ns, const double* __restrict__ sxyz,
                                const int2* __restrict__ si, const double* __restrict__ depth,
                                const double* __restrict__ rho, const double* __restrict__ res,
-                               double G5, double* __restrict__ g_rho,
-                               double* __restrict__ g_dep) {
+                               const uint32_t* __restrict__ mask, double G5,
+                               double* __restrict__ g_rho, double* __restrict__ g_dep) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int s = blockIdx.x * IF_NEAR_WPB + warp;
   if (s >= ns) return;
@@ -310,6 +366,7 @@ __global__ void iface_near_adj(IConst k, IMeshDesc m, int ns, const double* __re
   const int wx = x1 - x0 + 1, n = wx * (y1 - y0 + 1);
   const double xs = sxyz[3 * s], ys = sxyz[3 * s + 1], zs = sxyz[3 * s + 2];
   for (int q = lane; q < n; q += 32) {
+    if (!((mask[(size_t)s * k.words + (q >> 5)] >> (q & 31)) & 1u)) continue;
     const int ix = x0 + q % wx, iy = y0 + q / wx;
     const long long c = ix + (long long)m.nx * iy;
     const double xa = (m.x0 + ix * m.dx) - xs, xb = (m.x0 + (ix + 1) * m.dx) - xs;
@@ -408,6 +465,8 @@ size_t ztm_iface_ws(const IMeshDesc& m, int ns, int precision, int num_sms) {
   w += WsCarver::need((size_t)cha * nc * 8) * 2;                    // double adjoint partials
   w += WsCarver::need((size_t)nc * 16) + WsCarver::need((size_t)std::max(ns, 1) * 16) +
        WsCarver::need((size_t)std::max(ns, 1) * 8) * 4;
+  // near masks (forward and adjoint), up to near_q = 16
+  w += 2 * WsCarver::need((size_t)std::max(ns, 1) * 4 * 64);
   (void)precision;
   return w;
 }
@@ -433,6 +492,7 @@ static int iface_forward_impl(ztm_ctx* c, const IMeshDesc& m, const double* d_de
   }
   const double nq = (o && o->near_q > 0) ? o->near_q : 6.0;
   IConst k = make_iconst(m, nq);
+  if (k.words > 64) return ztm_fail(c, ZTM_ERR_RANGE, "near_q too large for the interface window");
   IStation* sf = wc.take<IStation>(ns);
   int2* si = wc.take<int2>(ns);
   float4* cf = wc.take<float4>(nc);
@@ -440,22 +500,27 @@ static int iface_forward_impl(ztm_ctx* c, const IMeshDesc& m, const double* d_de
   iface_station_prep<<<(ns + 127) / 128, 128, 0, c->stream>>>(m, k.L0, ns, d_sxyz, nullptr, sf,
                                                               si);
   iface_col_prep<<<(unsigned)((nc + 255) / 256), 256, 0, c->stream>>>(m, k.L0, d_depth, d_rho, cf);
+  uint32_t* mask = wc.take<uint32_t>((size_t)ns * k.words);
+  iface_near_mask<<<(ns + 3) / 4, 128, 0, c->stream>>>(k, ns, d_sxyz, si, d_depth, mask);
+  // double near columns on the side stream, concurrently with the float far field
+  ztm_fork(c);
   {
-    ZtmProf prof_(c, "iface_near");
-    iface_near_fwd<<<(ns + IF_NEAR_WPB - 1) / IF_NEAR_WPB, IF_NEAR_WPB * 32, 0, c->stream>>>(
-        k, m, ns, d_sxyz, si, d_depth, d_rho, near);
+    ZtmProf prof_(c, "iface_near", c->aux);
+    iface_near_fwd<<<(ns + IF_NEAR_WPB - 1) / IF_NEAR_WPB, IF_NEAR_WPB * 32, 0, c->aux>>>(
+        k, m, ns, d_sxyz, si, d_depth, d_rho, mask, near);
   }
   int tiles = std::max(1, (ns + IF_TS - 1) / IF_TS), len;
   int ch = chunks_for(nc, tiles, c->num_sms, IF_TILE, &len);
   double* partial = wc.take<double>((size_t)ch * ns);
   {
     ZtmProf prof_(c, "iface_far");
-    iface_far_fwd<<<dim3(tiles, ch), IF_TS, 0, c->stream>>>(k, ns, sf, si, cf, len, partial);
+    iface_far_fwd<<<dim3(tiles, ch), IF_TS, 0, c->stream>>>(k, ns, sf, si, cf, mask, len, partial);
   }
+  ztm_join(c);
   iface_finalize<<<(ns + 255) / 256, 256, 0, c->stream>>>(ns, ch, partial,
                                                           k.L0 * (double)k.dxn * k.dyn, near, G5,
                                                           d_gz);
-  c->launches += 5;
+  c->launches += 6;
   return ztm_after_launch(c, "interface mixed forward");
 }
 
@@ -493,6 +558,7 @@ int ztm_launch_iface_adj(ztm_ctx* c, const IMeshDesc& m, const double* d_depth,
   }
   const double nq = (o && o->near_q > 0) ? o->near_q : 6.0;
   IConst k = make_iconst(m, nq);
+  if (k.words > 64) return ztm_fail(c, ZTM_ERR_RANGE, "near_q too large for the interface window");
   IStation* sf = wc.take<IStation>(ns);
   int2* si = wc.take<int2>(ns);
   float4* cf = wc.take<float4>(nc);
@@ -501,17 +567,19 @@ int ztm_launch_iface_adj(ztm_ctx* c, const IMeshDesc& m, const double* d_depth,
   // face integral is dimensionless: dx dy / L0^2 * (u / r^3 in 1/L0^2 units)
   const double sc_rho = G5 * k.L0 * (double)k.dxn * k.dyn;
   const double sc_dep = G5 * (double)k.dxn * k.dyn;
+  uint32_t* mask = wc.take<uint32_t>((size_t)ns * k.words);
+  iface_near_mask<<<(ns + 3) / 4, 128, 0, c->stream>>>(k, ns, d_sxyz, si, d_depth, mask);
   {
     ZtmProf prof_(c, "iface_far");
     iface_far_adj<<<(unsigned)((nc + IF_TS - 1) / IF_TS), IF_TS, 0, c->stream>>>(
-        k, ns, sf, si, cf, sc_rho, sc_dep, d_grho, d_gdep);
+        k, ns, sf, si, cf, mask, sc_rho, sc_dep, d_grho, d_gdep);
   }
-  {
+  {  // after the far kernel has written every entry: double atomics add the near pairs
     ZtmProf prof_(c, "iface_near");
     iface_near_adj<<<(ns + IF_NEAR_WPB - 1) / IF_NEAR_WPB, IF_NEAR_WPB * 32, 0, c->stream>>>(
-        k, m, ns, d_sxyz, si, d_depth, d_rho, d_res, G5, d_grho, d_gdep);
+        k, m, ns, d_sxyz, si, d_depth, d_rho, d_res, mask, G5, d_grho, d_gdep);
   }
-  c->launches += 4;
+  c->launches += 5;
   return ztm_after_launch(c, "interface mixed adjoint");
 }
 
