@@ -179,6 +179,23 @@ int ztm_gfm_pointmass_noalloc(const ztm_grid* grid, const double* drho,
                               const double* surf, double* G, int precision,
                               void* stream);
 
+/* Density-perturbation builder of TFM.cpp:83-89 on the GPU.  vm, ro, dr are
+ * the mantle velocity, the crust/mantle contrast as used in the loop
+ * (TFM.cpp:84 negates the parameter) and the velocity-to-density ratio; rc
+ * is TFM's RC vector (TFM.cpp:218: ref lat, lon, depth, origin x, y, z
+ * offsets, spacing h, di, dj, dk).  sea, M (di*dj) and v (di*dj*dk) are the
+ * reference's sea-level map, rendered Moho and velocity grids.  drho gets
+ * the fine-grid perturbation, zero where TFM.cpp:89 leaves a node out of nn;
+ * *n_selected (host mode only, else -1) the number of selected nodes. */
+typedef struct {
+  int di, dj, dk, fh, fv;
+  double vm, ro, dr;
+  double rc[10];
+} ztm_density_params;
+int ztm_density_build(ztm_ctx* ctx, const ztm_density_params* p,
+                      const double* sea, const double* M, const double* v,
+                      double* drho, long long* n_selected, int flags);
+
 /* ---- prism mode -------------------------------------------------------- */
 /* gz[s] = sum over all prisms of the closed-form attraction of prism p at
  * station s (sxyz is ns x 3: x, y, z).  No counterpart in the reference code

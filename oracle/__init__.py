@@ -46,6 +46,7 @@ def _load():
         lib.ora_mesh_adjoint.argtypes = [P, I, P, P, D, P, I]
         lib.ora_interface_fwd.argtypes = [P, P, P, I, P, D, P, I]
         lib.ora_interface_adj.argtypes = [P, P, P, I, P, P, D, P, P, I]
+        lib.ora_density_tfm.argtypes = [I, I, I, I, I, D, D, D, P, P, P, P, P, I]
         _lib = lib
     return _lib
 
@@ -180,6 +181,18 @@ def interface_adj(imesh, depth, rho_col, stations, resid, G=6.67e-11, nthreads=N
     lib.ora_interface_adj(_p(ip), _p(depth), _p(rho_col), st.shape[0], _p(st), _p(res), G,
                           _p(gr), _p(gd), nthreads or NTHREADS)
     return gr, gd
+
+
+def density_tfm(di, dj, dk, fh, fv, vm, ro, dr, rc, sea, M, v, nthreads=None):
+    """TFM.cpp:85-89: the fine-grid density perturbation drho."""
+    lib = _load()
+    rc = _f64(rc)
+    sea, M, v = _f64(sea), _f64(M), _f64(v)
+    N = ((di - 1) * fh + 1) * ((dj - 1) * fh + 1) * ((dk - 1) * fv + 1)
+    out = np.zeros(N)
+    lib.ora_density_tfm(di, dj, dk, fh, fv, vm, ro, dr, _p(rc), _p(sea), _p(M), _p(v), _p(out),
+                        nthreads or NTHREADS)
+    return out
 
 
 # ---- the reference GF kernel itself (GPU host only) ----------------------

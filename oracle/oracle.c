@@ -421,3 +421,118 @@ void ora_interface_adj(const double* imp, const double* depth,
   long nc = (long)imp[0] * (long)imp[1];
   parallel_for(nc, nthreads, iface_adj_rows, &a);
 }
+
+/* ---------------------------------------------------------------------- */
+/* density-perturbation builder (TFM.cpp:83-89)                            */
+
+/* zmath.cpp:225-235, 2-D linear interpolation with unit spacing.  The
+ * reference reads f[i+1] / f[(j+1)*di] even when the weight of that
+ * neighbour is 0 (x = di-1 or y = dj-1), one element past the row or the
+ * array; the index is clamped here, which changes nothing but the read. */
+static double interp2_tfm(const double* f, double x, double y, int di, int dj) {
+  double ii = fmin(fmax(x / 1.0, 0), (di - 1)), jj = fmin(fmax(y / 1.0, 0), (dj - 1));
+  int i = (int)ii, j = (int)jj;
+  double si = ii - i, sj = jj - j;
+  int i1 = i + 1 < di ? i + 1 : i, j1 = j + 1 < dj ? j + 1 : j;
+  double c00 = f[i + j * di], c10 = f[i1 + j * di];
+  double c01 = f[i + j1 * di], c11 = f[i1 + j1 * di];
+  double c0 = c00 * (1 - si) + c10 * si, c1 = c01 * (1 - si) + c11 * si;
+  return c0 * (1 - sj) + c1 * sj;
+}
+
+/* zmath.cpp:238-252, 3-D linear interpolation with unit spacing. */
+static double interp3_tfm(const double* f, double x, double y, double z, int di, int dj,
+                          int dk) {
+  double ii = fmin(fmax(x / 1.0, 0), (di - 2)), jj = fmin(fmax(y / 1.0, 0), (dj - 2)),
+         kk = fmin(fmax(z / 1.0, 0), (dk - 2));
+  int i = (int)ii, j = (int)jj, k = (int)kk;
+  double si = ii - i, sj = jj - j, sk = kk - k;
+  long p = (long)di * dj;
+  double c000 = f[i + j * di + k * p], c100 = f[i + 1 + j * di + k * p];
+  double c010 = f[i + (j + 1) * di + k * p], c110 = f[i + 1 + (j + 1) * di + k * p];
+  double c001 = f[i + j * di + (k + 1) * p], c101 = f[i + 1 + j * di + (k + 1) * p];
+  double c011 = f[i + (j + 1) * di + (k + 1) * p], c111 = f[i + 1 + (j + 1) * di + (k + 1) * p];
+  double c00 = c000 * (1 - si) + c100 * si, c01 = c001 * (1 - si) + c101 * si;
+  double c10 = c010 * (1 - si) + c110 * si, c11 = c011 * (1 - si) + c111 * si;
+  double c0 = c00 * (1 - sj) + c10 * sj, c1 = c01 * (1 - sj) + c11 * sj;
+  return c0 * (1 - sk) + c1 * sk;
+}
+
+/* Depth (km) of grid point (i, j, k): c2g of TFM.cpp:56 through enu2geo of
+ * SET.cpp:86-99 (ECEF rotation about the reference, r by sqrtf).  g holds
+ * the reference-point terms: m[9], xr, yr, zr, then RC[3], RC[4], RC[5],
+ * RC[6]. */
+static double depth_tfm(const double* g, double i, double j, double k) {
+  const double* m = g;
+  double x = i * g[15] - g[12], y = j * g[15] - g[13], z = k * g[15] - g[14];
+  double xi = m[0] * x + m[1] * y + m[2] * z + g[9];
+  double yi = m[3] * x + m[4] * y + m[5] * z + g[10];
+  double zi = m[6] * x + m[7] * y + m[8] * z + g[11];
+  double r = sqrtf(xi * xi + yi * yi + zi * zi);
+  return 6371 - r;
+}
+
+/* The reference-point terms of enu2geo (SET.cpp:87-93) for RC. */
+void ora_density_geo(const double* rc, double* g) {
+  double rad = 57.295, R = 6371;
+  double lat_ref = rc[0], lon_ref = rc[1], d_ref = rc[2];
+  double phi = lat_ref / rad, theta = lon_ref / rad;
+  double m[9] = {-sin(theta), -sin(phi) * cos(theta), cos(phi) * cos(theta),
+                 cos(theta),  -sin(phi) * sin(theta), cos(phi) * sin(theta),
+                 0,           cos(phi),               sin(phi)};
+  for (int t = 0; t < 9; t++) g[t] = m[t];
+  g[9] = (R - d_ref) * cos(lon_ref / rad) * cos(lat_ref / rad);
+  g[10] = (R - d_ref) * sin(lon_ref / rad) * cos(lat_ref / rad);
+  g[11] = (R - d_ref) * sin(lat_ref / rad);
+  g[12] = rc[3];
+  g[13] = rc[4];
+  g[14] = rc[5];
+  g[15] = rc[6];
+}
+
+typedef struct {
+  int di, dj, dk, fh, fv, ii, jj;
+  double vm, ro, dr;
+  const double *sea, *M, *v, *geo;
+  double* drho;
+} dens_args;
+
+static void dens_rows(long lo, long hi, void* p) {
+  dens_args* a = (dens_args*)p;
+  const int fh = a->fh, fv = a->fv, ii = a->ii, jj = a->jj;
+  for (long n = lo; n < hi; n++) {
+    double i = (n % ii) / (1. * fh), j = ((n / ii) % jj) / (1. * fh),
+           k = (n / ((long)ii * jj)) / (1. * fv), li = 1. / fv, m0, m1, r0, r1;
+    m0 = interp2_tfm(a->sea, i, j, a->di, a->dj) - 3.5;
+    m1 = interp2_tfm(a->M, i, j, a->di, a->dj);
+    r0 = 0;
+    r1 = a->dr * (interp3_tfm(a->v, i, j, k, a->di, a->dj, a->dk) - a->vm);
+    if (k > m0 + li) {
+      r0 = a->ro;
+    } else if (fabs(k - m0) < li) {
+      r0 = r0 + (k - m0 + li) * (r0 + a->ro) / (2 * li);
+    }
+    if (k > m1 + li) {
+      r1 = a->ro;
+    } else if (fabs(k - m1) < li) {
+      r1 = r1 + (k - m1 + li) * (r1 + a->ro) / (2 * li);
+    }
+    a->drho[n] = (fabs(r0 - r1) > .001 && depth_tfm(a->geo, i, j, k) > 10) ? r1 - r0 : 0.0;
+  }
+}
+
+/* TFM.cpp:85-89: drho on the fine grid (zero where the node is not in nn). */
+void ora_density_tfm(int di, int dj, int dk, int fh, int fv, double vm, double ro, double dr,
+                     const double* rc, const double* sea, const double* M, const double* v,
+                     double* drho, int nthreads) {
+  double geo[16];
+  ora_density_geo(rc, geo);
+  dens_args a;
+  a.di = di; a.dj = dj; a.dk = dk; a.fh = fh; a.fv = fv;
+  a.ii = (di - 1) * fh + 1;
+  a.jj = (dj - 1) * fh + 1;
+  a.vm = vm; a.ro = ro; a.dr = dr;
+  a.sea = sea; a.M = M; a.v = v; a.geo = geo; a.drho = drho;
+  long N = (long)a.ii * a.jj * ((dk - 1) * fv + 1);
+  parallel_for(N, nthreads, dens_rows, &a);
+}

@@ -54,6 +54,12 @@ void ora_interface_adj(const double* imp, const double* depth,
                        const double* resid, double G, double* g_rho,
                        double* g_depth, int nthreads);
 
+/* density builder (TFM.cpp:85-89); rc is TFM's RC (TFM.cpp:218) */
+void ora_density_geo(const double* rc, double* geo16);
+void ora_density_tfm(int di, int dj, int dk, int fh, int fv, double vm, double ro, double dr,
+                     const double* rc, const double* sea, const double* M, const double* v,
+                     double* drho, int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -63,3 +63,19 @@ def awkward_stations(mesh, n_random=40, seed=1):
     zs = rng.uniform(zt + 1.0, zt + 3000.0, n_random)
     st += list(zip(xs, ys, zs))
     return np.array(st, dtype=np.float64)
+
+
+def tfm_density_inputs(di=61, dj=61, dk=33, seed=0):
+    """Synthetic inputs of the density builder shaped like TFM's: RC as
+    TFM.cpp:218 builds it (h = 10 km), sea level near the top of the grid,
+    a Moho about 35 km below it with relief, and a velocity field around
+    the mantle velocity (crust slower)."""
+    rng = np.random.default_rng(seed)
+    h = 10.0
+    rc = [-15.25, -72.5, (dk - 3) * h / 2 - 5, (di - 1) * h / 2, (dj - 1) * h / 2,
+          (dk - 1) * h / 2, h, float(di), float(dj), float(dk)]
+    X, Y = np.meshgrid(np.arange(di), np.arange(dj), indexing="xy")
+    sea = (dk - 3) - 0.02 * ((X - di / 2) ** 2 + (Y - dj / 2) ** 2) / di + 0.05 * rng.random((dj, di))
+    M = sea - 3.5 + 0.8 * np.sin(X / 7.0) * np.cos(Y / 5.0) + 0.1 * rng.random((dj, di))
+    v = 8.0 + 0.3 * rng.standard_normal((dk, dj, di))
+    return rc, sea.ravel(), M.ravel(), v.ravel()

@@ -222,3 +222,28 @@ def test_interface_adjoint_against_central_differences():
         e[c] = 1.0
         fd = (misfit(depth, rho + e) - misfit(depth, rho - e)) / 2.0
         assert g_rho[c] == pytest.approx(fd, rel=1e-6)
+
+
+# ---- density builder (TFM.cpp:85-89) ---------------------------------------
+def test_density_builder_by_hand():
+    from helpers import tfm_density_inputs
+    rc, sea, M, v = tfm_density_inputs(21, 19, 13, seed=1)
+    di, dj, dk, fh, fv = 21, 19, 13, 1, 2
+    vm, ro, dr = 8.0, -0.4, 0.3
+    d = oracle.density_tfm(di, dj, dk, fh, fv, vm, ro, dr, rc, sea, M, v)
+    ii, jj, kk = di, dj, (dk - 1) * fv + 1
+    assert d.size == ii * jj * kk
+    # a node far above both Mohos: r0 = r1 = ro -> not selected
+    n_top = 5 + 7 * ii + (kk - 1) * ii * jj
+    assert d[n_top] == 0.0
+    # a node between the two Mohos is selected when deep enough and the
+    # contrast exceeds 0.001
+    sel = np.count_nonzero(d)
+    assert 0 < sel < d.size
+    # by hand for one node below both Mohos: r0 = 0, r1 = dr*(v-vm)
+    i, j, kf = 10, 9, 4  # k = 2.0 grid units, far below the Moho (~6.5)
+    n = i + j * ii + kf * ii * jj
+    k = kf / fv
+    vv = v.reshape(dk, dj, di)[int(k), j, i]  # k integer: the node value itself
+    r1 = dr * (vv - vm)
+    assert d[n] == (r1 if abs(r1) > 0.001 else 0.0)

@@ -30,7 +30,7 @@ EXPORTS = (
     "ztm_gfm_pointmass", "ztm_gfm_prism", "ztm_gfm_prism_list", "ztm_gfm_adjoint",
     "ztm_gfm_interface", "ztm_gfm_interface_adjoint", "ztm_gfm_interface_misfit",
     "ztm_gfm_batch", "ztm_ctx_profile", "ztm_ctx_profile_read", "ztm_measure_peak",
-    "ztm_invert_interface", "ztm_gfm_pointmass_noalloc",
+    "ztm_invert_interface", "ztm_gfm_pointmass_noalloc", "ztm_density_build",
 )
 
 
@@ -57,6 +57,12 @@ class Opts(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("flags", ctypes.c_int),
                 ("G", ctypes.c_double), ("near_q", ctypes.c_double),
                 ("tile", ctypes.c_int), ("chunk", ctypes.c_int)]
+
+
+class DensityParams(ctypes.Structure):
+    _fields_ = [("di", ctypes.c_int), ("dj", ctypes.c_int), ("dk", ctypes.c_int),
+                ("fh", ctypes.c_int), ("fv", ctypes.c_int), ("vm", ctypes.c_double),
+                ("ro", ctypes.c_double), ("dr", ctypes.c_double), ("rc", ctypes.c_double * 10)]
 
 
 class Job(ctypes.Structure):
@@ -89,6 +95,8 @@ _SIGS = {
     "ztm_gfm_interface_misfit": (_I, [_P, ctypes.POINTER(IMesh), _P, _P, _I, _P, _P, _P, _P,
                                       _P, _P, ctypes.POINTER(Opts)]),
     "ztm_gfm_batch": (_I, [_P, ctypes.POINTER(Job), _I, ctypes.POINTER(Opts)]),
+    "ztm_density_build": (_I, [_P, ctypes.POINTER(DensityParams), _P, _P, _P, _P,
+                               ctypes.POINTER(_LL), _I]),
     "ztm_ctx_profile": (_I, [_P, _I]),
     "ztm_ctx_profile_read": (_I, [_P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double),
                                   ctypes.POINTER(_LL)]),

@@ -1,0 +1,185 @@
+// density.cu - the density-perturbation builder of TFM.cpp:83-89 on the GPU.
+//
+// For every fine-grid node the reference interpolates the IASP91 Moho
+// (sea-level map - 3.5), the rendered Moho M and the velocity field v
+// (zmath.cpp:225-252), ramps the crust/mantle contrast ro across one fine
+// cell around each Moho, scales the velocity perturbation by dr, and keeps
+// r1 - r0 where it exceeds 0.001 g/cc at depths below 10 km (c2g, TFM.cpp:56,
+// through enu2geo, SET.cpp:86-99).  Running it here leaves drho in device
+// memory for ztm_gfm_pointmass (ZTM_FLAG_DEVICE_PTRS) instead of building it
+// on one CPU thread and copying it in every forward.
+//
+// Same arithmetic as the reference, operation by operation: products and
+// sums are written with __dmul_rn / __dadd_rn so that nothing is contracted
+// into an FMA, the distance is taken with sqrtf as in SET.cpp:97, and the
+// reference-point trigonometry (cos/sin of the reference latitude and
+// longitude) is evaluated once on the host with the host's libm, as the
+// reference does.  One difference: the 2-D interpolation of the reference
+// reads one element past the row (or the array) at the last column/row with
+// weight 0; that index is clamped here.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "ztm_internal.cuh"
+
+namespace {
+
+struct DensGeo {
+  double m[9], xr, yr, zr, ox, oy, oz, h;
+};
+
+struct DensArgs {
+  int di, dj, dk, fh, fv, ii, jj;
+  long long N;
+  double vm, ro, dr;
+  DensGeo g;
+};
+
+__device__ __forceinline__ double lerp_rn(double a, double b, double s) {
+  // a*(1-s) + b*s without contraction
+  return __dadd_rn(__dmul_rn(a, __dadd_rn(1.0, -s)), __dmul_rn(b, s));
+}
+
+__device__ double interp2_dev(const double* __restrict__ f, double x, double y, int di, int dj) {
+  const double ii = fmin(fmax(x, 0.0), (double)(di - 1)), jj = fmin(fmax(y, 0.0), (double)(dj - 1));
+  const int i = (int)ii, j = (int)jj;
+  const double si = ii - i, sj = jj - j;
+  const int i1 = i + 1 < di ? i + 1 : i, j1 = j + 1 < dj ? j + 1 : j;
+  const double c0 = lerp_rn(f[i + j * di], f[i1 + j * di], si);
+  const double c1 = lerp_rn(f[i + j1 * di], f[i1 + j1 * di], si);
+  return lerp_rn(c0, c1, sj);
+}
+
+__device__ double interp3_dev(const double* __restrict__ f, double x, double y, double z, int di,
+                              int dj, int dk) {
+  const double ii = fmin(fmax(x, 0.0), (double)(di - 2)), jj = fmin(fmax(y, 0.0), (double)(dj - 2)),
+               kk = fmin(fmax(z, 0.0), (double)(dk - 2));
+  const int i = (int)ii, j = (int)jj, k = (int)kk;
+  const double si = ii - i, sj = jj - j, sk = kk - k;
+  const long long p = (long long)di * dj;
+  auto F = [&](int a, int b, int c) { return f[(i + a) + (long long)(j + b) * di + (k + c) * p]; };
+  const double c00 = lerp_rn(F(0, 0, 0), F(1, 0, 0), si), c01 = lerp_rn(F(0, 0, 1), F(1, 0, 1), si);
+  const double c10 = lerp_rn(F(0, 1, 0), F(1, 1, 0), si), c11 = lerp_rn(F(0, 1, 1), F(1, 1, 1), si);
+  const double c0 = lerp_rn(c00, c10, sj), c1 = lerp_rn(c01, c11, sj);
+  return lerp_rn(c0, c1, sk);
+}
+
+__device__ double depth_dev(const DensGeo& g, double i, double j, double k) {
+  const double x = __dadd_rn(__dmul_rn(i, g.h), -g.ox);
+  const double y = __dadd_rn(__dmul_rn(j, g.h), -g.oy);
+  const double z = __dadd_rn(__dmul_rn(k, g.h), -g.oz);
+  auto row = [&](int r, double o) {
+    return __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(g.m[3 * r], x), __dmul_rn(g.m[3 * r + 1], y)),
+                               __dmul_rn(g.m[3 * r + 2], z)),
+                     o);
+  };
+  const double xi = row(0, g.xr), yi = row(1, g.yr), zi = row(2, g.zr);
+  const double s2 = __dadd_rn(__dadd_rn(__dmul_rn(xi, xi), __dmul_rn(yi, yi)), __dmul_rn(zi, zi));
+  const float r = sqrtf((float)s2);
+  return 6371.0 - (double)r;
+}
+
+__device__ double ramp(double r, double k, double m, double li, double ro) {
+  // if k > m+li: ro;  else if |k-m| < li: r + (k-m+li)*(r+ro)/(2*li)
+  if (k > __dadd_rn(m, li)) return ro;
+  const double d = __dadd_rn(k, -m);
+  if (fabs(d) < li) return __dadd_rn(r, __dmul_rn(__dadd_rn(d, li), __dadd_rn(r, ro)) / (2 * li));
+  return r;
+}
+
+__global__ void density_kernel(DensArgs a, const double* __restrict__ sea,
+                               const double* __restrict__ M, const double* __restrict__ v,
+                               double* __restrict__ drho, unsigned long long* __restrict__ count) {
+  const long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  bool sel = false;
+  if (n < a.N) {
+    const double i = (n % a.ii) / (1. * a.fh), j = ((n / a.ii) % a.jj) / (1. * a.fh),
+                 k = (n / ((long long)a.ii * a.jj)) / (1. * a.fv), li = 1. / a.fv;
+    const double m0 = __dadd_rn(interp2_dev(sea, i, j, a.di, a.dj), -3.5);
+    const double m1 = interp2_dev(M, i, j, a.di, a.dj);
+    const double r0 = ramp(0.0, k, m0, li, a.ro);
+    const double r1 = ramp(__dmul_rn(a.dr, __dadd_rn(interp3_dev(v, i, j, k, a.di, a.dj, a.dk), -a.vm)),
+                           k, m1, li, a.ro);
+    const double d = __dadd_rn(r1, -r0);
+    sel = fabs(__dadd_rn(r0, -r1)) > .001 && depth_dev(a.g, i, j, k) > 10;
+    drho[n] = sel ? d : 0.0;
+  }
+  const unsigned b = __ballot_sync(0xffffffffu, sel);
+  if ((threadIdx.x & 31) == 0 && b) atomicAdd(count, (unsigned long long)__popc(b));
+}
+
+}  // namespace
+
+extern "C" int ztm_density_build(ztm_ctx* c, const ztm_density_params* p, const double* sea,
+                                 const double* M, const double* v, double* drho,
+                                 long long* n_selected, int flags) {
+  if (!c) return ZTM_ERR_ARG;
+  c->err.clear();
+  if (!p || !sea || !M || !v || !drho) return ztm_fail(c, ZTM_ERR_ARG, "null argument");
+  if (flags & ~ZTM_FLAG_DEVICE_PTRS) return ztm_fail(c, ZTM_ERR_ARG, "unknown flag");
+  if (p->di < 2 || p->dj < 2 || p->dk < 2 || p->fh < 1 || p->fv < 1)
+    return ztm_fail(c, ZTM_ERR_ARG, "grid dims must be >= 2 and refinements >= 1");
+  const bool dev = (flags & ZTM_FLAG_DEVICE_PTRS) != 0;
+  DensArgs a;
+  a.di = p->di; a.dj = p->dj; a.dk = p->dk; a.fh = p->fh; a.fv = p->fv;
+  a.ii = (p->di - 1) * p->fh + 1;
+  a.jj = (p->dj - 1) * p->fh + 1;
+  a.N = (long long)a.ii * a.jj * ((p->dk - 1) * p->fv + 1);
+  if (a.N > (1LL << 31) - 1) return ztm_fail(c, ZTM_ERR_RANGE, "fine grid exceeds 2^31-1 nodes");
+  a.vm = p->vm; a.ro = p->ro; a.dr = p->dr;
+  // enu2geo's reference-point terms (SET.cpp:87-93), host libm as in the reference
+  const double rad = 57.295, R = 6371;
+  const double* rc = p->rc;
+  const double phi = rc[0] / rad, theta = rc[1] / rad;
+  const double m[9] = {-sin(theta), -sin(phi) * cos(theta), cos(phi) * cos(theta),
+                       cos(theta),  -sin(phi) * sin(theta), cos(phi) * sin(theta),
+                       0,           cos(phi),               sin(phi)};
+  for (int t = 0; t < 9; t++) a.g.m[t] = m[t];
+  a.g.xr = (R - rc[2]) * cos(rc[1] / rad) * cos(rc[0] / rad);
+  a.g.yr = (R - rc[2]) * sin(rc[1] / rad) * cos(rc[0] / rad);
+  a.g.zr = (R - rc[2]) * sin(rc[0] / rad);
+  a.g.ox = rc[3]; a.g.oy = rc[4]; a.g.oz = rc[5]; a.g.h = rc[6];
+  int prev = -1;
+  cudaGetDevice(&prev);
+  if (prev != c->device) cudaSetDevice(c->device);
+  struct Restore {
+    int p, d;
+    ~Restore() {
+      if (p >= 0 && p != d) cudaSetDevice(p);
+    }
+  } restore{prev, c->device};
+  const size_t M2 = (size_t)p->di * p->dj, M3 = M2 * p->dk;
+  size_t need = 2 * WsCarver::need(M2 * 8) + WsCarver::need(M3 * 8) + WsCarver::need(a.N * 8) +
+                WsCarver::need(8) + 4096;
+  int rc2 = ztm_ws_reserve(c, need);
+  if (rc2) return rc2;
+  WsCarver wc(c->ws);
+  double* s_sea = wc.take<double>(M2);
+  double* s_M = wc.take<double>(M2);
+  double* s_v = wc.take<double>(M3);
+  double* s_d = wc.take<double>(a.N);
+  unsigned long long* cnt = wc.take<unsigned long long>(1);
+  const void *ps, *pm, *pv;
+  if ((rc2 = ztm_stage_in(c, sea, M2 * 8, dev, s_sea, &ps))) return rc2;
+  if ((rc2 = ztm_stage_in(c, M, M2 * 8, dev, s_M, &pm))) return rc2;
+  if ((rc2 = ztm_stage_in(c, v, M3 * 8, dev, s_v, &pv))) return rc2;
+  double* out = dev ? drho : s_d;
+  cudaMemsetAsync(cnt, 0, 8, c->stream);
+  {
+    ZtmProf prof_(c, "density");
+    density_kernel<<<(unsigned)((a.N + 255) / 256), 256, 0, c->stream>>>(
+        a, (const double*)ps, (const double*)pm, (const double*)pv, out, cnt);
+  }
+  c->launches++;
+  if ((rc2 = ztm_after_launch(c, "density builder"))) return rc2;
+  if (!dev) {
+    unsigned long long h = 0;
+    cudaMemcpyAsync(drho, s_d, a.N * 8, cudaMemcpyDeviceToHost, c->stream);
+    cudaMemcpyAsync(&h, cnt, 8, cudaMemcpyDeviceToHost, c->stream);
+    if ((rc2 = ztm_cuda_check(c, cudaStreamSynchronize(c->stream), "density builder"))) return rc2;
+    if (n_selected) *n_selected = (long long)h;
+  } else if (n_selected) {
+    *n_selected = -1;  // not waited for with device pointers
+  }
+  return ZTM_OK;
+}

@@ -190,6 +190,22 @@ class GravityContext:
                                                 prec, a.flags))
         return out
 
+    # -- density builder (TFM.cpp:83-89) -------------------------------
+    def density(self, di, dj, dk, sea, M, v, vm, ro, dr, rc, fh=1, fv=2):
+        """drho on the fine grid from the sea-level map, rendered Moho and
+        velocity grids; returns (drho, number of selected nodes or -1)."""
+        p = _lib.DensityParams(di, dj, dk, fh, fv, vm, ro, dr, (ctypes.c_double * 10)(*rc))
+        N = ((di - 1) * fh + 1) * ((dj - 1) * fh + 1) * ((dk - 1) * fv + 1)
+        a = _Args()
+        ps = a.arr(sea, di * dj, name="sea")
+        pm = a.arr(M, di * dj, name="M")
+        pv = a.arr(v, di * dj * dk, name="v")
+        out, po = a.out(N, sea)
+        n = ctypes.c_longlong(0)
+        self._check(self._lib.ztm_density_build(self._h, ctypes.byref(p), ps, pm, pv, po,
+                                                ctypes.byref(n), a.flags))
+        return out, n.value
+
     # -- prism mesh -----------------------------------------------------
     def prism(self, mesh, rho, stations, precision="mixed", G=None, near_q=None, tile=0, chunk=0,
               autotune=False):
