@@ -132,3 +132,14 @@ def test_autotuned_shape_gives_the_same_field(ctx):
     b = ctx.prism(mesh, rho, st, precision="mixed", autotune=True)  # cached shape
     assert np.array_equal(a, b)
     assert rel_err(a, ref) <= 1e-7  # only the summation grouping differs
+
+
+def test_config1_full_size_vs_oracle(ctx):
+    """Config 1 (64x64x32 prisms of 2x2x1 km, 32x32 stations at +100 m):
+    the plain double kernel and the mixed kernel against the CPU oracle on
+    every station."""
+    from ztm_gb300 import synth
+    mesh, rho, st = synth.config1()
+    ref = oracle.prism_mesh(mesh, rho, st)
+    assert rel_err(ctx.prism(mesh, rho, st, precision="fp64"), ref) <= TOL64
+    assert rel_err(ctx.prism(mesh, rho, st, precision="mixed"), ref) <= TOLMIX

@@ -57,6 +57,8 @@ struct BArgs {
   long long n_near, n_items;
   int* counter;
   int* err;
+  double* phi;   // [block][warp][phi_cap] near-box vertex values (global scratch)
+  int phi_cap;
 };
 
 // tile completion: the last item of a tile writes gz for its stations
@@ -78,9 +80,9 @@ __device__ void tile_done(const BJob& J, int tile, int expected, int* s_flag) {
   }
 }
 
-__device__ void near_item(const BJob& J, int tile, double* phi_all) {
+__device__ void near_item(const BJob& J, int tile, double* phi_all, int phi_cap) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  double* phi = phi_all + (size_t)warp * J.nv_cap;
+  double* phi = phi_all + (size_t)warp * phi_cap;
   const MeshDesc& m = J.m;
   const long long plane = (long long)m.nx * m.ny;
   const long long np = plane * m.nz;
@@ -126,7 +128,7 @@ __device__ void near_item(const BJob& J, int tile, double* phi_all) {
   }
 }
 
-__global__ void __launch_bounds__(B_TS) batch_kernel(BArgs a) {
+__global__ void __launch_bounds__(B_TS, 5) batch_kernel(BArgs a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
   float* stage = reinterpret_cast<float*>(smem_raw + 128);
@@ -151,7 +153,7 @@ __global__ void __launch_bounds__(B_TS) batch_kernel(BArgs a) {
       while (j + 1 < a.njobs && a.jobs[j + 1].near_base <= item) j++;
       const BJob& J = a.jobs[j];
       const int tile = (int)(item - J.near_base);
-      near_item(J, tile, phi);
+      near_item(J, tile, phi, a.phi_cap);
       __syncthreads();
       tile_done(J, tile, J.chunks * J.mgroups + 1, &s_flag);
       continue;
@@ -224,33 +226,34 @@ __global__ void __launch_bounds__(B_TS) batch_kernel(BArgs a) {
           const unsigned espan = ncl ? (unsigned)(nb.l1 - nb.l0) : 0u;
           const float* col = rs + q * k.nzp;
           const int mstride = J.sc * k.nzp;
+          const ColPoly2 cp2 = col_poly2(cp, fc.a1);
+          const float2 dz2 = make_float2(k.dzn, k.dzn);
           float zf = (float)(-izs);  // (l0 - izs), exact, stepped by 8
           for (int l0 = 0; l0 < k.nz; l0 += 8, zf += 8.f) {
             const float Zg = fmaf(zf, k.dzn, ez);
-            float K[8];
+            const float2 zg2 = make_float2(Zg, Zg);
+            float2 K2[4];  // kernel values of layers (l0+2j, l0+2j+1)
 #pragma unroll
-            for (int j = 0; j < 8; j++) {
-              const int l = l0 + j;
-              const float v = far_unit(fmaf((float)j, k.dzn, Zg), cp, fc.a1);
-              const bool excl = (l < Lm && (unsigned)(l - elo) <= espan) || l >= k.nz;
-              K[j] = excl ? 0.f : v;  // select: a NaN at a box prism is dropped
+            for (int j = 0; j < 4; j++) {
+              K2[j] = far_unit2(__ffma2_rn(make_float2((float)(2 * j), (float)(2 * j + 1)), dz2, zg2),
+                                cp2);
+              const int la = l0 + 2 * j, lb = la + 1;
+              // select: a NaN at a box prism is dropped
+              if ((la < Lm && (unsigned)(la - elo) <= espan) || la >= k.nz) K2[j].x = 0.f;
+              if ((lb < Lm && (unsigned)(lb - elo) <= espan) || lb >= k.nz) K2[j].y = 0.f;
             }
-            // one kernel value per pair, applied to every model of the group;
-            // plain sums over 8 layers, compensated across groups
+            // one kernel value per pair applied to every model of the group,
+            // packed over layer pairs; plain over 8 layers, compensated across
 #pragma unroll
             for (int md = 0; md < B_MG; md++) {
               if (md < mcnt) {
                 const float4 ra = *reinterpret_cast<const float4*>(col + md * mstride + l0);
                 const float4 rb = *reinterpret_cast<const float4*>(col + md * mstride + l0 + 4);
-                float g = K[0] * ra.x;
-                g = fmaf(K[1], ra.y, g);
-                g = fmaf(K[2], ra.z, g);
-                g = fmaf(K[3], ra.w, g);
-                g = fmaf(K[4], rb.x, g);
-                g = fmaf(K[5], rb.y, g);
-                g = fmaf(K[6], rb.z, g);
-                g = fmaf(K[7], rb.w, g);
-                acc[md].add(g);
+                float2 g = __fmul2_rn(K2[0], make_float2(ra.x, ra.y));
+                g = __ffma2_rn(K2[1], make_float2(ra.z, ra.w), g);
+                g = __ffma2_rn(K2[2], make_float2(rb.x, rb.y), g);
+                g = __ffma2_rn(K2[3], make_float2(rb.z, rb.w), g);
+                acc[md].add(g.x + g.y);
               }
             }
           }
@@ -281,6 +284,7 @@ struct Plan {
   long long n_near = 0, n_items = 0;
   size_t smem = 128;
   size_t ws_bytes = 0;
+  int phi_cap = 0;
 };
 
 // Shapes only (no pointers): per-job tiles, chunks, stage widths, workspace.
@@ -300,7 +304,7 @@ Plan plan(const ztm_job* jobs, int njobs, double near_q, int num_sms) {
     J.ns = q.ns;
     J.tiles = std::max(1, (q.ns + B_TS - 1) / B_TS);
     J.mgroups = (q.nmodels + B_MG - 1) / B_MG;
-    int sc = std::max(1, (24 * 1024) / (J.k.nzp * 4 * B_MG));
+    int sc = std::max(1, (16 * 1024) / (J.k.nzp * 4 * B_MG));
     sc = std::min(sc, 32);
     J.sc = sc;
     // aim for ~16 items per SM over the whole batch: split columns so that a
@@ -317,7 +321,7 @@ Plan plan(const ztm_job* jobs, int njobs, double near_q, int num_sms) {
                (std::min(2 * J.k.wl + 1, m.nz) + 1);
     J.far_scale = J.k.L0 * (double)J.k.dxn * J.k.dyn * J.k.dzn;
     p.smem = std::max(p.smem, 128 + (size_t)2 * sc * J.k.nzp * 4 * B_MG);
-    p.smem = std::max(p.smem, 128 + (size_t)B_WARPS * J.nv_cap * 8);
+    p.phi_cap = std::max(p.phi_cap, J.nv_cap);
     ws += WsCarver::need((size_t)q.nmodels * J.k.ncols * J.k.nzp * 4);
     ws += WsCarver::need((size_t)q.ns * 16) * 2;
     ws += WsCarver::need((size_t)q.nmodels * J.chunks * q.ns * 8);
@@ -391,11 +395,20 @@ extern "C" int ztm_gfm_batch(ztm_ctx* c, const ztm_job* jobs, int njobs, const z
                      WsCarver::need((size_t)q.ns * 24) +
                      WsCarver::need((size_t)q.nmodels * q.ns * 8);
     }
-  int rc = ztm_ws_reserve(c, p.ws_bytes + stage_bytes + 8192);
+  // persistent grid: as many blocks as fit on the device at once
+  cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)std::max<size_t>(p.smem, 48 * 1024));
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, B_TS, p.smem);
+  per_sm = std::max(1, per_sm);
+  const long long grid = std::min<long long>((long long)per_sm * c->num_sms, p.n_items);
+  const size_t phi_elems = (size_t)grid * B_WARPS * std::max(p.phi_cap, 1);
+  int rc = ztm_ws_reserve(c, p.ws_bytes + stage_bytes + WsCarver::need(phi_elems * 8) + 8192);
   if (rc) return rc;
   WsCarver wc(c->ws);
   int* counter = wc.take<int>(16);
   BJob* d_jobs = wc.take<BJob>(njobs);
+  double* phi = wc.take<double>(phi_elems);
   std::vector<const double*> rho_d(njobs), xyz_d(njobs);
   std::vector<double*> gz_d(njobs);
   for (int j = 0; j < njobs; j++) {
@@ -465,13 +478,9 @@ extern "C" int ztm_gfm_batch(ztm_ctx* c, const ztm_job* jobs, int njobs, const z
       destroy_entry(c->graphs.front());
       c->graphs.erase(c->graphs.begin());
     }
-    cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)std::max<size_t>(p.smem, 48 * 1024));
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, B_TS, p.smem);
-    per_sm = std::max(1, per_sm);
-    long long grid = std::min<long long>((long long)per_sm * c->num_sms, p.n_items);
     BArgs args;
+    args.phi = phi;
+    args.phi_cap = std::max(p.phi_cap, 1);
     args.jobs = d_jobs;
     args.njobs = njobs;
     args.n_near = p.n_near;

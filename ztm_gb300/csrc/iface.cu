@@ -75,7 +75,10 @@ IConst make_iconst(const IMeshDesc& m, double near_q) {
   int w = (int)ceil(near_q * ellh / std::min(m.dx, m.dy) - 0.5);
   k.w = std::max(w, 0);
   k.words = ((2 * k.w + 1) * (2 * k.w + 1) + 31) / 32;
-  k.near_h = near_q * ellh;
+  // vertically the column's top face is what the station sees first; its
+  // face term converges more slowly than the column's, so keep columns in
+  // double until the station is twice as far above the top
+  k.near_h = 2.0 * near_q * ellh;
   return k;
 }
 
@@ -112,10 +115,11 @@ __global__ void iface_col_prep(IMeshDesc m, double L0, const double* __restrict_
 }
 
 // Near columns of a station: inside the (2w+1)^2 window around its home
-// column (clamped to the mesh) AND with the station less than near_h above
-// the column's top.  Outside the window the horizontal distance alone is
-// >= near_q half-diagonals; inside it, a station that high above the top is
-// as far from every point of the column.  The window slot of (ix, iy):
+// column (clamped to the mesh) AND with the station less than near_h
+// (2 near_q half-diagonals) above the column's top.  Outside the window the
+// horizontal distance alone is >= near_q half-diagonals; inside it, a station
+// that high above the top is at least as far from every point of the column.
+// The window slot of (ix, iy):
 __device__ __forceinline__ bool window_slot(int ixs, int iys, int ix, int iy, const IConst& k,
                                             int* slot) {
   const int cx = clampi(ixs, 0, k.nx - 1), cy = clampi(iys, 0, k.ny - 1);

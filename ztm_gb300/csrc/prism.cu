@@ -146,7 +146,7 @@ __device__ __forceinline__ float far_pair(float rho, float Z, float rh, float a0
   return fmaf(base, t, base);
 }
 
-__global__ void __launch_bounds__(FAR_TS, 10) far_kernel(FarArgs a) {
+__global__ void __launch_bounds__(FAR_TS, 9) far_kernel(FarArgs a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
   float* stage = reinterpret_cast<float*>(smem_raw + 128);
@@ -221,6 +221,9 @@ __global__ void __launch_bounds__(FAR_TS, 10) far_kernel(FarArgs a) {
         // a column lies in some lane's near box only near the warp's
         // stations: test that once per column for the whole warp
         const bool warp_near = __any_sync(0xffffffffu, ncl);
+        // every lane of the warp far enough for the second-order form
+        const bool warp_t2 = __all_sync(0xffffffffu, cp.rh >= k.rh_t2);
+        const float2 c2t = make_float2(cp.C2 - fc.h2, cp.C2 - fc.h2);
         float zf = (float)(-izs);  // (l0 - izs), exact in float, stepped by 8
         for (int l0 = 0; l0 < k.nz; l0 += 8, zf += 8.f) {
           const float4 ra = *reinterpret_cast<const float4*>(col + l0);
@@ -232,8 +235,13 @@ __global__ void __launch_bounds__(FAR_TS, 10) far_kernel(FarArgs a) {
           for (int j = 0; j < 4; j++)
             Zj[j] = __ffma2_rn(make_float2((float)(2 * j), (float)(2 * j + 1)), dz2, zg2);
           float2 v[4];
+          if (warp_t2) {
 #pragma unroll
-          for (int j = 0; j < 4; j++) v[j] = far_unit2(Zj[j], cp2);
+            for (int j = 0; j < 4; j++) v[j] = far_unit2_t2(Zj[j], cp2, c2t);
+          } else {
+#pragma unroll
+            for (int j = 0; j < 4; j++) v[j] = far_unit2(Zj[j], cp2);
+          }
           if ((warp_near && l0 < Lm) || l0 + 8 > k.nz) {  // warp-uniform
 #pragma unroll
             for (int j = 0; j < 4; j++) {
@@ -422,9 +430,9 @@ struct FarShape {
 };
 
 // Launch shape of the far kernel: bps blocks per SM wanted (a full wave is
-// 10 at 47 registers), sc columns per shared-memory stage (0 = as many as fit
+// 9 at <= 56 registers), sc columns per shared-memory stage (0 = as many as fit
 // 24 KB).
-FarShape far_shape(const MeshConst& k, int ns, int num_sms, const ztm_opts* o, int bps = 10,
+FarShape far_shape(const MeshConst& k, int ns, int num_sms, const ztm_opts* o, int bps = 9,
                    int sc_want = 0) {
   FarShape f;
   f.tiles = std::max(1, (ns + FAR_TS - 1) / FAR_TS);
@@ -474,6 +482,8 @@ MeshConst make_mesh_const(const MeshDesc& m, double near_q) {
   k.dyn = (float)(m.dy / k.L0);
   k.dzn = (float)(m.dz / k.L0);
   k.fc = far_coef(m.dx / k.L0, m.dy / k.L0, m.dz / k.L0);
+  const double ell = 0.5 * sqrt(m.dx * m.dx + m.dy * m.dy + m.dz * m.dz) / k.L0;
+  k.rh_t2 = (float)((48.0 * ell) * (48.0 * ell));
   return k;
 }
 
@@ -521,7 +531,7 @@ size_t ztm_prism_ws(const MeshDesc& m, int ns, int precision, int num_sms, const
   double nq = (o && o->near_q > 0) ? o->near_q : 6.0;
   MeshConst k = make_mesh_const(m, nq);
   int chunks = 0;
-  for (int bps : {5, 10, 20}) chunks = std::max(chunks, far_shape(k, ns, num_sms, o, bps, 8).chunks);
+  for (int bps : {5, 9, 18}) chunks = std::max(chunks, far_shape(k, ns, num_sms, o, bps, 8).chunks);
   chunks = std::max(chunks, far_shape(k, ns, num_sms, o).chunks);
   return WsCarver::need((size_t)k.ncols * k.nzp * 4) + WsCarver::need((size_t)ns * 16) * 2 +
          WsCarver::need((size_t)ns * 8) + WsCarver::need((size_t)chunks * ns * 8);
@@ -548,7 +558,7 @@ int ztm_launch_prism(ztm_ctx* c, const MeshDesc& m, const double* d_rho, int ns,
   }
   const double nq = (o && o->near_q > 0) ? o->near_q : 6.0;
   MeshConst k = make_mesh_const(m, nq);
-  int bps = 10, scw = 0;
+  int bps = 9, scw = 0;
   auto it = c->tuned.find(tune_key(k, ns));
   if (it != c->tuned.end()) {
     bps = it->second[0];
@@ -559,7 +569,7 @@ int ztm_launch_prism(ztm_ctx* c, const MeshDesc& m, const double* d_rho, int ns,
   int4* si = wc.take<int4>(ns);
   double* near = wc.take<double>(ns);
   int max_chunks = 0;
-  for (int b : {5, 10, 20}) max_chunks = std::max(max_chunks, far_shape(k, ns, c->num_sms, o, b, 8).chunks);
+  for (int b : {5, 9, 18}) max_chunks = std::max(max_chunks, far_shape(k, ns, c->num_sms, o, b, 8).chunks);
   max_chunks = std::max(max_chunks, far_shape(k, ns, c->num_sms, o).chunks);
   double* partial = wc.take<double>((size_t)max_chunks * ns);
   launch_mesh_transpose(c, k, 1, d_rho, rhoT);
@@ -573,7 +583,7 @@ int ztm_launch_prism(ztm_ctx* c, const MeshDesc& m, const double* d_rho, int ns,
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     float best = 1e30f;
-    for (int b : {5, 10, 20})
+    for (int b : {5, 9, 18})
       for (int w : {8, 16, 0}) {
         FarShape t = far_shape(k, ns, c->num_sms, o, b, w);
         a.chunk_cols = t.chunk_cols;

@@ -110,12 +110,26 @@ __device__ __forceinline__ float2 far_unit2(float2 Z, const ColPoly2& c) {
   return __fmul2_rn(__fmul2_rn(Z, s), __fmul2_rn(rinv, u));
 }
 
+// Second-order form for pairs at least 48 half-diagonals away (horizontal
+// distance alone): 1 + t2 = 1 + u (a1 + u C2t), C2t = a0 - a1 rh.  The
+// dropped fourth-order term is below 2e-8 of the pair's monopole there.
+__device__ __forceinline__ float2 far_unit2_t2(float2 Z, const ColPoly2& c, float2 C2t) {
+  const float2 r2 = __ffma2_rn(Z, Z, c.rh);
+  const float2 rinv = make_float2(rsqrt_ftz(r2.x), rsqrt_ftz(r2.y));
+  const float2 u = __fmul2_rn(rinv, rinv);
+  const float2 p = __ffma2_rn(C2t, u, c.a1);
+  const float2 s = __ffma2_rn(p, u, make_float2(1.f, 1.f));
+  return __fmul2_rn(__fmul2_rn(Z, s), __fmul2_rn(rinv, u));
+}
+
 // Regular-mesh constants for the mixed kernels.
 struct MeshConst {
   int nx, ny, nz, nzp;  // nzp: layers padded to a multiple of 8
   int ncols;
   int wx, wy, wl;       // near-box half widths (columns, columns, layers)
   float dxn, dyn, dzn;  // cell edges / L0
+  float rh_t2;          // horizontal distance^2 (units of L0) beyond which
+                        // the second-order form is exact enough
   double L0;
   FarCoef fc;
 };
