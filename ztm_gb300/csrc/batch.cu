@@ -80,9 +80,13 @@ __device__ void tile_done(const BJob& J, int tile, int expected, int* s_flag) {
   }
 }
 
-__device__ void near_item(const BJob& J, int tile, double* phi_all, int phi_cap) {
+__device__ void near_item(const BJob& J, int tile, double* phi_all, int phi_cap, int* err) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double* phi = phi_all + (size_t)warp * phi_cap;
+  if (J.nv_cap > phi_cap) {  // the host sizes phi_cap as the largest nv_cap
+    if (threadIdx.x == 0) atomicOr(err, ZTM_DEVERR_BOUNDS);
+    return;
+  }
   const MeshDesc& m = J.m;
   const long long plane = (long long)m.nx * m.ny;
   const long long np = plane * m.nz;
@@ -132,7 +136,9 @@ __global__ void __launch_bounds__(B_TS, 5) batch_kernel(BArgs a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
   float* stage = reinterpret_cast<float*>(smem_raw + 128);
-  double* phi = reinterpret_cast<double*>(smem_raw + 128);
+  // near-box vertex values: this block's slice of the global scratch
+  // (grid x warps x phi_cap doubles, sized from the same grid on the host)
+  double* phi = a.phi + (size_t)blockIdx.x * B_WARPS * a.phi_cap;
   __shared__ long long s_item;
   __shared__ int s_flag, s_lm;
   if (threadIdx.x == 0) {
@@ -153,7 +159,7 @@ __global__ void __launch_bounds__(B_TS, 5) batch_kernel(BArgs a) {
       while (j + 1 < a.njobs && a.jobs[j + 1].near_base <= item) j++;
       const BJob& J = a.jobs[j];
       const int tile = (int)(item - J.near_base);
-      near_item(J, tile, phi, a.phi_cap);
+      near_item(J, tile, phi, a.phi_cap, a.err);
       __syncthreads();
       tile_done(J, tile, J.chunks * J.mgroups + 1, &s_flag);
       continue;
