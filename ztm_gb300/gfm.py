@@ -34,11 +34,22 @@ def _is_torch_cuda(x):
 
 
 class _Args:
-    """Collects array arguments of one call; all host or all device."""
+    """Collects array arguments of one call; all host or all device.
 
-    def __init__(self):
+    Device tensors are used by kernels queued on the context's stream after
+    the call returns; record_stream tells PyTorch's caching allocator not to
+    hand their memory to another tensor until that stream's work is done
+    (otherwise a temporary input freed right after the call could be
+    overwritten while a kernel still reads it)."""
+
+    def __init__(self, gctx=None):
         self.device = None
         self.keep = []
+        self.gctx = gctx
+
+    def _record(self, t):
+        if self.gctx is not None:
+            t.record_stream(self.gctx._torch_stream())
 
     def _kind(self, dev):
         if self.device is None:
@@ -60,6 +71,7 @@ class _Args:
                 raise ValueError("%s has %d elements, expected %d" % (name, x.numel(), n))
             self._kind(True)
             self.keep.append(x)
+            self._record(x)
             return ctypes.c_void_p(x.data_ptr())
         a = np.ascontiguousarray(x, dtype=dtype)
         if n is not None and a.size != n:
@@ -73,6 +85,7 @@ class _Args:
             import torch
             t = torch.empty(n, dtype=torch.float64, device=like.device if like is not None else "cuda")
             self.keep.append(t)
+            self._record(t)
             return t, ctypes.c_void_p(t.data_ptr())
         a = np.empty(n, dtype=np.float64)
         self.keep.append(a)
@@ -113,6 +126,7 @@ class GravityContext:
             raise GravityError(rc, "context creation failed on device %d" % device)
         self._h = h
         self.device = device
+        self._tstream = None
 
     # -- lifetime ------------------------------------------------------
     def close(self):
@@ -143,6 +157,14 @@ class GravityContext:
 
     def set_stream(self, stream_ptr):
         self._check(self._lib.ztm_ctx_set_stream(self._h, ctypes.c_void_p(stream_ptr or 0)))
+        self._tstream = None
+
+    def _torch_stream(self):
+        """The context's stream as a torch stream object (for record_stream)."""
+        if self._tstream is None:
+            import torch
+            self._tstream = torch.cuda.ExternalStream(self.stream, device=self.device)
+        return self._tstream
 
     def launches(self):
         return int(self._lib.ztm_ctx_launches(self._h))
@@ -177,7 +199,7 @@ class GravityContext:
         ii = (grid.di - 1) * grid.fh + 1
         jj = (grid.dj - 1) * grid.fh + 1
         kk = (grid.dk - 1) * grid.fv + 1
-        a = _Args()
+        a = _Args(self)
         pd = a.arr(drho, ii * jj * kk, name="drho")
         ps = a.arr(surf, grid.di * grid.dj, name="surf")
         pn, n_nn = None, 0
@@ -196,7 +218,7 @@ class GravityContext:
         velocity grids; returns (drho, number of selected nodes or -1)."""
         p = _lib.DensityParams(di, dj, dk, fh, fv, vm, ro, dr, (ctypes.c_double * 10)(*rc))
         N = ((di - 1) * fh + 1) * ((dj - 1) * fh + 1) * ((dk - 1) * fv + 1)
-        a = _Args()
+        a = _Args(self)
         ps = a.arr(sea, di * dj, name="sea")
         pm = a.arr(M, di * dj, name="M")
         pv = a.arr(v, di * dj * dk, name="v")
@@ -210,7 +232,7 @@ class GravityContext:
     def prism(self, mesh, rho, stations, precision="mixed", G=None, near_q=None, tile=0, chunk=0,
               autotune=False):
         np_ = mesh.nx * mesh.ny * mesh.nz
-        a = _Args()
+        a = _Args(self)
         pr = a.arr(rho, np_, name="rho")
         ns = _nstations(stations)
         px = a.arr(stations, 3 * ns, name="stations")
@@ -222,7 +244,7 @@ class GravityContext:
 
     def prism_list(self, geom, rho, stations, precision="fp64", G=None, near_q=None):
         n = _nstations_list(geom)
-        a = _Args()
+        a = _Args(self)
         pg = a.arr(geom, 6 * n, name="geom")
         pr = a.arr(rho, n, name="rho")
         ns = _nstations(stations)
@@ -235,7 +257,7 @@ class GravityContext:
     def adjoint(self, mesh, stations, resid, precision="mixed", G=None, near_q=None):
         np_ = mesh.nx * mesh.ny * mesh.nz
         ns = _nstations(stations)
-        a = _Args()
+        a = _Args(self)
         px = a.arr(stations, 3 * ns, name="stations")
         pr = a.arr(resid, ns, name="resid")
         out, po = a.out(np_, resid)
@@ -248,7 +270,7 @@ class GravityContext:
     def interface(self, imesh, depth, rho_col, stations, precision="mixed", G=None, near_q=None):
         nc = imesh.nx * imesh.ny
         ns = _nstations(stations)
-        a = _Args()
+        a = _Args(self)
         pd = a.arr(depth, nc, name="depth")
         pr = a.arr(rho_col, nc, name="rho_col")
         px = a.arr(stations, 3 * ns, name="stations")
@@ -262,7 +284,7 @@ class GravityContext:
                           G=None, near_q=None):
         nc = imesh.nx * imesh.ny
         ns = _nstations(stations)
-        a = _Args()
+        a = _Args(self)
         pd = a.arr(depth, nc, name="depth")
         pr = a.arr(rho_col, nc, name="rho_col")
         px = a.arr(stations, 3 * ns, name="stations")
@@ -279,7 +301,7 @@ class GravityContext:
         """Returns (misfit, gz, g_rho, g_depth) for misfit 0.5*|gz - data|^2."""
         nc = imesh.nx * imesh.ny
         ns = _nstations(stations)
-        a = _Args()
+        a = _Args(self)
         pd = a.arr(depth, nc, name="depth")
         pr = a.arr(rho_col, nc, name="rho_col")
         px = a.arr(stations, 3 * ns, name="stations")
@@ -292,6 +314,7 @@ class GravityContext:
             import torch
             mt = torch.zeros(1, dtype=torch.float64, device=depth.device)
             a.keep.append(mt)
+            a._record(mt)
             pmis = ctypes.c_void_p(mt.data_ptr())
         else:
             pmis = ctypes.cast(ctypes.pointer(mis), ctypes.c_void_p)
@@ -308,7 +331,7 @@ class GravityContext:
         (depth, data-misfit history, iterations taken)."""
         nc = imesh.nx * imesh.ny
         ns = _nstations(stations)
-        a = _Args()
+        a = _Args(self)
         depth = np.array(depth0, dtype=np.float64, copy=True)
         if depth.size != nc:
             raise ValueError("depth0 has %d values, expected %d" % (depth.size, nc))
@@ -331,7 +354,7 @@ class GravityContext:
     def batch(self, jobs, precision="mixed", G=None, near_q=None):
         """jobs: list of (mesh, rho[nmodels, nprisms], stations[ns, 3]).
         Returns a list of gz arrays [nmodels, ns]."""
-        a = _Args()
+        a = _Args(self)
         arr = (_lib.Job * len(jobs))()
         outs = []
         for i, (mesh, rho, st) in enumerate(jobs):
