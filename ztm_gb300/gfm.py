@@ -151,6 +151,23 @@ class GravityContext:
             msg = self._lib.ztm_last_error(self._h)
             raise GravityError(rc, msg.decode() if msg else "")
 
+    def _run(self, a, fn, *args):
+        """Call an entry point.  With device tensors, order the library's
+        stream after PyTorch's current stream (inputs written there are
+        complete) and PyTorch's after the library's (results are visible
+        to later torch work); the host is not blocked."""
+        if not a.device:
+            self._check(fn(*args))
+            return
+        import torch
+        ts = self._torch_stream()
+        cur = torch.cuda.current_stream(self.device)
+        if cur.cuda_stream != ts.cuda_stream:
+            ts.wait_stream(cur)
+        self._check(fn(*args))
+        if cur.cuda_stream != ts.cuda_stream:
+            cur.wait_stream(ts)
+
     @property
     def stream(self):
         return self._lib.ztm_ctx_stream(self._h)
@@ -208,8 +225,8 @@ class GravityContext:
             n_nn = int(nn.numel() if _is_torch_cuda(nn) else np.asarray(nn).size)
         out, po = a.out(grid.di * grid.dj, drho)
         prec = PRECISIONS[precision] if isinstance(precision, str) else precision
-        self._check(self._lib.ztm_gfm_pointmass(self._h, ctypes.byref(grid), pd, pn, n_nn, ps, po,
-                                                prec, a.flags))
+        self._run(a, self._lib.ztm_gfm_pointmass, self._h, ctypes.byref(grid), pd, pn, n_nn, ps, po,
+                                                prec, a.flags)
         return out
 
     # -- density builder (TFM.cpp:83-89) -------------------------------
@@ -224,8 +241,8 @@ class GravityContext:
         pv = a.arr(v, di * dj * dk, name="v")
         out, po = a.out(N, sea)
         n = ctypes.c_longlong(0)
-        self._check(self._lib.ztm_density_build(self._h, ctypes.byref(p), ps, pm, pv, po,
-                                                ctypes.byref(n), a.flags))
+        self._run(a, self._lib.ztm_density_build, self._h, ctypes.byref(p), ps, pm, pv, po,
+                                                ctypes.byref(n), a.flags)
         return out, n.value
 
     # -- prism mesh -----------------------------------------------------
@@ -238,8 +255,8 @@ class GravityContext:
         px = a.arr(stations, 3 * ns, name="stations")
         out, po = a.out(ns, rho)
         o = _opts(precision, a.flags | (AUTOTUNE if autotune else 0), G, near_q, tile, chunk)
-        self._check(self._lib.ztm_gfm_prism(self._h, ctypes.byref(mesh), pr, ns, px, po,
-                                            ctypes.byref(o)))
+        self._run(a, self._lib.ztm_gfm_prism, self._h, ctypes.byref(mesh), pr, ns, px, po,
+                                            ctypes.byref(o))
         return out
 
     def prism_list(self, geom, rho, stations, precision="fp64", G=None, near_q=None):
@@ -251,7 +268,7 @@ class GravityContext:
         px = a.arr(stations, 3 * ns, name="stations")
         out, po = a.out(ns, rho)
         o = _opts(precision, a.flags, G, near_q)
-        self._check(self._lib.ztm_gfm_prism_list(self._h, n, pg, pr, ns, px, po, ctypes.byref(o)))
+        self._run(a, self._lib.ztm_gfm_prism_list, self._h, n, pg, pr, ns, px, po, ctypes.byref(o))
         return out
 
     def adjoint(self, mesh, stations, resid, precision="mixed", G=None, near_q=None):
@@ -262,8 +279,8 @@ class GravityContext:
         pr = a.arr(resid, ns, name="resid")
         out, po = a.out(np_, resid)
         o = _opts(precision, a.flags, G, near_q)
-        self._check(self._lib.ztm_gfm_adjoint(self._h, ctypes.byref(mesh), ns, px, pr, po,
-                                              ctypes.byref(o)))
+        self._run(a, self._lib.ztm_gfm_adjoint, self._h, ctypes.byref(mesh), ns, px, pr, po,
+                                              ctypes.byref(o))
         return out
 
     # -- interface --------------------------------------------------------
@@ -276,8 +293,8 @@ class GravityContext:
         px = a.arr(stations, 3 * ns, name="stations")
         out, po = a.out(ns, depth)
         o = _opts(precision, a.flags, G, near_q)
-        self._check(self._lib.ztm_gfm_interface(self._h, ctypes.byref(imesh), pd, pr, ns, px, po,
-                                                ctypes.byref(o)))
+        self._run(a, self._lib.ztm_gfm_interface, self._h, ctypes.byref(imesh), pd, pr, ns, px, po,
+                                                ctypes.byref(o))
         return out
 
     def interface_adjoint(self, imesh, depth, rho_col, stations, resid, precision="mixed",
@@ -292,8 +309,8 @@ class GravityContext:
         g_rho, pgr = a.out(nc, depth)
         g_dep, pgd = a.out(nc, depth)
         o = _opts(precision, a.flags, G, near_q)
-        self._check(self._lib.ztm_gfm_interface_adjoint(self._h, ctypes.byref(imesh), pd, pr, ns,
-                                                        px, pres, pgr, pgd, ctypes.byref(o)))
+        self._run(a, self._lib.ztm_gfm_interface_adjoint, self._h, ctypes.byref(imesh), pd, pr, ns,
+                                                        px, pres, pgr, pgd, ctypes.byref(o))
         return g_rho, g_dep
 
     def interface_misfit(self, imesh, depth, rho_col, stations, data, precision="mixed",
@@ -319,9 +336,9 @@ class GravityContext:
         else:
             pmis = ctypes.cast(ctypes.pointer(mis), ctypes.c_void_p)
         o = _opts(precision, a.flags, G, near_q)
-        self._check(self._lib.ztm_gfm_interface_misfit(self._h, ctypes.byref(imesh), pd, pr, ns,
+        self._run(a, self._lib.ztm_gfm_interface_misfit, self._h, ctypes.byref(imesh), pd, pr, ns,
                                                        px, pdat, pmis, pgz, pgr, pgd,
-                                                       ctypes.byref(o)))
+                                                       ctypes.byref(o))
         misfit = mt if a.device else mis.value
         return misfit, gz, g_rho, g_dep
 
@@ -372,7 +389,7 @@ class GravityContext:
             arr[i].sxyz = px
             arr[i].gz = po
         o = _opts(precision, a.flags, G, near_q)
-        self._check(self._lib.ztm_gfm_batch(self._h, arr, len(jobs), ctypes.byref(o)))
+        self._run(a, self._lib.ztm_gfm_batch, self._h, arr, len(jobs), ctypes.byref(o))
         return [out.reshape(nm, ns) for out, nm, ns in outs]
 
 
