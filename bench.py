@@ -345,8 +345,24 @@ def extras(ctx, mesh, rho, st, d_rho, d_st, gz_mixed):
     msa = e0.elapsed_time(e1)
     out["gradient"] = {"value": np_ * len(st) / (msa * 1e-3), "unit": "gradient evals/s",
                        "ms": msa, "what": "d misfit / d rho, all pairs, mixed"}
+    # the reference's own point-mass model on the same geometry (its grid,
+    # every node as a station): our float and double gathers
+    g, drho, surf = pointmass_mapping(mesh, rho, st)
+    nodes32 = int(np.count_nonzero(np.abs(drho.astype(np.float32)) > 0.001))
+    nodes64 = int(np.count_nonzero(np.abs(drho) > 0.001))
+    dd, dsf = torch.tensor(drho, device="cuda"), torch.tensor(surf, device="cuda")
+    pm = {}
+    for prec, nodes in (("fp32", nodes32), ("fp64", nodes64)):
+        ctx.pointmass(g, dd, dsf, precision=prec)
+        e0.record(stream)
+        ctx.pointmass(g, dd, dsf, precision=prec)
+        e1.record(stream)
+        ctx.sync()
+        ms = e0.elapsed_time(e1)
+        pm[prec] = {"value": nodes * mesh.nx * mesh.ny / (ms * 1e-3), "unit": "point-mass pairs/s",
+                    "ms": ms}
+    out["pointmass_gpu"] = pm
     if oracle.ref_gf_available():
-        g, drho, surf = pointmass_mapping(mesh, rho, st)
         gf, ms = oracle.ref_gf(g, drho.astype(np.float32), surf.astype(np.float32), reps=3)
         nodes = int(np.count_nonzero(np.abs(drho.astype(np.float32)) > 0.001))
         out["reference_gf_gpu"] = {

@@ -117,6 +117,105 @@ __global__ void __launch_bounds__(PM_TS)
   if (active) partial[(long long)blockIdx.y * p.ns + s] = F64 ? acc64 : acc32.value();
 }
 
+// Float gather on the packed FP32 path: the tile keeps only the selected
+// nodes (order preserved by a block scan), stored as (-i, -j, -k, w), and
+// two nodes are evaluated per FADD2/FFMA2/FMUL2; the rsqrt stays scalar
+// (rsqrt.approx.ftz).  Plain float sums over 16 nodes, Kahan across groups.
+__device__ __forceinline__ float pm_rsqrt_ftz(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+__global__ void __launch_bounds__(PM_TS)
+    pm_gather_f32_kernel(PmParams p, const double* __restrict__ drho,
+                         const int* __restrict__ nn, const double* __restrict__ surf,
+                         long long chunk_len, double* __restrict__ partial, int* err) {
+  __shared__ float4 tile[PM_TILE + 2];
+  __shared__ int s_wcount[PM_TS / 32];
+  __shared__ int s_total;
+  const int s = blockIdx.x * PM_TS + threadIdx.x;
+  const bool active = s < p.ns;
+  float i0 = 0.f, j0 = 0.f, k0 = 0.f;
+  if (active) {
+    const int si = p.bfr + s % p.ni, sj = p.bfr + s / p.ni;
+    i0 = (float)si;
+    j0 = (float)sj;
+    k0 = (float)surf[si + sj * p.di];
+  }
+  const long long n0 = (long long)blockIdx.y * chunk_len;
+  const long long n1 = min(p.nnodes, n0 + chunk_len);
+  const double ifh = 1.0 / p.fh, ifv = 1.0 / p.fv;
+  const long long plane = (long long)p.ii * p.jj;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const float2 I0 = make_float2(i0, i0), J0 = make_float2(j0, j0), K0 = make_float2(k0, k0);
+  Kahan acc;
+  for (long long t0 = n0; t0 < n1; t0 += PM_TILE) {
+    // each thread owns nodes t0 + 2*tid and t0 + 2*tid + 1 (in order)
+    float4 v[2];
+    bool sel[2];
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const long long t = t0 + 2 * threadIdx.x + h;
+      sel[h] = false;
+      v[h] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (t < n1) {
+        const long long n = nn ? (long long)nn[t] : t;
+        if (n < 0 || n >= p.N) {
+          atomicOr(err, ZTM_DEVERR_BOUNDS);  // bad list entry: recorded, skipped
+        } else {
+          const double w = drho[n];
+          sel[h] = nn ? true : (fabsf((float)w) > (float)p.thr);
+          const long long ni = n % p.ii, nj = (n / p.ii) % p.jj, nk = n / plane;
+          v[h] = make_float4(-(float)(ni * ifh), -(float)(nj * ifh), -(float)(nk * ifv), (float)w);
+        }
+      }
+    }
+    // order-preserving compaction of the selected nodes into the tile
+    const int mine = (int)sel[0] + (int)sel[1];
+    int incl = mine;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    __syncthreads();  // the previous tile is fully consumed
+    if (lane == 31) s_wcount[warp] = incl;
+    __syncthreads();
+    int base = 0;
+    for (int w = 0; w < warp; w++) base += s_wcount[w];
+    if (threadIdx.x == PM_TS - 1) s_total = base + incl;
+    int pos = base + incl - mine;
+    if (sel[0]) tile[pos++] = v[0];
+    if (sel[1]) tile[pos++] = v[1];
+    __syncthreads();
+    const int cnt = s_total;  // <= PM_TILE (two nodes per thread)
+    if (threadIdx.x == 0 && (cnt & 1))  // pad to an even count: zero mass far away
+      tile[cnt] = make_float4(-1.0e18f, 0.f, 0.f, 0.f);
+    __syncthreads();
+    if (!active) continue;
+    float2 g = make_float2(0.f, 0.f);
+    for (int q = 0; q < cnt; q += 2) {
+      const float4 a = tile[q], b = tile[q + 1];
+      const float2 dx = __fadd2_rn(I0, make_float2(a.x, b.x));
+      const float2 dy = __fadd2_rn(J0, make_float2(a.y, b.y));
+      const float2 dz = __fadd2_rn(K0, make_float2(a.z, b.z));
+      float2 d2 = __fmul2_rn(dz, dz);
+      d2 = __ffma2_rn(dy, dy, d2);
+      d2 = __ffma2_rn(dx, dx, d2);
+      const float2 rs = make_float2(pm_rsqrt_ftz(d2.x), pm_rsqrt_ftz(d2.y));
+      const float2 tw = __fmul2_rn(make_float2(a.w, b.w), dz);
+      g = __ffma2_rn(__fmul2_rn(tw, __fmul2_rn(rs, rs)), rs, g);
+      if ((q & 30) == 30) {  // every 16 nodes
+        acc.add(g.x + g.y);
+        g = make_float2(0.f, 0.f);
+      }
+    }
+    acc.add(g.x + g.y);
+  }
+  if (active) partial[(long long)blockIdx.y * p.ns + s] = acc.value();
+}
+
 // G[m] = factor * sum_chunks partial for interior m, 0 elsewhere.
 __global__ void pm_finalize_kernel(PmParams p, int nchunks,
                                    const double* __restrict__ partial,
@@ -176,7 +275,8 @@ int ztm_launch_pointmass(ztm_ctx* c, const PmParams& p, const double* d_drho,
     else
       {
         ZtmProf prof_(c, "pointmass");
-        pm_gather_kernel<false><<<grid, PM_TS, 0, c->stream>>>(p, d_drho, d_nn, d_surf, len, partial, c->d_err);
+        pm_gather_f32_kernel<<<grid, PM_TS, 0, c->stream>>>(p, d_drho, d_nn, d_surf, len,
+                                                            partial, c->d_err);
       }
     c->launches++;
   } else {

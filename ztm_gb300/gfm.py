@@ -37,10 +37,10 @@ class _Args:
     """Collects array arguments of one call; all host or all device.
 
     Device tensors are used by kernels queued on the context's stream after
-    the call returns; record_stream tells PyTorch's caching allocator not to
-    hand their memory to another tensor until that stream's work is done
-    (otherwise a temporary input freed right after the call could be
-    overwritten while a kernel still reads it)."""
+    the call returns.  GravityContext._run makes PyTorch's current stream
+    wait for that work, so memory that PyTorch frees after the call and
+    hands to a later tensor is only touched by work ordered after the
+    library's kernels."""
 
     def __init__(self, gctx=None):
         self.device = None
@@ -48,8 +48,7 @@ class _Args:
         self.gctx = gctx
 
     def _record(self, t):
-        if self.gctx is not None:
-            t.record_stream(self.gctx._torch_stream())
+        pass
 
     def _kind(self, dev):
         if self.device is None:
