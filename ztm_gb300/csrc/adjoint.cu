@@ -35,8 +35,8 @@ constexpr int ADJ_STILE = 256; // stations per shared-memory tile
 // grid.x covers ncols * ceil(nz/LG) threads.  g[p] = G5*L0*Vn * sum.
 __global__ void __launch_bounds__(ADJ_TS)
     adj_far_kernel(MeshConst k, int ns, const float4* __restrict__ sf,
-                   const int4* __restrict__ si, const double* __restrict__ res,
-                   double scale, double* __restrict__ g) {
+                   const int4* __restrict__ si, const short2* __restrict__ iv,
+                   const double* __restrict__ res, double scale, double* __restrict__ g) {
   __shared__ float4 s_f[ADJ_STILE];
   __shared__ int4 s_i[ADJ_STILE];
   __shared__ float s_r[ADJ_STILE];
@@ -83,9 +83,18 @@ __global__ void __launch_bounds__(ADJ_TS)
         const float Y = fmaf((float)(i.y - iy), k.dyn, f.y);
         const ColPoly cp = col_poly(X, Y, fc);
         const NearBox b = near_box(i, k);
-        const bool ncl = ix >= b.x0 && ix <= b.x1 && iy >= b.y0 && iy <= b.y1;
-        const int elo = ncl ? b.l0 : k.nz;
-        const unsigned espan = ncl ? (unsigned)(b.l1 - b.l0) : 0u;
+        bool ncl = ix >= b.x0 && ix <= b.x1 && iy >= b.y0 && iy <= b.y1;
+        int elo = k.nz;
+        unsigned espan = 0u;
+        if (ncl) {  // the column's near-region layers for this station
+          const short2 t = iv[(size_t)(s0 + q) * k.nslots + near_slot(b, ix, iy)];
+          if (t.x <= t.y) {
+            elo = t.x;
+            espan = (unsigned)(t.y - t.x);
+          } else {
+            ncl = false;
+          }
+        }
         const float Zg = fmaf((float)(l0 - i.z), k.dzn, f.z);
         const ColPoly2 cp2 = col_poly2(cp, fc.a1);
         const float2 zg2 = make_float2(Zg, Zg), dz2 = make_float2(k.dzn, k.dzn);
@@ -127,7 +136,8 @@ __global__ void __launch_bounds__(ADJ_TS)
 // to g with double atomics.
 template <typename T>
 __global__ void adj_near_kernel(MeshConst k, MeshDesc m, int ns, const double* __restrict__ sxyz,
-                                const int4* __restrict__ si, const double* __restrict__ res,
+                                const int4* __restrict__ si, const short2* __restrict__ iv,
+                                const int2* __restrict__ lr, const double* __restrict__ res,
                                 double G5, int nv_cap, double* __restrict__ g) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -136,15 +146,18 @@ __global__ void adj_near_kernel(MeshConst k, MeshDesc m, int ns, const double* _
   if (s >= ns) return;
   const double r = res[s];
   if (r == 0.0) return;
+  const int2 L = lr[s];
+  if (L.x > L.y) return;  // no near prism
   const NearBox b = near_box(si[s], k);
+  const short2* ivs = iv + (size_t)s * k.nslots;
   const double xs = sxyz[3 * s], ys = sxyz[3 * s + 1], zs = sxyz[3 * s + 2];
-  const int nvx = b.x1 - b.x0 + 2, nvy = b.y1 - b.y0 + 2, nvz = b.l1 - b.l0 + 2;
+  const int nvx = b.x1 - b.x0 + 2, nvy = b.y1 - b.y0 + 2, nvz = L.y - L.x + 2;
   const int nv = nvx * nvy * nvz;
-  if (nv > nv_cap) return;  // host sizes nv_cap for the largest box
+  if (nv > nv_cap) return;  // the host sizes nv_cap for the largest box
   for (int v = lane; v < nv; v += 32) {
     const int a = b.x0 + v % nvx;
     const int bb = b.y0 + (v / nvx) % nvy;
-    const int cz = b.l0 + v / (nvx * nvy);
+    const int cz = L.x + v / (nvx * nvy);
     phi[v] = ztm_phi<T>((T)((m.x0 + a * m.dx) - xs), (T)((m.y0 + bb * m.dy) - ys),
                         (T)((m.zt - cz * m.dz) - zs));
   }
@@ -154,6 +167,9 @@ __global__ void adj_near_kernel(MeshConst k, MeshDesc m, int ns, const double* _
   const long long plane = (long long)m.nx * m.ny;
   for (int q = lane; q < nb; q += 32) {
     const int qx = q % bx, qy = (q / bx) % by, qz = q / (bx * by);
+    const int ix = b.x0 + qx, iy = b.y0 + qy, l = L.x + qz;
+    const short2 t = ivs[near_slot(b, ix, iy)];
+    if (l < t.x || l > t.y) continue;  // not in the near region
     // vertices: x lower qx (-), upper qx+1 (+); z: layer top index qz (+),
     // bottom qz+1 (-)
     auto P = [&](int dx_, int dy_, int dz_) {
@@ -161,7 +177,7 @@ __global__ void adj_near_kernel(MeshConst k, MeshDesc m, int ns, const double* _
     };
     T u = P(1, 1, 0) - P(0, 1, 0) - P(1, 0, 0) + P(0, 0, 0) - P(1, 1, 1) + P(0, 1, 1) + P(1, 0, 1) -
           P(0, 0, 1);
-    const long long p = (b.x0 + qx) + (long long)m.nx * (b.y0 + qy) + plane * (b.l0 + qz);
+    const long long p = ix + (long long)m.nx * iy + plane * l;
     atomicAdd(&g[p], G5 * r * (double)u);
   }
 }
@@ -236,14 +252,17 @@ int near_cap(const MeshConst& k) {
 
 }  // namespace
 
-size_t ztm_adjoint_ws(const MeshDesc& m, int ns, int precision, int num_sms) {
+size_t ztm_adjoint_ws(const MeshDesc& m, int ns, int precision, int num_sms, double near_q) {
   long long np = (long long)m.nx * m.ny * m.nz;
   if (precision == ZTM_PREC_FP64) {
     int len;
     int ch = adj_f64_chunks(np, std::max(ns, 1), num_sms, &len);
     return WsCarver::need((size_t)ch * np * 8);
   }
-  return 2 * WsCarver::need((size_t)std::max(ns, 1) * 16);
+  const MeshConst k = make_mesh_const(m, near_q > 0 ? near_q : 6.0);
+  return 2 * WsCarver::need((size_t)std::max(ns, 1) * 16) +
+         WsCarver::need((size_t)std::max(ns, 1) * k.nslots * 4) +
+         WsCarver::need((size_t)std::max(ns, 1) * 8);
 }
 
 int ztm_launch_adjoint(ztm_ctx* c, const MeshDesc& m, int ns, const double* d_sxyz,
@@ -270,16 +289,20 @@ int ztm_launch_adjoint(ztm_ctx* c, const MeshDesc& m, int ns, const double* d_sx
   }
   const double nq = (o && o->near_q > 0) ? o->near_q : 6.0;
   MeshConst k = make_mesh_const(m, nq);
+  if (m.nz > 32767) return ztm_fail(c, ZTM_ERR_RANGE, "mixed adjoint supports nz <= 32767");
   float4* sf = wc.take<float4>(ns);
   int4* si = wc.take<int4>(ns);
+  short2* iv = wc.take<short2>((size_t)ns * k.nslots);
+  int2* lr = wc.take<int2>(ns);
   launch_mesh_station_prep(c, m, k.L0, ns, d_sxyz, sf, si);
+  launch_mesh_near_iv(c, k, ns, si, iv, lr);
   const int ngroups = (k.nz + ADJ_LG - 1) / ADJ_LG;
   const long long threads = (long long)k.ncols * ngroups;
   const double scale = G5 * k.L0 * (double)k.dxn * k.dyn * k.dzn;
   {
     ZtmProf prof_(c, "adjoint_far");
     adj_far_kernel<<<(unsigned)((threads + ADJ_TS - 1) / ADJ_TS), ADJ_TS, 0, c->stream>>>(
-        k, ns, sf, si, d_res, scale, d_g);
+        k, ns, sf, si, iv, d_res, scale, d_g);
   }
   c->launches++;
   const int cap = near_cap(k);
@@ -295,7 +318,7 @@ int ztm_launch_adjoint(ztm_ctx* c, const MeshDesc& m, int ns, const double* d_sx
     {
       ZtmProf prof_(c, "adjoint_near");
       adj_near_kernel<double><<<(ns + wpb - 1) / wpb, wpb * 32, smem, c->stream>>>(
-          k, m, ns, d_sxyz, si, d_res, G5, cap, d_g);
+          k, m, ns, d_sxyz, si, iv, lr, d_res, G5, cap, d_g);
     }
   } else {
     cudaFuncSetAttribute(adj_near_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -303,7 +326,7 @@ int ztm_launch_adjoint(ztm_ctx* c, const MeshDesc& m, int ns, const double* d_sx
     {
       ZtmProf prof_(c, "adjoint_near");
       adj_near_kernel<float><<<(ns + wpb - 1) / wpb, wpb * 32, smem, c->stream>>>(
-          k, m, ns, d_sxyz, si, d_res, G5, cap, d_g);
+          k, m, ns, d_sxyz, si, iv, lr, d_res, G5, cap, d_g);
     }
   }
   c->launches++;

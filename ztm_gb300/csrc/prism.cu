@@ -68,27 +68,70 @@ __global__ void transpose_kernel(MeshConst k, int nmodels, const double* __restr
   }
 }
 
+// Near-region intervals of every (station, box column), in double.
+__global__ void near_iv_kernel(MeshConst k, int ns, const int4* __restrict__ si,
+                               short2* __restrict__ iv, int2* __restrict__ lr) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= ns) return;
+  const int4 h = si[s];
+  const NearBox b = near_box(h, k);
+  const int bw = b.x1 - b.x0 + 1, bh = b.y1 - b.y0 + 1;
+  int lmin = 1 << 30, lmax = -1;
+  for (int slot = 0; slot < k.nslots; slot++) {
+    short2 out = make_short2(1, 0);
+    if (slot < bw * bh) {
+      const int ix = b.x0 + slot % bw, iy = b.y0 + slot / bw;
+      const double hx = fmax(fabs((double)(ix - h.x)) - 0.5, 0.0) * k.dxm;
+      const double hy = fmax(fabs((double)(iy - h.y)) - 0.5, 0.0) * k.dym;
+      const double h2 = hx * hx + hy * hy;
+      int lo = 1 << 30, hi = -1;
+      for (int l = b.l0; l <= b.l1; l++) {
+        const double hz = fmax(fabs((double)(l - h.z)) - 0.5, 0.0) * k.dzm;
+        if (h2 + hz * hz < k.R2) {  // one interval: the bound is unimodal in l
+          lo = min(lo, l);
+          hi = l;
+        }
+      }
+      if (hi >= 0) {
+        out = make_short2((short)lo, (short)hi);
+        lmin = min(lmin, lo);
+        lmax = max(lmax, hi);
+      }
+    }
+    iv[(size_t)s * k.nslots + slot] = out;
+  }
+  lr[s] = (lmax >= 0) ? make_int2(lmin, lmax) : make_int2(1, 0);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(NEAR_WPB * 32)
     near_kernel(MeshConst k, MeshDesc m, int ns, const double* __restrict__ sxyz,
-                const int4* __restrict__ si, const double* __restrict__ rho,
+                const int4* __restrict__ si, const short2* __restrict__ iv,
+                const int2* __restrict__ lr, const double* __restrict__ rho,
                 double* __restrict__ out) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int s = blockIdx.x * NEAR_WPB + warp;
   if (s >= ns) return;
   const NearBox b = near_box(si[s], k);
+  const int2 L = lr[s];
+  if (L.x > L.y) {  // no near prism
+    if (lane == 0) out[s] = 0.0;
+    return;
+  }
+  const short2* ivs = iv + (size_t)s * k.nslots;
   const double xs = sxyz[3 * s], ys = sxyz[3 * s + 1], zs = sxyz[3 * s + 2];
-  const int nvx = b.x1 - b.x0 + 2, nvy = b.y1 - b.y0 + 2, nvz = b.l1 - b.l0 + 2;
+  const int nvx = b.x1 - b.x0 + 2, nvy = b.y1 - b.y0 + 2, nvz = L.y - L.x + 2;
   const int nv = nvx * nvy * nvz;
   const long long plane = (long long)m.nx * m.ny;
   T acc = T(0);
   for (int v = lane; v < nv; v += 32) {
     const int a = b.x0 + v % nvx;
     const int bb = b.y0 + (v / nvx) % nvy;
-    const int cz = b.l0 + v / (nvx * nvy);
-    // signed triple difference of the box density around vertex (a, bb, cz):
-    // prism ix = a-1 has the vertex as its upper x limit (+), ix = a lower (-);
-    // layer l = cz has it as its upper z limit (+), l = cz-1 lower (-).
+    const int cz = L.x + v / (nvx * nvy);
+    // signed triple difference of the region's density around vertex
+    // (a, bb, cz): prism ix = a-1 has the vertex as its upper x limit (+),
+    // ix = a lower (-); layer l = cz has it as its upper z limit (+), l = cz-1
+    // lower (-).
     double D = 0.0;
 #pragma unroll
     for (int da = 0; da < 2; da++) {
@@ -98,10 +141,11 @@ __global__ void __launch_bounds__(NEAR_WPB * 32)
       for (int db = 0; db < 2; db++) {
         const int iy = bb - 1 + db;
         if (iy < b.y0 || iy > b.y1) continue;
+        const short2 t = ivs[near_slot(b, ix, iy)];
 #pragma unroll
         for (int dc = 0; dc < 2; dc++) {
           const int l = cz - 1 + dc;
-          if (l < b.l0 || l > b.l1) continue;
+          if (l < t.x || l > t.y) continue;
           const double r = rho[ix + (long long)m.nx * iy + plane * l];
           const int neg = (da == 1) ^ (db == 1) ^ (dc == 0);
           D += neg ? -r : r;
@@ -128,6 +172,7 @@ struct FarArgs {
   int sc;          // columns per shared-memory stage
   const float4* sf;
   const int4* si;
+  const short2* iv;  // near-region intervals [station][box column]
   const float* rhoT;
   double* partial;  // [chunk][ns]
   int* err;
@@ -214,8 +259,15 @@ __global__ void __launch_bounds__(FAR_TS, 9) far_kernel(FarArgs a) {
         const float Y = fmaf((float)(iys - iy), k.dyn, ey);
         const ColPoly cp = col_poly(X, Y, fc);
         const bool ncl = ix >= nb.x0 && ix <= nb.x1 && iy >= nb.y0 && iy <= nb.y1;
-        const int elo = ncl ? nb.l0 : k.nz;
-        const unsigned espan = ncl ? (unsigned)(nb.l1 - nb.l0) : 0u;
+        int elo = k.nz;
+        unsigned espan = 0u;
+        if (ncl) {  // the column's near-region layers
+          const short2 t = a.iv[(size_t)s * k.nslots + near_slot(nb, ix, iy)];
+          if (t.x <= t.y) {
+            elo = t.x;
+            espan = (unsigned)(t.y - t.x);
+          }
+        }
         const float* col = rs + q * k.nzp;
         const ColPoly2 cp2 = col_poly2(cp, fc.a1);
         // a column lies in some lane's near box only near the warp's
@@ -484,6 +536,12 @@ MeshConst make_mesh_const(const MeshDesc& m, double near_q) {
   k.fc = far_coef(m.dx / k.L0, m.dy / k.L0, m.dz / k.L0);
   const double ell = 0.5 * sqrt(m.dx * m.dx + m.dy * m.dy + m.dz * m.dz) / k.L0;
   k.rh_t2 = (float)((48.0 * ell) * (48.0 * ell));
+  k.dxm = m.dx;
+  k.dym = m.dy;
+  k.dzm = m.dz;
+  const double R = near_q * 0.5 * sqrt(m.dx * m.dx + m.dy * m.dy + m.dz * m.dz);
+  k.R2 = R * R;
+  k.nslots = (2 * k.wx + 1) * (2 * k.wy + 1);
   return k;
 }
 
@@ -502,21 +560,30 @@ void launch_mesh_transpose(ztm_ctx* c, const MeshConst& k, int nmodels, const do
   c->launches++;
 }
 
+void launch_mesh_near_iv(ztm_ctx* c, const MeshConst& k, int ns, const int4* si, short2* iv,
+                         int2* lr) {
+  if (ns <= 0) return;
+  near_iv_kernel<<<(ns + 127) / 128, 128, 0, c->stream>>>(k, ns, si, iv, lr);
+  c->launches++;
+}
+
 void launch_mesh_near(ztm_ctx* c, const MeshConst& k, const MeshDesc& m, int ns,
-                      const double* sxyz, const int4* si, const double* rho, double* out,
-                      bool f64, cudaStream_t stream) {
+                      const double* sxyz, const int4* si, const short2* iv, const int2* lr,
+                      const double* rho, double* out, bool f64, cudaStream_t stream) {
   if (ns <= 0) return;
   if (!stream) stream = c->stream;
   int blocks = (ns + NEAR_WPB - 1) / NEAR_WPB;
   if (f64)
     {
       ZtmProf prof_(c, "prism_near", stream);
-      near_kernel<double><<<blocks, NEAR_WPB * 32, 0, stream>>>(k, m, ns, sxyz, si, rho, out);
+      near_kernel<double><<<blocks, NEAR_WPB * 32, 0, stream>>>(k, m, ns, sxyz, si, iv, lr, rho,
+                                                                out);
     }
   else
     {
       ZtmProf prof_(c, "prism_near", stream);
-      near_kernel<float><<<blocks, NEAR_WPB * 32, 0, stream>>>(k, m, ns, sxyz, si, rho, out);
+      near_kernel<float><<<blocks, NEAR_WPB * 32, 0, stream>>>(k, m, ns, sxyz, si, iv, lr, rho,
+                                                               out);
     }
   c->launches++;
 }
@@ -534,7 +601,8 @@ size_t ztm_prism_ws(const MeshDesc& m, int ns, int precision, int num_sms, const
   for (int bps : {5, 9, 18}) chunks = std::max(chunks, far_shape(k, ns, num_sms, o, bps, 8).chunks);
   chunks = std::max(chunks, far_shape(k, ns, num_sms, o).chunks);
   return WsCarver::need((size_t)k.ncols * k.nzp * 4) + WsCarver::need((size_t)ns * 16) * 2 +
-         WsCarver::need((size_t)ns * 8) + WsCarver::need((size_t)chunks * ns * 8);
+         WsCarver::need((size_t)ns * 8) + WsCarver::need((size_t)chunks * ns * 8) +
+         WsCarver::need((size_t)ns * k.nslots * 4) + WsCarver::need((size_t)ns * 8);
 }
 
 int ztm_launch_prism(ztm_ctx* c, const MeshDesc& m, const double* d_rho, int ns,
@@ -558,6 +626,7 @@ int ztm_launch_prism(ztm_ctx* c, const MeshDesc& m, const double* d_rho, int ns,
   }
   const double nq = (o && o->near_q > 0) ? o->near_q : 6.0;
   MeshConst k = make_mesh_const(m, nq);
+  if (m.nz > 32767) return ztm_fail(c, ZTM_ERR_RANGE, "mixed prism forward supports nz <= 32767");
   int bps = 9, scw = 0;
   auto it = c->tuned.find(tune_key(k, ns));
   if (it != c->tuned.end()) {
@@ -572,11 +641,15 @@ int ztm_launch_prism(ztm_ctx* c, const MeshDesc& m, const double* d_rho, int ns,
   for (int b : {5, 9, 18}) max_chunks = std::max(max_chunks, far_shape(k, ns, c->num_sms, o, b, 8).chunks);
   max_chunks = std::max(max_chunks, far_shape(k, ns, c->num_sms, o).chunks);
   double* partial = wc.take<double>((size_t)max_chunks * ns);
+  short2* iv = wc.take<short2>((size_t)ns * k.nslots);
+  int2* lr = wc.take<int2>(ns);
   launch_mesh_transpose(c, k, 1, d_rho, rhoT);
   launch_mesh_station_prep(c, m, k.L0, ns, d_sxyz, sf, si);
+  launch_mesh_near_iv(c, k, ns, si, iv, lr);
   cudaFuncSetAttribute(far_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
   FarArgs a;
-  a.k = k; a.ns = ns; a.sf = sf; a.si = si; a.rhoT = rhoT; a.partial = partial; a.err = c->d_err;
+  a.k = k; a.ns = ns; a.sf = sf; a.si = si; a.iv = iv; a.rhoT = rhoT; a.partial = partial;
+  a.err = c->d_err;
   if (o && (o->flags & ZTM_FLAG_AUTOTUNE) && !(o->chunk > 0) && it == c->tuned.end()) {
     // time each candidate once (after one untimed launch) and keep the fastest
     cudaEvent_t e0, e1;
@@ -611,7 +684,8 @@ int ztm_launch_prism(ztm_ctx* c, const MeshDesc& m, const double* d_rho, int ns,
   // the double near box runs on the side stream, concurrently with the float
   // far field (different pipes: FP64 vs FMA/MUFU)
   ztm_fork(c);
-  launch_mesh_near(c, k, m, ns, d_sxyz, si, d_rho, near, precision == ZTM_PREC_MIXED, c->aux);
+  launch_mesh_near(c, k, m, ns, d_sxyz, si, iv, lr, d_rho, near, precision == ZTM_PREC_MIXED,
+                   c->aux);
   {
     ZtmProf prof_(c, "prism_far");
     far_kernel<<<dim3(f.tiles, f.chunks), FAR_TS, f.smem, c->stream>>>(a);

@@ -131,6 +131,9 @@ struct MeshConst {
   float rh_t2;          // horizontal distance^2 (units of L0) beyond which
                         // the second-order form is exact enough
   double L0;
+  double dxm, dym, dzm;  // cell edges (m)
+  double R2;             // (near_q * half diagonal)^2 (m^2)
+  int nslots;            // (2wx+1)(2wy+1): columns of a near box
   FarCoef fc;
 };
 
@@ -171,6 +174,19 @@ __device__ __forceinline__ NearBox near_box(int4 si, const MeshConst& k) {
   return b;
 }
 
+// Near region of a station: the prisms of its near box whose centre lies
+// closer than near_q half-diagonals by the lower bound
+//   d^2 >= sum over axes of (max(|index offset| - 1/2, 0) * cell edge)^2
+// (the station is somewhere in its home cell).  Everything outside the
+// region is at least that far away, so the far-field expansion holds there.
+// In each box column the region's layers are one interval; the interval of
+// every (station, box column) is computed once, in double, by
+// launch_mesh_near_iv, and every kernel that splits near from far pairs
+// reads the same intervals (lo > hi: the column has no near prism).
+__device__ __forceinline__ int near_slot(const NearBox& b, int ix, int iy) {
+  return (ix - b.x0) + (b.x1 - b.x0 + 1) * (iy - b.y0);
+}
+
 // ---- host launchers (prism.cu) ------------------------------------------
 MeshConst make_mesh_const(const MeshDesc& m, double near_q);
 // Station-relative integer/float decomposition (computed in double once per
@@ -188,5 +204,9 @@ void launch_mesh_transpose(ztm_ctx* c, const MeshConst& k, int nmodels, const do
 // difference of the density over the (up to 8) box prisms around the vertex.
 // One warp per station.  out[s] = that sum (metres x density, without G).
 void launch_mesh_near(ztm_ctx* c, const MeshConst& k, const MeshDesc& m, int ns,
-                      const double* sxyz, const int4* si, const double* rho, double* out,
-                      bool f64, cudaStream_t stream = nullptr);
+                      const double* sxyz, const int4* si, const short2* iv, const int2* lr,
+                      const double* rho, double* out, bool f64, cudaStream_t stream = nullptr);
+// Near-region intervals: iv[s*nslots + slot] (layers lo..hi) and the
+// station's overall layer range lr[s] = (lmin, lmax) (lmin > lmax: none).
+void launch_mesh_near_iv(ztm_ctx* c, const MeshConst& k, int ns, const int4* si, short2* iv,
+                         int2* lr);

@@ -422,7 +422,7 @@ int ztm_gfm_adjoint(ztm_ctx* c, const ztm_mesh* mesh, int ns, const double* sxyz
   DeviceGuard dg(c->device);
   if (!dg.ok) return ztm_fail(c, ZTM_ERR_NODEV, "cannot select device");
   size_t need = WsCarver::need((size_t)ns * 24) + WsCarver::need((size_t)ns * 8) +
-                WsCarver::need(np * 8) + ztm_adjoint_ws(m, ns, prec, c->num_sms) + 4096;
+                WsCarver::need(np * 8) + ztm_adjoint_ws(m, ns, prec, c->num_sms, o ? o->near_q : 0.0) + 4096;
   if ((rc = ztm_ws_reserve(c, need))) return rc;
   WsCarver wc(c->ws);
   double* s_xyz = wc.take<double>((size_t)ns * 3);

@@ -126,7 +126,7 @@ int ztm_launch_prism_list(ztm_ctx* c, long long np, const double* d_geom,
                           const double* d_rho, int ns, const double* d_sxyz,
                           double* d_gz, double G, int precision, double near_q,
                           WsCarver& wc);
-size_t ztm_adjoint_ws(const MeshDesc& m, int ns, int precision, int num_sms);
+size_t ztm_adjoint_ws(const MeshDesc& m, int ns, int precision, int num_sms, double near_q);
 int ztm_launch_adjoint(ztm_ctx* c, const MeshDesc& m, int ns,
                        const double* d_sxyz, const double* d_res,
                        double* d_grho, double G, int precision,
