@@ -38,11 +38,12 @@ struct BJob {
   MeshConst k;
   MeshDesc m;
   int nmodels, ns, tiles, chunks, chunk_cols, sc, mgroups, nv_cap;
+  int mgw;               // models interleaved per group: 1 or B_MG
   long long near_base, far_base;
   double far_scale, G5;
   const float4* sf;
   const int4* si;
-  const float* rhoT;     // nmodels x ncols x nzp
+  const float* rhoT;     // [group][column][layer][mgw] float densities
   const double* rho;     // nmodels x np (layer-major, as given)
   const double* sxyz;
   double* partial;       // [model][chunk][ns]
@@ -60,6 +61,86 @@ struct BArgs {
   double* phi;   // [block][warp][phi_cap] near-box vertex values (global scratch)
   int phi_cap;
 };
+
+// Float densities of a job, model-interleaved: rhoT[((g*ncols + c)*nzp + l)*W
+// + mm] = rho_{g*W+mm}(c, l), zero for padded layers or models.  A far item's
+// stage (a run of columns of one model group) is one contiguous range, and a
+// layer's W model densities are adjacent.
+__global__ void transpose_models_kernel(MeshConst k, int nmodels, int W,
+                                        const double* __restrict__ rho,
+                                        float* __restrict__ rhoT) {
+  const int ngroups = (nmodels + W - 1) / W;
+  const long long total = (long long)ngroups * k.ncols * k.nzp * W;
+  const long long np = (long long)k.ncols * k.nz;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int mm = (int)(t % W);
+    long long r = t / W;
+    const int l = (int)(r % k.nzp);
+    r /= k.nzp;
+    const int c = (int)(r % k.ncols);
+    const int g = (int)(r / k.ncols);
+    const int md = g * W + mm;
+    float v = 0.f;
+    if (l < k.nz && md < nmodels) v = (float)rho[(long long)md * np + (long long)l * k.ncols + c];
+    rhoT[t] = v;
+  }
+}
+
+// Far field of one column for every model of the group, W models
+// interleaved in `col` (layer-major, W per layer).  K is computed once per
+// (station, prism) pair; per model two packed FMAs per layer pair (W = 1) or
+// per model pair (W = 8); plain sums over 8 layers, Kahan across groups.
+template <int W>
+__device__ __forceinline__ void far_column(const float* __restrict__ col, const MeshConst& k,
+                                           const ColPoly2& cp2, float ez, int izs, int Lm,
+                                           int elo, unsigned espan, Kahan* acc) {
+  const float2 dz2 = make_float2(k.dzn, k.dzn);
+  float zf = (float)(-izs);  // (l0 - izs), exact, stepped by 8
+  for (int l0 = 0; l0 < k.nz; l0 += 8, zf += 8.f) {
+    const float Zg = fmaf(zf, k.dzn, ez);
+    const float2 zg2 = make_float2(Zg, Zg);
+    float2 K2[4];  // kernel values of layers (l0+2j, l0+2j+1)
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      K2[j] = far_unit2(__ffma2_rn(make_float2((float)(2 * j), (float)(2 * j + 1)), dz2, zg2), cp2);
+      const int la = l0 + 2 * j, lb = la + 1;
+      // select: a NaN at a near-region prism is dropped
+      if ((la < Lm && (unsigned)(la - elo) <= espan) || la >= k.nz) K2[j].x = 0.f;
+      if ((lb < Lm && (unsigned)(lb - elo) <= espan) || lb >= k.nz) K2[j].y = 0.f;
+    }
+    if constexpr (W == 1) {
+      const float4 ra = *reinterpret_cast<const float4*>(col + l0);
+      const float4 rb = *reinterpret_cast<const float4*>(col + l0 + 4);
+      float2 g = __fmul2_rn(K2[0], make_float2(ra.x, ra.y));
+      g = __ffma2_rn(K2[1], make_float2(ra.z, ra.w), g);
+      g = __ffma2_rn(K2[2], make_float2(rb.x, rb.y), g);
+      g = __ffma2_rn(K2[3], make_float2(rb.z, rb.w), g);
+      acc[0].add(g.x + g.y);
+    } else {
+      float2 g[W / 2];
+#pragma unroll
+      for (int m = 0; m < W / 2; m++) g[m] = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        const float Kj = (j & 1) ? K2[j >> 1].y : K2[j >> 1].x;
+        const float2 kk = make_float2(Kj, Kj);
+        const float* row = col + (l0 + j) * W;
+#pragma unroll
+        for (int m = 0; m < W / 4; m++) {
+          const float4 r4 = *reinterpret_cast<const float4*>(row + 4 * m);
+          g[2 * m] = __ffma2_rn(kk, make_float2(r4.x, r4.y), g[2 * m]);
+          g[2 * m + 1] = __ffma2_rn(kk, make_float2(r4.z, r4.w), g[2 * m + 1]);
+        }
+      }
+#pragma unroll
+      for (int m = 0; m < W / 2; m++) {
+        acc[2 * m].add(g[m].x);
+        acc[2 * m + 1].add(g[m].y);
+      }
+    }
+  }
+}
 
 // tile completion: the last item of a tile writes gz for its stations
 __device__ void tile_done(const BJob& J, int tile, int expected, int* s_flag) {
@@ -173,10 +254,10 @@ __global__ void __launch_bounds__(B_TS, 5) batch_kernel(BArgs a) {
     const int chunk = (int)(r % J.chunks);
     const int mg = (int)(r / J.chunks);
     const MeshConst& k = J.k;
-    const int m0 = mg * B_MG, mcnt = min(B_MG, J.nmodels - m0);
+    const int m0 = mg * J.mgw, mcnt = min(J.mgw, J.nmodels - m0);
     const int c0 = chunk * J.chunk_cols, c1 = min(k.ncols, c0 + J.chunk_cols);
     const int nst = (c1 - c0 + J.sc - 1) / J.sc;
-    const int stage_floats = J.sc * k.nzp * B_MG;
+    const int stage_floats = J.sc * k.nzp * J.mgw;
     const int s = tile * B_TS + threadIdx.x;
     const bool active = s < J.ns;
     float ex = 0.f, ey = 0.f, ez = 0.f;
@@ -196,11 +277,10 @@ __global__ void __launch_bounds__(B_TS, 5) batch_kernel(BArgs a) {
       const int buf = st & 1;
       const int cs = c0 + st * J.sc;
       const int ncol = min(J.sc, c1 - cs);
-      const uint32_t bytes = (uint32_t)ncol * k.nzp * 4u;
-      mbar_expect_tx(&bar[buf], bytes * (uint32_t)mcnt);
-      for (int q = 0; q < mcnt; q++)
-        bulk_g2s(stage + buf * stage_floats + q * J.sc * k.nzp,
-                 J.rhoT + ((size_t)(m0 + q) * k.ncols + cs) * k.nzp, bytes, &bar[buf]);
+      const uint32_t bytes = (uint32_t)ncol * k.nzp * J.mgw * 4u;
+      mbar_expect_tx(&bar[buf], bytes);
+      bulk_g2s(stage + buf * stage_floats,
+               J.rhoT + ((size_t)mg * k.ncols + cs) * k.nzp * J.mgw, bytes, &bar[buf]);
     };
     if (threadIdx.x == 0 && nst > 0) issue(0);
     __syncthreads();
@@ -230,39 +310,12 @@ __global__ void __launch_bounds__(B_TS, 5) batch_kernel(BArgs a) {
           const bool ncl = ix >= nb.x0 && ix <= nb.x1 && iy >= nb.y0 && iy <= nb.y1;
           const int elo = ncl ? nb.l0 : k.nz;
           const unsigned espan = ncl ? (unsigned)(nb.l1 - nb.l0) : 0u;
-          const float* col = rs + q * k.nzp;
-          const int mstride = J.sc * k.nzp;
+          const float* col = rs + q * k.nzp * J.mgw;
           const ColPoly2 cp2 = col_poly2(cp, fc.a1);
-          const float2 dz2 = make_float2(k.dzn, k.dzn);
-          float zf = (float)(-izs);  // (l0 - izs), exact, stepped by 8
-          for (int l0 = 0; l0 < k.nz; l0 += 8, zf += 8.f) {
-            const float Zg = fmaf(zf, k.dzn, ez);
-            const float2 zg2 = make_float2(Zg, Zg);
-            float2 K2[4];  // kernel values of layers (l0+2j, l0+2j+1)
-#pragma unroll
-            for (int j = 0; j < 4; j++) {
-              K2[j] = far_unit2(__ffma2_rn(make_float2((float)(2 * j), (float)(2 * j + 1)), dz2, zg2),
-                                cp2);
-              const int la = l0 + 2 * j, lb = la + 1;
-              // select: a NaN at a box prism is dropped
-              if ((la < Lm && (unsigned)(la - elo) <= espan) || la >= k.nz) K2[j].x = 0.f;
-              if ((lb < Lm && (unsigned)(lb - elo) <= espan) || lb >= k.nz) K2[j].y = 0.f;
-            }
-            // one kernel value per pair applied to every model of the group,
-            // packed over layer pairs; plain over 8 layers, compensated across
-#pragma unroll
-            for (int md = 0; md < B_MG; md++) {
-              if (md < mcnt) {
-                const float4 ra = *reinterpret_cast<const float4*>(col + md * mstride + l0);
-                const float4 rb = *reinterpret_cast<const float4*>(col + md * mstride + l0 + 4);
-                float2 g = __fmul2_rn(K2[0], make_float2(ra.x, ra.y));
-                g = __ffma2_rn(K2[1], make_float2(ra.z, ra.w), g);
-                g = __ffma2_rn(K2[2], make_float2(rb.x, rb.y), g);
-                g = __ffma2_rn(K2[3], make_float2(rb.z, rb.w), g);
-                acc[md].add(g.x + g.y);
-              }
-            }
-          }
+          if (J.mgw == 1)
+            far_column<1>(col, k, cp2, ez, izs, Lm, elo, espan, acc);
+          else
+            far_column<B_MG>(col, k, cp2, ez, izs, Lm, elo, espan, acc);
           if (++ix == k.nx) {
             ix = 0;
             ++iy;
@@ -309,8 +362,9 @@ Plan plan(const ztm_job* jobs, int njobs, double near_q, int num_sms) {
     J.nmodels = q.nmodels;
     J.ns = q.ns;
     J.tiles = std::max(1, (q.ns + B_TS - 1) / B_TS);
-    J.mgroups = (q.nmodels + B_MG - 1) / B_MG;
-    int sc = std::max(1, (16 * 1024) / (J.k.nzp * 4 * B_MG));
+    J.mgw = q.nmodels > 1 ? B_MG : 1;
+    J.mgroups = (q.nmodels + J.mgw - 1) / J.mgw;
+    int sc = std::max(1, (16 * 1024) / (J.k.nzp * 4 * J.mgw));
     sc = std::min(sc, 32);
     J.sc = sc;
     // aim for ~16 items per SM over the whole batch: split columns so that a
@@ -326,9 +380,9 @@ Plan plan(const ztm_job* jobs, int njobs, double near_q, int num_sms) {
     J.nv_cap = (std::min(2 * J.k.wx + 1, m.nx) + 1) * (std::min(2 * J.k.wy + 1, m.ny) + 1) *
                (std::min(2 * J.k.wl + 1, m.nz) + 1);
     J.far_scale = J.k.L0 * (double)J.k.dxn * J.k.dyn * J.k.dzn;
-    p.smem = std::max(p.smem, 128 + (size_t)2 * sc * J.k.nzp * 4 * B_MG);
+    p.smem = std::max(p.smem, 128 + (size_t)2 * sc * J.k.nzp * 4 * J.mgw);
     p.phi_cap = std::max(p.phi_cap, J.nv_cap);
-    ws += WsCarver::need((size_t)q.nmodels * J.k.ncols * J.k.nzp * 4);
+    ws += WsCarver::need((size_t)J.mgroups * J.mgw * J.k.ncols * J.k.nzp * 4);
     ws += WsCarver::need((size_t)q.ns * 16) * 2;
     ws += WsCarver::need((size_t)q.nmodels * J.chunks * q.ns * 8);
     ws += WsCarver::need((size_t)q.nmodels * q.ns * 8);
@@ -442,7 +496,7 @@ extern "C" int ztm_gfm_batch(ztm_ctx* c, const ztm_job* jobs, int njobs, const z
     J.sxyz = xyz_d[j];
     J.gz = gz_d[j];
     J.G5 = G * 1.0e5;
-    float* rhoT = wc.take<float>((size_t)J.nmodels * J.k.ncols * J.k.nzp);
+    float* rhoT = wc.take<float>((size_t)J.mgroups * J.mgw * J.k.ncols * J.k.nzp);
     J.rhoT = rhoT;
     float4* sf = wc.take<float4>(J.ns);
     int4* si = wc.take<int4>(J.ns);
@@ -502,7 +556,12 @@ extern "C" int ztm_gfm_batch(ztm_ctx* c, const ztm_job* jobs, int njobs, const z
       return rc;
     for (int j = 0; j < njobs; j++) {
       BJob& J = p.jobs[j];
-      launch_mesh_transpose(c, J.k, J.nmodels, J.rho, const_cast<float*>(J.rhoT));
+      {
+        const long long total = (long long)J.mgroups * J.mgw * J.k.ncols * J.k.nzp;
+        const int blocks = (int)std::min<long long>((total + 255) / 256, 32LL * c->num_sms);
+        transpose_models_kernel<<<std::max(blocks, 1), 256, 0, c->stream>>>(
+            J.k, J.nmodels, J.mgw, J.rho, const_cast<float*>(J.rhoT));
+      }
       launch_mesh_station_prep(c, J.m, J.k.L0, J.ns, J.sxyz, const_cast<float4*>(J.sf),
                                const_cast<int4*>(J.si));
       cudaMemsetAsync(J.done, 0, sizeof(int) * J.tiles, c->stream);

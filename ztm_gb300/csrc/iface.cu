@@ -137,6 +137,12 @@ __device__ __forceinline__ bool is_near(const uint32_t* __restrict__ mask, int s
   return (__ldg(mask + (size_t)s * k.words + (slot >> 5)) >> (slot & 31)) & 1u;
 }
 
+// The near bit of window slot `slot` of station s.
+__device__ __forceinline__ bool near_bit(const uint32_t* __restrict__ mask, int s, int slot,
+                                         const IConst& k) {
+  return (__ldg(mask + (size_t)s * k.words + (slot >> 5)) >> (slot & 31)) & 1u;
+}
+
 // One warp per station: the near bit of every window column, in double.
 __global__ void iface_near_mask(IConst k, int ns, const double* __restrict__ sxyz,
                                 const int2* __restrict__ si, const double* __restrict__ depth,
@@ -162,44 +168,56 @@ __global__ void iface_near_mask(IConst k, int ns, const double* __restrict__ sxy
   }
 }
 
-// Unit column integral (normalised, without dx dy) and, if wanted, the unit
-// face integral, for one far pair.
-__device__ __forceinline__ float col_unit(float X2, float Y2, float rh, float ut, float th,
-                                          float Q2, float P4, float P2, const IConst& k) {
-  const float ub = ut + th;
-  const float rt2 = fmaf(ut, ut, rh), rb2 = fmaf(ub, ub, rh);
-  const float it = rsqrt_ftz(rt2), ib = rsqrt_ftz(rb2);
-  const float itb = it * ib;
-  const float L = __fdividef(th * (ut + ub) * itb * itb, it + ib);
-  const float it2 = it * it, ib2 = ib * ib;
-  const float ct = it2 * it2 * it * fmaf(k.Q0, rt2, Q2) +
-                   (it2 * it2) * (it2 * it2) * it * fmaf(fmaf(k.P0, rt2, P2), rt2, P4);
-  const float cb = ib2 * ib2 * ib * fmaf(k.Q0, rb2, Q2) +
-                   (ib2 * ib2) * (ib2 * ib2) * ib * fmaf(fmaf(k.P0, rb2, P2), rb2, P4);
-  return L + (ct - cb);
+// The unit face integral of the far expansion for two pairs, given 1/r of
+// the column top.
+__device__ __forceinline__ float2 face_unit_far2(float2 X2, float2 Y2, float2 ut, float2 rinv,
+                                                 const FarCoef& f) {
+  const float2 Z2 = __fmul2_rn(ut, ut);
+  const float2 ri2 = __fmul2_rn(rinv, rinv), ri4 = __fmul2_rn(ri2, ri2);
+  const float2 a0 = __ffma2_rn(X2, make_float2(f.cA, f.cA), __fmul2_rn(Y2, make_float2(f.cB, f.cB)));
+  const float2 h1 = __ffma2_rn(X2, make_float2(f.cX1, f.cX1), __fmul2_rn(Y2, make_float2(f.cY1, f.cY1)));
+  const float2 h0 = __ffma2_rn(X2,
+                               __ffma2_rn(X2, make_float2(f.cXX, f.cXX), __fmul2_rn(Y2, make_float2(f.cXY, f.cXY))),
+                               __fmul2_rn(__fmul2_rn(Y2, Y2), make_float2(f.cYY, f.cYY)));
+  const float2 n2 = __ffma2_rn(make_float2(f.a1, f.a1), Z2, a0);
+  const float2 H = __ffma2_rn(__ffma2_rn(make_float2(f.h2, f.h2), Z2, h1), Z2, h0);
+  const float2 t = __fmul2_rn(__ffma2_rn(H, ri4, n2), ri4);
+  const float2 base = __fmul2_rn(__fmul2_rn(ut, rinv), ri2);
+  return __ffma2_rn(base, t, base);
 }
 
-__device__ __forceinline__ float face_unit_far(float X2, float Y2, float rh, float ut,
-                                               const FarCoef& f) {
-  const float Z2 = ut * ut;
-  const float rinv = rsqrt_ftz(rh + Z2);
-  const float ri2 = rinv * rinv, ri4 = ri2 * ri2;
-  const float a0 = fmaf(X2, f.cA, Y2 * f.cB);
-  const float h1 = fmaf(X2, f.cX1, Y2 * f.cY1);
-  const float h0 = fmaf(X2, fmaf(X2, f.cXX, Y2 * f.cXY), Y2 * Y2 * f.cYY);
-  const float n2 = fmaf(f.a1, Z2, a0);
-  const float H = fmaf(fmaf(f.h2, Z2, h1), Z2, h0);
-  const float t = fmaf(H, ri4, n2) * ri4;
-  const float base = ut * rinv * ri2;
-  return fmaf(base, t, base);
+// Unit column integral (normalised, without dx dy) for two far pairs on the
+// packed FP32 path: the exact vertical integral of the column axis plus the
+// 4th-order horizontal correction at its top and bottom.  The three SFU
+// operations per pair stay scalar.  Also hands back 1/r of the column top.
+__device__ __forceinline__ float2 col_unit2_it(float2 rh, float2 ut, float2 th, float2 Q2, float2 P4,
+                                               float2 P2, const IConst& k, float2* it_out) {
+  const float2 ub = __fadd2_rn(ut, th);
+  const float2 rt2 = __ffma2_rn(ut, ut, rh), rb2 = __ffma2_rn(ub, ub, rh);
+  const float2 it = make_float2(rsqrt_ftz(rt2.x), rsqrt_ftz(rt2.y));
+  const float2 ib = make_float2(rsqrt_ftz(rb2.x), rsqrt_ftz(rb2.y));
+  *it_out = it;
+  const float2 itb = __fmul2_rn(it, ib);
+  const float2 num = __fmul2_rn(__fmul2_rn(th, __fadd2_rn(ut, ub)), __fmul2_rn(itb, itb));
+  const float2 den = __fadd2_rn(it, ib);
+  const float2 L = make_float2(__fdividef(num.x, den.x), __fdividef(num.y, den.y));
+  const float2 Q0 = make_float2(k.Q0, k.Q0), P0 = make_float2(k.P0, k.P0);
+  const float2 it2 = __fmul2_rn(it, it), ib2 = __fmul2_rn(ib, ib);
+  const float2 it5 = __fmul2_rn(__fmul2_rn(it2, it2), it), ib5 = __fmul2_rn(__fmul2_rn(ib2, ib2), ib);
+  const float2 it9 = __fmul2_rn(__fmul2_rn(it2, it2), it5), ib9 = __fmul2_rn(__fmul2_rn(ib2, ib2), ib5);
+  const float2 ct = __ffma2_rn(it9, __ffma2_rn(__ffma2_rn(P0, rt2, P2), rt2, P4),
+                               __fmul2_rn(it5, __ffma2_rn(Q0, rt2, Q2)));
+  const float2 cb = __ffma2_rn(ib9, __ffma2_rn(__ffma2_rn(P0, rb2, P2), rb2, P4),
+                               __fmul2_rn(ib5, __ffma2_rn(Q0, rb2, Q2)));
+  return __fadd2_rn(L, __fadd2_rn(ct, make_float2(-cb.x, -cb.y)));
 }
 
 // ---- forward, far (thread per station) ------------------------------------
-__global__ void __launch_bounds__(IF_TS)
+__global__ void __launch_bounds__(IF_TS, 8)
     iface_far_fwd(IConst k, int ns, const IStation* __restrict__ sf, const int2* __restrict__ si,
                   const float4* __restrict__ cf, const uint32_t* __restrict__ mask, int chunk_len,
                   double* __restrict__ partial) {
-  __shared__ float4 s_c[IF_TILE];
+  __shared__ float4 s_c[IF_TILE + 2];
   const int s = blockIdx.x * IF_TS + threadIdx.x;
   const bool active = s < ns;
   IStation st = {0.f, 0.f, 0.f, 0.f};
@@ -209,36 +227,63 @@ __global__ void __launch_bounds__(IF_TS)
     hi = si[s];
   }
   const int c0 = blockIdx.y * chunk_len, c1 = min(k.ncols, c0 + chunk_len);
+  // this station's near window (clamped), for the per-column test
+  const int wcx = clampi(hi.x, 0, k.nx - 1), wcy = clampi(hi.y, 0, k.ny - 1);
+  const int wx0 = active ? max(0, wcx - k.w) : 1, wx1 = active ? min(k.nx - 1, wcx + k.w) : 0;
+  const int wy0 = max(0, wcy - k.w), wy1 = min(k.ny - 1, wcy + k.w);
+  const int wbw = wx1 - wx0 + 1;
   Kahan acc;
   for (int t0 = c0; t0 < c1; t0 += IF_TILE) {
     __syncthreads();
-    for (int q = threadIdx.x; q < IF_TILE; q += IF_TS)
+    for (int q = threadIdx.x; q < IF_TILE + 2; q += IF_TS)
       s_c[q] = (t0 + q < c1) ? cf[t0 + q] : make_float4(0.f, 0.f, 0.f, 0.f);
     __syncthreads();
     if (!active) continue;
     const int cnt = min(IF_TILE, c1 - t0);
-    int ix = t0 % k.nx, iy = t0 / k.nx;
-    float g = 0.f;  // plain sum over 8 columns, compensated across groups
-    for (int q = 0; q < cnt; q++) {
-      const float4 col = s_c[q];
-      const float X = fmaf((float)(hi.x - ix), k.dxn, st.ex);
-      const float Y = fmaf((float)(hi.y - iy), k.dyn, st.ey);
-      const float X2 = X * X, Y2 = Y * Y, rh = X2 + Y2;
-      const float Q2 = fmaf(k.q2x, X2, k.q2y * Y2);
-      const float P4 = fmaf(k.p4x * X2, X2, fmaf(k.p4y * Y2, Y2, k.p4xy * X2 * Y2));
-      const float P2 = fmaf(k.p2x, X2, k.p2y * Y2);
-      const float v = col.x * col_unit(X2, Y2, rh, st.zs + col.y, col.z, Q2, P4, P2, k);
-      g += is_near(mask, s, hi.x, hi.y, ix, iy, k) ? 0.f : v;  // select drops a NaN
-      if ((q & 7) == 7) {
-        acc.add(g);
-        g = 0.f;
+    float2 g = make_float2(0.f, 0.f);  // plain sums over 16 columns, Kahan across
+    int ixa = t0 % k.nx, iya = t0 / k.nx;
+    for (int q = 0; q < cnt; q += 2) {
+      // columns q and q+1 (the second is dropped past the end of the tile)
+      int ixb = ixa + 1, iyb = iya;
+      if (ixb == k.nx) {
+        ixb = 0;
+        ++iyb;
       }
-      if (++ix == k.nx) {
-        ix = 0;
-        ++iy;
+      const float4 A = s_c[q], B = s_c[q + 1];
+      const float2 X = make_float2(fmaf((float)(hi.x - ixa), k.dxn, st.ex),
+                                   fmaf((float)(hi.x - ixb), k.dxn, st.ex));
+      const float2 Y = make_float2(fmaf((float)(hi.y - iya), k.dyn, st.ey),
+                                   fmaf((float)(hi.y - iyb), k.dyn, st.ey));
+      const float2 X2 = __fmul2_rn(X, X), Y2 = __fmul2_rn(Y, Y), rh = __fadd2_rn(X2, Y2);
+      const float2 Q2 = __ffma2_rn(make_float2(k.q2x, k.q2x), X2, __fmul2_rn(make_float2(k.q2y, k.q2y), Y2));
+      const float2 P4 = __ffma2_rn(__fmul2_rn(make_float2(k.p4x, k.p4x), X2), X2,
+                                   __ffma2_rn(__fmul2_rn(make_float2(k.p4y, k.p4y), Y2), Y2,
+                                              __fmul2_rn(__fmul2_rn(make_float2(k.p4xy, k.p4xy), X2), Y2)));
+      const float2 P2 = __ffma2_rn(make_float2(k.p2x, k.p2x), X2, __fmul2_rn(make_float2(k.p2y, k.p2y), Y2));
+      const float2 ut = __fadd2_rn(make_float2(st.zs, st.zs), make_float2(A.y, B.y));
+      float2 itop;
+      float2 v = __fmul2_rn(make_float2(A.x, B.x),
+                            col_unit2_it(rh, ut, make_float2(A.z, B.z), Q2, P4, P2, k, &itop));
+      // near columns (and the padding column) contribute through the double
+      // path or not at all: select, which also drops a NaN
+      if (ixa >= wx0 && ixa <= wx1 && iya >= wy0 && iya <= wy1 && near_bit(mask, s, ixa - wx0 + wbw * (iya - wy0), k))
+        v.x = 0.f;
+      if (q + 1 >= cnt || (ixb >= wx0 && ixb <= wx1 && iyb >= wy0 && iyb <= wy1 &&
+                           near_bit(mask, s, ixb - wx0 + wbw * (iyb - wy0), k)))
+        v.y = 0.f;
+      g = __fadd2_rn(g, v);
+      if ((q & 14) == 14) {
+        acc.add(g.x + g.y);
+        g = make_float2(0.f, 0.f);
+      }
+      ixa = ixb + 1;
+      iya = iyb;
+      if (ixa == k.nx) {
+        ixa = 0;
+        ++iya;
       }
     }
-    acc.add(g);
+    acc.add(g.x + g.y);
   }
   if (active) partial[(size_t)blockIdx.y * ns + s] = acc.value();
 }
@@ -312,16 +357,17 @@ __global__ void __launch_bounds__(IF_TS)
                   const float4* __restrict__ cf, const uint32_t* __restrict__ mask, double sc_rho,
                   double sc_dep,
                   double* __restrict__ g_rho, double* __restrict__ g_dep) {
-  __shared__ IStation s_f[IF_TILE];
-  __shared__ int2 s_i[IF_TILE];
+  __shared__ IStation s_f[IF_TILE + 2];
+  __shared__ int2 s_i[IF_TILE + 2];
   const int c = blockIdx.x * IF_TS + threadIdx.x;
   const bool active = c < k.ncols;
   const int ix = active ? c % k.nx : 0, iy = active ? c / k.nx : 0;
   const float4 col = active ? cf[c] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float2 cy2 = make_float2(col.y, col.y), cz2 = make_float2(col.z, col.z);
   Kahan ar, ad;
   for (int t0 = 0; t0 < ns; t0 += IF_TILE) {
     __syncthreads();
-    for (int q = threadIdx.x; q < IF_TILE; q += IF_TS) {
+    for (int q = threadIdx.x; q < IF_TILE + 2; q += IF_TS) {
       const bool ok = t0 + q < ns;
       IStation z = {0.f, 0.f, 0.f, 0.f};
       s_f[q] = ok ? sf[t0 + q] : z;
@@ -330,22 +376,41 @@ __global__ void __launch_bounds__(IF_TS)
     __syncthreads();
     if (!active) continue;
     const int cnt = min(IF_TILE, ns - t0);
-    for (int q = 0; q < cnt; q++) {
-      const IStation st = s_f[q];
-      const int2 h = s_i[q];
-      const float X = fmaf((float)(h.x - ix), k.dxn, st.ex);
-      const float Y = fmaf((float)(h.y - iy), k.dyn, st.ey);
-      const float X2 = X * X, Y2 = Y * Y, rh = X2 + Y2;
-      const float Q2 = fmaf(k.q2x, X2, k.q2y * Y2);
-      const float P4 = fmaf(k.p4x * X2, X2, fmaf(k.p4y * Y2, Y2, k.p4xy * X2 * Y2));
-      const float P2 = fmaf(k.p2x, X2, k.p2y * Y2);
-      const float ut = st.zs + col.y;
-      const float u = col_unit(X2, Y2, rh, ut, col.z, Q2, P4, P2, k);
-      const float f = face_unit_far(X2, Y2, rh, ut, k.face);
-      const bool near = is_near(mask, t0 + q, h.x, h.y, ix, iy, k);
-      ar.add(near ? 0.f : st.r * u);
-      ad.add(near ? 0.f : st.r * f);
+    float2 gr = make_float2(0.f, 0.f), gd = make_float2(0.f, 0.f);  // 16 stations, Kahan across
+    for (int q = 0; q < cnt; q += 2) {
+      // stations q and q+1 (the second is dropped past the end of the tile)
+      const IStation sa = s_f[q], sb = s_f[q + 1];
+      const int2 ha = s_i[q], hb = s_i[q + 1];
+      const float2 X = make_float2(fmaf((float)(ha.x - ix), k.dxn, sa.ex),
+                                   fmaf((float)(hb.x - ix), k.dxn, sb.ex));
+      const float2 Y = make_float2(fmaf((float)(ha.y - iy), k.dyn, sa.ey),
+                                   fmaf((float)(hb.y - iy), k.dyn, sb.ey));
+      const float2 X2 = __fmul2_rn(X, X), Y2 = __fmul2_rn(Y, Y), rh = __fadd2_rn(X2, Y2);
+      const float2 Q2 = __ffma2_rn(make_float2(k.q2x, k.q2x), X2, __fmul2_rn(make_float2(k.q2y, k.q2y), Y2));
+      const float2 P4 = __ffma2_rn(__fmul2_rn(make_float2(k.p4x, k.p4x), X2), X2,
+                                   __ffma2_rn(__fmul2_rn(make_float2(k.p4y, k.p4y), Y2), Y2,
+                                              __fmul2_rn(__fmul2_rn(make_float2(k.p4xy, k.p4xy), X2), Y2)));
+      const float2 P2 = __ffma2_rn(make_float2(k.p2x, k.p2x), X2, __fmul2_rn(make_float2(k.p2y, k.p2y), Y2));
+      const float2 ut = __fadd2_rn(make_float2(sa.zs, sb.zs), cy2);
+      float2 itop;
+      const float2 u = col_unit2_it(rh, ut, cz2, Q2, P4, P2, k, &itop);
+      const float2 f = face_unit_far2(X2, Y2, ut, itop, k.face);
+      const float2 r = make_float2(sa.r, sb.r);
+      float2 vr = __fmul2_rn(r, u), vd = __fmul2_rn(r, f);
+      // near pairs (and the padding station) go through the double path or
+      // nowhere: select, which also drops a NaN
+      if (is_near(mask, t0 + q, ha.x, ha.y, ix, iy, k)) vr.x = vd.x = 0.f;
+      if (q + 1 >= cnt || is_near(mask, t0 + q + 1, hb.x, hb.y, ix, iy, k)) vr.y = vd.y = 0.f;
+      gr = __fadd2_rn(gr, vr);
+      gd = __fadd2_rn(gd, vd);
+      if ((q & 14) == 14) {
+        ar.add(gr.x + gr.y);
+        ad.add(gd.x + gd.y);
+        gr = gd = make_float2(0.f, 0.f);
+      }
     }
+    ar.add(gr.x + gr.y);
+    ad.add(gd.x + gd.y);
   }
   if (!active) return;
   if (g_rho) g_rho[c] = sc_rho * ar.value();
