@@ -195,6 +195,17 @@ typedef struct {
 int ztm_density_build(ztm_ctx* ctx, const ztm_density_params* p,
                       const double* sea, const double* M, const double* v,
                       double* drho, long long* n_selected, int flags);
+/* TFM.cpp:83-99 in one call: the density builder above followed by the
+ * point-mass forward over the nodes it selects, with drho kept in device
+ * memory between the two (no drho round trip through the host).  grid
+ * supplies bfr, threshold and scale and must have the dims of p; surf and G
+ * are as in ztm_gfm_pointmass.  With the reference's threshold 0.001 the
+ * result equals ztm_density_build + ztm_gfm_pointmass with TFM's nn list. */
+int ztm_gfm_pointmass_model(ztm_ctx* ctx, const ztm_density_params* p,
+                            const ztm_grid* grid, const double* sea,
+                            const double* M, const double* v,
+                            const double* surf, double* G, int precision,
+                            int flags);
 
 /* ---- prism mode -------------------------------------------------------- */
 /* gz[s] = sum over all prisms of the closed-form attraction of prism p at

@@ -31,6 +31,7 @@ EXPORTS = (
     "ztm_gfm_interface", "ztm_gfm_interface_adjoint", "ztm_gfm_interface_misfit",
     "ztm_gfm_batch", "ztm_ctx_profile", "ztm_ctx_profile_read", "ztm_measure_peak",
     "ztm_invert_interface", "ztm_gfm_pointmass_noalloc", "ztm_density_build",
+    "ztm_gfm_pointmass_model",
 )
 
 
@@ -97,6 +98,8 @@ _SIGS = {
     "ztm_gfm_batch": (_I, [_P, ctypes.POINTER(Job), _I, ctypes.POINTER(Opts)]),
     "ztm_density_build": (_I, [_P, ctypes.POINTER(DensityParams), _P, _P, _P, _P,
                                ctypes.POINTER(_LL), _I]),
+    "ztm_gfm_pointmass_model": (_I, [_P, ctypes.POINTER(DensityParams), ctypes.POINTER(Grid),
+                                     _P, _P, _P, _P, _P, _I, _I]),
     "ztm_ctx_profile": (_I, [_P, _I]),
     "ztm_ctx_profile_read": (_I, [_P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double),
                                   ctypes.POINTER(_LL)]),

@@ -108,6 +108,69 @@ __global__ void density_kernel(DensArgs a, const double* __restrict__ sea,
   if ((threadIdx.x & 31) == 0 && b) atomicAdd(count, (unsigned long long)__popc(b));
 }
 
+// Checks the parameters and fills the kernel arguments.
+int dens_setup(ztm_ctx* c, const ztm_density_params* p, DensArgs* a) {
+  if (p->di < 2 || p->dj < 2 || p->dk < 2 || p->fh < 1 || p->fv < 1)
+    return ztm_fail(c, ZTM_ERR_ARG, "grid dims must be >= 2 and refinements >= 1");
+  a->di = p->di; a->dj = p->dj; a->dk = p->dk; a->fh = p->fh; a->fv = p->fv;
+  a->ii = (p->di - 1) * p->fh + 1;
+  a->jj = (p->dj - 1) * p->fh + 1;
+  a->N = (long long)a->ii * a->jj * ((p->dk - 1) * p->fv + 1);
+  if (a->N > (1LL << 31) - 1) return ztm_fail(c, ZTM_ERR_RANGE, "fine grid exceeds 2^31-1 nodes");
+  a->vm = p->vm; a->ro = p->ro; a->dr = p->dr;
+  // enu2geo's reference-point terms (SET.cpp:87-93), host libm as in the reference
+  const double rad = 57.295, R = 6371;
+  const double* rc = p->rc;
+  const double phi = rc[0] / rad, theta = rc[1] / rad;
+  const double m[9] = {-sin(theta), -sin(phi) * cos(theta), cos(phi) * cos(theta),
+                       cos(theta),  -sin(phi) * sin(theta), cos(phi) * sin(theta),
+                       0,           cos(phi),               sin(phi)};
+  for (int t = 0; t < 9; t++) a->g.m[t] = m[t];
+  a->g.xr = (R - rc[2]) * cos(rc[1] / rad) * cos(rc[0] / rad);
+  a->g.yr = (R - rc[2]) * sin(rc[1] / rad) * cos(rc[0] / rad);
+  a->g.zr = (R - rc[2]) * sin(rc[0] / rad);
+  a->g.ox = rc[3]; a->g.oy = rc[4]; a->g.oz = rc[5]; a->g.h = rc[6];
+  return ZTM_OK;
+}
+
+struct DevRestore {
+  int p = -1, d;
+  explicit DevRestore(int dev) : d(dev) {
+    cudaGetDevice(&p);
+    if (p != d) cudaSetDevice(d);
+  }
+  ~DevRestore() {
+    if (p >= 0 && p != d) cudaSetDevice(p);
+  }
+};
+
+// Stages sea, M, v and launches the builder into `out` (device).
+int dens_run(ztm_ctx* c, const DensArgs& a, const double* sea, const double* M, const double* v,
+             bool dev, WsCarver& wc, double* out, unsigned long long* cnt) {
+  const size_t M2 = (size_t)a.di * a.dj, M3 = M2 * a.dk;
+  double* s_sea = wc.take<double>(M2);
+  double* s_M = wc.take<double>(M2);
+  double* s_v = wc.take<double>(M3);
+  const void *ps, *pm, *pv;
+  int rc;
+  if ((rc = ztm_stage_in(c, sea, M2 * 8, dev, s_sea, &ps))) return rc;
+  if ((rc = ztm_stage_in(c, M, M2 * 8, dev, s_M, &pm))) return rc;
+  if ((rc = ztm_stage_in(c, v, M3 * 8, dev, s_v, &pv))) return rc;
+  cudaMemsetAsync(cnt, 0, 8, c->stream);
+  {
+    ZtmProf prof_(c, "density");
+    density_kernel<<<(unsigned)((a.N + 255) / 256), 256, 0, c->stream>>>(
+        a, (const double*)ps, (const double*)pm, (const double*)pv, out, cnt);
+  }
+  c->launches++;
+  return ztm_after_launch(c, "density builder");
+}
+
+size_t dens_ws(const DensArgs& a) {
+  const size_t M2 = (size_t)a.di * a.dj, M3 = M2 * a.dk;
+  return 2 * WsCarver::need(M2 * 8) + WsCarver::need(M3 * 8) + WsCarver::need(8);
+}
+
 }  // namespace
 
 extern "C" int ztm_density_build(ztm_ctx* c, const ztm_density_params* p, const double* sea,
@@ -117,61 +180,18 @@ extern "C" int ztm_density_build(ztm_ctx* c, const ztm_density_params* p, const 
   c->err.clear();
   if (!p || !sea || !M || !v || !drho) return ztm_fail(c, ZTM_ERR_ARG, "null argument");
   if (flags & ~ZTM_FLAG_DEVICE_PTRS) return ztm_fail(c, ZTM_ERR_ARG, "unknown flag");
-  if (p->di < 2 || p->dj < 2 || p->dk < 2 || p->fh < 1 || p->fv < 1)
-    return ztm_fail(c, ZTM_ERR_ARG, "grid dims must be >= 2 and refinements >= 1");
   const bool dev = (flags & ZTM_FLAG_DEVICE_PTRS) != 0;
   DensArgs a;
-  a.di = p->di; a.dj = p->dj; a.dk = p->dk; a.fh = p->fh; a.fv = p->fv;
-  a.ii = (p->di - 1) * p->fh + 1;
-  a.jj = (p->dj - 1) * p->fh + 1;
-  a.N = (long long)a.ii * a.jj * ((p->dk - 1) * p->fv + 1);
-  if (a.N > (1LL << 31) - 1) return ztm_fail(c, ZTM_ERR_RANGE, "fine grid exceeds 2^31-1 nodes");
-  a.vm = p->vm; a.ro = p->ro; a.dr = p->dr;
-  // enu2geo's reference-point terms (SET.cpp:87-93), host libm as in the reference
-  const double rad = 57.295, R = 6371;
-  const double* rc = p->rc;
-  const double phi = rc[0] / rad, theta = rc[1] / rad;
-  const double m[9] = {-sin(theta), -sin(phi) * cos(theta), cos(phi) * cos(theta),
-                       cos(theta),  -sin(phi) * sin(theta), cos(phi) * sin(theta),
-                       0,           cos(phi),               sin(phi)};
-  for (int t = 0; t < 9; t++) a.g.m[t] = m[t];
-  a.g.xr = (R - rc[2]) * cos(rc[1] / rad) * cos(rc[0] / rad);
-  a.g.yr = (R - rc[2]) * sin(rc[1] / rad) * cos(rc[0] / rad);
-  a.g.zr = (R - rc[2]) * sin(rc[0] / rad);
-  a.g.ox = rc[3]; a.g.oy = rc[4]; a.g.oz = rc[5]; a.g.h = rc[6];
-  int prev = -1;
-  cudaGetDevice(&prev);
-  if (prev != c->device) cudaSetDevice(c->device);
-  struct Restore {
-    int p, d;
-    ~Restore() {
-      if (p >= 0 && p != d) cudaSetDevice(p);
-    }
-  } restore{prev, c->device};
-  const size_t M2 = (size_t)p->di * p->dj, M3 = M2 * p->dk;
-  size_t need = 2 * WsCarver::need(M2 * 8) + WsCarver::need(M3 * 8) + WsCarver::need(a.N * 8) +
-                WsCarver::need(8) + 4096;
-  int rc2 = ztm_ws_reserve(c, need);
+  int rc2 = dens_setup(c, p, &a);
   if (rc2) return rc2;
+  DevRestore restore(c->device);
+  size_t need = dens_ws(a) + WsCarver::need(a.N * 8) + 4096;
+  if ((rc2 = ztm_ws_reserve(c, need))) return rc2;
   WsCarver wc(c->ws);
-  double* s_sea = wc.take<double>(M2);
-  double* s_M = wc.take<double>(M2);
-  double* s_v = wc.take<double>(M3);
   double* s_d = wc.take<double>(a.N);
   unsigned long long* cnt = wc.take<unsigned long long>(1);
-  const void *ps, *pm, *pv;
-  if ((rc2 = ztm_stage_in(c, sea, M2 * 8, dev, s_sea, &ps))) return rc2;
-  if ((rc2 = ztm_stage_in(c, M, M2 * 8, dev, s_M, &pm))) return rc2;
-  if ((rc2 = ztm_stage_in(c, v, M3 * 8, dev, s_v, &pv))) return rc2;
   double* out = dev ? drho : s_d;
-  cudaMemsetAsync(cnt, 0, 8, c->stream);
-  {
-    ZtmProf prof_(c, "density");
-    density_kernel<<<(unsigned)((a.N + 255) / 256), 256, 0, c->stream>>>(
-        a, (const double*)ps, (const double*)pm, (const double*)pv, out, cnt);
-  }
-  c->launches++;
-  if ((rc2 = ztm_after_launch(c, "density builder"))) return rc2;
+  if ((rc2 = dens_run(c, a, sea, M, v, dev, wc, out, cnt))) return rc2;
   if (!dev) {
     unsigned long long h = 0;
     cudaMemcpyAsync(drho, s_d, a.N * 8, cudaMemcpyDeviceToHost, c->stream);
@@ -182,4 +202,45 @@ extern "C" int ztm_density_build(ztm_ctx* c, const ztm_density_params* p, const 
     *n_selected = -1;  // not waited for with device pointers
   }
   return ZTM_OK;
+}
+
+// TFM.cpp:83-99 in one call: the builder writes drho into the workspace and
+// the point-mass forward reads it there (nodes with |drho| > threshold; the
+// builder has zeroed every node TFM.cpp:89 leaves out of nn).
+extern "C" int ztm_gfm_pointmass_model(ztm_ctx* c, const ztm_density_params* dp,
+                                       const ztm_grid* g, const double* sea, const double* M,
+                                       const double* v, const double* surf, double* G,
+                                       int precision, int flags) {
+  if (!c) return ZTM_ERR_ARG;
+  c->err.clear();
+  if (!dp || !g || !sea || !M || !v || !surf || !G)
+    return ztm_fail(c, ZTM_ERR_ARG, "null argument");
+  if (flags & ~ZTM_FLAG_DEVICE_PTRS) return ztm_fail(c, ZTM_ERR_ARG, "unknown flag");
+  if (precision != ZTM_PREC_FP64 && precision != ZTM_PREC_FP32)
+    return ztm_fail(c, ZTM_ERR_ARG, "point-mass precision must be FP64 or FP32");
+  if (dp->di != g->di || dp->dj != g->dj || dp->dk != g->dk || dp->fh != g->fh || dp->fv != g->fv)
+    return ztm_fail(c, ZTM_ERR_ARG, "density and grid dimensions differ");
+  const bool dev = (flags & ZTM_FLAG_DEVICE_PTRS) != 0;
+  DensArgs a;
+  int rc = dens_setup(c, dp, &a);
+  if (rc) return rc;
+  PmParams p;
+  if ((rc = ztm_pm_setup(c, g, &p))) return rc;
+  DevRestore restore(c->device);
+  const size_t M2 = (size_t)g->di * g->dj;
+  size_t need = dens_ws(a) + WsCarver::need(a.N * 8) + 2 * WsCarver::need(M2 * 8) +
+                ztm_pointmass_ws(p, precision, c->num_sms) + 4096;
+  if ((rc = ztm_ws_reserve(c, need))) return rc;
+  WsCarver wc(c->ws);
+  double* d_rho = wc.take<double>(a.N);
+  unsigned long long* cnt = wc.take<unsigned long long>(1);
+  double* s_surf = wc.take<double>(M2);
+  double* s_G = wc.take<double>(M2);
+  if ((rc = dens_run(c, a, sea, M, v, dev, wc, d_rho, cnt))) return rc;
+  const void* ps;
+  if ((rc = ztm_stage_in(c, surf, M2 * 8, dev, s_surf, &ps))) return rc;
+  double* outG = dev ? G : s_G;
+  rc = ztm_launch_pointmass(c, p, d_rho, nullptr, (const double*)ps, outG, g->scale, precision, wc);
+  if (rc) return rc;
+  return ztm_finish(c, dev, G, outG, M2 * 8, "density + point-mass forward");
 }

@@ -115,6 +115,31 @@ int finish(ztm_ctx* c, bool dev, void* host_out, const void* dev_out,
 
 // ---------------------------------------------------------------------------
 // shared host helpers (declared in ztm_internal.cuh)
+int ztm_finish(ztm_ctx* c, bool dev, void* host_out, const void* dev_out, size_t bytes,
+               const char* what) {
+  return finish(c, dev, host_out, dev_out, bytes, what);
+}
+
+int ztm_pm_setup(ztm_ctx* c, const ztm_grid* g, PmParams* p) {
+  if (g->di < 1 || g->dj < 1 || g->dk < 1 || g->fh < 1 || g->fv < 1 || g->bfr < 0)
+    return ztm_fail(c, ZTM_ERR_ARG, "grid dims must be >= 1 and bfr >= 0");
+  if (!(g->threshold >= 0) || !isfinite(g->scale))
+    return ztm_fail(c, ZTM_ERR_ARG, "bad threshold or scale");
+  p->di = g->di; p->dj = g->dj; p->fh = g->fh; p->fv = g->fv; p->bfr = g->bfr;
+  p->ii = (g->di - 1) * g->fh + 1;
+  p->jj = (g->dj - 1) * g->fh + 1;
+  p->kk = (g->dk - 1) * g->fv + 1;
+  p->N = (long long)p->ii * p->jj * p->kk;
+  if (p->N > (1LL << 31) - 1)
+    return ztm_fail(c, ZTM_ERR_RANGE, "fine grid exceeds 2^31-1 nodes");
+  p->ni = std::max(0, g->di - 2 * g->bfr);
+  p->nj = std::max(0, g->dj - 2 * g->bfr);
+  p->ns = p->ni * p->nj;
+  p->thr = g->threshold;
+  p->nnodes = p->N;
+  return ZTM_OK;
+}
+
 int ztm_fail(ztm_ctx* c, int code, const std::string& msg) {
   if (c) c->err = msg;
   return code;
@@ -288,24 +313,12 @@ int ztm_gfm_pointmass(ztm_ctx* c, const ztm_grid* g, const double* drho,
   if (precision != ZTM_PREC_FP64 && precision != ZTM_PREC_FP32)
     return ztm_fail(c, ZTM_ERR_ARG, "point-mass precision must be FP64 or FP32");
   if (flags & ~ZTM_FLAG_DEVICE_PTRS) return ztm_fail(c, ZTM_ERR_ARG, "unknown flag");
-  if (g->di < 1 || g->dj < 1 || g->dk < 1 || g->fh < 1 || g->fv < 1 || g->bfr < 0)
-    return ztm_fail(c, ZTM_ERR_ARG, "grid dims must be >= 1 and bfr >= 0");
-  if (!(g->threshold >= 0) || !isfinite(g->scale))
-    return ztm_fail(c, ZTM_ERR_ARG, "bad threshold or scale");
   PmParams p;
-  p.di = g->di; p.dj = g->dj; p.fh = g->fh; p.fv = g->fv; p.bfr = g->bfr;
-  p.ii = (g->di - 1) * g->fh + 1;
-  p.jj = (g->dj - 1) * g->fh + 1;
-  p.kk = (g->dk - 1) * g->fv + 1;
-  long long N = (long long)p.ii * p.jj * p.kk;
-  if (N > (1LL << 31) - 1) return ztm_fail(c, ZTM_ERR_RANGE, "fine grid exceeds 2^31-1 nodes");
-  p.ni = std::max(0, g->di - 2 * g->bfr);
-  p.nj = std::max(0, g->dj - 2 * g->bfr);
-  p.ns = p.ni * p.nj;
-  p.thr = g->threshold;
+  int rc = ztm_pm_setup(c, g, &p);
+  if (rc) return rc;
+  const long long N = p.N;
   if (nn && n_nn < 0) return ztm_fail(c, ZTM_ERR_ARG, "n_nn < 0");
   p.nnodes = nn ? n_nn : N;
-  p.N = N;
   const bool dev = is_dev(flags);
   if (nn && !dev) {
     for (long long t = 0; t < n_nn; t++)
@@ -317,7 +330,7 @@ int ztm_gfm_pointmass(ztm_ctx* c, const ztm_grid* g, const double* drho,
   if (!dg.ok) return ztm_fail(c, ZTM_ERR_NODEV, "cannot select device");
   size_t need = WsCarver::need(N * 8) + WsCarver::need((nn ? n_nn : 0) * 4) +
                 2 * WsCarver::need(M * 8) + ztm_pointmass_ws(p, precision, c->num_sms) + 4096;
-  int rc = ztm_ws_reserve(c, need);
+  rc = ztm_ws_reserve(c, need);
   if (rc) return rc;
   WsCarver wc(c->ws);
   double* s_drho = wc.take<double>(N);

@@ -111,6 +111,12 @@ int ztm_launch_pointmass(ztm_ctx* c, const PmParams& p, const double* d_drho,
                          const int* d_nn, const double* d_surf, double* d_G,
                          double scale, int precision, WsCarver& wc);
 size_t ztm_pointmass_ws(const PmParams& p, int precision, int num_sms);
+// Checks a point-mass grid and fills p (nnodes = N, every node).
+int ztm_pm_setup(ztm_ctx* c, const ztm_grid* g, PmParams* p);
+// End of a call: launch/device error check; in host mode copy `bytes` of
+// dev_out to host_out and synchronise.
+int ztm_finish(ztm_ctx* c, bool dev, void* host_out, const void* dev_out, size_t bytes,
+               const char* what);
 
 struct MeshDesc {
   int nx, ny, nz;

@@ -244,6 +244,22 @@ class GravityContext:
                                                 ctypes.byref(n), a.flags)
         return out, n.value
 
+    def pointmass_model(self, grid, sea, M, v, surf, vm, ro, dr, rc, precision="fp64"):
+        """TFM.cpp:83-99 in one call: G (di*dj, mGal) from the sea-level map,
+        rendered Moho and velocity grids, drho staying on the device."""
+        p = _lib.DensityParams(grid.di, grid.dj, grid.dk, grid.fh, grid.fv, vm, ro, dr,
+                               (ctypes.c_double * 10)(*rc))
+        a = _Args(self)
+        ps = a.arr(sea, grid.di * grid.dj, name="sea")
+        pm = a.arr(M, grid.di * grid.dj, name="M")
+        pv = a.arr(v, grid.di * grid.dj * grid.dk, name="v")
+        pf = a.arr(surf, grid.di * grid.dj, name="surf")
+        out, po = a.out(grid.di * grid.dj, sea)
+        prec = PRECISIONS[precision] if isinstance(precision, str) else precision
+        self._run(a, self._lib.ztm_gfm_pointmass_model, self._h, ctypes.byref(p),
+                  ctypes.byref(grid), ps, pm, pv, pf, po, prec, a.flags)
+        return out
+
     # -- prism mesh -----------------------------------------------------
     def prism(self, mesh, rho, stations, precision="mixed", G=None, near_q=None, tile=0, chunk=0,
               autotune=False):
