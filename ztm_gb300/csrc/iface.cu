@@ -352,11 +352,10 @@ __global__ void __launch_bounds__(64)
 }
 
 // ---- adjoint, far (thread per column) --------------------------------------
-__global__ void __launch_bounds__(IF_TS)
+__global__ void __launch_bounds__(IF_TS, 8)
     iface_far_adj(IConst k, int ns, const IStation* __restrict__ sf, const int2* __restrict__ si,
-                  const float4* __restrict__ cf, const uint32_t* __restrict__ mask, double sc_rho,
-                  double sc_dep,
-                  double* __restrict__ g_rho, double* __restrict__ g_dep) {
+                  const float4* __restrict__ cf, const uint32_t* __restrict__ mask, int chunk_len,
+                  double* __restrict__ p_rho, double* __restrict__ p_dep) {
   __shared__ IStation s_f[IF_TILE + 2];
   __shared__ int2 s_i[IF_TILE + 2];
   const int c = blockIdx.x * IF_TS + threadIdx.x;
@@ -364,18 +363,20 @@ __global__ void __launch_bounds__(IF_TS)
   const int ix = active ? c % k.nx : 0, iy = active ? c / k.nx : 0;
   const float4 col = active ? cf[c] : make_float4(0.f, 0.f, 0.f, 0.f);
   const float2 cy2 = make_float2(col.y, col.y), cz2 = make_float2(col.z, col.z);
+  // this block's slice of the stations (grid.y)
+  const int s0 = blockIdx.y * chunk_len, s1 = min(ns, s0 + chunk_len);
   Kahan ar, ad;
-  for (int t0 = 0; t0 < ns; t0 += IF_TILE) {
+  for (int t0 = s0; t0 < s1; t0 += IF_TILE) {
     __syncthreads();
     for (int q = threadIdx.x; q < IF_TILE + 2; q += IF_TS) {
-      const bool ok = t0 + q < ns;
+      const bool ok = t0 + q < s1;
       IStation z = {0.f, 0.f, 0.f, 0.f};
       s_f[q] = ok ? sf[t0 + q] : z;
       s_i[q] = ok ? si[t0 + q] : make_int2(0, 0);
     }
     __syncthreads();
     if (!active) continue;
-    const int cnt = min(IF_TILE, ns - t0);
+    const int cnt = min(IF_TILE, s1 - t0);
     float2 gr = make_float2(0.f, 0.f), gd = make_float2(0.f, 0.f);  // 16 stations, Kahan across
     for (int q = 0; q < cnt; q += 2) {
       // stations q and q+1 (the second is dropped past the end of the tile)
@@ -413,8 +414,26 @@ __global__ void __launch_bounds__(IF_TS)
     ad.add(gd.x + gd.y);
   }
   if (!active) return;
-  if (g_rho) g_rho[c] = sc_rho * ar.value();
-  if (g_dep) g_dep[c] = -sc_dep * (double)col.x * ad.value();
+  const size_t o = (size_t)blockIdx.y * k.ncols + c;
+  p_rho[o] = ar.value();
+  p_dep[o] = (double)col.x * ad.value();
+}
+
+// g_rho[c] = sc_rho * sum_chunks p_rho,  g_dep[c] = -sc_dep * sum_chunks p_dep
+// (fixed order: bitwise reproducible for a launch shape)
+__global__ void iface_far_adj_finalize(long long nc, int nchunks, const double* __restrict__ p_rho,
+                                       const double* __restrict__ p_dep, double sc_rho,
+                                       double sc_dep, double* __restrict__ g_rho,
+                                       double* __restrict__ g_dep) {
+  const long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  double r = 0.0, d = 0.0;
+  for (int q = 0; q < nchunks; q++) {
+    r += p_rho[(size_t)q * nc + c];
+    d += p_dep[(size_t)q * nc + c];
+  }
+  if (g_rho) g_rho[c] = sc_rho * r;
+  if (g_dep) g_dep[c] = -sc_dep * d;
 }
 
 // ---- adjoint, near window in double (warp per station, atomics) ------------
@@ -522,6 +541,23 @@ int chunks_for(long long units, int tiles, int num_sms, int minlen, int* len) {
   return (int)((units + *len - 1) / *len);
 }
 
+// Station slices of the mixed adjoint: about three waves of blocks of
+// column tiles x slices, slices of at least one shared-memory tile.
+int iface_adj_chunks(int ns, long long nc, int num_sms, int* len) {
+  int occ = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, iface_far_adj, IF_TS, 0) != cudaSuccess ||
+      occ < 1) {
+    cudaGetLastError();
+    occ = 1;
+  }
+  const long long tiles = std::max(1LL, (nc + IF_TS - 1) / IF_TS);
+  long long ch = std::max(1LL, 3LL * occ * std::max(num_sms, 1) / tiles);
+  ch = std::min(ch, std::max(1LL, (long long)(ns + IF_TILE - 1) / IF_TILE));
+  ch = std::min(ch, 65535LL);
+  *len = (int)((std::max(ns, 1) + ch - 1) / ch);
+  return (int)((std::max(ns, 1) + *len - 1) / *len);
+}
+
 }  // namespace
 
 size_t ztm_iface_ws(const IMeshDesc& m, int ns, int precision, int num_sms) {
@@ -532,6 +568,10 @@ size_t ztm_iface_ws(const IMeshDesc& m, int ns, int precision, int num_sms) {
   int cha = chunks_for(std::max(ns, 1), (int)((nc + IF_TS - 1) / IF_TS), num_sms, 32, &len);
   size_t w = WsCarver::need((size_t)ch * std::max(ns, 1) * 8) * 2;  // forward partials (x2 slack)
   w += WsCarver::need((size_t)cha * nc * 8) * 2;                    // double adjoint partials
+  const int chm = iface_adj_chunks(ns, nc, num_sms, &len);
+  w += WsCarver::need((size_t)chm * nc * 8) * 2;                    // mixed adjoint partials
+  // a second set of station and column arrays (forward + adjoint in one call)
+  w += WsCarver::need((size_t)nc * 16) + WsCarver::need((size_t)std::max(ns, 1) * 24);
   w += WsCarver::need((size_t)nc * 16) + WsCarver::need((size_t)std::max(ns, 1) * 16) +
        WsCarver::need((size_t)std::max(ns, 1) * 8) * 4;
   // near masks (forward and adjoint), up to near_q = 16
@@ -638,17 +678,23 @@ int ztm_launch_iface_adj(ztm_ctx* c, const IMeshDesc& m, const double* d_depth,
   const double sc_dep = G5 * (double)k.dxn * k.dyn;
   uint32_t* mask = wc.take<uint32_t>((size_t)ns * k.words);
   iface_near_mask<<<(ns + 3) / 4, 128, 0, c->stream>>>(k, ns, d_sxyz, si, d_depth, mask);
+  int alen;
+  const int ach = iface_adj_chunks(ns, nc, c->num_sms, &alen);
+  double* p_rho = wc.take<double>((size_t)ach * nc);
+  double* p_dep = wc.take<double>((size_t)ach * nc);
   {
     ZtmProf prof_(c, "iface_far");
-    iface_far_adj<<<(unsigned)((nc + IF_TS - 1) / IF_TS), IF_TS, 0, c->stream>>>(
-        k, ns, sf, si, cf, mask, sc_rho, sc_dep, d_grho, d_gdep);
+    iface_far_adj<<<dim3((unsigned)((nc + IF_TS - 1) / IF_TS), ach), IF_TS, 0, c->stream>>>(
+        k, ns, sf, si, cf, mask, alen, p_rho, p_dep);
   }
+  iface_far_adj_finalize<<<(unsigned)((nc + 255) / 256), 256, 0, c->stream>>>(
+      nc, ach, p_rho, p_dep, sc_rho, sc_dep, d_grho, d_gdep);
   {  // after the far kernel has written every entry: double atomics add the near pairs
     ZtmProf prof_(c, "iface_near");
     iface_near_adj<<<(ns + IF_NEAR_WPB - 1) / IF_NEAR_WPB, IF_NEAR_WPB * 32, 0, c->stream>>>(
         k, m, ns, d_sxyz, si, d_depth, d_rho, d_res, mask, G5, d_grho, d_gdep);
   }
-  c->launches += 5;
+  c->launches += 6;
   return ztm_after_launch(c, "interface mixed adjoint");
 }
 

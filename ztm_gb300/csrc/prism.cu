@@ -168,8 +168,10 @@ __global__ void __launch_bounds__(NEAR_WPB * 32)
 struct FarArgs {
   MeshConst k;
   int ns;
-  int chunk_cols;  // columns per block (grid.y slices the mesh)
-  int sc;          // columns per shared-memory stage
+  int tiles, chunks;  // work items: tiles x chunks
+  int chunk_cols;     // columns per item
+  int sc;             // columns per shared-memory stage
+  int* counter;       // next work item (zeroed before the launch)
   const float4* sf;
   const int4* si;
   const short2* iv;  // near-region intervals [station][box column]
@@ -191,143 +193,194 @@ __device__ __forceinline__ float far_pair(float rho, float Z, float rh, float a0
   return fmaf(base, t, base);
 }
 
+// Per-thread station state of the far kernel for one tile of stations.
+struct FarStation {
+  float ex, ey, ez;
+  int ixs, iys, izs;
+  NearBox nb;
+};
+
+// One shared-memory stage (ncol columns starting at column cs) against this
+// thread's station; adds to acc.  Every lane runs the loop (inactive lanes
+// on dummy data) for the warp votes.
+__device__ __forceinline__ void far_stage(const FarArgs& a, const MeshConst& k, const FarCoef& fc,
+                                          const FarStation& t, int s, int Lm, const float* rs,
+                                          int cs, int ncol, Kahan& acc) {
+  const float2 dz2 = make_float2(k.dzn, k.dzn);
+  int ix = cs % k.nx, iy = cs / k.nx;
+  for (int q = 0; q < ncol; q++) {
+    const float X = fmaf((float)(t.ixs - ix), k.dxn, t.ex);
+    const float Y = fmaf((float)(t.iys - iy), k.dyn, t.ey);
+    const ColPoly cp = col_poly(X, Y, fc);
+    const bool ncl = ix >= t.nb.x0 && ix <= t.nb.x1 && iy >= t.nb.y0 && iy <= t.nb.y1;
+    int elo = k.nz;
+    unsigned espan = 0u;
+    if (ncl) {  // the column's near-region layers
+      const short2 iv = a.iv[(size_t)s * k.nslots + near_slot(t.nb, ix, iy)];
+      if (iv.x <= iv.y) {
+        elo = iv.x;
+        espan = (unsigned)(iv.y - iv.x);
+      }
+    }
+    const float* col = rs + q * k.nzp;
+    const ColPoly2 cp2 = col_poly2(cp, fc.a1);
+    // a column lies in some lane's near box only near the warp's stations:
+    // test that once per column for the whole warp
+    const bool warp_near = __any_sync(0xffffffffu, ncl);
+    // every lane of the warp far enough for the second-order form
+    const bool warp_t2 = __all_sync(0xffffffffu, cp.rh >= k.rh_t2);
+    const float2 c2t = make_float2(cp.C2 - fc.h2, cp.C2 - fc.h2);
+    float zf = (float)(-t.izs);  // (l0 - izs), exact in float, stepped by 8
+    for (int l0 = 0; l0 < k.nz; l0 += 8, zf += 8.f) {
+      const float4 ra = *reinterpret_cast<const float4*>(col + l0);
+      const float4 rb = *reinterpret_cast<const float4*>(col + l0 + 4);
+      const float Zg = fmaf(zf, k.dzn, t.ez);  // Z(l) = (l - izs) dz + ez
+      const float2 zg2 = make_float2(Zg, Zg);
+      float2 Zj[4];
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+        Zj[j] = __ffma2_rn(make_float2((float)(2 * j), (float)(2 * j + 1)), dz2, zg2);
+      float2 v[4];
+      if (warp_t2) {
+#pragma unroll
+        for (int j = 0; j < 4; j++) v[j] = far_unit2_t2(Zj[j], cp2, c2t);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 4; j++) v[j] = far_unit2(Zj[j], cp2);
+      }
+      if ((warp_near && l0 < Lm) || l0 + 8 > k.nz) {  // warp-uniform
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          const int la = l0 + 2 * j, lb = la + 1;
+          // select, not multiply: a NaN at a box prism is dropped
+          if (((unsigned)(la - elo) <= espan) || la >= k.nz) v[j].x = 0.f;
+          if (((unsigned)(lb - elo) <= espan) || lb >= k.nz) v[j].y = 0.f;
+        }
+      }
+      float2 g = __fmul2_rn(make_float2(ra.x, ra.y), v[0]);
+      g = __ffma2_rn(make_float2(ra.z, ra.w), v[1], g);
+      g = __ffma2_rn(make_float2(rb.x, rb.y), v[2], g);
+      g = __ffma2_rn(make_float2(rb.z, rb.w), v[3], g);
+      acc.add(g.x + g.y);
+    }
+    if (++ix == k.nx) {
+      ix = 0;
+      ++iy;
+    }
+  }
+}
+
+// Persistent far-field kernel.  The work is tiles x chunks items (a tile of
+// FAR_TS stations against a chunk of chunk_cols columns); the grid is the
+// number of blocks that are resident at once, and each block takes items
+// from a counter in order until none are left, so no block waits for a
+// second wave.  Each item writes its own partial sums (partial[chunk][s]), so
+// the result does not depend on which block ran it.  The density of an item's
+// columns streams through two shared-memory stages by 1-D bulk copies; the
+// copy of the next item's first stage is issued before the current item's
+// last stage is processed.
 __global__ void __launch_bounds__(FAR_TS, 9) far_kernel(FarArgs a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
   float* stage = reinterpret_cast<float*>(smem_raw + 128);
   __shared__ int s_lm;
+  __shared__ int s_item[2];
   const MeshConst& k = a.k;
   const int stage_floats = a.sc * k.nzp;
+  const int n_items = a.tiles * a.chunks;
+  const FarCoef fc = k.fc;
 
-  const int c0 = blockIdx.y * a.chunk_cols;
-  const int c1 = min(k.ncols, c0 + a.chunk_cols);
-  if (c0 >= c1) return;  // uniform over the block
-  const int nst = (c1 - c0 + a.sc - 1) / a.sc;
+  // columns [cs, cs + ncol) of stage st of an item
+  auto stage_cols = [&](int item, int st, int* cs) {
+    const int c0 = (item / a.tiles) * a.chunk_cols;
+    const int c1 = min(k.ncols, c0 + a.chunk_cols);
+    *cs = c0 + st * a.sc;
+    return min(a.sc, c1 - *cs);
+  };
+  auto n_stages = [&](int item) {
+    const int c0 = (item / a.tiles) * a.chunk_cols;
+    const int c1 = min(k.ncols, c0 + a.chunk_cols);
+    return (c1 - c0 + a.sc - 1) / a.sc;
+  };
+  // thread 0 only: copy stage st of item into buffer (seq & 1)
+  auto issue = [&](int item, int st, int seq) {
+    int cs;
+    const int ncol = stage_cols(item, st, &cs);
+    const uint32_t bytes = (uint32_t)ncol * k.nzp * 4u;
+    mbar_expect_tx(&bar[seq & 1], bytes);
+    bulk_g2s(stage + (seq & 1) * stage_floats, a.rhoT + (size_t)cs * k.nzp, bytes, &bar[seq & 1]);
+  };
 
-  const int s = blockIdx.x * FAR_TS + threadIdx.x;
-  const bool active = s < a.ns;
-  float ex = 0.f, ey = 0.f, ez = 0.f;
-  int ixs = 0, iys = 0, izs = 0;
-  NearBox nb = {1, 0, 1, 0, 1, 0};
-  if (active) {
-    float4 f = a.sf[s];
-    int4 i = a.si[s];
-    ex = f.x; ey = f.y; ez = f.z;
-    ixs = i.x; iys = i.y; izs = i.z;
-    nb = near_box(i, k);
-  }
   if (threadIdx.x == 0) {
-    s_lm = 0;
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
     fence_mbar_init();
+    const int first = atomicAdd(a.counter, 1);
+    s_item[0] = first;
+    s_item[1] = first < n_items ? atomicAdd(a.counter, 1) : n_items;
+    if (first < n_items) issue(first, 0, 0);
   }
   __syncthreads();
-  if (active) atomicMax(&s_lm, nb.l1 + 1);
 
-  auto issue = [&](int st) {
-    const int buf = st & 1;
-    const int cs = c0 + st * a.sc;
-    const int ncol = min(a.sc, c1 - cs);
-    const uint32_t bytes = (uint32_t)ncol * k.nzp * 4u;
-    mbar_expect_tx(&bar[buf], bytes);
-    bulk_g2s(stage + buf * stage_floats, a.rhoT + (size_t)cs * k.nzp, bytes, &bar[buf]);
-  };
-  if (threadIdx.x == 0) issue(0);
-  __syncthreads();
-  const int Lm = min(s_lm, k.nz);
-  const FarCoef fc = k.fc;
-  const float2 dz2 = make_float2(k.dzn, k.dzn);
-
-  Kahan acc;
-  int st = 0;
+  int seq = 0;     // stages waited for so far (buffer seq & 1, parity (seq >> 1) & 1)
+  int issued = 0;  // stages issued so far (thread 0's count; others keep it too)
+  if (s_item[0] < n_items) issued = 1;
   bool timed_out = false;
-  for (; st < nst; st++) {
-    if (threadIdx.x == 0 && st + 1 < nst) issue(st + 1);
-    const bool ok = mbar_wait(&bar[st & 1], (st >> 1) & 1);
-    if (__syncthreads_or(!ok)) {
-      timed_out = true;
-      break;
+  int par = 0;
+  for (;;) {
+    const int item = s_item[par];
+    if (item >= n_items) break;
+    const int nxt = s_item[par ^ 1];
+    const int tile = item % a.tiles, chunk = item / a.tiles;
+    const int s = tile * FAR_TS + threadIdx.x;
+    const bool active = s < a.ns;
+    FarStation t = {0.f, 0.f, 0.f, 0, 0, 0, {1, 0, 1, 0, 1, 0}};
+    if (active) {
+      const float4 f = a.sf[s];
+      const int4 i = a.si[s];
+      t.ex = f.x; t.ey = f.y; t.ez = f.z;
+      t.ixs = i.x; t.iys = i.y; t.izs = i.z;
+      t.nb = near_box(i, k);
     }
-    const float* rs = stage + (st & 1) * stage_floats;
-    const int cs = c0 + st * a.sc;
-    const int ncol = min(a.sc, c1 - cs);
-    {  // every lane runs the loop (inactive lanes on dummy data) for the warp vote
-      int ix = cs % k.nx, iy = cs / k.nx;
-      for (int q = 0; q < ncol; q++) {
-        const float X = fmaf((float)(ixs - ix), k.dxn, ex);
-        const float Y = fmaf((float)(iys - iy), k.dyn, ey);
-        const ColPoly cp = col_poly(X, Y, fc);
-        const bool ncl = ix >= nb.x0 && ix <= nb.x1 && iy >= nb.y0 && iy <= nb.y1;
-        int elo = k.nz;
-        unsigned espan = 0u;
-        if (ncl) {  // the column's near-region layers
-          const short2 t = a.iv[(size_t)s * k.nslots + near_slot(nb, ix, iy)];
-          if (t.x <= t.y) {
-            elo = t.x;
-            espan = (unsigned)(t.y - t.x);
-          }
-        }
-        const float* col = rs + q * k.nzp;
-        const ColPoly2 cp2 = col_poly2(cp, fc.a1);
-        // a column lies in some lane's near box only near the warp's
-        // stations: test that once per column for the whole warp
-        const bool warp_near = __any_sync(0xffffffffu, ncl);
-        // every lane of the warp far enough for the second-order form
-        const bool warp_t2 = __all_sync(0xffffffffu, cp.rh >= k.rh_t2);
-        const float2 c2t = make_float2(cp.C2 - fc.h2, cp.C2 - fc.h2);
-        float zf = (float)(-izs);  // (l0 - izs), exact in float, stepped by 8
-        for (int l0 = 0; l0 < k.nz; l0 += 8, zf += 8.f) {
-          const float4 ra = *reinterpret_cast<const float4*>(col + l0);
-          const float4 rb = *reinterpret_cast<const float4*>(col + l0 + 4);
-          const float Zg = fmaf(zf, k.dzn, ez);  // Z(l) = (l - izs) dz + ez
-          const float2 zg2 = make_float2(Zg, Zg);
-          float2 Zj[4];
-#pragma unroll
-          for (int j = 0; j < 4; j++)
-            Zj[j] = __ffma2_rn(make_float2((float)(2 * j), (float)(2 * j + 1)), dz2, zg2);
-          float2 v[4];
-          if (warp_t2) {
-#pragma unroll
-            for (int j = 0; j < 4; j++) v[j] = far_unit2_t2(Zj[j], cp2, c2t);
-          } else {
-#pragma unroll
-            for (int j = 0; j < 4; j++) v[j] = far_unit2(Zj[j], cp2);
-          }
-          if ((warp_near && l0 < Lm) || l0 + 8 > k.nz) {  // warp-uniform
-#pragma unroll
-            for (int j = 0; j < 4; j++) {
-              const int la = l0 + 2 * j, lb = la + 1;
-              // select, not multiply: a NaN at a box prism is dropped
-              if (((unsigned)(la - elo) <= espan) || la >= k.nz) v[j].x = 0.f;
-              if (((unsigned)(lb - elo) <= espan) || lb >= k.nz) v[j].y = 0.f;
-            }
-          }
-          float2 g = __fmul2_rn(make_float2(ra.x, ra.y), v[0]);
-          g = __ffma2_rn(make_float2(ra.z, ra.w), v[1], g);
-          g = __ffma2_rn(make_float2(rb.x, rb.y), v[2], g);
-          g = __ffma2_rn(make_float2(rb.z, rb.w), v[3], g);
-          acc.add(g.x + g.y);
-        }
-        if (++ix == k.nx) {
-          ix = 0;
-          ++iy;
-        }
-      }
-    }
+    if (threadIdx.x == 0) s_lm = 0;
     __syncthreads();
-  }
-  if (timed_out) {
-    if (threadIdx.x == 0) {
-      atomicOr(a.err, ZTM_DEVERR_TIMEOUT);
-      // let copies already in flight land before the block's shared memory
-      // is released (bounded as well)
-      mbar_wait(&bar[st & 1], (st >> 1) & 1);
-      if (st + 1 < nst) mbar_wait(&bar[(st + 1) & 1], ((st + 1) >> 1) & 1);
+    if (active) atomicMax(&s_lm, t.nb.l1 + 1);
+    __syncthreads();
+    const int Lm = min(s_lm, k.nz);
+    Kahan acc;
+    const int nst = n_stages(item);
+    for (int st = 0; st < nst; st++) {
+      if (threadIdx.x == 0) {
+        if (st + 1 < nst)
+          issue(item, st + 1, seq + 1);
+        else if (nxt < n_items)
+          issue(nxt, 0, seq + 1);
+      }
+      if (st + 1 < nst || nxt < n_items) issued = seq + 2;
+      const bool ok = mbar_wait(&bar[seq & 1], (seq >> 1) & 1);
+      if (__syncthreads_or(!ok)) {
+        timed_out = true;
+        break;
+      }
+      int cs;
+      const int ncol = stage_cols(item, st, &cs);
+      far_stage(a, k, fc, t, s, Lm, stage + (seq & 1) * stage_floats, cs, ncol, acc);
+      __syncthreads();
+      seq++;
     }
-    return;
+    if (timed_out) break;
+    if (active) a.partial[(size_t)chunk * a.ns + s] = acc.value();
+    // the next item is s_item[par ^ 1]; refill s_item[par] for the one after
+    if (threadIdx.x == 0) s_item[par] = nxt < n_items ? atomicAdd(a.counter, 1) : n_items;
+    __syncthreads();
+    par ^= 1;
   }
-  if (active) a.partial[(size_t)blockIdx.y * a.ns + s] = acc.value();
+  if (timed_out && threadIdx.x == 0) {
+    atomicOr(a.err, ZTM_DEVERR_TIMEOUT);
+    // let copies already in flight land before the block's shared memory is
+    // released (bounded as well)
+    for (int q = seq; q < issued; q++) mbar_wait(&bar[q & 1], (q >> 1) & 1);
+  }
 }
 
 // gz[s] = G5 * (far_scale * sum_c partial[c][s] + near[s])
@@ -477,31 +530,47 @@ __global__ void __launch_bounds__(F64_TS)
 
 // ---------------------------------------------------------------------------
 struct FarShape {
-  int tiles, chunks, chunk_cols, sc;
+  int tiles, chunks, chunk_cols, sc, grid;
   size_t smem;
 };
 
-// Launch shape of the far kernel: bps blocks per SM wanted (a full wave is
-// 9 at <= 56 registers), sc columns per shared-memory stage (0 = as many as fit
-// 24 KB).
-FarShape far_shape(const MeshConst& k, int ns, int num_sms, const ztm_opts* o, int bps = 9,
-                   int sc_want = 0) {
+// Launch shapes the autotuner tries: {columns per shared-memory stage, work
+// items per resident block}.  The first is the default.
+constexpr int FAR_SHAPES[][2] = {{16, 16}, {8, 16}, {16, 8}, {16, 32}, {32, 16}, {64, 16}};
+
+// Launch shape of the far kernel: sc columns per stage, the grid = the blocks
+// resident at once, about ipb work items per block (more items: a shorter
+// tail when blocks finish unevenly; fewer: less partial-sum traffic).
+FarShape far_shape(const MeshConst& k, int ns, int num_sms, const ztm_opts* o, int sc_want = 16,
+                   int ipb = 16) {
   FarShape f;
   f.tiles = std::max(1, (ns + FAR_TS - 1) / FAR_TS);
   int sc = std::max(1, (24 * 1024) / (k.nzp * 4));
   sc = std::min(sc, 64);
   if (sc_want > 0) sc = std::max(1, std::min(sc, sc_want));
   f.sc = sc;
-  int want_blocks = bps * std::max(num_sms, 1);
-  int chunks = std::max(1, want_blocks / f.tiles);
-  if (o && o->chunk > 0) chunks = std::max(1, (k.ncols + o->chunk - 1) / o->chunk);
-  chunks = std::min(chunks, std::max(1, k.ncols / sc));
-  chunks = std::min(chunks, 65535);
-  int cc = (k.ncols + chunks - 1) / chunks;
+  f.smem = 128 + 2 * (size_t)sc * k.nzp * 4;
+  // stages above the default 48 KB need the opt-in (very deep meshes)
+  if (f.smem > 48 * 1024 &&
+      cudaFuncSetAttribute(far_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)f.smem) != cudaSuccess)
+    cudaGetLastError();
+  int occ = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, far_kernel, FAR_TS, f.smem) !=
+          cudaSuccess ||
+      occ < 1) {
+    cudaGetLastError();
+    occ = 1;
+  }
+  const long long resident = (long long)occ * std::max(num_sms, 1);
+  long long chunks = (ipb * resident + f.tiles - 1) / f.tiles;
+  if (o && o->chunk > 0) chunks = (k.ncols + o->chunk - 1) / o->chunk;
+  chunks = std::max(1LL, std::min(chunks, (long long)std::max(1, k.ncols / sc)));
+  int cc = (int)((k.ncols + chunks - 1) / chunks);
   cc = ((cc + sc - 1) / sc) * sc;
   f.chunk_cols = cc;
   f.chunks = (k.ncols + cc - 1) / cc;
-  f.smem = 128 + 2 * (size_t)sc * k.nzp * 4;
+  f.grid = (int)std::min(resident, (long long)f.tiles * f.chunks);
   return f;
 }
 
@@ -598,9 +667,10 @@ size_t ztm_prism_ws(const MeshDesc& m, int ns, int precision, int num_sms, const
   double nq = (o && o->near_q > 0) ? o->near_q : 6.0;
   MeshConst k = make_mesh_const(m, nq);
   int chunks = 0;
-  for (int bps : {5, 9, 18}) chunks = std::max(chunks, far_shape(k, ns, num_sms, o, bps, 8).chunks);
-  chunks = std::max(chunks, far_shape(k, ns, num_sms, o).chunks);
-  return WsCarver::need((size_t)k.ncols * k.nzp * 4) + WsCarver::need((size_t)ns * 16) * 2 +
+  for (const auto& sh : FAR_SHAPES)
+    chunks = std::max(chunks, far_shape(k, ns, num_sms, o, sh[0], sh[1]).chunks);
+  return WsCarver::need(sizeof(int)) + WsCarver::need((size_t)k.ncols * k.nzp * 4) +
+         WsCarver::need((size_t)ns * 16) * 2 +
          WsCarver::need((size_t)ns * 8) + WsCarver::need((size_t)chunks * ns * 8) +
          WsCarver::need((size_t)ns * k.nslots * 4) + WsCarver::need((size_t)ns * 8);
 }
@@ -627,60 +697,69 @@ int ztm_launch_prism(ztm_ctx* c, const MeshDesc& m, const double* d_rho, int ns,
   const double nq = (o && o->near_q > 0) ? o->near_q : 6.0;
   MeshConst k = make_mesh_const(m, nq);
   if (m.nz > 32767) return ztm_fail(c, ZTM_ERR_RANGE, "mixed prism forward supports nz <= 32767");
-  int bps = 9, scw = 0;
-  auto it = c->tuned.find(tune_key(k, ns));
-  if (it != c->tuned.end()) {
-    bps = it->second[0];
-    scw = it->second[1];
+  {  // two one-column stages of the far kernel must fit in shared memory
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
+    const long long nzp = (m.nz + 7) & ~7;
+    if (optin > 0 && 128 + 8 * nzp > optin)
+      return ztm_fail(c, ZTM_ERR_RANGE,
+                      "mixed prism forward: nz too large for two one-column stages in shared memory");
   }
+  int shape = 0;
+  auto it = c->tuned.find(tune_key(k, ns));
+  if (it != c->tuned.end()) shape = (int)it->second[0];
+  int* counter = wc.take<int>(1);
   float* rhoT = wc.take<float>((size_t)k.ncols * k.nzp);
   float4* sf = wc.take<float4>(ns);
   int4* si = wc.take<int4>(ns);
   double* near = wc.take<double>(ns);
   int max_chunks = 0;
-  for (int b : {5, 9, 18}) max_chunks = std::max(max_chunks, far_shape(k, ns, c->num_sms, o, b, 8).chunks);
-  max_chunks = std::max(max_chunks, far_shape(k, ns, c->num_sms, o).chunks);
+  for (const auto& sh : FAR_SHAPES)
+    max_chunks = std::max(max_chunks, far_shape(k, ns, c->num_sms, o, sh[0], sh[1]).chunks);
   double* partial = wc.take<double>((size_t)max_chunks * ns);
   short2* iv = wc.take<short2>((size_t)ns * k.nslots);
   int2* lr = wc.take<int2>(ns);
   launch_mesh_transpose(c, k, 1, d_rho, rhoT);
   launch_mesh_station_prep(c, m, k.L0, ns, d_sxyz, sf, si);
   launch_mesh_near_iv(c, k, ns, si, iv, lr);
-  cudaFuncSetAttribute(far_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
   FarArgs a;
   a.k = k; a.ns = ns; a.sf = sf; a.si = si; a.iv = iv; a.rhoT = rhoT; a.partial = partial;
   a.err = c->d_err;
+  a.counter = counter;
+  auto launch_far = [&](const FarShape& t) {
+    a.tiles = t.tiles;
+    a.chunks = t.chunks;
+    a.chunk_cols = t.chunk_cols;
+    a.sc = t.sc;
+    cudaMemsetAsync(counter, 0, sizeof(int), c->stream);
+    far_kernel<<<t.grid, FAR_TS, t.smem, c->stream>>>(a);
+    c->launches++;
+  };
   if (o && (o->flags & ZTM_FLAG_AUTOTUNE) && !(o->chunk > 0) && it == c->tuned.end()) {
     // time each candidate once (after one untimed launch) and keep the fastest
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     float best = 1e30f;
-    for (int b : {5, 9, 18})
-      for (int w : {8, 16, 0}) {
-        FarShape t = far_shape(k, ns, c->num_sms, o, b, w);
-        a.chunk_cols = t.chunk_cols;
-        a.sc = t.sc;
-        far_kernel<<<dim3(t.tiles, t.chunks), FAR_TS, t.smem, c->stream>>>(a);
-        cudaEventRecord(e0, c->stream);
-        far_kernel<<<dim3(t.tiles, t.chunks), FAR_TS, t.smem, c->stream>>>(a);
-        cudaEventRecord(e1, c->stream);
-        c->launches += 2;
-        float ms = 0.f;
-        if (cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) ==
-                                                           cudaSuccess && ms < best) {
-          best = ms;
-          bps = b;
-          scw = w;
-        }
+    const int nshapes = (int)(sizeof(FAR_SHAPES) / sizeof(FAR_SHAPES[0]));
+    for (int q = 0; q < nshapes; q++) {
+      FarShape t = far_shape(k, ns, c->num_sms, o, FAR_SHAPES[q][0], FAR_SHAPES[q][1]);
+      launch_far(t);
+      cudaEventRecord(e0, c->stream);
+      launch_far(t);
+      cudaEventRecord(e1, c->stream);
+      float ms = 0.f;
+      if (cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) ==
+                                                         cudaSuccess && ms < best) {
+        best = ms;
+        shape = q;
       }
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    c->tuned[tune_key(k, ns)] = {bps, scw};
+    c->tuned[tune_key(k, ns)] = {shape};
   }
-  FarShape f = far_shape(k, ns, c->num_sms, o, bps, scw);
-  a.chunk_cols = f.chunk_cols;
-  a.sc = f.sc;
+  FarShape f = far_shape(k, ns, c->num_sms, o, FAR_SHAPES[shape][0], FAR_SHAPES[shape][1]);
   // the double near box runs on the side stream, concurrently with the float
   // far field (different pipes: FP64 vs FMA/MUFU)
   ztm_fork(c);
@@ -688,13 +767,13 @@ int ztm_launch_prism(ztm_ctx* c, const MeshDesc& m, const double* d_rho, int ns,
                    c->aux);
   {
     ZtmProf prof_(c, "prism_far");
-    far_kernel<<<dim3(f.tiles, f.chunks), FAR_TS, f.smem, c->stream>>>(a);
+    launch_far(f);
   }
   ztm_join(c);
   const double far_scale = k.L0 * (double)k.dxn * k.dyn * k.dzn;
   finalize_kernel<<<(ns + 255) / 256, 256, 0, c->stream>>>(ns, f.chunks, partial, far_scale, near,
                                                            G5, d_gz);
-  c->launches += 2;
+  c->launches++;
   return ztm_after_launch(c, "prism mixed kernels");
 }
 
