@@ -200,13 +200,81 @@ struct FarStation {
   NearBox nb;
 };
 
+// Eight layers l0..l0+7 of one column: adds rho * (far value) to g (two
+// lanes: even and odd layers).  T2: the second-order form for the whole warp.
+// MASK: drop the layers of the station's near region [elo, elo + espan] and
+// the padding layers >= nz (select, not multiply: a NaN there is dropped).
+template <bool T2, bool MASK>
+__device__ __forceinline__ float2 far_group(const float* col, int l0, const float2 (&Zb)[4],
+                                            float2 zstep, const ColPoly2& cp2, float2 c2t,
+                                            int elo, unsigned espan, int nz, float2 g) {
+  const float4 ra = *reinterpret_cast<const float4*>(col + l0);
+  const float4 rb = *reinterpret_cast<const float4*>(col + l0 + 4);
+  const float fl = (float)l0;
+  const float2 l2 = make_float2(fl, fl);
+  float2 v[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    const float2 Z = __ffma2_rn(l2, zstep, Zb[j]);  // Z(l) = (l - izs) dz + ez
+    v[j] = T2 ? far_unit2_t2(Z, cp2, c2t) : far_unit2(Z, cp2);
+  }
+  if (MASK) {
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const int la = l0 + 2 * j, lb = la + 1;
+      if (((unsigned)(la - elo) <= espan) || la >= nz) v[j].x = 0.f;
+      if (((unsigned)(lb - elo) <= espan) || lb >= nz) v[j].y = 0.f;
+    }
+  }
+  g = __ffma2_rn(make_float2(ra.x, ra.y), v[0], g);
+  g = __ffma2_rn(make_float2(ra.z, ra.w), v[1], g);
+  g = __ffma2_rn(make_float2(rb.x, rb.y), v[2], g);
+  return __ffma2_rn(make_float2(rb.z, rb.w), v[3], g);
+}
+
+// All layers of one column: groups [0, lmask) with the near mask, full
+// groups up to nz8 without, a masked tail group if nz is not a multiple of 8.
+// Plain float sums over 16 layers, compensated across.
+template <bool T2>
+__device__ __forceinline__ void far_column(const float* col, int lmask, int nz8, int nz,
+                                           const float2 (&Zb)[4], float2 zstep,
+                                           const ColPoly2& cp2, float2 c2t, int elo,
+                                           unsigned espan, Kahan& acc) {
+  float2 g = make_float2(0.f, 0.f);
+  int l0 = 0;
+  for (; l0 < lmask; l0 += 8) {
+    g = far_group<T2, true>(col, l0, Zb, zstep, cp2, c2t, elo, espan, nz, g);
+    if (l0 & 8) {
+      acc.add(g.x + g.y);
+      g = make_float2(0.f, 0.f);
+    }
+  }
+  for (; l0 < nz8; l0 += 8) {
+    g = far_group<T2, false>(col, l0, Zb, zstep, cp2, c2t, elo, espan, nz, g);
+    if (l0 & 8) {
+      acc.add(g.x + g.y);
+      g = make_float2(0.f, 0.f);
+    }
+  }
+  if (nz8 < nz) g = far_group<T2, true>(col, nz8, Zb, zstep, cp2, c2t, elo, espan, nz, g);
+  acc.add(g.x + g.y);
+}
+
 // One shared-memory stage (ncol columns starting at column cs) against this
 // thread's station; adds to acc.  Every lane runs the loop (inactive lanes
 // on dummy data) for the warp votes.
 __device__ __forceinline__ void far_stage(const FarArgs& a, const MeshConst& k, const FarCoef& fc,
                                           const FarStation& t, int s, int Lm, const float* rs,
                                           int cs, int ncol, Kahan& acc) {
-  const float2 dz2 = make_float2(k.dzn, k.dzn);
+  const float2 zstep = make_float2(k.dzn, k.dzn);
+  // Z of layers 2j, 2j+1 of a group at l0 = 0; a group at l0 adds l0 dz
+  float2 Zb[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++)
+    Zb[j] = make_float2(fmaf((float)(2 * j - t.izs), k.dzn, t.ez),
+                        fmaf((float)(2 * j + 1 - t.izs), k.dzn, t.ez));
+  const int nz8 = k.nz & ~7;
+  const int lm8 = min((Lm + 7) & ~7, nz8);
   int ix = cs % k.nx, iy = cs / k.nx;
   for (int q = 0; q < ncol; q++) {
     const float X = fmaf((float)(t.ixs - ix), k.dxn, t.ex);
@@ -226,43 +294,13 @@ __device__ __forceinline__ void far_stage(const FarArgs& a, const MeshConst& k, 
     const ColPoly2 cp2 = col_poly2(cp, fc.a1);
     // a column lies in some lane's near box only near the warp's stations:
     // test that once per column for the whole warp
-    const bool warp_near = __any_sync(0xffffffffu, ncl);
-    // every lane of the warp far enough for the second-order form
-    const bool warp_t2 = __all_sync(0xffffffffu, cp.rh >= k.rh_t2);
+    const int lmask = __any_sync(0xffffffffu, ncl) ? lm8 : 0;
     const float2 c2t = make_float2(cp.C2 - fc.h2, cp.C2 - fc.h2);
-    float zf = (float)(-t.izs);  // (l0 - izs), exact in float, stepped by 8
-    for (int l0 = 0; l0 < k.nz; l0 += 8, zf += 8.f) {
-      const float4 ra = *reinterpret_cast<const float4*>(col + l0);
-      const float4 rb = *reinterpret_cast<const float4*>(col + l0 + 4);
-      const float Zg = fmaf(zf, k.dzn, t.ez);  // Z(l) = (l - izs) dz + ez
-      const float2 zg2 = make_float2(Zg, Zg);
-      float2 Zj[4];
-#pragma unroll
-      for (int j = 0; j < 4; j++)
-        Zj[j] = __ffma2_rn(make_float2((float)(2 * j), (float)(2 * j + 1)), dz2, zg2);
-      float2 v[4];
-      if (warp_t2) {
-#pragma unroll
-        for (int j = 0; j < 4; j++) v[j] = far_unit2_t2(Zj[j], cp2, c2t);
-      } else {
-#pragma unroll
-        for (int j = 0; j < 4; j++) v[j] = far_unit2(Zj[j], cp2);
-      }
-      if ((warp_near && l0 < Lm) || l0 + 8 > k.nz) {  // warp-uniform
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-          const int la = l0 + 2 * j, lb = la + 1;
-          // select, not multiply: a NaN at a box prism is dropped
-          if (((unsigned)(la - elo) <= espan) || la >= k.nz) v[j].x = 0.f;
-          if (((unsigned)(lb - elo) <= espan) || lb >= k.nz) v[j].y = 0.f;
-        }
-      }
-      float2 g = __fmul2_rn(make_float2(ra.x, ra.y), v[0]);
-      g = __ffma2_rn(make_float2(ra.z, ra.w), v[1], g);
-      g = __ffma2_rn(make_float2(rb.x, rb.y), v[2], g);
-      g = __ffma2_rn(make_float2(rb.z, rb.w), v[3], g);
-      acc.add(g.x + g.y);
-    }
+    // every lane of the warp far enough for the second-order form
+    if (__all_sync(0xffffffffu, cp.rh >= k.rh_t2))
+      far_column<true>(col, lmask, nz8, k.nz, Zb, zstep, cp2, c2t, elo, espan, acc);
+    else
+      far_column<false>(col, lmask, nz8, k.nz, Zb, zstep, cp2, c2t, elo, espan, acc);
     if (++ix == k.nx) {
       ix = 0;
       ++iy;
@@ -279,7 +317,7 @@ __device__ __forceinline__ void far_stage(const FarArgs& a, const MeshConst& k, 
 // columns streams through two shared-memory stages by 1-D bulk copies; the
 // copy of the next item's first stage is issued before the current item's
 // last stage is processed.
-__global__ void __launch_bounds__(FAR_TS, 9) far_kernel(FarArgs a) {
+__global__ void __launch_bounds__(FAR_TS, 8) far_kernel(FarArgs a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
   float* stage = reinterpret_cast<float*>(smem_raw + 128);
