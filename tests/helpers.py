@@ -57,6 +57,10 @@ def awkward_stations(mesh, n_random=40, seed=1):
         (X1 + 3000.0, Y1 + 100.0, zt + 10.0),  # outside
         (0.5 * (x0 + X1), 0.5 * (y0 + Y1), 0.5 * (zt + Zb) + 0.25 * mesh.dz),  # inside
         (x0 - 500.0, y0 + mesh.dy, zt - mesh.dz),  # beside, on a layer plane
+        # below the bottom, at the centre of the first padding layer under a
+        # column centre (nz not a multiple of 8), and far below
+        (x0 + 1.5 * mesh.dx, y0 + 0.5 * mesh.dy, Zb - 0.5 * mesh.dz),
+        (x0 + 0.7 * mesh.dx, y0 + 1.2 * mesh.dy, Zb - 20.0 * mesh.dz),
     ]
     xs = rng.uniform(x0 - 2000.0, X1 + 2000.0, n_random)
     ys = rng.uniform(y0 - 2000.0, Y1 + 2000.0, n_random)

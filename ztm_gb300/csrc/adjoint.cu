@@ -39,6 +39,7 @@ __global__ void __launch_bounds__(ADJ_TS)
                    const double* __restrict__ res, double scale, double* __restrict__ g) {
   __shared__ float4 s_f[ADJ_STILE];
   __shared__ int4 s_i[ADJ_STILE];
+  __shared__ int4 s_b[ADJ_STILE];  // the station's near box columns x0, x1, y0, y1
   __shared__ float s_r[ADJ_STILE];
   const int ngroups = (k.nz + ADJ_LG - 1) / ADJ_LG;
   const long long t = blockIdx.x * (long long)ADJ_TS + threadIdx.x;
@@ -57,12 +58,16 @@ __global__ void __launch_bounds__(ADJ_TS)
     for (int q = threadIdx.x; q < ADJ_STILE; q += ADJ_TS) {
       const int s = s0 + q;
       if (s < ns) {
+        const int4 i = si[s];
+        const NearBox b = near_box(i, k);
         s_f[q] = sf[s];
-        s_i[q] = si[s];
+        s_i[q] = i;
+        s_b[q] = make_int4(b.x0, b.x1, b.y0, b.y1);
         s_r[q] = (float)res[s];
       } else {
         s_f[q] = make_float4(0.f, 0.f, 0.f, 0.f);
         s_i[q] = make_int4(0, 0, 0, 0);
+        s_b[q] = make_int4(1, 0, 1, 0);
         s_r[q] = 0.f;
       }
     }
@@ -82,12 +87,12 @@ __global__ void __launch_bounds__(ADJ_TS)
         const float X = fmaf((float)(i.x - ix), k.dxn, f.x);
         const float Y = fmaf((float)(i.y - iy), k.dyn, f.y);
         const ColPoly cp = col_poly(X, Y, fc);
-        const NearBox b = near_box(i, k);
-        bool ncl = ix >= b.x0 && ix <= b.x1 && iy >= b.y0 && iy <= b.y1;
+        const int4 b = s_b[q];
+        bool ncl = ix >= b.x && ix <= b.y && iy >= b.z && iy <= b.w;
         int elo = k.nz;
         unsigned espan = 0u;
         if (ncl) {  // the column's near-region layers for this station
-          const short2 t = iv[(size_t)(s0 + q) * k.nslots + near_slot(b, ix, iy)];
+          const short2 t = iv[(size_t)(s0 + q) * k.nslots + (ix - b.x) + (b.y - b.x + 1) * (iy - b.z)];
           if (t.x <= t.y) {
             elo = t.x;
             espan = (unsigned)(t.y - t.x);
@@ -99,10 +104,20 @@ __global__ void __launch_bounds__(ADJ_TS)
         const ColPoly2 cp2 = col_poly2(cp, fc.a1);
         const float2 zg2 = make_float2(Zg, Zg), dz2 = make_float2(k.dzn, k.dzn);
         float2 v[ADJ_LG / 2];
+        // the warp's columns all far enough for the second-order form (the
+        // lanes of a warp share the station, so this is mostly uniform)
+        if (__all_sync(__activemask(), cp.rh >= k.rh_t2)) {
+          const float2 c2t = make_float2(cp.C2 - fc.h2, cp.C2 - fc.h2);
 #pragma unroll
-        for (int j = 0; j < ADJ_LG / 2; j++)
-          v[j] = far_unit2(__ffma2_rn(make_float2((float)(2 * j), (float)(2 * j + 1)), dz2, zg2),
-                           cp2);
+          for (int j = 0; j < ADJ_LG / 2; j++)
+            v[j] = far_unit2_t2(
+                __ffma2_rn(make_float2((float)(2 * j), (float)(2 * j + 1)), dz2, zg2), cp2, c2t);
+        } else {
+#pragma unroll
+          for (int j = 0; j < ADJ_LG / 2; j++)
+            v[j] = far_unit2(
+                __ffma2_rn(make_float2((float)(2 * j), (float)(2 * j + 1)), dz2, zg2), cp2);
+        }
         if (ncl || l0 + ADJ_LG > k.nz) {
 #pragma unroll
           for (int j = 0; j < ADJ_LG / 2; j++) {

@@ -91,10 +91,13 @@ __global__ void transpose_models_kernel(MeshConst k, int nmodels, int W,
 // interleaved in `col` (layer-major, W per layer).  K is computed once per
 // (station, prism) pair; per model two packed FMAs per layer pair (W = 1) or
 // per model pair (W = 8); plain sums over 8 layers, Kahan across groups.
-template <int W>
+// T2: the second-order form (every lane of the warp far enough); MASK: some
+// lane of the warp has the column in its near box, or nz is not a multiple
+// of 8 (both warp-uniform, so the selects are skipped for most columns).
+template <int W, bool T2, bool MASK>
 __device__ __forceinline__ void far_column(const float* __restrict__ col, const MeshConst& k,
-                                           const ColPoly2& cp2, float ez, int izs, int Lm,
-                                           int elo, unsigned espan, Kahan* acc) {
+                                           const ColPoly2& cp2, float2 c2t, float ez, int izs,
+                                           int Lm, int elo, unsigned espan, Kahan* acc) {
   const float2 dz2 = make_float2(k.dzn, k.dzn);
   float zf = (float)(-izs);  // (l0 - izs), exact, stepped by 8
   for (int l0 = 0; l0 < k.nz; l0 += 8, zf += 8.f) {
@@ -103,11 +106,14 @@ __device__ __forceinline__ void far_column(const float* __restrict__ col, const 
     float2 K2[4];  // kernel values of layers (l0+2j, l0+2j+1)
 #pragma unroll
     for (int j = 0; j < 4; j++) {
-      K2[j] = far_unit2(__ffma2_rn(make_float2((float)(2 * j), (float)(2 * j + 1)), dz2, zg2), cp2);
-      const int la = l0 + 2 * j, lb = la + 1;
-      // select: a NaN at a near-region prism is dropped
-      if ((la < Lm && (unsigned)(la - elo) <= espan) || la >= k.nz) K2[j].x = 0.f;
-      if ((lb < Lm && (unsigned)(lb - elo) <= espan) || lb >= k.nz) K2[j].y = 0.f;
+      const float2 Z = __ffma2_rn(make_float2((float)(2 * j), (float)(2 * j + 1)), dz2, zg2);
+      K2[j] = T2 ? far_unit2_t2(Z, cp2, c2t) : far_unit2(Z, cp2);
+      if (MASK) {
+        const int la = l0 + 2 * j, lb = la + 1;
+        // select: a NaN at a near-region prism is dropped
+        if ((la < Lm && (unsigned)(la - elo) <= espan) || la >= k.nz) K2[j].x = 0.f;
+        if ((lb < Lm && (unsigned)(lb - elo) <= espan) || lb >= k.nz) K2[j].y = 0.f;
+      }
     }
     if constexpr (W == 1) {
       const float4 ra = *reinterpret_cast<const float4*>(col + l0);
@@ -213,7 +219,7 @@ __device__ void near_item(const BJob& J, int tile, double* phi_all, int phi_cap,
   }
 }
 
-__global__ void __launch_bounds__(B_TS, 5) batch_kernel(BArgs a) {
+__global__ void __launch_bounds__(B_TS, 4) batch_kernel(BArgs a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
   float* stage = reinterpret_cast<float*>(smem_raw + 128);
@@ -312,10 +318,25 @@ __global__ void __launch_bounds__(B_TS, 5) batch_kernel(BArgs a) {
           const unsigned espan = ncl ? (unsigned)(nb.l1 - nb.l0) : 0u;
           const float* col = rs + q * k.nzp * J.mgw;
           const ColPoly2 cp2 = col_poly2(cp, fc.a1);
-          if (J.mgw == 1)
-            far_column<1>(col, k, cp2, ez, izs, Lm, elo, espan, acc);
-          else
-            far_column<B_MG>(col, k, cp2, ez, izs, Lm, elo, espan, acc);
+          const float2 c2t = make_float2(cp.C2 - fc.h2, cp.C2 - fc.h2);
+          const unsigned am = __activemask();
+          const int form = (__all_sync(am, cp.rh >= k.rh_t2) ? 1 : 0) |
+                           ((__any_sync(am, ncl) || (k.nz & 7)) ? 2 : 0);
+          if (J.mgw == 1) {
+            switch (form) {
+              case 0: far_column<1, false, false>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, acc); break;
+              case 1: far_column<1, true, false>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, acc); break;
+              case 2: far_column<1, false, true>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, acc); break;
+              default: far_column<1, true, true>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, acc);
+            }
+          } else {
+            switch (form) {
+              case 0: far_column<B_MG, false, false>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, acc); break;
+              case 1: far_column<B_MG, true, false>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, acc); break;
+              case 2: far_column<B_MG, false, true>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, acc); break;
+              default: far_column<B_MG, true, true>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, acc);
+            }
+          }
           if (++ix == k.nx) {
             ix = 0;
             ++iy;
