@@ -49,6 +49,8 @@ struct IConst {
   float p4x, p4y, p4xy;  // P4
   float p2x, p2y;        // P2 = p2x X^2 + p2y Y^2
   FarCoef face;          // 2-D face expansion
+  float rt2_t2;          // squared distance to the column top (units of L0)
+                         // beyond which the 4th-order terms are dropped
 };
 
 IConst make_iconst(const IMeshDesc& m, double near_q) {
@@ -79,6 +81,9 @@ IConst make_iconst(const IMeshDesc& m, double near_q) {
   // face term converges more slowly than the column's, so keep columns in
   // double until the station is twice as far above the top
   k.near_h = 2.0 * near_q * ellh;
+  // 96 horizontal half diagonals: the dropped 4th-order horizontal terms of
+  // the column and of its top face are below 1e-8 of the pair's monopole
+  k.rt2_t2 = (float)((96.0 * ellh / k.L0) * (96.0 * ellh / k.L0));
   return k;
 }
 
@@ -169,31 +174,41 @@ __global__ void iface_near_mask(IConst k, int ns, const double* __restrict__ sxy
 }
 
 // The unit face integral of the far expansion for two pairs, given 1/r of
-// the column top.
+// the column top.  T2: second order only (pairs beyond rt2_t2).
+template <bool T2>
 __device__ __forceinline__ float2 face_unit_far2(float2 X2, float2 Y2, float2 ut, float2 rinv,
                                                  const FarCoef& f) {
   const float2 Z2 = __fmul2_rn(ut, ut);
   const float2 ri2 = __fmul2_rn(rinv, rinv), ri4 = __fmul2_rn(ri2, ri2);
   const float2 a0 = __ffma2_rn(X2, make_float2(f.cA, f.cA), __fmul2_rn(Y2, make_float2(f.cB, f.cB)));
-  const float2 h1 = __ffma2_rn(X2, make_float2(f.cX1, f.cX1), __fmul2_rn(Y2, make_float2(f.cY1, f.cY1)));
-  const float2 h0 = __ffma2_rn(X2,
-                               __ffma2_rn(X2, make_float2(f.cXX, f.cXX), __fmul2_rn(Y2, make_float2(f.cXY, f.cXY))),
-                               __fmul2_rn(__fmul2_rn(Y2, Y2), make_float2(f.cYY, f.cYY)));
   const float2 n2 = __ffma2_rn(make_float2(f.a1, f.a1), Z2, a0);
-  const float2 H = __ffma2_rn(__ffma2_rn(make_float2(f.h2, f.h2), Z2, h1), Z2, h0);
-  const float2 t = __fmul2_rn(__ffma2_rn(H, ri4, n2), ri4);
+  float2 t;
+  if (T2) {
+    t = __fmul2_rn(n2, ri4);
+  } else {
+    const float2 h1 = __ffma2_rn(X2, make_float2(f.cX1, f.cX1), __fmul2_rn(Y2, make_float2(f.cY1, f.cY1)));
+    const float2 h0 = __ffma2_rn(
+        X2, __ffma2_rn(X2, make_float2(f.cXX, f.cXX), __fmul2_rn(Y2, make_float2(f.cXY, f.cXY))),
+        __fmul2_rn(__fmul2_rn(Y2, Y2), make_float2(f.cYY, f.cYY)));
+    const float2 H = __ffma2_rn(__ffma2_rn(make_float2(f.h2, f.h2), Z2, h1), Z2, h0);
+    t = __fmul2_rn(__ffma2_rn(H, ri4, n2), ri4);
+  }
   const float2 base = __fmul2_rn(__fmul2_rn(ut, rinv), ri2);
   return __ffma2_rn(base, t, base);
 }
 
 // Unit column integral (normalised, without dx dy) for two far pairs on the
 // packed FP32 path: the exact vertical integral of the column axis plus the
-// 4th-order horizontal correction at its top and bottom.  The three SFU
-// operations per pair stay scalar.  Also hands back 1/r of the column top.
-__device__ __forceinline__ float2 col_unit2_it(float2 rh, float2 ut, float2 th, float2 Q2, float2 P4,
-                                               float2 P2, const IConst& k, float2* it_out) {
+// horizontal correction at its top and bottom, to 4th order, or to 2nd order
+// when T2 (pairs beyond rt2_t2).  rt2 = ut^2 + rh.  The SFU operations stay
+// scalar.  Also hands back 1/r of the column top.
+template <bool T2>
+__device__ __forceinline__ float2 col_unit2(float2 X2, float2 Y2, float2 rh, float2 ut,
+                                            float2 rt2, float2 th, const IConst& k,
+                                            float2* it_out) {
+  const float2 Q2 = __ffma2_rn(make_float2(k.q2x, k.q2x), X2, __fmul2_rn(make_float2(k.q2y, k.q2y), Y2));
   const float2 ub = __fadd2_rn(ut, th);
-  const float2 rt2 = __ffma2_rn(ut, ut, rh), rb2 = __ffma2_rn(ub, ub, rh);
+  const float2 rb2 = __ffma2_rn(ub, ub, rh);
   const float2 it = make_float2(rsqrt_ftz(rt2.x), rsqrt_ftz(rt2.y));
   const float2 ib = make_float2(rsqrt_ftz(rb2.x), rsqrt_ftz(rb2.y));
   *it_out = it;
@@ -201,14 +216,25 @@ __device__ __forceinline__ float2 col_unit2_it(float2 rh, float2 ut, float2 th, 
   const float2 num = __fmul2_rn(__fmul2_rn(th, __fadd2_rn(ut, ub)), __fmul2_rn(itb, itb));
   const float2 den = __fadd2_rn(it, ib);
   const float2 L = make_float2(__fdividef(num.x, den.x), __fdividef(num.y, den.y));
-  const float2 Q0 = make_float2(k.Q0, k.Q0), P0 = make_float2(k.P0, k.P0);
+  const float2 Q0 = make_float2(k.Q0, k.Q0);
   const float2 it2 = __fmul2_rn(it, it), ib2 = __fmul2_rn(ib, ib);
   const float2 it5 = __fmul2_rn(__fmul2_rn(it2, it2), it), ib5 = __fmul2_rn(__fmul2_rn(ib2, ib2), ib);
-  const float2 it9 = __fmul2_rn(__fmul2_rn(it2, it2), it5), ib9 = __fmul2_rn(__fmul2_rn(ib2, ib2), ib5);
-  const float2 ct = __ffma2_rn(it9, __ffma2_rn(__ffma2_rn(P0, rt2, P2), rt2, P4),
-                               __fmul2_rn(it5, __ffma2_rn(Q0, rt2, Q2)));
-  const float2 cb = __ffma2_rn(ib9, __ffma2_rn(__ffma2_rn(P0, rb2, P2), rb2, P4),
-                               __fmul2_rn(ib5, __ffma2_rn(Q0, rb2, Q2)));
+  float2 ct, cb;
+  if (T2) {
+    ct = __fmul2_rn(it5, __ffma2_rn(Q0, rt2, Q2));
+    cb = __fmul2_rn(ib5, __ffma2_rn(Q0, rb2, Q2));
+  } else {
+    const float2 P4 = __ffma2_rn(__fmul2_rn(make_float2(k.p4x, k.p4x), X2), X2,
+                                 __ffma2_rn(__fmul2_rn(make_float2(k.p4y, k.p4y), Y2), Y2,
+                                            __fmul2_rn(__fmul2_rn(make_float2(k.p4xy, k.p4xy), X2), Y2)));
+    const float2 P2 = __ffma2_rn(make_float2(k.p2x, k.p2x), X2, __fmul2_rn(make_float2(k.p2y, k.p2y), Y2));
+    const float2 P0 = make_float2(k.P0, k.P0);
+    const float2 it9 = __fmul2_rn(__fmul2_rn(it2, it2), it5), ib9 = __fmul2_rn(__fmul2_rn(ib2, ib2), ib5);
+    ct = __ffma2_rn(it9, __ffma2_rn(__ffma2_rn(P0, rt2, P2), rt2, P4),
+                    __fmul2_rn(it5, __ffma2_rn(Q0, rt2, Q2)));
+    cb = __ffma2_rn(ib9, __ffma2_rn(__ffma2_rn(P0, rb2, P2), rb2, P4),
+                    __fmul2_rn(ib5, __ffma2_rn(Q0, rb2, Q2)));
+  }
   return __fadd2_rn(L, __fadd2_rn(ct, make_float2(-cb.x, -cb.y)));
 }
 
@@ -255,15 +281,15 @@ __global__ void __launch_bounds__(IF_TS, 8)
       const float2 Y = make_float2(fmaf((float)(hi.y - iya), k.dyn, st.ey),
                                    fmaf((float)(hi.y - iyb), k.dyn, st.ey));
       const float2 X2 = __fmul2_rn(X, X), Y2 = __fmul2_rn(Y, Y), rh = __fadd2_rn(X2, Y2);
-      const float2 Q2 = __ffma2_rn(make_float2(k.q2x, k.q2x), X2, __fmul2_rn(make_float2(k.q2y, k.q2y), Y2));
-      const float2 P4 = __ffma2_rn(__fmul2_rn(make_float2(k.p4x, k.p4x), X2), X2,
-                                   __ffma2_rn(__fmul2_rn(make_float2(k.p4y, k.p4y), Y2), Y2,
-                                              __fmul2_rn(__fmul2_rn(make_float2(k.p4xy, k.p4xy), X2), Y2)));
-      const float2 P2 = __ffma2_rn(make_float2(k.p2x, k.p2x), X2, __fmul2_rn(make_float2(k.p2y, k.p2y), Y2));
       const float2 ut = __fadd2_rn(make_float2(st.zs, st.zs), make_float2(A.y, B.y));
+      const float2 rt2 = __ffma2_rn(ut, ut, rh);
+      const float2 th = make_float2(A.z, B.z);
       float2 itop;
-      float2 v = __fmul2_rn(make_float2(A.x, B.x),
-                            col_unit2_it(rh, ut, make_float2(A.z, B.z), Q2, P4, P2, k, &itop));
+      // second order when every lane's pairs are far enough (warp-uniform)
+      const float2 u = __all_sync(__activemask(), fminf(rt2.x, rt2.y) >= k.rt2_t2)
+                           ? col_unit2<true>(X2, Y2, rh, ut, rt2, th, k, &itop)
+                           : col_unit2<false>(X2, Y2, rh, ut, rt2, th, k, &itop);
+      float2 v = __fmul2_rn(make_float2(A.x, B.x), u);
       // near columns (and the padding column) contribute through the double
       // path or not at all: select, which also drops a NaN
       if (ixa >= wx0 && ixa <= wx1 && iya >= wy0 && iya <= wy1 && near_bit(mask, s, ixa - wx0 + wbw * (iya - wy0), k))
@@ -387,15 +413,17 @@ __global__ void __launch_bounds__(IF_TS, 8)
       const float2 Y = make_float2(fmaf((float)(ha.y - iy), k.dyn, sa.ey),
                                    fmaf((float)(hb.y - iy), k.dyn, sb.ey));
       const float2 X2 = __fmul2_rn(X, X), Y2 = __fmul2_rn(Y, Y), rh = __fadd2_rn(X2, Y2);
-      const float2 Q2 = __ffma2_rn(make_float2(k.q2x, k.q2x), X2, __fmul2_rn(make_float2(k.q2y, k.q2y), Y2));
-      const float2 P4 = __ffma2_rn(__fmul2_rn(make_float2(k.p4x, k.p4x), X2), X2,
-                                   __ffma2_rn(__fmul2_rn(make_float2(k.p4y, k.p4y), Y2), Y2,
-                                              __fmul2_rn(__fmul2_rn(make_float2(k.p4xy, k.p4xy), X2), Y2)));
-      const float2 P2 = __ffma2_rn(make_float2(k.p2x, k.p2x), X2, __fmul2_rn(make_float2(k.p2y, k.p2y), Y2));
       const float2 ut = __fadd2_rn(make_float2(sa.zs, sb.zs), cy2);
-      float2 itop;
-      const float2 u = col_unit2_it(rh, ut, cz2, Q2, P4, P2, k, &itop);
-      const float2 f = face_unit_far2(X2, Y2, ut, itop, k.face);
+      const float2 rt2 = __ffma2_rn(ut, ut, rh);
+      float2 itop, u, f;
+      // second order when every lane's pairs are far enough (warp-uniform)
+      if (__all_sync(__activemask(), fminf(rt2.x, rt2.y) >= k.rt2_t2)) {
+        u = col_unit2<true>(X2, Y2, rh, ut, rt2, cz2, k, &itop);
+        f = face_unit_far2<true>(X2, Y2, ut, itop, k.face);
+      } else {
+        u = col_unit2<false>(X2, Y2, rh, ut, rt2, cz2, k, &itop);
+        f = face_unit_far2<false>(X2, Y2, ut, itop, k.face);
+      }
       const float2 r = make_float2(sa.r, sb.r);
       float2 vr = __fmul2_rn(r, u), vd = __fmul2_rn(r, f);
       // near pairs (and the padding station) go through the double path or
