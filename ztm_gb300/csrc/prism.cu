@@ -33,7 +33,7 @@ namespace {
 
 constexpr int FAR_TS = 128;   // stations per block in the far kernel
 constexpr int F64_TS = 64;    // stations per block in the plain double kernel
-constexpr int NEAR_WPB = 4;   // warps (stations) per block in the near kernel
+constexpr int FAR_NEAR_ST = 32;  // stations per near item of the far kernel's queue
 
 // ---------------------------------------------------------------------------
 __global__ void station_prep_kernel(MeshDesc m, double L0, int ns,
@@ -103,15 +103,18 @@ __global__ void near_iv_kernel(MeshConst k, int ns, const int4* __restrict__ si,
   lr[s] = (lmax >= 0) ? make_int2(lmin, lmax) : make_int2(1, 0);
 }
 
+// Near region of station s in T (double: the mixed method; float: the FP32
+// method), by one warp: Phi once per vertex of the region times the signed
+// triple difference of the region's densities around the vertex; lane 0
+// writes out[s].
 template <typename T>
-__global__ void __launch_bounds__(NEAR_WPB * 32)
-    near_kernel(MeshConst k, MeshDesc m, int ns, const double* __restrict__ sxyz,
-                const int4* __restrict__ si, const short2* __restrict__ iv,
-                const int2* __restrict__ lr, const double* __restrict__ rho,
-                double* __restrict__ out) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int s = blockIdx.x * NEAR_WPB + warp;
-  if (s >= ns) return;
+__device__ __forceinline__ void near_station(const MeshConst& k, const MeshDesc& m, int s,
+                                             const double* __restrict__ sxyz,
+                                             const int4* __restrict__ si,
+                                             const short2* __restrict__ iv,
+                                             const int2* __restrict__ lr,
+                                             const double* __restrict__ rho,
+                                             double* __restrict__ out, int lane) {
   const NearBox b = near_box(si[s], k);
   const int2 L = lr[s];
   if (L.x > L.y) {  // no near prism
@@ -172,6 +175,13 @@ struct FarArgs {
   int chunk_cols;     // columns per item
   int sc;             // columns per shared-memory stage
   int* counter;       // next work item (zeroed before the launch)
+  int n_near;         // near items (FAR_NEAR_ST stations each), spread through the queue
+  bool near_f64;      // near region in double (mixed) or float (FP32 method)
+  MeshDesc m;
+  const double* sxyz;
+  const double* rho;  // caller's double density (near region)
+  const int2* lr;     // per-station near layer range
+  double* near;       // [ns] near-region sums
   const float4* sf;
   const int4* si;
   const short2* iv;  // near-region intervals [station][box column]
@@ -308,102 +318,145 @@ __device__ __forceinline__ void far_stage(const FarArgs& a, const MeshConst& k, 
   }
 }
 
-// Persistent far-field kernel.  The work is tiles x chunks items (a tile of
-// FAR_TS stations against a chunk of chunk_cols columns); the grid is the
-// number of blocks that are resident at once, and each block takes items
-// from a counter in order until none are left, so no block waits for a
-// second wave.  Each item writes its own partial sums (partial[chunk][s]), so
-// the result does not depend on which block ran it.  The density of an item's
-// columns streams through two shared-memory stages by 1-D bulk copies; the
-// copy of the next item's first stage is issued before the current item's
-// last stage is processed.
-__global__ void __launch_bounds__(FAR_TS, 8) far_kernel(FarArgs a) {
+// Persistent kernel of the mixed forward.  The work is tiles x chunks far
+// items (a tile of FAR_TS stations against a chunk of chunk_cols columns) and
+// n_near near items (the double near regions of FAR_NEAR_ST stations, one
+// warp per station), spread evenly through one queue so that while some
+// blocks of an SM sum near regions on the FP64 pipe the others sum far
+// fields on the FMA pipe.  The grid is the number of blocks resident at once;
+// each block takes items from a counter until none are left.  Each far item
+// writes its own partial sums (partial[chunk][s]) and each near item its
+// stations' near[s], so the result does not depend on which block ran what.
+// The density of a far item's columns streams through two shared-memory
+// stages by 1-D bulk copies; the next far item's first stage is copied while
+// the current item's last stage (or a near item) is processed.
+__global__ void __launch_bounds__(FAR_TS, 7) far_kernel(FarArgs a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
   float* stage = reinterpret_cast<float*>(smem_raw + 128);
   __shared__ int s_lm;
   __shared__ int s_item[2];
+  __shared__ int s_to[2];  // a copy wait gave up (by stage parity)
   const MeshConst& k = a.k;
   const int stage_floats = a.sc * k.nzp;
-  const int n_items = a.tiles * a.chunks;
+  const int n_far = a.tiles * a.chunks;
+  const int n_items = n_far + a.n_near;
   const FarCoef fc = k.fc;
 
-  // columns [cs, cs + ncol) of stage st of an item
-  auto stage_cols = [&](int item, int st, int* cs) {
-    const int c0 = (item / a.tiles) * a.chunk_cols;
+  // queue position i: near iff floor((i+1) n_near / n) > floor(i n_near / n);
+  // floor(i n_near / n) near positions come before it
+  auto near_before = [&](int i) { return (int)((long long)i * a.n_near / n_items); };
+  auto is_near = [&](int i) { return near_before(i + 1) > near_before(i); };
+  auto far_index = [&](int i) { return i - near_before(i); };
+  // columns [cs, cs + ncol) of stage st of far item f
+  auto stage_cols = [&](int f, int st, int* cs) {
+    const int c0 = (f / a.tiles) * a.chunk_cols;
     const int c1 = min(k.ncols, c0 + a.chunk_cols);
     *cs = c0 + st * a.sc;
     return min(a.sc, c1 - *cs);
   };
-  auto n_stages = [&](int item) {
-    const int c0 = (item / a.tiles) * a.chunk_cols;
+  auto n_stages = [&](int f) {
+    const int c0 = (f / a.tiles) * a.chunk_cols;
     const int c1 = min(k.ncols, c0 + a.chunk_cols);
     return (c1 - c0 + a.sc - 1) / a.sc;
   };
-  // thread 0 only: copy stage st of item into buffer (seq & 1)
-  auto issue = [&](int item, int st, int seq) {
+  // thread 0 only: copy stage st of far item f into buffer (q & 1)
+  auto issue = [&](int f, int st, int q) {
     int cs;
-    const int ncol = stage_cols(item, st, &cs);
+    const int ncol = stage_cols(f, st, &cs);
     const uint32_t bytes = (uint32_t)ncol * k.nzp * 4u;
-    mbar_expect_tx(&bar[seq & 1], bytes);
-    bulk_g2s(stage + (seq & 1) * stage_floats, a.rhoT + (size_t)cs * k.nzp, bytes, &bar[seq & 1]);
+    mbar_expect_tx(&bar[q & 1], bytes);
+    bulk_g2s(stage + (q & 1) * stage_floats, a.rhoT + (size_t)cs * k.nzp, bytes, &bar[q & 1]);
   };
 
   if (threadIdx.x == 0) {
+    s_to[0] = s_to[1] = 0;
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
     fence_mbar_init();
     const int first = atomicAdd(a.counter, 1);
     s_item[0] = first;
     s_item[1] = first < n_items ? atomicAdd(a.counter, 1) : n_items;
-    if (first < n_items) issue(first, 0, 0);
   }
   __syncthreads();
 
   int seq = 0;     // stages waited for so far (buffer seq & 1, parity (seq >> 1) & 1)
-  int issued = 0;  // stages issued so far (thread 0's count; others keep it too)
-  if (s_item[0] < n_items) issued = 1;
+  int issued = 0;  // stages issued so far (thread 0 issues; every thread keeps the count)
   bool timed_out = false;
   int par = 0;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (;;) {
     const int item = s_item[par];
     if (item >= n_items) break;
     const int nxt = s_item[par ^ 1];
-    const int tile = item % a.tiles, chunk = item / a.tiles;
+    const bool nxt_far = nxt < n_items && !is_near(nxt);
+    if (is_near(item)) {
+      // copy the next far item's first stage meanwhile
+      if (issued == seq && nxt_far) {
+        if (threadIdx.x == 0) issue(far_index(nxt), 0, seq);
+        issued = seq + 1;
+      }
+      const int s0 = near_before(item) * FAR_NEAR_ST;
+      for (int j = warp; j < FAR_NEAR_ST; j += FAR_TS / 32) {
+        const int s = s0 + j;
+        if (s >= a.ns) break;
+        if (a.near_f64)
+          near_station<double>(k, a.m, s, a.sxyz, a.si, a.iv, a.lr, a.rho, a.near, lane);
+        else
+          near_station<float>(k, a.m, s, a.sxyz, a.si, a.iv, a.lr, a.rho, a.near, lane);
+      }
+      if (threadIdx.x == 0) s_item[par] = nxt < n_items ? atomicAdd(a.counter, 1) : n_items;
+      __syncthreads();
+      par ^= 1;
+      continue;
+    }
+    const int f = far_index(item);
+    const int tile = f % a.tiles, chunk = f / a.tiles;
     const int s = tile * FAR_TS + threadIdx.x;
     const bool active = s < a.ns;
     FarStation t = {0.f, 0.f, 0.f, 0, 0, 0, {1, 0, 1, 0, 1, 0}};
     if (active) {
-      const float4 f = a.sf[s];
+      const float4 fv = a.sf[s];
       const int4 i = a.si[s];
-      t.ex = f.x; t.ey = f.y; t.ez = f.z;
+      t.ex = fv.x; t.ey = fv.y; t.ez = fv.z;
       t.ixs = i.x; t.iys = i.y; t.izs = i.z;
       t.nb = near_box(i, k);
     }
-    if (threadIdx.x == 0) s_lm = 0;
+    if (threadIdx.x == 0) {
+      s_lm = 0;
+      if (issued == seq) issue(f, 0, seq);  // not prefetched
+    }
+    if (issued == seq) issued = seq + 1;
     __syncthreads();
     if (active) atomicMax(&s_lm, t.nb.l1 + 1);
     __syncthreads();
     const int Lm = min(s_lm, k.nz);
     Kahan acc;
-    const int nst = n_stages(item);
+    const int nst = n_stages(f);
     for (int st = 0; st < nst; st++) {
       if (threadIdx.x == 0) {
         if (st + 1 < nst)
-          issue(item, st + 1, seq + 1);
-        else if (nxt < n_items)
-          issue(nxt, 0, seq + 1);
+          issue(f, st + 1, seq + 1);
+        else if (nxt_far)
+          issue(far_index(nxt), 0, seq + 1);
       }
-      if (st + 1 < nst || nxt < n_items) issued = seq + 2;
-      const bool ok = mbar_wait(&bar[seq & 1], (seq >> 1) & 1);
-      if (__syncthreads_or(!ok)) {
+      if (st + 1 < nst || nxt_far) issued = seq + 2;
+      // a thread that gives up on the copy raises the stage's flag and skips
+      // the stage; the block leaves together after the stage's barrier (the
+      // flags alternate by stage, so a flag raised in the next stage cannot
+      // be read by a thread still finishing this one)
+      if (mbar_wait(&bar[seq & 1], (seq >> 1) & 1)) {
+        int cs;
+        const int ncol = stage_cols(f, st, &cs);
+        far_stage(a, k, fc, t, s, Lm, stage + (seq & 1) * stage_floats, cs, ncol, acc);
+      } else {
+        s_to[seq & 1] = 1;
+      }
+      __syncthreads();
+      if (s_to[seq & 1]) {
         timed_out = true;
         break;
       }
-      int cs;
-      const int ncol = stage_cols(item, st, &cs);
-      far_stage(a, k, fc, t, s, Lm, stage + (seq & 1) * stage_floats, cs, ncol, acc);
-      __syncthreads();
       seq++;
     }
     if (timed_out) break;
@@ -574,7 +627,7 @@ struct FarShape {
 
 // Launch shapes the autotuner tries: {columns per shared-memory stage, work
 // items per resident block}.  The first is the default.
-constexpr int FAR_SHAPES[][2] = {{16, 16}, {8, 16}, {16, 8}, {16, 32}, {32, 16}, {64, 16}};
+constexpr int FAR_SHAPES[][2] = {{32, 8}, {16, 16}, {16, 8}, {32, 16}, {64, 16}, {64, 8}};
 
 // Launch shape of the far kernel: sc columns per stage, the grid = the blocks
 // resident at once, about ipb work items per block (more items: a shorter
@@ -674,27 +727,6 @@ void launch_mesh_near_iv(ztm_ctx* c, const MeshConst& k, int ns, const int4* si,
   c->launches++;
 }
 
-void launch_mesh_near(ztm_ctx* c, const MeshConst& k, const MeshDesc& m, int ns,
-                      const double* sxyz, const int4* si, const short2* iv, const int2* lr,
-                      const double* rho, double* out, bool f64, cudaStream_t stream) {
-  if (ns <= 0) return;
-  if (!stream) stream = c->stream;
-  int blocks = (ns + NEAR_WPB - 1) / NEAR_WPB;
-  if (f64)
-    {
-      ZtmProf prof_(c, "prism_near", stream);
-      near_kernel<double><<<blocks, NEAR_WPB * 32, 0, stream>>>(k, m, ns, sxyz, si, iv, lr, rho,
-                                                                out);
-    }
-  else
-    {
-      ZtmProf prof_(c, "prism_near", stream);
-      near_kernel<float><<<blocks, NEAR_WPB * 32, 0, stream>>>(k, m, ns, sxyz, si, iv, lr, rho,
-                                                               out);
-    }
-  c->launches++;
-}
-
 size_t ztm_prism_ws(const MeshDesc& m, int ns, int precision, int num_sms, const ztm_opts* o) {
   if (precision == ZTM_PREC_FP64) {
     long long np = (long long)m.nx * m.ny * m.nz, len;
@@ -764,6 +796,13 @@ int ztm_launch_prism(ztm_ctx* c, const MeshDesc& m, const double* d_rho, int ns,
   a.k = k; a.ns = ns; a.sf = sf; a.si = si; a.iv = iv; a.rhoT = rhoT; a.partial = partial;
   a.err = c->d_err;
   a.counter = counter;
+  a.n_near = (ns + FAR_NEAR_ST - 1) / FAR_NEAR_ST;
+  a.near_f64 = precision == ZTM_PREC_MIXED;
+  a.m = m;
+  a.sxyz = d_sxyz;
+  a.rho = d_rho;
+  a.lr = lr;
+  a.near = near;
   auto launch_far = [&](const FarShape& t) {
     a.tiles = t.tiles;
     a.chunks = t.chunks;
@@ -798,16 +837,11 @@ int ztm_launch_prism(ztm_ctx* c, const MeshDesc& m, const double* d_rho, int ns,
     c->tuned[tune_key(k, ns)] = {shape};
   }
   FarShape f = far_shape(k, ns, c->num_sms, o, FAR_SHAPES[shape][0], FAR_SHAPES[shape][1]);
-  // the double near box runs on the side stream, concurrently with the float
-  // far field (different pipes: FP64 vs FMA/MUFU)
-  ztm_fork(c);
-  launch_mesh_near(c, k, m, ns, d_sxyz, si, iv, lr, d_rho, near, precision == ZTM_PREC_MIXED,
-                   c->aux);
+  // near regions (FP64 pipe) and far fields (FMA pipe) in one persistent grid
   {
     ZtmProf prof_(c, "prism_far");
     launch_far(f);
   }
-  ztm_join(c);
   const double far_scale = k.L0 * (double)k.dxn * k.dyn * k.dzn;
   finalize_kernel<<<(ns + 255) / 256, 256, 0, c->stream>>>(ns, f.chunks, partial, far_scale, near,
                                                            G5, d_gz);

@@ -203,9 +203,6 @@ void launch_mesh_transpose(ztm_ctx* c, const MeshConst& k, int nmodels, const do
 // sum over box vertices of Phi(vertex - station) times the signed triple
 // difference of the density over the (up to 8) box prisms around the vertex.
 // One warp per station.  out[s] = that sum (metres x density, without G).
-void launch_mesh_near(ztm_ctx* c, const MeshConst& k, const MeshDesc& m, int ns,
-                      const double* sxyz, const int4* si, const short2* iv, const int2* lr,
-                      const double* rho, double* out, bool f64, cudaStream_t stream = nullptr);
 // Near-region intervals: iv[s*nslots + slot] (layers lo..hi) and the
 // station's overall layer range lr[s] = (lmin, lmax) (lmin > lmax: none).
 void launch_mesh_near_iv(ztm_ctx* c, const MeshConst& k, int ns, const int4* si, short2* iv,

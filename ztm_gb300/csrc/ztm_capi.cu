@@ -236,10 +236,15 @@ int ztm_ctx_create(int device, ztm_ctx** out) {
     delete c;
     return ZTM_ERR_NODEV;
   }
+  int lo_prio = 0, hi_prio = 0;
   if (cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device) !=
           cudaSuccess ||
       cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking) != cudaSuccess ||
+      // the side stream carries the short double near-field kernels that run
+      // beside a persistent far-field grid: give it the highest priority so
+      // its blocks are placed first whenever a slot frees up
+      cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio) != cudaSuccess ||
+      cudaStreamCreateWithPriority(&c->aux, cudaStreamNonBlocking, hi_prio) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
       cudaMalloc((void**)&c->d_err, sizeof(int)) != cudaSuccess ||
