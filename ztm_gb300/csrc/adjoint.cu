@@ -10,15 +10,17 @@
 //   FP64 plain  thread per prism, stations streamed through shared memory,
 //               8-corner closed form in double; station chunks reduced in a
 //               fixed order.
-//   MIXED/FP32  far pairs: thread per (column, group of 8 layers), the
-//               column's horizontal offsets computed once per station and the
-//               4th-order far-field expansion per layer in float with Kahan
-//               sums.  Near pairs (prisms in the station's near box): one
-//               warp per station computes Phi once per box vertex in shared
-//               memory, combines the 8 corners of each box prism and adds
-//               r[s]*U to g_rho with double atomics.  The far kernel writes
-//               every g_rho entry first, so the result is complete after the
-//               near kernel; the atomics make the last bits order-dependent.
+//   MIXED/FP32  far pairs: thread per (column, group of 16 layers) and
+//               station slice, the column's horizontal offsets and polynomial
+//               computed once per station and the far-field expansion per
+//               layer in float (second order where the whole warp is far
+//               enough), float sums over 32 stations, double beyond; the
+//               slices meet in g_rho by double atomics.  Near pairs (prisms in
+//               the station's near region): one warp per station computes
+//               Phi once per vertex in shared memory, combines the 8 corners
+//               of each near prism and adds r[s]*U to g_rho with double
+//               atomics.  g_rho is zeroed first; the atomics make the last
+//               bits order-dependent.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -29,18 +31,27 @@
 namespace {
 
 constexpr int ADJ_TS = 128;
-constexpr int ADJ_LG = 8;      // layers per thread in the far kernel
+constexpr int ADJ_LG = 16;     // layers per thread in the far kernel
 constexpr int ADJ_STILE = 256; // stations per shared-memory tile
+constexpr int ADJ_SGRP = 32;   // stations per float sum
 
 // grid.x covers ncols * ceil(nz/LG) threads.  g[p] = G5*L0*Vn * sum.
-__global__ void __launch_bounds__(ADJ_TS)
+// A thread sums its column's 16 layers over its block's slice of the
+// stations (grid.y): float over 32 stations (packed, two layers per lane
+// pair), then double in shared memory, then one double atomic per layer into
+// g (zeroed before the launch).
+// The per-(station, column) setup (offsets, the horizontal polynomial, the
+// near box test) is shared by the 16 layers.
+__global__ void __launch_bounds__(ADJ_TS, 6)
     adj_far_kernel(MeshConst k, int ns, const float4* __restrict__ sf,
                    const int4* __restrict__ si, const short2* __restrict__ iv,
-                   const double* __restrict__ res, double scale, double* __restrict__ g) {
+                   const double* __restrict__ res, double scale, int slice,
+                   double* __restrict__ g) {
   __shared__ float4 s_f[ADJ_STILE];
   __shared__ int4 s_i[ADJ_STILE];
   __shared__ int4 s_b[ADJ_STILE];  // the station's near box columns x0, x1, y0, y1
   __shared__ float s_r[ADJ_STILE];
+  __shared__ double s_acc[ADJ_LG][ADJ_TS];
   const int ngroups = (k.nz + ADJ_LG - 1) / ADJ_LG;
   const long long t = blockIdx.x * (long long)ADJ_TS + threadIdx.x;
   const bool active = t < (long long)k.ncols * ngroups;
@@ -52,12 +63,16 @@ __global__ void __launch_bounds__(ADJ_TS)
   const int ix = c % k.nx, iy = c / k.nx;
   const int l0 = lg * ADJ_LG;
   const FarCoef fc = k.fc;
-  Kahan acc[ADJ_LG];
-  for (int s0 = 0; s0 < ns; s0 += ADJ_STILE) {
+#pragma unroll
+  for (int j = 0; j < ADJ_LG; j++) s_acc[j][threadIdx.x] = 0.0;
+  const float2 dz2 = make_float2(k.dzn, k.dzn);
+  // this block's slice of the stations (grid.y)
+  const int sb = blockIdx.y * slice, se = min(ns, sb + slice);
+  for (int s0 = sb; s0 < se; s0 += ADJ_STILE) {
     __syncthreads();
     for (int q = threadIdx.x; q < ADJ_STILE; q += ADJ_TS) {
       const int s = s0 + q;
-      if (s < ns) {
+      if (s < se) {
         const int4 i = si[s];
         const NearBox b = near_box(i, k);
         s_f[q] = sf[s];
@@ -73,17 +88,15 @@ __global__ void __launch_bounds__(ADJ_TS)
     }
     __syncthreads();
     if (!active) continue;
-    const int cnt = min(ADJ_STILE, ns - s0);
-    // plain float sums over 16 stations, compensated across the groups
-    for (int q0 = 0; q0 < cnt; q0 += 16) {
+    const int cnt = min(ADJ_STILE, se - s0);
+    for (int q0 = 0; q0 < cnt; q0 += ADJ_SGRP) {
       float2 gs[ADJ_LG / 2];
 #pragma unroll
       for (int j = 0; j < ADJ_LG / 2; j++) gs[j] = make_float2(0.f, 0.f);
-      const int q1 = min(cnt, q0 + 16);
+      const int q1 = min(cnt, q0 + ADJ_SGRP);
       for (int q = q0; q < q1; q++) {
         const float4 f = s_f[q];
         const int4 i = s_i[q];
-        const float w = s_r[q];
         const float X = fmaf((float)(i.x - ix), k.dxn, f.x);
         const float Y = fmaf((float)(i.y - iy), k.dyn, f.y);
         const ColPoly cp = col_poly(X, Y, fc);
@@ -92,17 +105,19 @@ __global__ void __launch_bounds__(ADJ_TS)
         int elo = k.nz;
         unsigned espan = 0u;
         if (ncl) {  // the column's near-region layers for this station
-          const short2 t = iv[(size_t)(s0 + q) * k.nslots + (ix - b.x) + (b.y - b.x + 1) * (iy - b.z)];
-          if (t.x <= t.y) {
-            elo = t.x;
-            espan = (unsigned)(t.y - t.x);
+          const short2 tv =
+              iv[(size_t)(s0 + q) * k.nslots + (ix - b.x) + (b.y - b.x + 1) * (iy - b.z)];
+          if (tv.x <= tv.y) {
+            elo = tv.x;
+            espan = (unsigned)(tv.y - tv.x);
           } else {
             ncl = false;
           }
         }
         const float Zg = fmaf((float)(l0 - i.z), k.dzn, f.z);
         const ColPoly2 cp2 = col_poly2(cp, fc.a1);
-        const float2 zg2 = make_float2(Zg, Zg), dz2 = make_float2(k.dzn, k.dzn);
+        const float2 zg2 = make_float2(Zg, Zg);
+        const float2 w2 = make_float2(s_r[q], s_r[q]);
         float2 v[ADJ_LG / 2];
         // the warp's columns all far enough for the second-order form (the
         // lanes of a warp share the station, so this is mostly uniform)
@@ -126,14 +141,15 @@ __global__ void __launch_bounds__(ADJ_TS)
             if (((unsigned)(lb - elo) <= espan) || lb >= k.nz) v[j].y = 0.f;
           }
         }
-        const float2 w2 = make_float2(w, w);
 #pragma unroll
         for (int j = 0; j < ADJ_LG / 2; j++) gs[j] = __ffma2_rn(w2, v[j], gs[j]);
       }
+      // the group's float sums into the double accumulators (FP64 pipe,
+      // otherwise idle in this kernel)
 #pragma unroll
       for (int j = 0; j < ADJ_LG / 2; j++) {
-        acc[2 * j].add(gs[j].x);
-        acc[2 * j + 1].add(gs[j].y);
+        s_acc[2 * j][threadIdx.x] += (double)gs[j].x;
+        s_acc[2 * j + 1][threadIdx.x] += (double)gs[j].y;
       }
     }
   }
@@ -142,7 +158,7 @@ __global__ void __launch_bounds__(ADJ_TS)
 #pragma unroll
   for (int j = 0; j < ADJ_LG; j++) {
     const int l = l0 + j;
-    if (l < k.nz) g[c + plane * l] = scale * acc[j].value();
+    if (l < k.nz) atomicAdd(&g[c + plane * l], scale * s_acc[j][threadIdx.x]);
   }
 }
 
@@ -314,10 +330,28 @@ int ztm_launch_adjoint(ztm_ctx* c, const MeshDesc& m, int ns, const double* d_sx
   const int ngroups = (k.nz + ADJ_LG - 1) / ADJ_LG;
   const long long threads = (long long)k.ncols * ngroups;
   const double scale = G5 * k.L0 * (double)k.dxn * k.dyn * k.dzn;
+  // station slices (grid.y) so that the grid is many waves of resident
+  // blocks; the slices' sums meet in g by double atomics (g zeroed first)
+  const long long blocks = (threads + ADJ_TS - 1) / ADJ_TS;
+  int occ = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, adj_far_kernel, ADJ_TS, 0) !=
+          cudaSuccess ||
+      occ < 1) {
+    cudaGetLastError();
+    occ = 1;
+  }
+  const long long resident = (long long)occ * c->num_sms;
+  long long slices = std::max(1LL, (8 * resident + blocks - 1) / blocks);
+  slices = std::min(slices, std::max(1LL, (long long)(ns + ADJ_STILE - 1) / ADJ_STILE));
+  slices = std::min(slices, 65535LL);
+  int slice = (int)((ns + slices - 1) / slices);
+  slice = ((slice + ADJ_STILE - 1) / ADJ_STILE) * ADJ_STILE;
+  slices = (ns + slice - 1) / slice;
+  cudaMemsetAsync(d_g, 0, (size_t)k.ncols * k.nz * sizeof(double), c->stream);
   {
     ZtmProf prof_(c, "adjoint_far");
-    adj_far_kernel<<<(unsigned)((threads + ADJ_TS - 1) / ADJ_TS), ADJ_TS, 0, c->stream>>>(
-        k, ns, sf, si, iv, d_res, scale, d_g);
+    adj_far_kernel<<<dim3((unsigned)blocks, (unsigned)slices), ADJ_TS, 0, c->stream>>>(
+        k, ns, sf, si, iv, d_res, scale, slice, d_g);
   }
   c->launches++;
   const int cap = near_cap(k);
