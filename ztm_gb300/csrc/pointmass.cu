@@ -117,23 +117,146 @@ __global__ void __launch_bounds__(PM_TS)
   if (active) partial[(long long)blockIdx.y * p.ns + s] = F64 ? acc64 : acc32.value();
 }
 
-// Float gather on the packed FP32 path: the tile keeps only the selected
-// nodes (order preserved by a block scan), stored as (-i, -j, -k, w), and
-// two nodes are evaluated per FADD2/FFMA2/FMUL2; the rsqrt stays scalar
-// (rsqrt.approx.ftz).  Plain float sums over 16 nodes, Kahan across groups.
+// Float path in two steps.
+//
+// 1. Node list (pm_nodes_count / pm_nodes_scan / pm_nodes_write): the
+//    selected nodes, in order, as float4 (-i, -j, -k, w) in grid units, built
+//    once per call (O(nodes), memory bound).  A block covers PM_NB nodes;
+//    the blocks' counts are scanned so that each block writes its nodes at
+//    its offset in node order.
+// 2. Gather (pm_gather_f32_kernel): a thread owns a station; the compacted
+//    nodes stream through shared memory in tiles of PM_TILE (coalesced float4
+//    loads, the next tile's loads in flight while the current one is
+//    summed); two nodes per FADD2/FFMA2/FMUL2, the rsqrt on the SFU
+//    (rsqrt.approx.ftz).  Plain float sums over 16
+//    nodes, Kahan across groups.  grid.y splits the node list; the list's
+//    length is read on the device.
+constexpr int PM_NB = 1024;  // nodes per block of the node-list kernels
+constexpr int PM_NT = 256;   // threads of the node-list kernels (4 nodes each)
+
 __device__ __forceinline__ float pm_rsqrt_ftz(float x) {
   float y;
   asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
   return y;
 }
 
+// Node t of the list (t < nnodes): its selection and its float4.  A bad nn
+// entry is not selected (and recorded in *err when err is given).
+__device__ __forceinline__ bool pm_node(const PmParams& p, const double* __restrict__ drho,
+                                        const int* __restrict__ nn, long long t, float4* v,
+                                        int* err) {
+  const long long n = nn ? (long long)nn[t] : t;
+  if (n < 0 || n >= p.N) {
+    if (err) atomicOr(err, ZTM_DEVERR_BOUNDS);
+    return false;
+  }
+  const double w = drho[n];
+  const bool sel = nn ? true : (fabsf((float)w) > (float)p.thr);
+  if (sel) {
+    // index map of TFM.cpp:85,97 (fine grid ii = (di-1)*fh+1); N < 2^31
+    const int ni = (int)n % p.ii, nj = ((int)n / p.ii) % p.jj, nk = (int)n / (p.ii * p.jj);
+    *v = make_float4(-(float)(ni * (1.0 / p.fh)), -(float)(nj * (1.0 / p.fh)),
+                     -(float)(nk * (1.0 / p.fv)), (float)w);
+  }
+  return sel;
+}
+
+__global__ void __launch_bounds__(PM_NT)
+    pm_nodes_count(PmParams p, const double* __restrict__ drho, const int* __restrict__ nn,
+                   int* __restrict__ counts, int* err) {
+  __shared__ int s_c;
+  if (threadIdx.x == 0) s_c = 0;
+  __syncthreads();
+  int c = 0;
+  for (int q = threadIdx.x; q < PM_NB; q += PM_NT) {
+    const long long t = (long long)blockIdx.x * PM_NB + q;
+    float4 v;
+    if (t < p.nnodes && pm_node(p, drho, nn, t, &v, err)) c++;
+  }
+  c += __shfl_xor_sync(0xffffffffu, c, 16);
+  c += __shfl_xor_sync(0xffffffffu, c, 8);
+  c += __shfl_xor_sync(0xffffffffu, c, 4);
+  c += __shfl_xor_sync(0xffffffffu, c, 2);
+  c += __shfl_xor_sync(0xffffffffu, c, 1);
+  if ((threadIdx.x & 31) == 0) atomicAdd(&s_c, c);
+  __syncthreads();
+  if (threadIdx.x == 0) counts[blockIdx.x] = s_c;
+}
+
+// One block: exclusive scan of the nb block counts in place; *total = sum.
+__global__ void __launch_bounds__(1024) pm_nodes_scan(int nb, int* __restrict__ counts,
+                                                      int* __restrict__ total) {
+  __shared__ int s_w[32];
+  __shared__ int s_carry;
+  if (threadIdx.x == 0) s_carry = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int b0 = 0; b0 < nb; b0 += 1024) {
+    const int b = b0 + threadIdx.x;
+    const int v = b < nb ? counts[b] : 0;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) s_w[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      int w = s_w[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += y;
+      }
+      s_w[lane] = w;  // inclusive over warps
+    }
+    __syncthreads();
+    const int before = s_carry + (warp ? s_w[warp - 1] : 0) + x - v;
+    if (b < nb) counts[b] = before;
+    __syncthreads();
+    if (threadIdx.x == 0) s_carry += s_w[31];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total = s_carry;
+}
+
+__global__ void __launch_bounds__(PM_NT)
+    pm_nodes_write(PmParams p, const double* __restrict__ drho, const int* __restrict__ nn,
+                   const int* __restrict__ offsets, float4* __restrict__ nodes) {
+  __shared__ int s_w[PM_NT / 32];
+  __shared__ int s_base;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) s_base = offsets[blockIdx.x];
+  __syncthreads();
+  // PM_NB / PM_NT rounds in node order; each an order-preserving block scan
+  for (int q0 = 0; q0 < PM_NB; q0 += PM_NT) {
+    const long long t = (long long)blockIdx.x * PM_NB + q0 + threadIdx.x;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    // bad entries were recorded by pm_nodes_count
+    const bool sel = t < p.nnodes && pm_node(p, drho, nn, t, &v, nullptr);
+    const unsigned bal = __ballot_sync(0xffffffffu, sel);
+    const int below = __popc(bal & ((1u << lane) - 1u));
+    if (lane == 0) s_w[warp] = __popc(bal);
+    __syncthreads();
+    int wbase = 0;
+    for (int w = 0; w < warp; w++) wbase += s_w[w];
+    if (sel) nodes[s_base + wbase + below] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int tot = 0;
+      for (int w = 0; w < PM_NT / 32; w++) tot += s_w[w];
+      s_base += tot;
+    }
+    __syncthreads();
+  }
+}
+
 __global__ void __launch_bounds__(PM_TS)
-    pm_gather_f32_kernel(PmParams p, const double* __restrict__ drho,
-                         const int* __restrict__ nn, const double* __restrict__ surf,
-                         long long chunk_len, double* __restrict__ partial, int* err) {
-  __shared__ float4 tile[PM_TILE + 2];
-  __shared__ int s_wcount[PM_TS / 32];
-  __shared__ int s_total;
+    pm_gather_f32_kernel(PmParams p, const float4* __restrict__ nodes,
+                         const int* __restrict__ n_nodes, const double* __restrict__ surf,
+                         long long chunk_len, double* __restrict__ partial) {
+  __shared__ float4 tile[PM_TILE];
   const int s = blockIdx.x * PM_TS + threadIdx.x;
   const bool active = s < p.ns;
   float i0 = 0.f, j0 = 0.f, k0 = 0.f;
@@ -143,59 +266,29 @@ __global__ void __launch_bounds__(PM_TS)
     j0 = (float)sj;
     k0 = (float)surf[si + sj * p.di];
   }
+  const long long M = *n_nodes;
   const long long n0 = (long long)blockIdx.y * chunk_len;
-  const long long n1 = min(p.nnodes, n0 + chunk_len);
-  const double ifh = 1.0 / p.fh, ifv = 1.0 / p.fv;
-  const long long plane = (long long)p.ii * p.jj;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const long long n1 = min(M, n0 + chunk_len);
   const float2 I0 = make_float2(i0, i0), J0 = make_float2(j0, j0), K0 = make_float2(k0, k0);
   Kahan acc;
+  // this thread's two nodes of the next tile (zero mass far away past the end)
+  const float4 pad = make_float4(-1.0e18f, 0.f, 0.f, 0.f);
+  float4 na = pad, nb = pad;
+  if (n0 + threadIdx.x < n1) na = nodes[n0 + threadIdx.x];
+  if (n0 + PM_TS + threadIdx.x < n1) nb = nodes[n0 + PM_TS + threadIdx.x];
   for (long long t0 = n0; t0 < n1; t0 += PM_TILE) {
-    // each thread owns nodes t0 + 2*tid and t0 + 2*tid + 1 (in order)
-    float4 v[2];
-    bool sel[2];
-#pragma unroll
-    for (int h = 0; h < 2; h++) {
-      const long long t = t0 + 2 * threadIdx.x + h;
-      sel[h] = false;
-      v[h] = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (t < n1) {
-        const long long n = nn ? (long long)nn[t] : t;
-        if (n < 0 || n >= p.N) {
-          atomicOr(err, ZTM_DEVERR_BOUNDS);  // bad list entry: recorded, skipped
-        } else {
-          const double w = drho[n];
-          sel[h] = nn ? true : (fabsf((float)w) > (float)p.thr);
-          const long long ni = n % p.ii, nj = (n / p.ii) % p.jj, nk = n / plane;
-          v[h] = make_float4(-(float)(ni * ifh), -(float)(nj * ifh), -(float)(nk * ifv), (float)w);
-        }
-      }
-    }
-    // order-preserving compaction of the selected nodes into the tile
-    const int mine = (int)sel[0] + (int)sel[1];
-    int incl = mine;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += y;
-    }
-    __syncthreads();  // the previous tile is fully consumed
-    if (lane == 31) s_wcount[warp] = incl;
+    __syncthreads();  // the previous tile is consumed
+    tile[threadIdx.x] = na;
+    tile[PM_TS + threadIdx.x] = nb;
     __syncthreads();
-    int base = 0;
-    for (int w = 0; w < warp; w++) base += s_wcount[w];
-    if (threadIdx.x == PM_TS - 1) s_total = base + incl;
-    int pos = base + incl - mine;
-    if (sel[0]) tile[pos++] = v[0];
-    if (sel[1]) tile[pos++] = v[1];
-    __syncthreads();
-    const int cnt = s_total;  // <= PM_TILE (two nodes per thread)
-    if (threadIdx.x == 0 && (cnt & 1))  // pad to an even count: zero mass far away
-      tile[cnt] = make_float4(-1.0e18f, 0.f, 0.f, 0.f);
-    __syncthreads();
+    const long long t1 = t0 + PM_TILE;
+    na = nb = pad;
+    if (t1 + threadIdx.x < n1) na = nodes[t1 + threadIdx.x];
+    if (t1 + PM_TS + threadIdx.x < n1) nb = nodes[t1 + PM_TS + threadIdx.x];
     if (!active) continue;
+    const int cnt = (int)min((long long)PM_TILE, n1 - t0);
     float2 g = make_float2(0.f, 0.f);
-    for (int q = 0; q < cnt; q += 2) {
+    for (int q = 0; q < cnt; q += 2) {  // an odd count reads the zero-mass pad
       const float4 a = tile[q], b = tile[q + 1];
       const float2 dx = __fadd2_rn(I0, make_float2(a.x, b.x));
       const float2 dy = __fadd2_rn(J0, make_float2(a.y, b.y));
@@ -251,11 +344,16 @@ void pm_shape(const PmParams& p, int num_sms, int* tiles, int* chunks, long long
 }  // namespace
 
 size_t ztm_pointmass_ws(const PmParams& p, int precision, int num_sms) {
-  (void)precision;
   int tiles, chunks;
   long long len;
   pm_shape(p, num_sms, &tiles, &chunks, &len);
-  return WsCarver::need((size_t)chunks * std::max(p.ns, 1) * sizeof(double));
+  size_t w = WsCarver::need((size_t)chunks * std::max(p.ns, 1) * sizeof(double));
+  if (precision != ZTM_PREC_FP64) {  // the float node list
+    const long long nb = std::max(1LL, (p.nnodes + PM_NB - 1) / PM_NB);
+    w += WsCarver::need((size_t)std::max(p.nnodes, 1LL) * sizeof(float4)) +
+         WsCarver::need((size_t)nb * sizeof(int)) + WsCarver::need(sizeof(int));
+  }
+  return w;
 }
 
 int ztm_launch_pointmass(ztm_ctx* c, const PmParams& p, const double* d_drho,
@@ -267,18 +365,26 @@ int ztm_launch_pointmass(ztm_ctx* c, const PmParams& p, const double* d_drho,
   double* partial = wc.take<double>((size_t)chunks * std::max(p.ns, 1));
   if (p.ns > 0 && p.nnodes > 0) {
     dim3 grid(tiles, chunks);
-    if (precision == ZTM_PREC_FP64)
+    if (precision == ZTM_PREC_FP64) {
+      ZtmProf prof_(c, "pointmass");
+      pm_gather_kernel<true><<<grid, PM_TS, 0, c->stream>>>(p, d_drho, d_nn, d_surf, len, partial,
+                                                            c->d_err);
+      c->launches++;
+    } else {
+      const long long nb = (p.nnodes + PM_NB - 1) / PM_NB;
+      if (nb > (1LL << 31) - 1) return ztm_fail(c, ZTM_ERR_RANGE, "too many point-mass nodes");
+      float4* nodes = wc.take<float4>((size_t)p.nnodes);
+      int* counts = wc.take<int>((size_t)nb);
+      int* total = wc.take<int>(1);
+      pm_nodes_count<<<(unsigned)nb, PM_NT, 0, c->stream>>>(p, d_drho, d_nn, counts, c->d_err);
+      pm_nodes_scan<<<1, 1024, 0, c->stream>>>((int)nb, counts, total);
+      pm_nodes_write<<<(unsigned)nb, PM_NT, 0, c->stream>>>(p, d_drho, d_nn, counts, nodes);
       {
         ZtmProf prof_(c, "pointmass");
-        pm_gather_kernel<true><<<grid, PM_TS, 0, c->stream>>>(p, d_drho, d_nn, d_surf, len, partial, c->d_err);
+        pm_gather_f32_kernel<<<grid, PM_TS, 0, c->stream>>>(p, nodes, total, d_surf, len, partial);
       }
-    else
-      {
-        ZtmProf prof_(c, "pointmass");
-        pm_gather_f32_kernel<<<grid, PM_TS, 0, c->stream>>>(p, d_drho, d_nn, d_surf, len,
-                                                            partial, c->d_err);
-      }
-    c->launches++;
+      c->launches += 4;
+    }
   } else {
     chunks = 0;
   }

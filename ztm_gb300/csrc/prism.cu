@@ -68,16 +68,26 @@ __global__ void transpose_kernel(MeshConst k, int nmodels, const double* __restr
   }
 }
 
-// Near-region intervals of every (station, box column), in double.
-__global__ void near_iv_kernel(MeshConst k, int ns, const int4* __restrict__ si,
-                               short2* __restrict__ iv, int2* __restrict__ lr) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= ns) return;
+// Near-region intervals of every (station, box column), in double: one
+// block per station, a thread per box column; the station's overall layer
+// range by shared-memory min/max.
+constexpr int NEAR_IV_TS = 128;
+__global__ void __launch_bounds__(NEAR_IV_TS)
+    near_iv_kernel(MeshConst k, int ns, const int4* __restrict__ si, short2* __restrict__ iv,
+                   int2* __restrict__ lr) {
+  __shared__ int s_min, s_max;
+  const int s = blockIdx.x;
+  if (s >= ns) return;  // uniform over the block
+  if (threadIdx.x == 0) {
+    s_min = 1 << 30;
+    s_max = -1;
+  }
+  __syncthreads();
   const int4 h = si[s];
   const NearBox b = near_box(h, k);
   const int bw = b.x1 - b.x0 + 1, bh = b.y1 - b.y0 + 1;
   int lmin = 1 << 30, lmax = -1;
-  for (int slot = 0; slot < k.nslots; slot++) {
+  for (int slot = threadIdx.x; slot < k.nslots; slot += NEAR_IV_TS) {
     short2 out = make_short2(1, 0);
     if (slot < bw * bh) {
       const int ix = b.x0 + slot % bw, iy = b.y0 + slot / bw;
@@ -100,7 +110,12 @@ __global__ void near_iv_kernel(MeshConst k, int ns, const int4* __restrict__ si,
     }
     iv[(size_t)s * k.nslots + slot] = out;
   }
-  lr[s] = (lmax >= 0) ? make_int2(lmin, lmax) : make_int2(1, 0);
+  if (lmax >= 0) {
+    atomicMin(&s_min, lmin);
+    atomicMax(&s_max, lmax);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) lr[s] = (s_max >= 0) ? make_int2(s_min, s_max) : make_int2(1, 0);
 }
 
 // Near region of station s in T (double: the mixed method; float: the FP32
@@ -723,7 +738,7 @@ void launch_mesh_transpose(ztm_ctx* c, const MeshConst& k, int nmodels, const do
 void launch_mesh_near_iv(ztm_ctx* c, const MeshConst& k, int ns, const int4* si, short2* iv,
                          int2* lr) {
   if (ns <= 0) return;
-  near_iv_kernel<<<(ns + 127) / 128, 128, 0, c->stream>>>(k, ns, si, iv, lr);
+  near_iv_kernel<<<ns, NEAR_IV_TS, 0, c->stream>>>(k, ns, si, iv, lr);
   c->launches++;
 }
 
