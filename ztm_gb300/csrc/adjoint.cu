@@ -48,8 +48,8 @@ __global__ void __launch_bounds__(ADJ_TS, 6)
                    const double* __restrict__ res, double scale, int slice,
                    double* __restrict__ g) {
   __shared__ float4 s_f[ADJ_STILE];
-  __shared__ int4 s_i[ADJ_STILE];
   __shared__ int4 s_b[ADJ_STILE];  // the station's near box columns x0, x1, y0, y1
+  __shared__ float4 s_h[ADJ_STILE];  // the home cell indices as floats (exact)
   __shared__ float s_r[ADJ_STILE];
   __shared__ double s_acc[ADJ_LG][ADJ_TS];
   const int ngroups = (k.nz + ADJ_LG - 1) / ADJ_LG;
@@ -62,6 +62,7 @@ __global__ void __launch_bounds__(ADJ_TS, 6)
   }
   const int ix = c % k.nx, iy = c / k.nx;
   const int l0 = lg * ADJ_LG;
+  const float fix = (float)ix, fiy = (float)iy, fl0 = (float)l0;
   const FarCoef fc = k.fc;
 #pragma unroll
   for (int j = 0; j < ADJ_LG; j++) s_acc[j][threadIdx.x] = 0.0;
@@ -76,13 +77,13 @@ __global__ void __launch_bounds__(ADJ_TS, 6)
         const int4 i = si[s];
         const NearBox b = near_box(i, k);
         s_f[q] = sf[s];
-        s_i[q] = i;
         s_b[q] = make_int4(b.x0, b.x1, b.y0, b.y1);
+        s_h[q] = make_float4((float)i.x, (float)i.y, (float)i.z, 0.f);
         s_r[q] = (float)res[s];
       } else {
         s_f[q] = make_float4(0.f, 0.f, 0.f, 0.f);
-        s_i[q] = make_int4(0, 0, 0, 0);
         s_b[q] = make_int4(1, 0, 1, 0);
+        s_h[q] = make_float4(0.f, 0.f, 0.f, 0.f);
         s_r[q] = 0.f;
       }
     }
@@ -96,9 +97,9 @@ __global__ void __launch_bounds__(ADJ_TS, 6)
       const int q1 = min(cnt, q0 + ADJ_SGRP);
       for (int q = q0; q < q1; q++) {
         const float4 f = s_f[q];
-        const int4 i = s_i[q];
-        const float X = fmaf((float)(i.x - ix), k.dxn, f.x);
-        const float Y = fmaf((float)(i.y - iy), k.dyn, f.y);
+        const float4 hf = s_h[q];
+        const float X = fmaf(hf.x - fix, k.dxn, f.x);
+        const float Y = fmaf(hf.y - fiy, k.dyn, f.y);
         const ColPoly cp = col_poly(X, Y, fc);
         const int4 b = s_b[q];
         bool ncl = ix >= b.x && ix <= b.y && iy >= b.z && iy <= b.w;
@@ -114,7 +115,7 @@ __global__ void __launch_bounds__(ADJ_TS, 6)
             ncl = false;
           }
         }
-        const float Zg = fmaf((float)(l0 - i.z), k.dzn, f.z);
+        const float Zg = fmaf(fl0 - hf.z, k.dzn, f.z);
         const ColPoly2 cp2 = col_poly2(cp, fc.a1);
         const float2 zg2 = make_float2(Zg, Zg);
         const float2 w2 = make_float2(s_r[q], s_r[q]);

@@ -258,6 +258,9 @@ __global__ void __launch_bounds__(IF_TS, 8)
   const int wx0 = active ? max(0, wcx - k.w) : 1, wx1 = active ? min(k.nx - 1, wcx + k.w) : 0;
   const int wy0 = max(0, wcy - k.w), wy1 = min(k.ny - 1, wcy + k.w);
   const int wbw = wx1 - wx0 + 1;
+  const float2 hx2 = make_float2((float)hi.x, (float)hi.x), hy2 = make_float2((float)hi.y, (float)hi.y);
+  const float2 dxn2 = make_float2(k.dxn, k.dxn), dyn2 = make_float2(k.dyn, k.dyn);
+  const float2 ex2 = make_float2(st.ex, st.ex), ey2 = make_float2(st.ey, st.ey);
   Kahan acc;
   for (int t0 = c0; t0 < c1; t0 += IF_TILE) {
     __syncthreads();
@@ -268,18 +271,22 @@ __global__ void __launch_bounds__(IF_TS, 8)
     const int cnt = min(IF_TILE, c1 - t0);
     float2 g = make_float2(0.f, 0.f);  // plain sums over 16 columns, Kahan across
     int ixa = t0 % k.nx, iya = t0 / k.nx;
+    // the column indices also carried as floats (exact integers): the offsets
+    // need no integer-to-float conversions
+    float fxa = (float)ixa, fya = (float)iya;
     for (int q = 0; q < cnt; q += 2) {
       // columns q and q+1 (the second is dropped past the end of the tile)
       int ixb = ixa + 1, iyb = iya;
+      float fxb = fxa + 1.f, fyb = fya;
       if (ixb == k.nx) {
         ixb = 0;
         ++iyb;
+        fxb = 0.f;
+        fyb += 1.f;
       }
       const float4 A = s_c[q], B = s_c[q + 1];
-      const float2 X = make_float2(fmaf((float)(hi.x - ixa), k.dxn, st.ex),
-                                   fmaf((float)(hi.x - ixb), k.dxn, st.ex));
-      const float2 Y = make_float2(fmaf((float)(hi.y - iya), k.dyn, st.ey),
-                                   fmaf((float)(hi.y - iyb), k.dyn, st.ey));
+      const float2 X = __ffma2_rn(__fadd2_rn(hx2, make_float2(-fxa, -fxb)), dxn2, ex2);
+      const float2 Y = __ffma2_rn(__fadd2_rn(hy2, make_float2(-fya, -fyb)), dyn2, ey2);
       const float2 X2 = __fmul2_rn(X, X), Y2 = __fmul2_rn(Y, Y), rh = __fadd2_rn(X2, Y2);
       const float2 ut = __fadd2_rn(make_float2(st.zs, st.zs), make_float2(A.y, B.y));
       const float2 rt2 = __ffma2_rn(ut, ut, rh);
@@ -304,9 +311,13 @@ __global__ void __launch_bounds__(IF_TS, 8)
       }
       ixa = ixb + 1;
       iya = iyb;
+      fxa = fxb + 1.f;
+      fya = fyb;
       if (ixa == k.nx) {
         ixa = 0;
         ++iya;
+        fxa = 0.f;
+        fya += 1.f;
       }
     }
     acc.add(g.x + g.y);
@@ -384,11 +395,14 @@ __global__ void __launch_bounds__(IF_TS, 8)
                   double* __restrict__ p_rho, double* __restrict__ p_dep) {
   __shared__ IStation s_f[IF_TILE + 2];
   __shared__ int2 s_i[IF_TILE + 2];
+  __shared__ float2 s_h[IF_TILE + 2];  // the home indices as floats (exact)
   const int c = blockIdx.x * IF_TS + threadIdx.x;
   const bool active = c < k.ncols;
   const int ix = active ? c % k.nx : 0, iy = active ? c / k.nx : 0;
   const float4 col = active ? cf[c] : make_float4(0.f, 0.f, 0.f, 0.f);
   const float2 cy2 = make_float2(col.y, col.y), cz2 = make_float2(col.z, col.z);
+  const float2 nix2 = make_float2(-(float)ix, -(float)ix), niy2 = make_float2(-(float)iy, -(float)iy);
+  const float2 dxn2 = make_float2(k.dxn, k.dxn), dyn2 = make_float2(k.dyn, k.dyn);
   // this block's slice of the stations (grid.y)
   const int s0 = blockIdx.y * chunk_len, s1 = min(ns, s0 + chunk_len);
   Kahan ar, ad;
@@ -398,7 +412,9 @@ __global__ void __launch_bounds__(IF_TS, 8)
       const bool ok = t0 + q < s1;
       IStation z = {0.f, 0.f, 0.f, 0.f};
       s_f[q] = ok ? sf[t0 + q] : z;
-      s_i[q] = ok ? si[t0 + q] : make_int2(0, 0);
+      const int2 h = ok ? si[t0 + q] : make_int2(0, 0);
+      s_i[q] = h;
+      s_h[q] = make_float2((float)h.x, (float)h.y);
     }
     __syncthreads();
     if (!active) continue;
@@ -408,10 +424,11 @@ __global__ void __launch_bounds__(IF_TS, 8)
       // stations q and q+1 (the second is dropped past the end of the tile)
       const IStation sa = s_f[q], sb = s_f[q + 1];
       const int2 ha = s_i[q], hb = s_i[q + 1];
-      const float2 X = make_float2(fmaf((float)(ha.x - ix), k.dxn, sa.ex),
-                                   fmaf((float)(hb.x - ix), k.dxn, sb.ex));
-      const float2 Y = make_float2(fmaf((float)(ha.y - iy), k.dyn, sa.ey),
-                                   fmaf((float)(hb.y - iy), k.dyn, sb.ey));
+      const float2 fa = s_h[q], fb = s_h[q + 1];
+      const float2 X = __ffma2_rn(__fadd2_rn(make_float2(fa.x, fb.x), nix2), dxn2,
+                                  make_float2(sa.ex, sb.ex));
+      const float2 Y = __ffma2_rn(__fadd2_rn(make_float2(fa.y, fb.y), niy2), dyn2,
+                                  make_float2(sa.ey, sb.ey));
       const float2 X2 = __fmul2_rn(X, X), Y2 = __fmul2_rn(Y, Y), rh = __fadd2_rn(X2, Y2);
       const float2 ut = __fadd2_rn(make_float2(sa.zs, sb.zs), cy2);
       const float2 rt2 = __ffma2_rn(ut, ut, rh);

@@ -230,13 +230,13 @@ struct FarStation {
 // MASK: drop the layers of the station's near region [elo, elo + espan] and
 // the padding layers >= nz (select, not multiply: a NaN there is dropped).
 template <bool T2, bool MASK>
-__device__ __forceinline__ float2 far_group(const float* col, int l0, const float2 (&Zb)[4],
-                                            float2 zstep, const ColPoly2& cp2, float2 c2t,
-                                            int elo, unsigned espan, int nz, float2 g) {
+__device__ __forceinline__ float2 far_group(const float* col, int l0, float fl,
+                                            const float2 (&Zb)[4], float2 zstep,
+                                            const ColPoly2& cp2, float2 c2t, int elo,
+                                            unsigned espan, int nz, float2 g) {
   const float4 ra = *reinterpret_cast<const float4*>(col + l0);
   const float4 rb = *reinterpret_cast<const float4*>(col + l0 + 4);
-  const float fl = (float)l0;
-  const float2 l2 = make_float2(fl, fl);
+  const float2 l2 = make_float2(fl, fl);  // fl = l0, carried in float (no conversion)
   float2 v[4];
 #pragma unroll
   for (int j = 0; j < 4; j++) {
@@ -267,21 +267,22 @@ __device__ __forceinline__ void far_column(const float* col, int lmask, int nz8,
                                            unsigned espan, Kahan& acc) {
   float2 g = make_float2(0.f, 0.f);
   int l0 = 0;
-  for (; l0 < lmask; l0 += 8) {
-    g = far_group<T2, true>(col, l0, Zb, zstep, cp2, c2t, elo, espan, nz, g);
+  float fl = 0.f;
+  for (; l0 < lmask; l0 += 8, fl += 8.f) {
+    g = far_group<T2, true>(col, l0, fl, Zb, zstep, cp2, c2t, elo, espan, nz, g);
     if (l0 & 8) {
       acc.add(g.x + g.y);
       g = make_float2(0.f, 0.f);
     }
   }
-  for (; l0 < nz8; l0 += 8) {
-    g = far_group<T2, false>(col, l0, Zb, zstep, cp2, c2t, elo, espan, nz, g);
+  for (; l0 < nz8; l0 += 8, fl += 8.f) {
+    g = far_group<T2, false>(col, l0, fl, Zb, zstep, cp2, c2t, elo, espan, nz, g);
     if (l0 & 8) {
       acc.add(g.x + g.y);
       g = make_float2(0.f, 0.f);
     }
   }
-  if (nz8 < nz) g = far_group<T2, true>(col, nz8, Zb, zstep, cp2, c2t, elo, espan, nz, g);
+  if (nz8 < nz) g = far_group<T2, true>(col, nz8, fl, Zb, zstep, cp2, c2t, elo, espan, nz, g);
   acc.add(g.x + g.y);
 }
 
