@@ -475,6 +475,14 @@ def run_workload(args, local_rank):
         what = ("32 line-search trials on the 256x256x64 mesh + 16 regional meshes, one "
                 "graph-captured persistent launch (model-pair evals)")
         step = lambda: ctx.batch(djobs)
+    elif args.workload == "pointmass":
+        mesh, rho, st = synth.config2()
+        g, drho, surf = pointmass_mapping(mesh, rho, st)
+        dd, dsf = d(drho), d(surf)
+        units = int(np.count_nonzero(np.abs(drho.astype(np.float32)) > 0.001)) * mesh.nx * mesh.ny
+        what = ("the reference's point-mass model (float) on the config-2 geometry, its grid: "
+                "every node a station (pairs of selected nodes x stations)")
+        step = lambda: ctx.pointmass(g, dd, dsf, precision="fp32")
     else:
         raise SystemExit("unknown workload " + args.workload)
     for _ in range(args.warmup):
@@ -502,7 +510,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quick", action="store_true", help="skip side measurements")
     ap.add_argument("--workload", default="forward",
-                    choices=["forward", "adjoint", "interface", "batch"],
+                    choices=["forward", "adjoint", "interface", "batch", "pointmass"],
                     help="forward (the headline) or another workload as the timed step")
     args = ap.parse_args()
     rank, local_rank, world = dist_env()
