@@ -325,10 +325,31 @@ __global__ void pm_finalize_kernel(PmParams p, int nchunks,
   G[m] = g;
 }
 
-void pm_shape(const PmParams& p, int num_sms, int* tiles, int* chunks, long long* clen) {
+// Resident blocks per SM of the gather kernel that a call runs (the float
+// path of the context entry points is the compacted-list kernel).
+int pm_occupancy(int precision, bool compacted) {
+  int occ = 0;
+  cudaError_t e;
+  if (precision == ZTM_PREC_FP64)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pm_gather_kernel<true>, PM_TS, 0);
+  else if (compacted)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pm_gather_f32_kernel, PM_TS, 0);
+  else
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pm_gather_kernel<false>, PM_TS, 0);
+  if (e != cudaSuccess || occ < 1) {
+    cudaGetLastError();
+    occ = 1;
+  }
+  return occ;
+}
+
+// Station tiles x node chunks: about four waves of resident blocks (occ per
+// SM), chunks of at least 1024 nodes.
+void pm_shape(const PmParams& p, int num_sms, int occ, int* tiles, int* chunks, long long* clen) {
   *tiles = (p.ns + PM_TS - 1) / PM_TS;
   if (*tiles < 1) *tiles = 1;
-  long long want = std::max(1LL, (long long)(8 * std::max(num_sms, 1)) / *tiles);
+  long long want =
+      std::max(1LL, (4LL * occ * std::max(num_sms, 1) + *tiles - 1) / *tiles);
   long long maxc = std::max(1LL, (p.nnodes + 1023) / 1024);
   long long ch = std::min(want, maxc);
   ch = std::min(ch, 65535LL);
@@ -346,7 +367,7 @@ void pm_shape(const PmParams& p, int num_sms, int* tiles, int* chunks, long long
 size_t ztm_pointmass_ws(const PmParams& p, int precision, int num_sms) {
   int tiles, chunks;
   long long len;
-  pm_shape(p, num_sms, &tiles, &chunks, &len);
+  pm_shape(p, num_sms, pm_occupancy(precision, true), &tiles, &chunks, &len);
   size_t w = WsCarver::need((size_t)chunks * std::max(p.ns, 1) * sizeof(double));
   if (precision != ZTM_PREC_FP64) {  // the float node list
     const long long nb = std::max(1LL, (p.nnodes + PM_NB - 1) / PM_NB);
@@ -361,7 +382,7 @@ int ztm_launch_pointmass(ztm_ctx* c, const PmParams& p, const double* d_drho,
                          double scale, int precision, WsCarver& wc) {
   int tiles, chunks;
   long long len;
-  pm_shape(p, c->num_sms, &tiles, &chunks, &len);
+  pm_shape(p, c->num_sms, pm_occupancy(precision, true), &tiles, &chunks, &len);
   double* partial = wc.take<double>((size_t)chunks * std::max(p.ns, 1));
   if (p.ns > 0 && p.nnodes > 0) {
     dim3 grid(tiles, chunks);
@@ -485,7 +506,7 @@ extern "C" int ztm_gfm_pointmass_noalloc(const ztm_grid* g, const double* drho,
 
   int tiles, chunks;
   long long len;
-  pm_shape(p, nsm, &tiles, &chunks, &len);
+  pm_shape(p, nsm, pm_occupancy(precision, false), &tiles, &chunks, &len);
   if (p.ns > 0 && (long long)chunks * p.ns > cap) {  // fewer, longer node chunks
     chunks = (int)std::max(1LL, cap / p.ns);
     len = (p.nnodes + chunks - 1) / chunks;

@@ -70,17 +70,6 @@ __device__ __forceinline__ float rsqrt_ftz(float x) {
   return y;
 }
 
-// Z/r^3 * (1 + t2 + t4) for one pair (unit density, normalised units).
-__device__ __forceinline__ float far_unit(float Z, const ColPoly& c, float a1) {
-  const float rinv = rsqrt_ftz(fmaf(Z, Z, c.rh));
-  const float u = rinv * rinv;
-  float p = fmaf(c.C4, u, c.C3);
-  p = fmaf(p, u, c.C2);
-  p = fmaf(p, u, a1);
-  const float s = fmaf(p, u, 1.f);
-  return (Z * s) * (rinv * u);
-}
-
 // Two layers at once on the packed FP32 path (Blackwell FFMA2/FMUL2: one
 // issue slot for two float FMAs with the same rounding as two FFMAs); the
 // two rsqrts stay scalar on the special-function unit.  Returns
