@@ -151,7 +151,7 @@ __device__ __forceinline__ bool near_bit(const uint32_t* __restrict__ mask, int 
 // One warp per station: the near bit of every window column, in double.
 __global__ void iface_near_mask(IConst k, int ns, const double* __restrict__ sxyz,
                                 const int2* __restrict__ si, const double* __restrict__ depth,
-                                uint32_t* __restrict__ mask) {
+                                uint32_t* __restrict__ mask, int* __restrict__ anynear) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int s = blockIdx.x * 4 + warp;
   if (s >= ns) return;
@@ -161,6 +161,7 @@ __global__ void iface_near_mask(IConst k, int ns, const double* __restrict__ sxy
   const int y0 = max(0, cy - k.w), y1 = min(k.ny - 1, cy + k.w);
   const int wx = x1 - x0 + 1, n = wx * (y1 - y0 + 1);
   const double zs = sxyz[3 * s + 2];
+  uint32_t any = 0u;
   for (int wd = 0; wd < k.words; wd++) {
     const int q = wd * 32 + lane;
     bool nb = false;
@@ -170,7 +171,9 @@ __global__ void iface_near_mask(IConst k, int ns, const double* __restrict__ sxy
     }
     const uint32_t bits = __ballot_sync(0xffffffffu, nb);
     if (lane == 0) mask[(size_t)s * k.words + wd] = bits;
+    any |= bits;
   }
+  if (lane == 0) anynear[s] = any != 0u;  // the station has a near column
 }
 
 // The unit face integral of the far expansion for two pairs, given 1/r of
@@ -239,19 +242,29 @@ __device__ __forceinline__ float2 col_unit2(float2 X2, float2 Y2, float2 rh, flo
 }
 
 // ---- forward, far (thread per station) ------------------------------------
+// Columns stream through shared memory in tiles, with their indices as
+// negated floats (exact) so that the offsets need no integer work.  The
+// near-window test runs only in warps where some station has a near column
+// (anynear, from the mask kernel): for stations well above the interface it
+// never runs.
 __global__ void __launch_bounds__(IF_TS, 8)
     iface_far_fwd(IConst k, int ns, const IStation* __restrict__ sf, const int2* __restrict__ si,
-                  const float4* __restrict__ cf, const uint32_t* __restrict__ mask, int chunk_len,
-                  double* __restrict__ partial) {
+                  const float4* __restrict__ cf, const uint32_t* __restrict__ mask,
+                  const int* __restrict__ anynear, int chunk_len, double* __restrict__ partial) {
   __shared__ float4 s_c[IF_TILE + 2];
+  __shared__ __align__(8) float s_nx[IF_TILE + 2];  // -ix of the tile's columns
+  __shared__ __align__(8) float s_ny[IF_TILE + 2];  // -iy
   const int s = blockIdx.x * IF_TS + threadIdx.x;
   const bool active = s < ns;
   IStation st = {0.f, 0.f, 0.f, 0.f};
   int2 hi = make_int2(0, 0);
+  bool mine_near = false;
   if (active) {
     st = sf[s];
     hi = si[s];
+    mine_near = anynear[s] != 0;
   }
+  const bool warp_near = __any_sync(0xffffffffu, mine_near);
   const int c0 = blockIdx.y * chunk_len, c1 = min(k.ncols, c0 + chunk_len);
   // this station's near window (clamped), for the per-column test
   const int wcx = clampi(hi.x, 0, k.nx - 1), wcy = clampi(hi.y, 0, k.ny - 1);
@@ -261,34 +274,31 @@ __global__ void __launch_bounds__(IF_TS, 8)
   const float2 hx2 = make_float2((float)hi.x, (float)hi.x), hy2 = make_float2((float)hi.y, (float)hi.y);
   const float2 dxn2 = make_float2(k.dxn, k.dxn), dyn2 = make_float2(k.dyn, k.dyn);
   const float2 ex2 = make_float2(st.ex, st.ex), ey2 = make_float2(st.ey, st.ey);
+  const float2 zs2 = make_float2(st.zs, st.zs);
   Kahan acc;
   for (int t0 = c0; t0 < c1; t0 += IF_TILE) {
     __syncthreads();
-    for (int q = threadIdx.x; q < IF_TILE + 2; q += IF_TS)
-      s_c[q] = (t0 + q < c1) ? cf[t0 + q] : make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int q = threadIdx.x; q < IF_TILE + 2; q += IF_TS) {
+      const int c = t0 + q;
+      const bool ok = c < c1;
+      s_c[q] = ok ? cf[c] : make_float4(0.f, 0.f, 0.f, 0.f);
+      // a padding column sits on the station column (finite values; dropped)
+      s_nx[q] = ok ? -(float)(c % k.nx) : -(float)hi.x;
+      s_ny[q] = ok ? -(float)(c / k.nx) : -(float)hi.y;
+    }
     __syncthreads();
     if (!active) continue;
     const int cnt = min(IF_TILE, c1 - t0);
     float2 g = make_float2(0.f, 0.f);  // plain sums over 16 columns, Kahan across
-    int ixa = t0 % k.nx, iya = t0 / k.nx;
-    // the column indices also carried as floats (exact integers): the offsets
-    // need no integer-to-float conversions
-    float fxa = (float)ixa, fya = (float)iya;
     for (int q = 0; q < cnt; q += 2) {
       // columns q and q+1 (the second is dropped past the end of the tile)
-      int ixb = ixa + 1, iyb = iya;
-      float fxb = fxa + 1.f, fyb = fya;
-      if (ixb == k.nx) {
-        ixb = 0;
-        ++iyb;
-        fxb = 0.f;
-        fyb += 1.f;
-      }
       const float4 A = s_c[q], B = s_c[q + 1];
-      const float2 X = __ffma2_rn(__fadd2_rn(hx2, make_float2(-fxa, -fxb)), dxn2, ex2);
-      const float2 Y = __ffma2_rn(__fadd2_rn(hy2, make_float2(-fya, -fyb)), dyn2, ey2);
+      const float2 nx2 = *reinterpret_cast<const float2*>(s_nx + q);
+      const float2 ny2 = *reinterpret_cast<const float2*>(s_ny + q);
+      const float2 X = __ffma2_rn(__fadd2_rn(hx2, nx2), dxn2, ex2);
+      const float2 Y = __ffma2_rn(__fadd2_rn(hy2, ny2), dyn2, ey2);
       const float2 X2 = __fmul2_rn(X, X), Y2 = __fmul2_rn(Y, Y), rh = __fadd2_rn(X2, Y2);
-      const float2 ut = __fadd2_rn(make_float2(st.zs, st.zs), make_float2(A.y, B.y));
+      const float2 ut = __fadd2_rn(zs2, make_float2(A.y, B.y));
       const float2 rt2 = __ffma2_rn(ut, ut, rh);
       const float2 th = make_float2(A.z, B.z);
       float2 itop;
@@ -297,27 +307,22 @@ __global__ void __launch_bounds__(IF_TS, 8)
                            ? col_unit2<true>(X2, Y2, rh, ut, rt2, th, k, &itop)
                            : col_unit2<false>(X2, Y2, rh, ut, rt2, th, k, &itop);
       float2 v = __fmul2_rn(make_float2(A.x, B.x), u);
-      // near columns (and the padding column) contribute through the double
-      // path or not at all: select, which also drops a NaN
-      if (ixa >= wx0 && ixa <= wx1 && iya >= wy0 && iya <= wy1 && near_bit(mask, s, ixa - wx0 + wbw * (iya - wy0), k))
-        v.x = 0.f;
-      if (q + 1 >= cnt || (ixb >= wx0 && ixb <= wx1 && iyb >= wy0 && iyb <= wy1 &&
-                           near_bit(mask, s, ixb - wx0 + wbw * (iyb - wy0), k)))
-        v.y = 0.f;
+      if (warp_near) {
+        // near columns contribute through the double path: select, which
+        // also drops a NaN
+        const int ixa = -(int)nx2.x, iya = -(int)ny2.x, ixb = -(int)nx2.y, iyb = -(int)ny2.y;
+        if (ixa >= wx0 && ixa <= wx1 && iya >= wy0 && iya <= wy1 &&
+            near_bit(mask, s, ixa - wx0 + wbw * (iya - wy0), k))
+          v.x = 0.f;
+        if (ixb >= wx0 && ixb <= wx1 && iyb >= wy0 && iyb <= wy1 &&
+            near_bit(mask, s, ixb - wx0 + wbw * (iyb - wy0), k))
+          v.y = 0.f;
+      }
+      if (q + 1 >= cnt) v.y = 0.f;  // the padding column
       g = __fadd2_rn(g, v);
       if ((q & 14) == 14) {
         acc.add(g.x + g.y);
         g = make_float2(0.f, 0.f);
-      }
-      ixa = ixb + 1;
-      iya = iyb;
-      fxa = fxb + 1.f;
-      fya = fyb;
-      if (ixa == k.nx) {
-        ixa = 0;
-        ++iya;
-        fxa = 0.f;
-        fya += 1.f;
       }
     }
     acc.add(g.x + g.y);
@@ -391,11 +396,19 @@ __global__ void __launch_bounds__(64)
 // ---- adjoint, far (thread per column) --------------------------------------
 __global__ void __launch_bounds__(IF_TS, 8)
     iface_far_adj(IConst k, int ns, const IStation* __restrict__ sf, const int2* __restrict__ si,
-                  const float4* __restrict__ cf, const uint32_t* __restrict__ mask, int chunk_len,
-                  double* __restrict__ p_rho, double* __restrict__ p_dep) {
-  __shared__ IStation s_f[IF_TILE + 2];
+                  const float4* __restrict__ cf, const uint32_t* __restrict__ mask,
+                  const int* __restrict__ anynear, int chunk_len, double* __restrict__ p_rho,
+                  double* __restrict__ p_dep) {
+  // the tile's stations, one array per field so that a station pair is one
+  // 8-byte load per field
+  __shared__ __align__(8) float s_ex[IF_TILE + 2];
+  __shared__ __align__(8) float s_ey[IF_TILE + 2];
+  __shared__ __align__(8) float s_zs[IF_TILE + 2];
+  __shared__ __align__(8) float s_r[IF_TILE + 2];
+  __shared__ __align__(8) float s_hx[IF_TILE + 2];  // home column indices as floats (exact)
+  __shared__ __align__(8) float s_hy[IF_TILE + 2];
   __shared__ int2 s_i[IF_TILE + 2];
-  __shared__ float2 s_h[IF_TILE + 2];  // the home indices as floats (exact)
+  __shared__ int s_nf[IF_TILE + 2];  // the station has a near column
   const int c = blockIdx.x * IF_TS + threadIdx.x;
   const bool active = c < k.ncols;
   const int ix = active ? c % k.nx : 0, iy = active ? c / k.nx : 0;
@@ -411,10 +424,16 @@ __global__ void __launch_bounds__(IF_TS, 8)
     for (int q = threadIdx.x; q < IF_TILE + 2; q += IF_TS) {
       const bool ok = t0 + q < s1;
       IStation z = {0.f, 0.f, 0.f, 0.f};
-      s_f[q] = ok ? sf[t0 + q] : z;
+      const IStation f = ok ? sf[t0 + q] : z;
       const int2 h = ok ? si[t0 + q] : make_int2(0, 0);
+      s_ex[q] = f.ex;
+      s_ey[q] = f.ey;
+      s_zs[q] = f.zs;
+      s_r[q] = f.r;
+      s_hx[q] = (float)h.x;
+      s_hy[q] = (float)h.y;
       s_i[q] = h;
-      s_h[q] = make_float2((float)h.x, (float)h.y);
+      s_nf[q] = ok ? anynear[t0 + q] : 0;
     }
     __syncthreads();
     if (!active) continue;
@@ -422,15 +441,14 @@ __global__ void __launch_bounds__(IF_TS, 8)
     float2 gr = make_float2(0.f, 0.f), gd = make_float2(0.f, 0.f);  // 16 stations, Kahan across
     for (int q = 0; q < cnt; q += 2) {
       // stations q and q+1 (the second is dropped past the end of the tile)
-      const IStation sa = s_f[q], sb = s_f[q + 1];
-      const int2 ha = s_i[q], hb = s_i[q + 1];
-      const float2 fa = s_h[q], fb = s_h[q + 1];
-      const float2 X = __ffma2_rn(__fadd2_rn(make_float2(fa.x, fb.x), nix2), dxn2,
-                                  make_float2(sa.ex, sb.ex));
-      const float2 Y = __ffma2_rn(__fadd2_rn(make_float2(fa.y, fb.y), niy2), dyn2,
-                                  make_float2(sa.ey, sb.ey));
+      const float2 hx = *reinterpret_cast<const float2*>(s_hx + q);
+      const float2 hy = *reinterpret_cast<const float2*>(s_hy + q);
+      const float2 X = __ffma2_rn(__fadd2_rn(hx, nix2), dxn2,
+                                  *reinterpret_cast<const float2*>(s_ex + q));
+      const float2 Y = __ffma2_rn(__fadd2_rn(hy, niy2), dyn2,
+                                  *reinterpret_cast<const float2*>(s_ey + q));
       const float2 X2 = __fmul2_rn(X, X), Y2 = __fmul2_rn(Y, Y), rh = __fadd2_rn(X2, Y2);
-      const float2 ut = __fadd2_rn(make_float2(sa.zs, sb.zs), cy2);
+      const float2 ut = __fadd2_rn(*reinterpret_cast<const float2*>(s_zs + q), cy2);
       const float2 rt2 = __ffma2_rn(ut, ut, rh);
       float2 itop, u, f;
       // second order when every lane's pairs are far enough (warp-uniform)
@@ -441,12 +459,16 @@ __global__ void __launch_bounds__(IF_TS, 8)
         u = col_unit2<false>(X2, Y2, rh, ut, rt2, cz2, k, &itop);
         f = face_unit_far2<false>(X2, Y2, ut, itop, k.face);
       }
-      const float2 r = make_float2(sa.r, sb.r);
+      const float2 r = *reinterpret_cast<const float2*>(s_r + q);
       float2 vr = __fmul2_rn(r, u), vd = __fmul2_rn(r, f);
-      // near pairs (and the padding station) go through the double path or
-      // nowhere: select, which also drops a NaN
-      if (is_near(mask, t0 + q, ha.x, ha.y, ix, iy, k)) vr.x = vd.x = 0.f;
-      if (q + 1 >= cnt || is_near(mask, t0 + q + 1, hb.x, hb.y, ix, iy, k)) vr.y = vd.y = 0.f;
+      // near pairs go through the double path: select, which also drops a
+      // NaN.  Every lane has the same stations, so the test is uniform.
+      if (s_nf[q] | s_nf[q + 1]) {
+        const int2 ha = s_i[q], hb = s_i[q + 1];
+        if (is_near(mask, t0 + q, ha.x, ha.y, ix, iy, k)) vr.x = vd.x = 0.f;
+        if (q + 1 < cnt && is_near(mask, t0 + q + 1, hb.x, hb.y, ix, iy, k)) vr.y = vd.y = 0.f;
+      }
+      if (q + 1 >= cnt) vr.y = vd.y = 0.f;  // the padding station
       gr = __fadd2_rn(gr, vr);
       gd = __fadd2_rn(gd, vd);
       if ((q & 14) == 14) {
@@ -621,6 +643,8 @@ size_t ztm_iface_ws(const IMeshDesc& m, int ns, int precision, int num_sms) {
        WsCarver::need((size_t)std::max(ns, 1) * 8) * 4;
   // near masks (forward and adjoint), up to near_q = 16
   w += 2 * WsCarver::need((size_t)std::max(ns, 1) * 4 * 64);
+  // per-station "has a near column" flags (forward and adjoint)
+  w += 2 * WsCarver::need((size_t)std::max(ns, 1) * 4);
   (void)precision;
   return w;
 }
@@ -655,7 +679,8 @@ static int iface_forward_impl(ztm_ctx* c, const IMeshDesc& m, const double* d_de
                                                               si);
   iface_col_prep<<<(unsigned)((nc + 255) / 256), 256, 0, c->stream>>>(m, k.L0, d_depth, d_rho, cf);
   uint32_t* mask = wc.take<uint32_t>((size_t)ns * k.words);
-  iface_near_mask<<<(ns + 3) / 4, 128, 0, c->stream>>>(k, ns, d_sxyz, si, d_depth, mask);
+  int* anynear = wc.take<int>((size_t)ns);
+  iface_near_mask<<<(ns + 3) / 4, 128, 0, c->stream>>>(k, ns, d_sxyz, si, d_depth, mask, anynear);
   // double near columns on the side stream, concurrently with the float far field
   ztm_fork(c);
   {
@@ -668,7 +693,8 @@ static int iface_forward_impl(ztm_ctx* c, const IMeshDesc& m, const double* d_de
   double* partial = wc.take<double>((size_t)ch * ns);
   {
     ZtmProf prof_(c, "iface_far");
-    iface_far_fwd<<<dim3(tiles, ch), IF_TS, 0, c->stream>>>(k, ns, sf, si, cf, mask, len, partial);
+    iface_far_fwd<<<dim3(tiles, ch), IF_TS, 0, c->stream>>>(k, ns, sf, si, cf, mask, anynear, len,
+                                                            partial);
   }
   ztm_join(c);
   iface_finalize<<<(ns + 255) / 256, 256, 0, c->stream>>>(ns, ch, partial,
@@ -722,7 +748,8 @@ int ztm_launch_iface_adj(ztm_ctx* c, const IMeshDesc& m, const double* d_depth,
   const double sc_rho = G5 * k.L0 * (double)k.dxn * k.dyn;
   const double sc_dep = G5 * (double)k.dxn * k.dyn;
   uint32_t* mask = wc.take<uint32_t>((size_t)ns * k.words);
-  iface_near_mask<<<(ns + 3) / 4, 128, 0, c->stream>>>(k, ns, d_sxyz, si, d_depth, mask);
+  int* anynear = wc.take<int>((size_t)ns);
+  iface_near_mask<<<(ns + 3) / 4, 128, 0, c->stream>>>(k, ns, d_sxyz, si, d_depth, mask, anynear);
   int alen;
   const int ach = iface_adj_chunks(ns, nc, c->num_sms, &alen);
   double* p_rho = wc.take<double>((size_t)ach * nc);
@@ -730,7 +757,7 @@ int ztm_launch_iface_adj(ztm_ctx* c, const IMeshDesc& m, const double* d_depth,
   {
     ZtmProf prof_(c, "iface_far");
     iface_far_adj<<<dim3((unsigned)((nc + IF_TS - 1) / IF_TS), ach), IF_TS, 0, c->stream>>>(
-        k, ns, sf, si, cf, mask, alen, p_rho, p_dep);
+        k, ns, sf, si, cf, mask, anynear, alen, p_rho, p_dep);
   }
   iface_far_adj_finalize<<<(unsigned)((nc + 255) / 256), 256, 0, c->stream>>>(
       nc, ach, p_rho, p_dep, sc_rho, sc_dep, d_grho, d_gdep);
