@@ -95,7 +95,7 @@ class ClockSampler:
 
 def read_traffic():
     """DRAM bytes per far-kernel launch from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "prism_far_config2.md")
+    p = os.path.join(ROOT, "profiles", "prism_far_256x256x64_draped.md")
     if not os.path.exists(p):
         return None
     for line in open(p):
@@ -151,7 +151,7 @@ def run_reference(args, rank):
     import numpy as np
     import oracle
     from ztm_gb300 import synth
-    mesh, rho, st = synth.config2()
+    mesh, rho, st = synth.draped_mesh_256x256x64()
     g, drho, surf = pointmass_mapping(mesh, rho, st)
     ns_sample = int(os.environ.get("ZTM_REF_SAMPLE", "128"))
     nn = np.nonzero(np.abs(drho) > g.threshold)[0].astype(np.int32)
@@ -200,7 +200,7 @@ def run_ours(args, rank, local_rank, world):
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     ctx = ztm_gb300.GravityContext(local_rank)
     stream = torch.cuda.ExternalStream(ctx.stream)
-    mesh, rho, st = synth.config2()
+    mesh, rho, st = synth.draped_mesh_256x256x64()
     np_ = mesh.nx * mesh.ny * mesh.nz
     pairs = np_ * len(st)
     d_rho = torch.tensor(rho, device="cuda")
@@ -387,13 +387,14 @@ def _timed(ctx, fn, reps=1):
 
 
 def other_configs(ctx):
-    """The other BASELINE workloads, once each (not the headline)."""
+    """The other workloads (interface adjoint, line-search batch, interface
+    inversion), once each (not the headline)."""
     import numpy as np
     import torch
     from ztm_gb300 import synth
     res = {}
     # adjoint workload: 256x256 interface columns, 128x128 stations
-    im, depth, rho, st, start = synth.config3()
+    im, depth, rho, st, start = synth.moho_columns()
     rng = np.random.default_rng(3)
     d = lambda a: torch.tensor(a, device="cuda")
     dd, dr, ds, d0 = d(depth), d(rho), d(st), d(start)
@@ -412,7 +413,7 @@ def other_configs(ctx):
                             "gz": err(out_m[1], out_d[1]), "g_rho": err(out_m[2], out_d[2]),
                             "g_depth": err(out_m[3], out_d[3])}}
     # batched workload: 32 line-search trials + 16 uneven regional meshes
-    jobs, alphas = synth.config4()
+    jobs, alphas = synth.line_search_batch()
     djobs = [(m_, d(r_.reshape(r_.shape[0], -1) if r_.ndim == 2 else r_), d(s_)) for m_, r_, s_ in jobs]
     ctx.batch(djobs)  # builds and caches the graph
     ctx.sync()
@@ -425,7 +426,7 @@ def other_configs(ctx):
         "launches_per_call": "1 graph: 2 prep kernels per job + 1 persistent kernel",
         "rel_err_trial5_vs_single_call": err(outs[0][5], one)}
     # inversion workload: 512x512 columns, 256x256 stations, 20 L-BFGS iterations
-    im5, dep5, rho5, st5, start5 = synth.config5()
+    im5, dep5, rho5, st5, start5 = synth.moho_columns_512()
     data5 = ctx.interface(im5, d(dep5), d(rho5), d(st5), precision="mixed")
     ctx.sync()
     data5 = data5.cpu().numpy() + np.random.default_rng(5).normal(0, 0.05, len(st5))
@@ -453,14 +454,14 @@ def run_workload(args, local_rank):
     stream = torch.cuda.ExternalStream(ctx.stream)
     d = lambda a: torch.tensor(np.ascontiguousarray(a), device="cuda")
     if args.workload == "adjoint":
-        mesh, rho, st = synth.config2()
+        mesh, rho, st = synth.draped_mesh_256x256x64()
         ds = d(st)
         res = d(np.random.default_rng(0).normal(0, 1, len(st)))
         units = mesh.nx * mesh.ny * mesh.nz * len(st)
         what = "d misfit/d rho of the 256x256x64 mesh at 128x128 stations (gradient evals)"
         step = lambda: ctx.adjoint(mesh, ds, res, precision="mixed")
     elif args.workload == "interface":
-        im, depth, rho, st, start = synth.config3()
+        im, depth, rho, st, start = synth.moho_columns()
         dd, dr, dst, d0 = d(depth), d(rho), d(st), d(start)
         data = ctx.interface(im, dd, dr, dst, precision="fp64")
         ctx.sync()
@@ -469,18 +470,18 @@ def run_workload(args, local_rank):
                 "128x128 stations (gz evals + gradient evals)")
         step = lambda: ctx.interface_misfit(im, d0, dr, dst, data, precision="mixed")
     elif args.workload == "batch":
-        jobs, _ = synth.config4()
+        jobs, _ = synth.line_search_batch()
         djobs = [(m_, d(r_), d(s_)) for m_, r_, s_ in jobs]
         units = sum(int(r_.shape[0]) * m_.nx * m_.ny * m_.nz * len(s_) for m_, r_, s_ in jobs)
         what = ("32 line-search trials on the 256x256x64 mesh + 16 regional meshes, one "
                 "graph-captured persistent launch (model-pair evals)")
         step = lambda: ctx.batch(djobs)
     elif args.workload == "pointmass":
-        mesh, rho, st = synth.config2()
+        mesh, rho, st = synth.draped_mesh_256x256x64()
         g, drho, surf = pointmass_mapping(mesh, rho, st)
         dd, dsf = d(drho), d(surf)
         units = int(np.count_nonzero(np.abs(drho.astype(np.float32)) > 0.001)) * mesh.nx * mesh.ny
-        what = ("the reference's point-mass model (float) on the config-2 geometry, its grid: "
+        what = ("the reference's point-mass model (float) on the 256x256x64 draped-mesh geometry, its grid: "
                 "every node a station (pairs of selected nodes x stations)")
         step = lambda: ctx.pointmass(g, dd, dsf, precision="fp32")
     else:

@@ -93,11 +93,11 @@ def test_interface_misfit_gradient_vs_central_differences(ctx):
     assert rel_err(gd_m, gd) <= 1e-6 * (1 + amp) and rel_err(gr_m, gr) <= 1e-6 * (1 + amp)
 
 
-def test_config3_gradients_mixed_vs_fp64(ctx):
+def test_moho_256_gradients_mixed_vs_fp64(ctx):
     """Config 3 (256x256 columns, 128x128 stations): mixed vs double
     gradients and the misfit, full size."""
     from ztm_gb300 import synth
-    im, depth, rho, st, start = synth.config3()
+    im, depth, rho, st, start = synth.moho_columns()
     rng = np.random.default_rng(3)
     data = ctx.interface(im, depth, rho, st, precision="fp64") + rng.normal(0, 0.05, len(st))
     m64 = ctx.interface_misfit(im, start, rho, st, data, precision="fp64")

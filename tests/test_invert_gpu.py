@@ -9,7 +9,7 @@ pytestmark = pytest.mark.gpu
 
 
 def test_inversion_mixed_matches_fp64_run(ctx):
-    im, depth_true, rho, st, start = synth.config3(seed=5, n=64, ns_side=32, cell=1000.0)
+    im, depth_true, rho, st, start = synth.moho_columns(seed=5, n=64, ns_side=32, cell=1000.0)
     rng = np.random.default_rng(5)
     data = ctx.interface(im, depth_true, rho, st, precision="fp64") + rng.normal(0, 0.05, len(st))
     d64, h64, n64 = ctx.invert_interface(im, start, rho, st, data, lam=1e-2, iterations=20,

@@ -109,10 +109,10 @@ def test_linearity_in_density(ctx):
     assert rel_err(c, 2.0 * a - 0.5 * b) <= 1e-7
 
 
-def test_config2_mixed_vs_fp64_subset(ctx):
-    """Full-size config-2 mesh (256x256x64); the double kernel on a subset."""
+def test_draped_mesh_256_mixed_vs_fp64_subset(ctx):
+    """The full 256x256x64 draped mesh; the double kernel on a station subset."""
     from ztm_gb300 import synth
-    mesh, rho, st = synth.config2()
+    mesh, rho, st = synth.draped_mesh_256x256x64()
     sub = st[np.random.default_rng(0).choice(len(st), 48, replace=False)]
     ref = ctx.prism(mesh, rho, sub, precision="fp64")
     out = ctx.prism(mesh, rho, sub, precision="mixed")
@@ -134,12 +134,12 @@ def test_autotuned_shape_gives_the_same_field(ctx):
     assert rel_err(a, ref) <= 1e-7  # only the summation grouping differs
 
 
-def test_config1_full_size_vs_oracle(ctx):
+def test_plain_mesh_64_full_size_vs_oracle(ctx):
     """Config 1 (64x64x32 prisms of 2x2x1 km, 32x32 stations at +100 m):
     the plain double kernel and the mixed kernel against the CPU oracle on
     every station."""
     from ztm_gb300 import synth
-    mesh, rho, st = synth.config1()
+    mesh, rho, st = synth.plain_mesh_64x64x32()
     ref = oracle.prism_mesh(mesh, rho, st)
     assert rel_err(ctx.prism(mesh, rho, st, precision="fp64"), ref) <= TOL64
     assert rel_err(ctx.prism(mesh, rho, st, precision="mixed"), ref) <= TOLMIX

@@ -48,7 +48,7 @@ def _layer_major(field_xyz):
     return np.ascontiguousarray(np.transpose(field_xyz, (2, 1, 0))).reshape(-1)
 
 
-def config1(seed=1):
+def plain_mesh_64x64x32(seed=1):
     """64x64x32 prisms of 2x2x1 km, top at z=0; density: Gaussian field,
     sigma 150 kg/m^3, correlation 8 km; 32x32 stations on a 4 km grid at
     z=+100 m, over the centres of the even columns."""
@@ -62,7 +62,7 @@ def config1(seed=1):
     return mesh, rho, st
 
 
-def config2(seed=2, n_boxes=20):
+def draped_mesh_256x256x64(seed=2, n_boxes=20):
     """256x256x64 prisms of 1x1x0.5 km, top at z=0; density: Gaussian field
     (correlation 5 km) scaled to max |rho| = 300 kg/m^3, plus 20 random box
     anomalies of +-300 kg/m^3; 128x128 stations over the even columns, draped
@@ -89,7 +89,7 @@ def config2(seed=2, n_boxes=20):
     return mesh, rho, st
 
 
-def config3(seed=3, n=256, ns_side=128, cell=1000.0, z_base=-45000.0, contrast=-400.0,
+def moho_columns(seed=3, n=256, ns_side=128, cell=1000.0, z_base=-45000.0, contrast=-400.0,
             noise_mgal=0.05):
     """Interface columns: n x n cells, bases at 45 km, tops on a smooth
     Moho-like surface between 20 and 45 km depth (Gaussian field, correlation
@@ -110,12 +110,12 @@ def config3(seed=3, n=256, ns_side=128, cell=1000.0, z_base=-45000.0, contrast=-
     return im, depth, rho, st, start
 
 
-def config4(seed=4, n_trials=32, n_regional=16):
+def line_search_batch(seed=4, n_trials=32, n_regional=16):
     """Batched workload: 32 line-search trials m + alpha*p (alpha in [0,2])
-    on the 256x256x64 mesh of config 2, and 16 regional meshes of uneven size
+    on the 256x256x64 draped mesh, and 16 regional meshes of uneven size
     (64^3 up to 192x192x48 prisms, 32^2 to 128^2 stations)."""
     rng = np.random.default_rng(seed)
-    mesh, rho, st = config2()
+    mesh, rho, st = draped_mesh_256x256x64()
     p = _layer_major(gaussian_field((256, 256, 64), (1000.0, 1000.0, 500.0), 10000.0, rng) * 30.0)
     alphas = np.linspace(0.0, 2.0, n_trials)
     trials = rho[None, :] + alphas[:, None] * p[None, :]
@@ -138,6 +138,6 @@ def config4(seed=4, n_trials=32, n_regional=16):
     return jobs, alphas
 
 
-def config5(seed=5):
+def moho_columns_512(seed=5):
     """Interface inversion: 512x512 columns of 0.5 km, 256x256 stations."""
-    return config3(seed=seed, n=512, ns_side=256, cell=500.0)
+    return moho_columns(seed=seed, n=512, ns_side=256, cell=500.0)
