@@ -305,7 +305,7 @@ __device__ __forceinline__ void far_stage(const FarArgs& a, const MeshConst& k, 
   for (int q = 0; q < ncol; q++) {
     const float X = fmaf((float)(t.ixs - ix), k.dxn, t.ex);
     const float Y = fmaf((float)(t.iys - iy), k.dyn, t.ey);
-    const ColPoly cp = col_poly(X, Y, fc);
+    const float X2 = X * X, Y2 = Y * Y, rh = X2 + Y2;
     const bool ncl = ix >= t.nb.x0 && ix <= t.nb.x1 && iy >= t.nb.y0 && iy <= t.nb.y1;
     int elo = k.nz;
     unsigned espan = 0u;
@@ -317,16 +317,24 @@ __device__ __forceinline__ void far_stage(const FarArgs& a, const MeshConst& k, 
       }
     }
     const float* col = rs + q * k.nzp;
-    const ColPoly2 cp2 = col_poly2(cp, fc.a1);
     // a column lies in some lane's near box only near the warp's stations:
     // test that once per column for the whole warp
     const int lmask = __any_sync(0xffffffffu, ncl) ? lm8 : 0;
-    const float2 c2t = make_float2(cp.C2 - fc.h2, cp.C2 - fc.h2);
-    // every lane of the warp far enough for the second-order form
-    if (__all_sync(0xffffffffu, cp.rh >= k.rh_t2))
-      far_column<true>(col, lmask, nz8, k.nz, Zb, zstep, cp2, c2t, elo, espan, acc);
-    else
-      far_column<false>(col, lmask, nz8, k.nz, Zb, zstep, cp2, c2t, elo, espan, acc);
+    // every lane of the warp far enough for the second-order form, which
+    // needs only C2t = a0 - a1 rh of the column polynomial
+    if (__all_sync(0xffffffffu, rh >= k.rh_t2)) {
+      const float c2t = fmaf(-fc.a1, rh, fmaf(X2, fc.cA, Y2 * fc.cB));
+      ColPoly2 cp2;
+      cp2.rh = make_float2(rh, rh);
+      cp2.a1 = make_float2(fc.a1, fc.a1);
+      cp2.C2 = cp2.C3 = cp2.C4 = make_float2(0.f, 0.f);  // unused by the form
+      far_column<true>(col, lmask, nz8, k.nz, Zb, zstep, cp2, make_float2(c2t, c2t), elo, espan,
+                       acc);
+    } else {
+      const ColPoly2 cp2 = col_poly2(col_poly(X, Y, fc), fc.a1);
+      far_column<false>(col, lmask, nz8, k.nz, Zb, zstep, cp2, make_float2(0.f, 0.f), elo, espan,
+                        acc);
+    }
     if (++ix == k.nx) {
       ix = 0;
       ++iy;
