@@ -241,7 +241,7 @@ int ztm_ctx_create(int device, ztm_ctx** out) {
           cudaSuccess ||
       cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
       // the side stream carries the short double near-field kernels that run
-      // beside a persistent far-field grid: give it the highest priority so
+      // beside the float far-field kernels: give it the highest priority so
       // its blocks are placed first whenever a slot frees up
       cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio) != cudaSuccess ||
       cudaStreamCreateWithPriority(&c->aux, cudaStreamNonBlocking, hi_prio) != cudaSuccess ||
