@@ -182,8 +182,9 @@ def run_reference(args, rank):
 def config_dict(n):
     return {"workload": WORKLOAD, "prisms": [256, 256, 64], "cell_m": [1000, 1000, 500],
             "stations": [128, 128], "pairs_per_step": 256 * 256 * 64 * 128 * 128,
-            "precision": "mixed: far pairs float (4th-order expansion, Kahan), near box and "
-                         "per-station sums double", "near_q": 6,
+            "precision": "mixed: far pairs float (4th-order expansion, second order beyond 48 "
+                         "half-diagonals, compensated sums), near region and per-station sums "
+                         "double", "near_q": 6,
             "l2": "flushed between timed steps (256 MiB write)",
             "parallelism": "replica per GPU" if n > 1 else "single GPU"}
 
@@ -301,7 +302,7 @@ def run_ours(args, rank, local_rank, world):
         line.update(extras(ctx, mesh, rho, st, d_rho, d_st, gz))
         if world == 1:
             line["cpu_baseline"] = cpu_baseline_prism(mesh, rho, st)
-            line["other_configs"] = other_configs(ctx)
+            line["other_workloads"] = other_workloads(ctx)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -386,7 +387,7 @@ def _timed(ctx, fn, reps=1):
     return e0.elapsed_time(e1) / reps, out
 
 
-def other_configs(ctx):
+def other_workloads(ctx):
     """The other workloads (interface adjoint, line-search batch, interface
     inversion), once each (not the headline)."""
     import numpy as np
