@@ -52,10 +52,12 @@ enum {
 /* ---- flags ----------------------------------------------------------- */
 enum {
   ZTM_FLAG_DEVICE_PTRS = 1, /* all array arguments are device pointers */
-  ZTM_FLAG_AUTOTUNE = 2     /* prism forward: on the first call for a mesh
-                               shape and station count, time the candidate
-                               launch shapes (blocks per SM x columns per
-                               stage) and keep the fastest on the context */
+  ZTM_FLAG_AUTOTUNE = 2     /* prism forward and batch: on the first call
+                               for these shapes (mesh and station counts;
+                               for a batch, every job's), time the candidate
+                               launch shapes (forward: columns per stage x
+                               items per block; batch: stage size x pairs
+                               per item) and keep the fastest on the context */
 };
 
 typedef struct ztm_ctx ztm_ctx;

@@ -43,3 +43,19 @@ def test_batch_line_search_trials(ctx):
     gp = ctx.prism(mesh, p, st, precision="fp64")
     for k, a in enumerate(alphas):
         assert rel_err(out[k], g0 + a * gp) <= 1e-6
+
+
+def test_batch_autotuned_shape_gives_the_same_field(ctx):
+    """With the autotuner the shape is measured on the first call and cached;
+    every shape computes the same sums (grouping of float partials aside)."""
+    rng = np.random.default_rng(2)
+    mesh, rho = small_mesh(40, 36, 16, seed=9)
+    models = np.stack([rho * (1 + 0.05 * k) for k in range(10)])
+    st = np.stack([rng.uniform(mesh.x0, mesh.x0 + 40e3, 90),
+                   rng.uniform(mesh.y0, mesh.y0 + 28.8e3, 90),
+                   rng.uniform(mesh.z_top + 10.0, mesh.z_top + 2500.0, 90)], 1)
+    ref = ctx.batch([(mesh, models, st)])[0]
+    tuned = ctx.batch([(mesh, models, st)], autotune=True)[0]
+    again = ctx.batch([(mesh, models, st)], autotune=True)[0]
+    assert rel_err(tuned, ref) <= 1e-6
+    assert np.array_equal(tuned, again)

@@ -368,7 +368,7 @@ struct Plan {
 };
 
 // Shapes only (no pointers): per-job tiles, chunks, stage widths, workspace.
-Plan plan(const ztm_job* jobs, int njobs, double near_q, int num_sms) {
+Plan plan(const ztm_job* jobs, int njobs, double near_q, int num_sms, int stage_kb, int tlog2) {
   Plan p;
   size_t ws = 0;
   for (int j = 0; j < njobs; j++) {
@@ -385,13 +385,13 @@ Plan plan(const ztm_job* jobs, int njobs, double near_q, int num_sms) {
     J.tiles = std::max(1, (q.ns + B_TS - 1) / B_TS);
     J.mgw = q.nmodels > 1 ? B_MG : 1;
     J.mgroups = (q.nmodels + J.mgw - 1) / J.mgw;
-    int sc = std::max(1, (16 * 1024) / (J.k.nzp * 4 * J.mgw));
+    int sc = std::max(1, (stage_kb * 1024) / (J.k.nzp * 4 * J.mgw));
     sc = std::min(sc, 32);
     J.sc = sc;
-    // aim for ~16 items per SM over the whole batch: split columns so that a
-    // far item holds roughly 2^22 pair-model evaluations at least
+    // split columns so that a far item holds about 2^tlog2 (station, prism)
+    // pairs (each applied to up to 8 models)
     long long pairs_tile = (long long)B_TS * J.k.ncols * m.nz;
-    long long target = 1LL << 24;
+    long long target = 1LL << tlog2;
     int chunks = (int)std::max(1LL, std::min<long long>(pairs_tile / target, J.k.ncols / sc));
     chunks = std::max(chunks, 1);
     int cc = (J.k.ncols + chunks - 1) / chunks;
@@ -433,6 +433,14 @@ void destroy_entry(ZtmGraphEntry& e) {
   e.graph = nullptr;
 }
 
+// Launch shapes the autotuner tries: {stage KB per model group, log2 of the
+// pairs per far item}.  The first is the default.
+constexpr int BATCH_SHAPES[][2] = {{16, 24}, {8, 24}, {32, 24}, {16, 23}, {16, 25},
+                                   {8, 23}, {32, 25}};
+
+int batch_run(ztm_ctx* c, const ztm_job* jobs, int njobs, bool dev, double G, double nq,
+              int stage_kb, int tlog2);
+
 }  // namespace
 
 extern "C" int ztm_gfm_batch(ztm_ctx* c, const ztm_job* jobs, int njobs, const ztm_opts* o) {
@@ -441,9 +449,11 @@ extern "C" int ztm_gfm_batch(ztm_ctx* c, const ztm_job* jobs, int njobs, const z
   if (njobs < 0 || (njobs > 0 && !jobs)) return ztm_fail(c, ZTM_ERR_ARG, "bad job list");
   if (njobs == 0) return ZTM_OK;
   if (njobs > 4096) return ztm_fail(c, ZTM_ERR_RANGE, "more than 4096 jobs");
-  if (o && (o->precision != ZTM_PREC_MIXED || (o->flags & ~ZTM_FLAG_DEVICE_PTRS)))
+  if (o && (o->precision != ZTM_PREC_MIXED ||
+            (o->flags & ~(ZTM_FLAG_DEVICE_PTRS | ZTM_FLAG_AUTOTUNE))))
     return ztm_fail(c, ZTM_ERR_ARG, "batched launches run the mixed method only");
   const bool dev = o && (o->flags & ZTM_FLAG_DEVICE_PTRS);
+  const bool tune = o && (o->flags & ZTM_FLAG_AUTOTUNE);
   const double G = (o && o->G > 0) ? o->G : 6.67e-11;
   const double nq = (o && o->near_q > 0) ? o->near_q : 6.0;
   for (int j = 0; j < njobs; j++) {
@@ -464,8 +474,48 @@ extern "C" int ztm_gfm_batch(ztm_ctx* c, const ztm_job* jobs, int njobs, const z
       if (p >= 0 && p != d) cudaSetDevice(p);
     }
   } restore{prev, c->device};
+  // the shape: cached for these job shapes, else measured (with
+  // ZTM_FLAG_AUTOTUNE: each candidate runs the whole batch once, the fastest
+  // is kept on the context), else the default
+  std::vector<long long> tkey = {2, njobs, (long long)(nq * 1e6)};
+  for (int j = 0; j < njobs; j++)
+    tkey.insert(tkey.end(), {jobs[j].mesh.nx, jobs[j].mesh.ny, jobs[j].mesh.nz,
+                             jobs[j].nmodels, jobs[j].ns});
+  auto it = c->tuned.find(tkey);
+  int stage_kb = BATCH_SHAPES[0][0], tlog2 = BATCH_SHAPES[0][1];
+  if (it != c->tuned.end()) {
+    stage_kb = it->second[0];
+    tlog2 = it->second[1];
+  } else if (tune) {
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    for (const auto& sh : BATCH_SHAPES) {
+      cudaEventRecord(e0, c->stream);
+      const int rc = batch_run(c, jobs, njobs, dev, G, nq, sh[0], sh[1]);
+      cudaEventRecord(e1, c->stream);
+      float ms = 0.f;
+      if (rc == ZTM_OK && cudaEventSynchronize(e1) == cudaSuccess &&
+          cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess && ms < best) {
+        best = ms;
+        stage_kb = sh[0];
+        tlog2 = sh[1];
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    c->err.clear();  // a candidate that did not fit is not the call's error
+    c->tuned[tkey] = {stage_kb, tlog2};
+  }
+  return batch_run(c, jobs, njobs, dev, G, nq, stage_kb, tlog2);
+}
 
-  Plan p = plan(jobs, njobs, nq, c->num_sms);
+namespace {
+
+int batch_run(ztm_ctx* c, const ztm_job* jobs, int njobs, bool dev, double G, double nq,
+              int stage_kb, int tlog2) {
+  Plan p = plan(jobs, njobs, nq, c->num_sms, stage_kb, tlog2);
   if (p.smem > 200 * 1024) return ztm_fail(c, ZTM_ERR_RANGE, "near box too large for a batch");
   size_t stage_bytes = 0;
   if (!dev)
@@ -533,6 +583,8 @@ extern "C" int ztm_gfm_batch(ztm_ctx* c, const ztm_job* jobs, int njobs, const z
   key.push_back((long long)(size_t)c->ws);
   key.push_back((long long)(size_t)c->stream);
   key.push_back((long long)(nq * 1e6));
+  key.push_back(stage_kb);
+  key.push_back(tlog2);
   for (int j = 0; j < njobs; j++) {
     const ztm_job& q = jobs[j];
     key.insert(key.end(), {q.mesh.nx, q.mesh.ny, q.mesh.nz, (long long)(q.mesh.dx * 1e3),
@@ -620,3 +672,5 @@ extern "C" int ztm_gfm_batch(ztm_ctx* c, const ztm_job* jobs, int njobs, const z
   if ((rc = ztm_cuda_check(c, cudaStreamSynchronize(c->stream), "batch"))) return rc;
   return ztm_check_device_error(c);
 }
+
+}  // namespace

@@ -383,9 +383,11 @@ class GravityContext:
         return depth, hist[:done.value + 1], done.value
 
     # -- batched ----------------------------------------------------------
-    def batch(self, jobs, precision="mixed", G=None, near_q=None):
+    def batch(self, jobs, precision="mixed", G=None, near_q=None, autotune=False):
         """jobs: list of (mesh, rho[nmodels, nprisms], stations[ns, 3]).
-        Returns a list of gz arrays [nmodels, ns]."""
+        Returns a list of gz arrays [nmodels, ns].  autotune: the first call
+        for these job shapes times the candidate launch shapes and keeps the
+        fastest on the context."""
         a = _Args(self)
         arr = (_lib.Job * len(jobs))()
         outs = []
@@ -403,7 +405,7 @@ class GravityContext:
             arr[i].ns = ns
             arr[i].sxyz = px
             arr[i].gz = po
-        o = _opts(precision, a.flags, G, near_q)
+        o = _opts(precision, a.flags | (AUTOTUNE if autotune else 0), G, near_q)
         self._run(a, self._lib.ztm_gfm_batch, self._h, arr, len(jobs), ctypes.byref(o))
         return [out.reshape(nm, ns) for out, nm, ns in outs]
 
