@@ -90,7 +90,7 @@ __global__ void transpose_models_kernel(MeshConst k, int nmodels, int W,
 // Far field of one column for every model of the group, W models
 // interleaved in `col` (layer-major, W per layer).  K is computed once per
 // (station, prism) pair; per model two packed FMAs per layer pair (W = 1) or
-// per model pair (W = 8); plain sums over 8 layers, Kahan across groups.
+// per model pair (W = 8); plain sums over 32 layers, Kahan across groups.
 // T2: the second-order form (every lane of the warp far enough); MASK: some
 // lane of the warp has the column in its near box, or nz is not a multiple
 // of 8 (both warp-uniform, so the selects are skipped for most columns).
@@ -100,6 +100,10 @@ __device__ __forceinline__ void far_column(const float* __restrict__ col, const 
                                            int Lm, int elo, unsigned espan, Kahan* acc) {
   const float2 dz2 = make_float2(k.dzn, k.dzn);
   float zf = (float)(-izs);  // (l0 - izs), exact, stepped by 8
+  // plain float sums over up to 32 layers per model, compensated across
+  float2 g[W == 1 ? 1 : W / 2];
+#pragma unroll
+  for (int m = 0; m < (W == 1 ? 1 : W / 2); m++) g[m] = make_float2(0.f, 0.f);
   for (int l0 = 0; l0 < k.nz; l0 += 8, zf += 8.f) {
     const float Zg = fmaf(zf, k.dzn, ez);
     const float2 zg2 = make_float2(Zg, Zg);
@@ -115,18 +119,19 @@ __device__ __forceinline__ void far_column(const float* __restrict__ col, const 
         if ((lb < Lm && (unsigned)(lb - elo) <= espan) || lb >= k.nz) K2[j].y = 0.f;
       }
     }
+    const bool flush = ((l0 >> 3) & 3) == 3 || l0 + 8 >= k.nz;
     if constexpr (W == 1) {
       const float4 ra = *reinterpret_cast<const float4*>(col + l0);
       const float4 rb = *reinterpret_cast<const float4*>(col + l0 + 4);
-      float2 g = __fmul2_rn(K2[0], make_float2(ra.x, ra.y));
-      g = __ffma2_rn(K2[1], make_float2(ra.z, ra.w), g);
-      g = __ffma2_rn(K2[2], make_float2(rb.x, rb.y), g);
-      g = __ffma2_rn(K2[3], make_float2(rb.z, rb.w), g);
-      acc[0].add(g.x + g.y);
+      g[0] = __ffma2_rn(K2[0], make_float2(ra.x, ra.y), g[0]);
+      g[0] = __ffma2_rn(K2[1], make_float2(ra.z, ra.w), g[0]);
+      g[0] = __ffma2_rn(K2[2], make_float2(rb.x, rb.y), g[0]);
+      g[0] = __ffma2_rn(K2[3], make_float2(rb.z, rb.w), g[0]);
+      if (flush) {
+        acc[0].add(g[0].x + g[0].y);
+        g[0] = make_float2(0.f, 0.f);
+      }
     } else {
-      float2 g[W / 2];
-#pragma unroll
-      for (int m = 0; m < W / 2; m++) g[m] = make_float2(0.f, 0.f);
 #pragma unroll
       for (int j = 0; j < 8; j++) {
         const float Kj = (j & 1) ? K2[j >> 1].y : K2[j >> 1].x;
@@ -139,10 +144,13 @@ __device__ __forceinline__ void far_column(const float* __restrict__ col, const 
           g[2 * m + 1] = __ffma2_rn(kk, make_float2(r4.z, r4.w), g[2 * m + 1]);
         }
       }
+      if (flush) {
 #pragma unroll
-      for (int m = 0; m < W / 2; m++) {
-        acc[2 * m].add(g[m].x);
-        acc[2 * m + 1].add(g[m].y);
+        for (int m = 0; m < W / 2; m++) {
+          acc[2 * m].add(g[m].x);
+          acc[2 * m + 1].add(g[m].y);
+          g[m] = make_float2(0.f, 0.f);
+        }
       }
     }
   }
