@@ -289,7 +289,7 @@ __global__ void __launch_bounds__(IF_TS, 8)
     __syncthreads();
     if (!active) continue;
     const int cnt = min(IF_TILE, c1 - t0);
-    float2 g = make_float2(0.f, 0.f);  // plain sums over 16 columns, Kahan across
+    float2 g = make_float2(0.f, 0.f);  // plain sums over 32 columns, Kahan across
     for (int q = 0; q < cnt; q += 2) {
       // columns q and q+1 (the second is dropped past the end of the tile)
       const float4 A = s_c[q], B = s_c[q + 1];
@@ -320,7 +320,7 @@ __global__ void __launch_bounds__(IF_TS, 8)
       }
       if (q + 1 >= cnt) v.y = 0.f;  // the padding column
       g = __fadd2_rn(g, v);
-      if ((q & 14) == 14) {
+      if ((q & 30) == 30) {
         acc.add(g.x + g.y);
         g = make_float2(0.f, 0.f);
       }
@@ -438,7 +438,7 @@ __global__ void __launch_bounds__(IF_TS, 8)
     __syncthreads();
     if (!active) continue;
     const int cnt = min(IF_TILE, s1 - t0);
-    float2 gr = make_float2(0.f, 0.f), gd = make_float2(0.f, 0.f);  // 16 stations, Kahan across
+    float2 gr = make_float2(0.f, 0.f), gd = make_float2(0.f, 0.f);  // 32 stations, Kahan across
     for (int q = 0; q < cnt; q += 2) {
       // stations q and q+1 (the second is dropped past the end of the tile)
       const float2 hx = *reinterpret_cast<const float2*>(s_hx + q);
@@ -471,7 +471,7 @@ __global__ void __launch_bounds__(IF_TS, 8)
       if (q + 1 >= cnt) vr.y = vd.y = 0.f;  // the padding station
       gr = __fadd2_rn(gr, vr);
       gd = __fadd2_rn(gd, vd);
-      if ((q & 14) == 14) {
+      if ((q & 30) == 30) {
         ar.add(gr.x + gr.y);
         ad.add(gd.x + gd.y);
         gr = gd = make_float2(0.f, 0.f);

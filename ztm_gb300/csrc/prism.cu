@@ -259,7 +259,7 @@ __device__ __forceinline__ float2 far_group(const float* col, int l0, float fl,
 
 // All layers of one column: groups [0, lmask) with the near mask, full
 // groups up to nz8 without, a masked tail group if nz is not a multiple of 8.
-// Plain float sums over 16 layers, compensated across.
+// Plain float sums over 32 layers (two lanes of 16), compensated across.
 template <bool T2>
 __device__ __forceinline__ void far_column(const float* col, int lmask, int nz8, int nz,
                                            const float2 (&Zb)[4], float2 zstep,
@@ -270,14 +270,14 @@ __device__ __forceinline__ void far_column(const float* col, int lmask, int nz8,
   float fl = 0.f;
   for (; l0 < lmask; l0 += 8, fl += 8.f) {
     g = far_group<T2, true>(col, l0, fl, Zb, zstep, cp2, c2t, elo, espan, nz, g);
-    if (l0 & 8) {
+    if ((l0 & 24) == 24) {
       acc.add(g.x + g.y);
       g = make_float2(0.f, 0.f);
     }
   }
   for (; l0 < nz8; l0 += 8, fl += 8.f) {
     g = far_group<T2, false>(col, l0, fl, Zb, zstep, cp2, c2t, elo, espan, nz, g);
-    if (l0 & 8) {
+    if ((l0 & 24) == 24) {
       acc.add(g.x + g.y);
       g = make_float2(0.f, 0.f);
     }
