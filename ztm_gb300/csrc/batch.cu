@@ -31,7 +31,7 @@
 namespace {
 
 constexpr int B_TS = 128;   // threads per block = stations per tile
-constexpr int B_MG = 8;     // models per far item
+constexpr int B_MG = 16;    // models per far item
 constexpr int B_WARPS = B_TS / 32;
 
 struct BJob {
@@ -94,10 +94,21 @@ __global__ void transpose_models_kernel(MeshConst k, int nmodels, int W,
 // T2: the second-order form (every lane of the warp far enough); MASK: some
 // lane of the warp has the column in its near box, or nz is not a multiple
 // of 8 (both warp-uniform, so the selects are skipped for most columns).
+// Kahan accumulators of this thread's models in shared memory (model m at
+// ks[m * B_TS], kc[m * B_TS]; the pointers are offset by the thread index).
+__device__ __forceinline__ void kahan_smem(float* ks, float* kc, int m, float x) {
+  const float y = x - kc[m * B_TS];
+  const float s0 = ks[m * B_TS];
+  const float t = s0 + y;
+  kc[m * B_TS] = (t - s0) - y;
+  ks[m * B_TS] = t;
+}
+
 template <int W, bool T2, bool MASK>
 __device__ __forceinline__ void far_column(const float* __restrict__ col, const MeshConst& k,
                                            const ColPoly2& cp2, float2 c2t, float ez, int izs,
-                                           int Lm, int elo, unsigned espan, Kahan* acc) {
+                                           int Lm, int elo, unsigned espan, float* ks,
+                                           float* kc) {
   const float2 dz2 = make_float2(k.dzn, k.dzn);
   float zf = (float)(-izs);  // (l0 - izs), exact, stepped by 8
   // plain float sums over up to 32 layers per model, compensated across
@@ -128,7 +139,7 @@ __device__ __forceinline__ void far_column(const float* __restrict__ col, const 
       g[0] = __ffma2_rn(K2[2], make_float2(rb.x, rb.y), g[0]);
       g[0] = __ffma2_rn(K2[3], make_float2(rb.z, rb.w), g[0]);
       if (flush) {
-        acc[0].add(g[0].x + g[0].y);
+        kahan_smem(ks, kc, 0, g[0].x + g[0].y);
         g[0] = make_float2(0.f, 0.f);
       }
     } else {
@@ -147,8 +158,8 @@ __device__ __forceinline__ void far_column(const float* __restrict__ col, const 
       if (flush) {
 #pragma unroll
         for (int m = 0; m < W / 2; m++) {
-          acc[2 * m].add(g[m].x);
-          acc[2 * m + 1].add(g[m].y);
+          kahan_smem(ks, kc, 2 * m, g[m].x);
+          kahan_smem(ks, kc, 2 * m + 1, g[m].y);
           g[m] = make_float2(0.f, 0.f);
         }
       }
@@ -236,6 +247,11 @@ __global__ void __launch_bounds__(B_TS, 4) batch_kernel(BArgs a) {
   double* phi = a.phi + (size_t)blockIdx.x * B_WARPS * a.phi_cap;
   __shared__ long long s_item;
   __shared__ int s_flag, s_lm;
+  // compensated sums of each thread's models (16 KB): in registers they
+  // would cost 32 per thread
+  __shared__ float s_ks[B_MG * B_TS], s_kc[B_MG * B_TS];
+  float* const ks = s_ks + threadIdx.x;
+  float* const kc = s_kc + threadIdx.x;
   if (threadIdx.x == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
@@ -300,7 +316,8 @@ __global__ void __launch_bounds__(B_TS, 4) batch_kernel(BArgs a) {
     __syncthreads();
     const int Lm = min(s_lm, k.nz);
     const FarCoef fc = k.fc;
-    Kahan acc[B_MG];
+#pragma unroll
+    for (int md = 0; md < B_MG; md++) ks[md * B_TS] = kc[md * B_TS] = 0.f;
     bool timed_out = false;
     for (int st = 0; st < nst; st++) {
       if (threadIdx.x == 0 && st + 1 < nst) issue(st + 1);
@@ -332,17 +349,17 @@ __global__ void __launch_bounds__(B_TS, 4) batch_kernel(BArgs a) {
                            ((__any_sync(am, ncl) || (k.nz & 7)) ? 2 : 0);
           if (J.mgw == 1) {
             switch (form) {
-              case 0: far_column<1, false, false>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, acc); break;
-              case 1: far_column<1, true, false>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, acc); break;
-              case 2: far_column<1, false, true>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, acc); break;
-              default: far_column<1, true, true>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, acc);
+              case 0: far_column<1, false, false>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc); break;
+              case 1: far_column<1, true, false>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc); break;
+              case 2: far_column<1, false, true>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc); break;
+              default: far_column<1, true, true>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc);
             }
           } else {
             switch (form) {
-              case 0: far_column<B_MG, false, false>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, acc); break;
-              case 1: far_column<B_MG, true, false>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, acc); break;
-              case 2: far_column<B_MG, false, true>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, acc); break;
-              default: far_column<B_MG, true, true>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, acc);
+              case 0: far_column<B_MG, false, false>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc); break;
+              case 1: far_column<B_MG, true, false>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc); break;
+              case 2: far_column<B_MG, false, true>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc); break;
+              default: far_column<B_MG, true, true>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc);
             }
           }
           if (++ix == k.nx) {
@@ -361,7 +378,8 @@ __global__ void __launch_bounds__(B_TS, 4) batch_kernel(BArgs a) {
 #pragma unroll
       for (int md = 0; md < B_MG; md++)
         if (md < mcnt)
-          J.partial[((size_t)(m0 + md) * J.chunks + chunk) * J.ns + s] = acc[md].value();
+          J.partial[((size_t)(m0 + md) * J.chunks + chunk) * J.ns + s] =
+              (double)ks[md * B_TS] - (double)kc[md * B_TS];
     }
     tile_done(J, tile, J.chunks * J.mgroups + 1, &s_flag);
   }
