@@ -94,7 +94,7 @@ def test_interface_misfit_gradient_vs_central_differences(ctx):
 
 
 def test_moho_256_gradients_mixed_vs_fp64(ctx):
-    """Config 3 (256x256 columns, 128x128 stations): mixed vs double
+    """256x256 Moho columns, 128x128 stations: mixed vs double
     gradients and the misfit, full size."""
     from ztm_gb300 import synth
     im, depth, rho, st, start = synth.moho_columns()

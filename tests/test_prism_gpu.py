@@ -135,7 +135,7 @@ def test_autotuned_shape_gives_the_same_field(ctx):
 
 
 def test_plain_mesh_64_full_size_vs_oracle(ctx):
-    """Config 1 (64x64x32 prisms of 2x2x1 km, 32x32 stations at +100 m):
+    """64x64x32 prisms of 2x2x1 km, 32x32 stations at +100 m:
     the plain double kernel and the mixed kernel against the CPU oracle on
     every station."""
     from ztm_gb300 import synth
@@ -143,3 +143,21 @@ def test_plain_mesh_64_full_size_vs_oracle(ctx):
     ref = oracle.prism_mesh(mesh, rho, st)
     assert rel_err(ctx.prism(mesh, rho, st, precision="fp64"), ref) <= TOL64
     assert rel_err(ctx.prism(mesh, rho, st, precision="mixed"), ref) <= TOLMIX
+
+
+def test_draped_mesh_256_linearity_and_batch(ctx):
+    """Size-independent checks on the full 256x256x64 draped mesh (every
+    station): the mixed forward is linear in the density, and a trial model
+    of a batched launch equals the single call."""
+    from ztm_gb300 import synth
+    mesh, rho, st = synth.draped_mesh_256x256x64()
+    rho2 = np.random.default_rng(12).normal(0.0, 150.0, rho.size)
+    a = ctx.prism(mesh, rho, st, precision="mixed")
+    b = ctx.prism(mesh, rho2, st, precision="mixed")
+    c = ctx.prism(mesh, 2.0 * rho - 0.5 * rho2, st, precision="mixed")
+    assert rel_err(c, 2.0 * a - 0.5 * b) <= 1e-7
+    trials = np.stack([rho + al * rho2 for al in (0.0, 0.5, 1.0)])
+    out = ctx.batch([(mesh, trials, st)])[0]
+    ref = ctx.prism(mesh, trials[1], st, precision="mixed")
+    assert rel_err(out[1], ref) <= 1e-6
+    assert rel_err(out[0], a) <= 1e-6

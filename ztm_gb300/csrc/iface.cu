@@ -219,24 +219,24 @@ __device__ __forceinline__ float2 col_unit2(float2 X2, float2 Y2, float2 rh, flo
   const float2 num = __fmul2_rn(__fmul2_rn(th, __fadd2_rn(ut, ub)), __fmul2_rn(itb, itb));
   const float2 den = __fadd2_rn(it, ib);
   const float2 L = make_float2(__fdividef(num.x, den.x), __fdividef(num.y, den.y));
+  // the corrections it^5 (Q0 rt^2 + Q2) + it^9 (P0 rt^4 + P2 rt^2 + P4) at the
+  // top (and the same at the bottom), with rt^2 it^2 = 1 folded in:
+  //   it^3 (Q0 + it^2 ((Q2 + P0) + it^2 (P2 + it^2 P4)))
   const float2 Q0 = make_float2(k.Q0, k.Q0);
   const float2 it2 = __fmul2_rn(it, it), ib2 = __fmul2_rn(ib, ib);
-  const float2 it5 = __fmul2_rn(__fmul2_rn(it2, it2), it), ib5 = __fmul2_rn(__fmul2_rn(ib2, ib2), ib);
+  const float2 it3 = __fmul2_rn(it2, it), ib3 = __fmul2_rn(ib2, ib);
   float2 ct, cb;
   if (T2) {
-    ct = __fmul2_rn(it5, __ffma2_rn(Q0, rt2, Q2));
-    cb = __fmul2_rn(ib5, __ffma2_rn(Q0, rb2, Q2));
+    ct = __fmul2_rn(it3, __ffma2_rn(it2, Q2, Q0));
+    cb = __fmul2_rn(ib3, __ffma2_rn(ib2, Q2, Q0));
   } else {
     const float2 P4 = __ffma2_rn(__fmul2_rn(make_float2(k.p4x, k.p4x), X2), X2,
                                  __ffma2_rn(__fmul2_rn(make_float2(k.p4y, k.p4y), Y2), Y2,
                                             __fmul2_rn(__fmul2_rn(make_float2(k.p4xy, k.p4xy), X2), Y2)));
     const float2 P2 = __ffma2_rn(make_float2(k.p2x, k.p2x), X2, __fmul2_rn(make_float2(k.p2y, k.p2y), Y2));
-    const float2 P0 = make_float2(k.P0, k.P0);
-    const float2 it9 = __fmul2_rn(__fmul2_rn(it2, it2), it5), ib9 = __fmul2_rn(__fmul2_rn(ib2, ib2), ib5);
-    ct = __ffma2_rn(it9, __ffma2_rn(__ffma2_rn(P0, rt2, P2), rt2, P4),
-                    __fmul2_rn(it5, __ffma2_rn(Q0, rt2, Q2)));
-    cb = __ffma2_rn(ib9, __ffma2_rn(__ffma2_rn(P0, rb2, P2), rb2, P4),
-                    __fmul2_rn(ib5, __ffma2_rn(Q0, rb2, Q2)));
+    const float2 QP = __fadd2_rn(Q2, make_float2(k.P0, k.P0));
+    ct = __fmul2_rn(it3, __ffma2_rn(it2, __ffma2_rn(it2, __ffma2_rn(it2, P4, P2), QP), Q0));
+    cb = __fmul2_rn(ib3, __ffma2_rn(ib2, __ffma2_rn(ib2, __ffma2_rn(ib2, P4, P2), QP), Q0));
   }
   return __fadd2_rn(L, __fadd2_rn(ct, make_float2(-cb.x, -cb.y)));
 }
