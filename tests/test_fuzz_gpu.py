@@ -1,0 +1,64 @@
+"""Seeded random shapes through the mixed kernels: mesh sizes that are not
+multiples of the tile, stage, layer-group or warp sizes, station counts that
+leave partial tiles and near items, stations above, inside, beside and below
+the mesh.  Each case is checked against the plain double kernels of the
+library (themselves pinned to the oracle in test_prism_gpu and
+test_adjoint_gpu)."""
+import numpy as np
+import pytest
+
+import ztm_gb300
+from helpers import rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _case(seed):
+    rng = np.random.default_rng(1000 + seed)
+    nx, ny = (int(v) for v in rng.integers(1, 72, 2))
+    nz = int(rng.integers(1, 41))
+    dx, dy, dz = (float(v) for v in rng.uniform(200.0, 2000.0, 3))
+    mesh = ztm_gb300.make_mesh(nx, ny, nz, dx, dy, dz, x0=float(rng.uniform(-5e3, 5e3)),
+                               y0=float(rng.uniform(-5e3, 5e3)), z_top=float(rng.uniform(-500, 500)))
+    rho = rng.normal(0.0, 250.0, nx * ny * nz)
+    rho[rng.random(rho.size) < 0.2] = 0.0
+    ns = int(rng.integers(1, 300))
+    X1, Y1 = mesh.x0 + nx * dx, mesh.y0 + ny * dy
+    Zb = mesh.z_top - nz * dz
+    x = rng.uniform(mesh.x0 - 3 * dx, X1 + 3 * dx, ns)
+    y = rng.uniform(mesh.y0 - 3 * dy, Y1 + 3 * dy, ns)
+    kind = rng.integers(0, 4, ns)  # above, inside, below, far above
+    z = np.where(kind == 0, mesh.z_top + rng.uniform(1.0, 3000.0, ns),
+                 np.where(kind == 1, rng.uniform(Zb + 1.0, mesh.z_top - 1.0, ns),
+                          np.where(kind == 2, Zb - rng.uniform(1.0, 2000.0, ns),
+                                   mesh.z_top + rng.uniform(5e3, 5e4, ns))))
+    st = np.stack([x, y, z], 1)
+    return mesh, rho, st, rng
+
+
+@pytest.mark.parametrize("seed", range(16))
+def test_random_meshes_mixed_vs_double(ctx, seed):
+    mesh, rho, st, rng = _case(seed)
+    ref = ctx.prism(mesh, rho, st, precision="fp64")
+    out = ctx.prism(mesh, rho, st, precision="mixed")
+    assert np.all(np.isfinite(out))
+    assert rel_err(out, ref) <= 1e-6
+    r = rng.normal(0.0, 1.0, len(st))
+    ga = ctx.adjoint(mesh, st, r, precision="fp64")
+    gm = ctx.adjoint(mesh, st, r, precision="mixed")
+    assert rel_err(gm, ga) <= 1e-6
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_random_batches_vs_single_calls(ctx, seed):
+    jobs, refs = [], []
+    for j in range(3):
+        mesh, rho, st, rng = _case(100 + 3 * seed + j)
+        nm = int(rng.integers(1, 20))
+        models = np.stack([rho * (1.0 + 0.1 * m) for m in range(nm)])
+        jobs.append((mesh, models, st))
+    outs = ctx.batch(jobs)
+    for (mesh, models, st), out in zip(jobs, outs):
+        for m in (0, models.shape[0] - 1):
+            ref = ctx.prism(mesh, models[m], st, precision="mixed")
+            assert rel_err(out[m], ref) <= 1e-6
