@@ -62,3 +62,36 @@ def test_random_batches_vs_single_calls(ctx, seed):
         for m in (0, models.shape[0] - 1):
             ref = ctx.prism(mesh, models[m], st, precision="mixed")
             assert rel_err(out[m], ref) <= 1e-6
+
+
+def _icase(seed):
+    rng = np.random.default_rng(2000 + seed)
+    nx, ny = (int(v) for v in rng.integers(1, 72, 2))
+    dx, dy = (float(v) for v in rng.uniform(300.0, 3000.0, 2))
+    z_base = -float(rng.uniform(20e3, 60e3))
+    im = ztm_gb300.make_imesh(nx, ny, dx, dy, z_base, x0=float(rng.uniform(-5e3, 5e3)),
+                              y0=float(rng.uniform(-5e3, 5e3)))
+    # tops between the surface and the base; some columns thin, some shallow
+    depth = rng.uniform(100.0, -z_base - 50.0, nx * ny)
+    rho = rng.normal(-300.0, 80.0, nx * ny)
+    ns = int(rng.integers(1, 300))
+    X1, Y1 = im.x0 + nx * dx, im.y0 + ny * dy
+    st = np.stack([rng.uniform(im.x0 - 2 * dx, X1 + 2 * dx, ns),
+                   rng.uniform(im.y0 - 2 * dy, Y1 + 2 * dy, ns),
+                   rng.uniform(-50.0, 3000.0, ns)], 1)  # some just below z = 0
+    return im, depth, rho, st, rng
+
+
+@pytest.mark.parametrize("seed", range(10))
+def test_random_interfaces_mixed_vs_double(ctx, seed):
+    """Interface columns with tops from 100 m below the surface to the base:
+    stations near shallow tops take the double near path."""
+    im, depth, rho, st, rng = _icase(seed)
+    ref = ctx.interface(im, depth, rho, st, precision="fp64")
+    out = ctx.interface(im, depth, rho, st, precision="mixed")
+    assert np.all(np.isfinite(out))
+    assert rel_err(out, ref) <= 1e-6
+    r = rng.normal(0.0, 1.0, len(st))
+    gr64, gd64 = ctx.interface_adjoint(im, depth, rho, st, r, precision="fp64")
+    grm, gdm = ctx.interface_adjoint(im, depth, rho, st, r, precision="mixed")
+    assert rel_err(grm, gr64) <= 1e-5 and rel_err(gdm, gd64) <= 1e-5
