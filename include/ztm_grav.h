@@ -246,6 +246,18 @@ int ztm_gfm_interface_adjoint(ztm_ctx* ctx, const ztm_imesh* mesh,
                               double* g_rho, double* g_depth,
                               const ztm_opts* opt);
 
+/* Directional derivative of the interface forward along a depth change
+ * (Jacobian times vector, the forward-mode counterpart of g_depth):
+ * dgz[s] = sum_c dgz[s]/ddepth[c] * d_depth[c] (mGal per metre of d_depth),
+ * from the same top-face integral as the adjoint.  With the adjoint it gives
+ * Gauss-Newton products J v and J^T w without forming J.  No counterpart in
+ * the reference, whose optimiser builds J by finite differences of whole
+ * forward runs (TFM.cpp:124-135). */
+int ztm_gfm_interface_jvp(ztm_ctx* ctx, const ztm_imesh* mesh,
+                          const double* depth, const double* rho_col,
+                          const double* d_depth, int ns, const double* sxyz,
+                          double* dgz, const ztm_opts* opt);
+
 /* Forward + misfit + adjoint in one call: gz = F(depth, rho_col),
  * *misfit = 0.5*sum (gz-data)^2, gradients as ztm_gfm_interface_adjoint.
  * gz, g_rho, g_depth may be NULL. */

@@ -122,3 +122,26 @@ def test_autograd_gradcheck(ctx):
     sti = torch.tensor(sti, device="cuda")
     g = lambda dd, rr: InterfaceGravity.apply(dd * 1000.0, rr * 100.0, ctx, im, sti, "fp64")
     assert torch.autograd.gradcheck(g, (d, rc), eps=1e-3, atol=1e-8, rtol=1e-5)
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("mixed", 1e-6)])
+def test_interface_depth_jvp_dot_product_and_differences(ctx, precision, tol):
+    """J v from ztm_gfm_interface_jvp against the depth adjoint (J^T w) by the
+    dot-product identity, and against central differences of the forward."""
+    from ztm_gb300 import synth
+    im, depth, rho, st, _ = synth.moho_columns(seed=8, n=48, ns_side=24, cell=1000.0)
+    rng = np.random.default_rng(9)
+    v = rng.normal(0.0, 100.0, depth.size)
+    w = rng.normal(0.0, 1.0, len(st))
+    jv = ctx.interface_jvp(im, depth, rho, st, v, precision=precision)
+    _, jtw = ctx.interface_adjoint(im, depth, rho, st, w, precision=precision)
+    lhs, rhs = float(np.dot(jv, w)), float(np.dot(v, jtw))
+    assert abs(lhs - rhs) <= tol * max(abs(lhs), abs(rhs))
+    if precision == "fp64":
+        h = 1e-3
+        fd = (ctx.interface(im, depth + h * v, rho, st, precision="fp64") -
+              ctx.interface(im, depth - h * v, rho, st, precision="fp64")) / (2 * h)
+        assert rel_err(jv, fd) <= 1e-5
+    else:
+        ref = ctx.interface_jvp(im, depth, rho, st, v, precision="fp64")
+        assert rel_err(jv, ref) <= 1e-6

@@ -31,7 +31,7 @@ EXPORTS = (
     "ztm_gfm_interface", "ztm_gfm_interface_adjoint", "ztm_gfm_interface_misfit",
     "ztm_gfm_batch", "ztm_ctx_profile", "ztm_ctx_profile_read", "ztm_measure_peak",
     "ztm_invert_interface", "ztm_gfm_pointmass_noalloc", "ztm_density_build",
-    "ztm_gfm_pointmass_model",
+    "ztm_gfm_pointmass_model", "ztm_gfm_interface_jvp",
 )
 
 
@@ -93,6 +93,8 @@ _SIGS = {
                                ctypes.POINTER(Opts)]),
     "ztm_gfm_interface_adjoint": (_I, [_P, ctypes.POINTER(IMesh), _P, _P, _I, _P, _P, _P, _P,
                                        ctypes.POINTER(Opts)]),
+    "ztm_gfm_interface_jvp": (_I, [_P, ctypes.POINTER(IMesh), _P, _P, _P, _I, _P, _P,
+                                   ctypes.POINTER(Opts)]),
     "ztm_gfm_interface_misfit": (_I, [_P, ctypes.POINTER(IMesh), _P, _P, _I, _P, _P, _P, _P,
                                       _P, _P, ctypes.POINTER(Opts)]),
     "ztm_gfm_batch": (_I, [_P, ctypes.POINTER(Job), _I, ctypes.POINTER(Opts)]),

@@ -110,13 +110,17 @@ __global__ void iface_station_prep(IMeshDesc m, double L0, int ns, const double*
 }
 
 // per column: (rho, depth/L0, thickness/L0, 0)
+// Per-column float data: (weight, top depth, thickness) in units of L0.  The
+// weight is rho, or rho * vdep[c] for the depth directional derivative.
 __global__ void iface_col_prep(IMeshDesc m, double L0, const double* __restrict__ depth,
-                               const double* __restrict__ rho, float4* __restrict__ cf) {
+                               const double* __restrict__ rho, const double* __restrict__ vdep,
+                               float4* __restrict__ cf) {
   long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (c >= (long long)m.nx * m.ny) return;
   double d = depth[c];
   double thick = (-d - m.zb) / L0;
-  cf[c] = make_float4((float)rho[c], (float)(d / L0), (float)thick, 0.f);
+  const double w = vdep ? rho[c] * vdep[c] : rho[c];
+  cf[c] = make_float4((float)w, (float)(d / L0), (float)thick, 0.f);
 }
 
 // Near columns of a station: inside the (2w+1)^2 window around its home
@@ -247,6 +251,9 @@ __device__ __forceinline__ float2 col_unit2(float2 X2, float2 Y2, float2 rh, flo
 // near-window test runs only in warps where some station has a near column
 // (anynear, from the mask kernel): for stations well above the interface it
 // never runs.
+// FACE: the top-face integral instead of the column integral (the depth
+// directional derivative, with the columns weighted by rho * direction).
+template <bool FACE>
 __global__ void __launch_bounds__(IF_TS, 8)
     iface_far_fwd(IConst k, int ns, const IStation* __restrict__ sf, const int2* __restrict__ si,
                   const float4* __restrict__ cf, const uint32_t* __restrict__ mask,
@@ -301,11 +308,17 @@ __global__ void __launch_bounds__(IF_TS, 8)
       const float2 ut = __fadd2_rn(zs2, make_float2(A.y, B.y));
       const float2 rt2 = __ffma2_rn(ut, ut, rh);
       const float2 th = make_float2(A.z, B.z);
-      float2 itop;
+      float2 itop, u;
       // second order when every lane's pairs are far enough (warp-uniform)
-      const float2 u = __all_sync(__activemask(), fminf(rt2.x, rt2.y) >= k.rt2_t2)
-                           ? col_unit2<true>(X2, Y2, rh, ut, rt2, th, k, &itop)
-                           : col_unit2<false>(X2, Y2, rh, ut, rt2, th, k, &itop);
+      const bool t2 = __all_sync(__activemask(), fminf(rt2.x, rt2.y) >= k.rt2_t2);
+      if (FACE) {
+        itop = make_float2(rsqrt_ftz(rt2.x), rsqrt_ftz(rt2.y));
+        u = t2 ? face_unit_far2<true>(X2, Y2, ut, itop, k.face)
+               : face_unit_far2<false>(X2, Y2, ut, itop, k.face);
+      } else {
+        u = t2 ? col_unit2<true>(X2, Y2, rh, ut, rt2, th, k, &itop)
+               : col_unit2<false>(X2, Y2, rh, ut, rt2, th, k, &itop);
+      }
       float2 v = __fmul2_rn(make_float2(A.x, B.x), u);
       if (warp_near) {
         // near columns contribute through the double path: select, which
@@ -331,10 +344,11 @@ __global__ void __launch_bounds__(IF_TS, 8)
 }
 
 // ---- forward, near window in double (warp per station) ---------------------
+template <bool FACE>
 __global__ void iface_near_fwd(IConst k, IMeshDesc m, int ns, const double* __restrict__ sxyz,
                                const int2* __restrict__ si, const double* __restrict__ depth,
-                               const double* __restrict__ rho, const uint32_t* __restrict__ mask,
-                               double* __restrict__ out) {
+                               const double* __restrict__ rho, const double* __restrict__ vdep,
+                               const uint32_t* __restrict__ mask, double* __restrict__ out) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int s = blockIdx.x * IF_NEAR_WPB + warp;
   if (s >= ns) return;
@@ -349,11 +363,14 @@ __global__ void iface_near_fwd(IConst k, IMeshDesc m, int ns, const double* __re
     if (!((mask[(size_t)s * k.words + (q >> 5)] >> (q & 31)) & 1u)) continue;
     const int ix = x0 + q % wx, iy = y0 + q / wx;
     const long long c = ix + (long long)m.nx * iy;
-    const double r = rho[c];
+    const double r = FACE ? rho[c] * vdep[c] : rho[c];
     if (r == 0.0) continue;
-    acc += r * ztm_prism_unit<double>((m.x0 + ix * m.dx) - xs, (m.x0 + (ix + 1) * m.dx) - xs,
-                                      (m.y0 + iy * m.dy) - ys, (m.y0 + (iy + 1) * m.dy) - ys,
-                                      m.zb - zs, -depth[c] - zs);
+    const double xa = (m.x0 + ix * m.dx) - xs, xb = (m.x0 + (ix + 1) * m.dx) - xs;
+    const double ya = (m.y0 + iy * m.dy) - ys, yb = (m.y0 + (iy + 1) * m.dy) - ys;
+    if (FACE)
+      acc += r * ztm_face_unit(xa, xb, ya, yb, zs + depth[c]);  // zs - z_top
+    else
+      acc += r * ztm_prism_unit<double>(xa, xb, ya, yb, m.zb - zs, -depth[c] - zs);
   }
   acc = warp_sum_d(acc);
   if (lane == 0) out[s] = acc;
@@ -372,10 +389,11 @@ __global__ void iface_finalize(int ns, int nchunks, const double* __restrict__ p
 }
 
 // ---- forward, plain double --------------------------------------------------
+template <bool FACE>
 __global__ void __launch_bounds__(64)
     iface_f64_fwd(IMeshDesc m, int ns, const double* __restrict__ sxyz,
-                  const double* __restrict__ depth, const double* __restrict__ rho, int chunk_len,
-                  double* __restrict__ partial) {
+                  const double* __restrict__ depth, const double* __restrict__ rho,
+                  const double* __restrict__ vdep, int chunk_len, double* __restrict__ partial) {
   const int s = blockIdx.x * 64 + threadIdx.x;
   if (s >= ns) return;
   const double xs = sxyz[3 * s], ys = sxyz[3 * s + 1], zs = sxyz[3 * s + 2];
@@ -383,12 +401,15 @@ __global__ void __launch_bounds__(64)
   const int c0 = blockIdx.y * chunk_len, c1 = min(nc, c0 + chunk_len);
   double acc = 0.0;
   for (int c = c0; c < c1; c++) {
-    const double r = rho[c];
+    const double r = FACE ? rho[c] * vdep[c] : rho[c];
     if (r == 0.0) continue;
     const int ix = c % m.nx, iy = c / m.nx;
-    acc += r * ztm_prism_unit<double>((m.x0 + ix * m.dx) - xs, (m.x0 + (ix + 1) * m.dx) - xs,
-                                      (m.y0 + iy * m.dy) - ys, (m.y0 + (iy + 1) * m.dy) - ys,
-                                      m.zb - zs, -depth[c] - zs);
+    const double xa = (m.x0 + ix * m.dx) - xs, xb = (m.x0 + (ix + 1) * m.dx) - xs;
+    const double ya = (m.y0 + iy * m.dy) - ys, yb = (m.y0 + (iy + 1) * m.dy) - ys;
+    if (FACE)
+      acc += r * ztm_face_unit(xa, xb, ya, yb, zs + depth[c]);  // zs - z_top
+    else
+      acc += r * ztm_prism_unit<double>(xa, xb, ya, yb, m.zb - zs, -depth[c] - zs);
   }
   partial[(size_t)blockIdx.y * ns + s] = acc;
 }
@@ -649,10 +670,17 @@ size_t ztm_iface_ws(const IMeshDesc& m, int ns, int precision, int num_sms) {
   return w;
 }
 
+// The forward (vdep == nullptr) or the depth directional derivative
+// dgz[s] = sum_c dgz[s]/ddepth[c] vdep[c] = -G5 rho_c * (top-face integral):
+// the same kernels with the face integral in place of the column integral
+// and the columns weighted by rho * vdep.
+template <bool FACE>
 static int iface_forward_impl(ztm_ctx* c, const IMeshDesc& m, const double* d_depth,
-                              const double* d_rho, int ns, const double* d_sxyz, double* d_gz,
-                              double G, int precision, const ztm_opts* o, WsCarver& wc) {
+                              const double* d_rho, const double* d_vdep, int ns,
+                              const double* d_sxyz, double* d_gz, double G, int precision,
+                              const ztm_opts* o, WsCarver& wc) {
   const double G5 = G * 1.0e5;
+  const double sign = FACE ? -1.0 : 1.0;
   const long long nc = (long long)m.nx * m.ny;
   if (precision == ZTM_PREC_FP64) {
     int tiles = std::max(1, (ns + 63) / 64), len;
@@ -660,13 +688,13 @@ static int iface_forward_impl(ztm_ctx* c, const IMeshDesc& m, const double* d_de
     double* partial = wc.take<double>((size_t)ch * ns);
     {
       ZtmProf prof_(c, "iface_f64");
-      iface_f64_fwd<<<dim3(tiles, ch), 64, 0, c->stream>>>(m, ns, d_sxyz, d_depth, d_rho, len,
-                                                           partial);
+      iface_f64_fwd<FACE><<<dim3(tiles, ch), 64, 0, c->stream>>>(m, ns, d_sxyz, d_depth, d_rho,
+                                                                 d_vdep, len, partial);
     }
-    iface_finalize<<<(ns + 255) / 256, 256, 0, c->stream>>>(ns, ch, partial, 1.0, nullptr, G5,
-                                                            d_gz);
+    iface_finalize<<<(ns + 255) / 256, 256, 0, c->stream>>>(ns, ch, partial, 1.0, nullptr,
+                                                            sign * G5, d_gz);
     c->launches += 2;
-    return ztm_after_launch(c, "interface FP64 forward");
+    return ztm_after_launch(c, "interface FP64 kernels");
   }
   const double nq = (o && o->near_q > 0) ? o->near_q : 6.0;
   IConst k = make_iconst(m, nq);
@@ -677,7 +705,8 @@ static int iface_forward_impl(ztm_ctx* c, const IMeshDesc& m, const double* d_de
   double* near = wc.take<double>(ns);
   iface_station_prep<<<(ns + 127) / 128, 128, 0, c->stream>>>(m, k.L0, ns, d_sxyz, nullptr, sf,
                                                               si);
-  iface_col_prep<<<(unsigned)((nc + 255) / 256), 256, 0, c->stream>>>(m, k.L0, d_depth, d_rho, cf);
+  iface_col_prep<<<(unsigned)((nc + 255) / 256), 256, 0, c->stream>>>(m, k.L0, d_depth, d_rho,
+                                                                   FACE ? d_vdep : nullptr, cf);
   uint32_t* mask = wc.take<uint32_t>((size_t)ns * k.words);
   int* anynear = wc.take<int>((size_t)ns);
   iface_near_mask<<<(ns + 3) / 4, 128, 0, c->stream>>>(k, ns, d_sxyz, si, d_depth, mask, anynear);
@@ -685,29 +714,40 @@ static int iface_forward_impl(ztm_ctx* c, const IMeshDesc& m, const double* d_de
   ztm_fork(c);
   {
     ZtmProf prof_(c, "iface_near", c->aux);
-    iface_near_fwd<<<(ns + IF_NEAR_WPB - 1) / IF_NEAR_WPB, IF_NEAR_WPB * 32, 0, c->aux>>>(
-        k, m, ns, d_sxyz, si, d_depth, d_rho, mask, near);
+    iface_near_fwd<FACE><<<(ns + IF_NEAR_WPB - 1) / IF_NEAR_WPB, IF_NEAR_WPB * 32, 0, c->aux>>>(
+        k, m, ns, d_sxyz, si, d_depth, d_rho, d_vdep, mask, near);
   }
   int tiles = std::max(1, (ns + IF_TS - 1) / IF_TS), len;
   int ch = chunks_for(nc, tiles, c->num_sms, IF_TILE, &len);
   double* partial = wc.take<double>((size_t)ch * ns);
   {
     ZtmProf prof_(c, "iface_far");
-    iface_far_fwd<<<dim3(tiles, ch), IF_TS, 0, c->stream>>>(k, ns, sf, si, cf, mask, anynear, len,
-                                                            partial);
+    iface_far_fwd<FACE><<<dim3(tiles, ch), IF_TS, 0, c->stream>>>(k, ns, sf, si, cf, mask,
+                                                                  anynear, len, partial);
   }
   ztm_join(c);
-  iface_finalize<<<(ns + 255) / 256, 256, 0, c->stream>>>(ns, ch, partial,
-                                                          k.L0 * (double)k.dxn * k.dyn, near, G5,
-                                                          d_gz);
+  // the column integral is in units of L0 (x dx dy / L0^2), the face
+  // integral is dimensionless (x dx dy / L0^2)
+  const double far_scale = (FACE ? 1.0 : k.L0) * (double)k.dxn * k.dyn;
+  iface_finalize<<<(ns + 255) / 256, 256, 0, c->stream>>>(ns, ch, partial, far_scale, near,
+                                                          sign * G5, d_gz);
   c->launches += 6;
-  return ztm_after_launch(c, "interface mixed forward");
+  return ztm_after_launch(c, "interface mixed kernels");
 }
 
 int ztm_launch_iface_fwd(ztm_ctx* c, const IMeshDesc& m, const double* d_depth,
                          const double* d_rho, int ns, const double* d_sxyz, double* d_gz,
                          double G, int precision, const ztm_opts* o, WsCarver& wc) {
-  return iface_forward_impl(c, m, d_depth, d_rho, ns, d_sxyz, d_gz, G, precision, o, wc);
+  return iface_forward_impl<false>(c, m, d_depth, d_rho, nullptr, ns, d_sxyz, d_gz, G, precision,
+                                   o, wc);
+}
+
+int ztm_launch_iface_jvp(ztm_ctx* c, const IMeshDesc& m, const double* d_depth,
+                         const double* d_rho, const double* d_vdep, int ns, const double* d_sxyz,
+                         double* d_dgz, double G, int precision, const ztm_opts* o,
+                         WsCarver& wc) {
+  return iface_forward_impl<true>(c, m, d_depth, d_rho, d_vdep, ns, d_sxyz, d_dgz, G, precision,
+                                  o, wc);
 }
 
 int ztm_launch_iface_adj(ztm_ctx* c, const IMeshDesc& m, const double* d_depth,
@@ -743,7 +783,8 @@ int ztm_launch_iface_adj(ztm_ctx* c, const IMeshDesc& m, const double* d_depth,
   int2* si = wc.take<int2>(ns);
   float4* cf = wc.take<float4>(nc);
   iface_station_prep<<<(ns + 127) / 128, 128, 0, c->stream>>>(m, k.L0, ns, d_sxyz, d_res, sf, si);
-  iface_col_prep<<<(unsigned)((nc + 255) / 256), 256, 0, c->stream>>>(m, k.L0, d_depth, d_rho, cf);
+  iface_col_prep<<<(unsigned)((nc + 255) / 256), 256, 0, c->stream>>>(m, k.L0, d_depth, d_rho,
+                                                                   nullptr, cf);
   // face integral is dimensionless: dx dy / L0^2 * (u / r^3 in 1/L0^2 units)
   const double sc_rho = G5 * k.L0 * (double)k.dxn * k.dyn;
   const double sc_dep = G5 * (double)k.dxn * k.dyn;
@@ -822,7 +863,8 @@ extern "C" int ztm_gfm_interface_misfit(ztm_ctx* c, const ztm_imesh* mesh, const
   if ((rc = ztm_stage_in(c, sxyz, (size_t)ns * 24, dev, s_xyz, &px))) return rc;
   if ((rc = ztm_stage_in(c, data, (size_t)ns * 8, dev, s_dat, &pdat))) return rc;
   double* ogz = (dev && gz) ? gz : s_gz;
-  rc = iface_forward_impl(c, m, (const double*)pd, (const double*)pr, ns, (const double*)px, ogz,
+  rc = iface_forward_impl<false>(c, m, (const double*)pd, (const double*)pr, nullptr, ns,
+                                 (const double*)px, ogz,
                           G, prec, o, wc);
   if (rc) return rc;
   double* omis = dev ? misfit : s_mis;

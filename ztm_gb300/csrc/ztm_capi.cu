@@ -494,6 +494,44 @@ int ztm_gfm_interface(ztm_ctx* c, const ztm_imesh* mesh, const double* depth,
   return finish(c, dev, gz, out, (size_t)ns * 8, "interface forward");
 }
 
+int ztm_gfm_interface_jvp(ztm_ctx* c, const ztm_imesh* mesh, const double* depth,
+                          const double* rho_col, const double* d_depth, int ns,
+                          const double* sxyz, double* dgz, const ztm_opts* o) {
+  if (!c) return ZTM_ERR_ARG;
+  c->err.clear();
+  int rc;
+  if ((rc = check_imesh(c, mesh)) || (rc = check_opts(c, o))) return rc;
+  if (ns < 0) return ztm_fail(c, ZTM_ERR_ARG, "ns < 0");
+  if (ns == 0) return ZTM_OK;
+  if (!depth || !rho_col || !d_depth || !sxyz || !dgz)
+    return ztm_fail(c, ZTM_ERR_ARG, "null argument");
+  const int prec = o ? o->precision : ZTM_PREC_FP64;
+  const bool dev = o && is_dev(o->flags);
+  IMeshDesc m = to_idesc(mesh);
+  long long nc = (long long)m.nx * m.ny;
+  DeviceGuard dg(c->device);
+  if (!dg.ok) return ztm_fail(c, ZTM_ERR_NODEV, "cannot select device");
+  size_t need = 3 * WsCarver::need(nc * 8) + WsCarver::need((size_t)ns * 24) +
+                WsCarver::need((size_t)ns * 8) + ztm_iface_ws(m, ns, prec, c->num_sms) + 4096;
+  if ((rc = ztm_ws_reserve(c, need))) return rc;
+  WsCarver wc(c->ws);
+  double* s_dep = wc.take<double>(nc);
+  double* s_rho = wc.take<double>(nc);
+  double* s_v = wc.take<double>(nc);
+  double* s_xyz = wc.take<double>((size_t)ns * 3);
+  double* s_out = wc.take<double>(ns);
+  const void *pd, *pr, *pv, *px;
+  if ((rc = ztm_stage_in(c, depth, nc * 8, dev, s_dep, &pd))) return rc;
+  if ((rc = ztm_stage_in(c, rho_col, nc * 8, dev, s_rho, &pr))) return rc;
+  if ((rc = ztm_stage_in(c, d_depth, nc * 8, dev, s_v, &pv))) return rc;
+  if ((rc = ztm_stage_in(c, sxyz, (size_t)ns * 24, dev, s_xyz, &px))) return rc;
+  double* out = dev ? dgz : s_out;
+  rc = ztm_launch_iface_jvp(c, m, (const double*)pd, (const double*)pr, (const double*)pv, ns,
+                            (const double*)px, out, pick_G(o), prec, o, wc);
+  if (rc) return rc;
+  return finish(c, dev, dgz, out, (size_t)ns * 8, "interface depth derivative");
+}
+
 int ztm_gfm_interface_adjoint(ztm_ctx* c, const ztm_imesh* mesh, const double* depth,
                               const double* rho_col, int ns, const double* sxyz,
                               const double* resid, double* g_rho, double* g_depth,

@@ -147,6 +147,11 @@ int ztm_launch_iface_fwd(ztm_ctx* c, const IMeshDesc& m, const double* d_depth,
                          const double* d_rho, int ns, const double* d_sxyz,
                          double* d_gz, double G, int precision,
                          const ztm_opts* o, WsCarver& wc);
+// dgz = J_depth * vdep (the depth directional derivative of the forward)
+int ztm_launch_iface_jvp(ztm_ctx* c, const IMeshDesc& m, const double* d_depth,
+                         const double* d_rho, const double* d_vdep, int ns, const double* d_sxyz,
+                         double* d_dgz, double G, int precision, const ztm_opts* o,
+                         WsCarver& wc);
 int ztm_launch_iface_adj(ztm_ctx* c, const IMeshDesc& m, const double* d_depth,
                          const double* d_rho, int ns, const double* d_sxyz,
                          const double* d_res, double* d_grho, double* d_gdep,

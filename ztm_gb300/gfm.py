@@ -328,6 +328,23 @@ class GravityContext:
                                                         px, pres, pgr, pgd, ctypes.byref(o))
         return g_rho, g_dep
 
+    def interface_jvp(self, imesh, depth, rho_col, stations, d_depth, precision="mixed", G=None,
+                      near_q=None):
+        """dgz = J_depth d_depth: the change of gz (mGal) per unit step along
+        d_depth (metres), without forming J."""
+        nc = imesh.nx * imesh.ny
+        ns = _nstations(stations)
+        a = _Args(self)
+        pd = a.arr(depth, nc, name="depth")
+        pr = a.arr(rho_col, nc, name="rho_col")
+        pv = a.arr(d_depth, nc, name="d_depth")
+        px = a.arr(stations, 3 * ns, name="stations")
+        out, po = a.out(ns, depth)
+        o = _opts(precision, a.flags, G, near_q)
+        self._run(a, self._lib.ztm_gfm_interface_jvp, self._h, ctypes.byref(imesh), pd, pr, pv, ns,
+                  px, po, ctypes.byref(o))
+        return out
+
     def interface_misfit(self, imesh, depth, rho_col, stations, data, precision="mixed",
                          G=None, near_q=None):
         """Returns (misfit, gz, g_rho, g_depth) for misfit 0.5*|gz - data|^2."""
