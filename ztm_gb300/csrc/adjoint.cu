@@ -349,12 +349,6 @@ int ztm_launch_adjoint(ztm_ctx* c, const MeshDesc& m, int ns, const double* d_sx
   slice = ((slice + ADJ_STILE - 1) / ADJ_STILE) * ADJ_STILE;
   slices = (ns + slice - 1) / slice;
   cudaMemsetAsync(d_g, 0, (size_t)k.ncols * k.nz * sizeof(double), c->stream);
-  {
-    ZtmProf prof_(c, "adjoint_far");
-    adj_far_kernel<<<dim3((unsigned)blocks, (unsigned)slices), ADJ_TS, 0, c->stream>>>(
-        k, ns, sf, si, iv, d_res, scale, slice, d_g);
-  }
-  c->launches++;
   const int cap = near_cap(k);
   const bool f64 = precision == ZTM_PREC_MIXED;
   const size_t per_warp = (size_t)cap * (f64 ? 8 : 4);
@@ -362,23 +356,34 @@ int ztm_launch_adjoint(ztm_ctx* c, const MeshDesc& m, int ns, const double* d_sx
     return ztm_fail(c, ZTM_ERR_RANGE, "near_q too large for the adjoint's near box");
   int wpb = (int)std::max<size_t>(1, std::min<size_t>(4, (96 * 1024) / per_warp));
   size_t smem = per_warp * wpb;
+  // Both kernels add into the zeroed g with double atomics, so the near
+  // regions (FP64 pipe) run on the side stream beside the far field (FMA
+  // pipe); the side stream's priority places their blocks first as far
+  // blocks retire.
+  ztm_fork(c);
   if (f64) {
     cudaFuncSetAttribute(adj_near_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)std::max<size_t>(smem, 48 * 1024));
     {
-      ZtmProf prof_(c, "adjoint_near");
-      adj_near_kernel<double><<<(ns + wpb - 1) / wpb, wpb * 32, smem, c->stream>>>(
+      ZtmProf prof_(c, "adjoint_near", c->aux);
+      adj_near_kernel<double><<<(ns + wpb - 1) / wpb, wpb * 32, smem, c->aux>>>(
           k, m, ns, d_sxyz, si, iv, lr, d_res, G5, cap, d_g);
     }
   } else {
     cudaFuncSetAttribute(adj_near_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)std::max<size_t>(smem, 48 * 1024));
     {
-      ZtmProf prof_(c, "adjoint_near");
-      adj_near_kernel<float><<<(ns + wpb - 1) / wpb, wpb * 32, smem, c->stream>>>(
+      ZtmProf prof_(c, "adjoint_near", c->aux);
+      adj_near_kernel<float><<<(ns + wpb - 1) / wpb, wpb * 32, smem, c->aux>>>(
           k, m, ns, d_sxyz, si, iv, lr, d_res, G5, cap, d_g);
     }
   }
-  c->launches++;
+  {
+    ZtmProf prof_(c, "adjoint_far");
+    adj_far_kernel<<<dim3((unsigned)blocks, (unsigned)slices), ADJ_TS, 0, c->stream>>>(
+        k, ns, sf, si, iv, d_res, scale, slice, d_g);
+  }
+  ztm_join(c);
+  c->launches += 2;
   return ztm_after_launch(c, "adjoint mixed kernels");
 }
