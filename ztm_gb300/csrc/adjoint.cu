@@ -327,7 +327,7 @@ int ztm_launch_adjoint(ztm_ctx* c, const MeshDesc& m, int ns, const double* d_sx
   short2* iv = wc.take<short2>((size_t)ns * k.nslots);
   int2* lr = wc.take<int2>(ns);
   launch_mesh_station_prep(c, m, k.L0, ns, d_sxyz, sf, si);
-  launch_mesh_near_iv(c, k, ns, si, iv, lr);
+  launch_mesh_near_iv(c, k, m, ns, si, d_sxyz, iv, lr);
   const int ngroups = (k.nz + ADJ_LG - 1) / ADJ_LG;
   const long long threads = (long long)k.ncols * ngroups;
   const double scale = G5 * k.L0 * (double)k.dxn * k.dyn * k.dzn;

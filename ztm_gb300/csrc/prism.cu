@@ -70,10 +70,13 @@ __global__ void transpose_kernel(MeshConst k, int nmodels, const double* __restr
 
 // Near-region intervals of every (station, box column), in double: one
 // block per station, a thread per box column; the station's overall layer
-// range by shared-memory min/max.
+// range by shared-memory min/max.  A prism is near when the distance from the
+// station to its centre is under near_q half-diagonals (exact coordinates;
+// every such prism lies in the near box).
 constexpr int NEAR_IV_TS = 128;
 __global__ void __launch_bounds__(NEAR_IV_TS)
-    near_iv_kernel(MeshConst k, int ns, const int4* __restrict__ si, short2* __restrict__ iv,
+    near_iv_kernel(MeshConst k, MeshDesc m, int ns, const int4* __restrict__ si,
+                   const double* __restrict__ sxyz, short2* __restrict__ iv,
                    int2* __restrict__ lr) {
   __shared__ int s_min, s_max;
   const int s = blockIdx.x;
@@ -85,19 +88,20 @@ __global__ void __launch_bounds__(NEAR_IV_TS)
   __syncthreads();
   const int4 h = si[s];
   const NearBox b = near_box(h, k);
+  const double xs = sxyz[3 * s], ys = sxyz[3 * s + 1], zs = sxyz[3 * s + 2];
   const int bw = b.x1 - b.x0 + 1, bh = b.y1 - b.y0 + 1;
   int lmin = 1 << 30, lmax = -1;
   for (int slot = threadIdx.x; slot < k.nslots; slot += NEAR_IV_TS) {
     short2 out = make_short2(1, 0);
     if (slot < bw * bh) {
       const int ix = b.x0 + slot % bw, iy = b.y0 + slot / bw;
-      const double hx = fmax(fabs((double)(ix - h.x)) - 0.5, 0.0) * k.dxm;
-      const double hy = fmax(fabs((double)(iy - h.y)) - 0.5, 0.0) * k.dym;
+      const double hx = (m.x0 + (ix + 0.5) * m.dx) - xs;
+      const double hy = (m.y0 + (iy + 0.5) * m.dy) - ys;
       const double h2 = hx * hx + hy * hy;
       int lo = 1 << 30, hi = -1;
       for (int l = b.l0; l <= b.l1; l++) {
-        const double hz = fmax(fabs((double)(l - h.z)) - 0.5, 0.0) * k.dzm;
-        if (h2 + hz * hz < k.R2) {  // one interval: the bound is unimodal in l
+        const double hz = (m.zt - (l + 0.5) * m.dz) - zs;
+        if (h2 + hz * hz < k.R2) {  // one interval: the distance is convex in l
           lo = min(lo, l);
           hi = l;
         }
@@ -744,10 +748,10 @@ void launch_mesh_transpose(ztm_ctx* c, const MeshConst& k, int nmodels, const do
   c->launches++;
 }
 
-void launch_mesh_near_iv(ztm_ctx* c, const MeshConst& k, int ns, const int4* si, short2* iv,
-                         int2* lr) {
+void launch_mesh_near_iv(ztm_ctx* c, const MeshConst& k, const MeshDesc& m, int ns,
+                         const int4* si, const double* sxyz, short2* iv, int2* lr) {
   if (ns <= 0) return;
-  near_iv_kernel<<<ns, NEAR_IV_TS, 0, c->stream>>>(k, ns, si, iv, lr);
+  near_iv_kernel<<<ns, NEAR_IV_TS, 0, c->stream>>>(k, m, ns, si, sxyz, iv, lr);
   c->launches++;
 }
 
@@ -815,7 +819,7 @@ int ztm_launch_prism(ztm_ctx* c, const MeshDesc& m, const double* d_rho, int ns,
   int2* lr = wc.take<int2>(ns);
   launch_mesh_transpose(c, k, 1, d_rho, rhoT);
   launch_mesh_station_prep(c, m, k.L0, ns, d_sxyz, sf, si);
-  launch_mesh_near_iv(c, k, ns, si, iv, lr);
+  launch_mesh_near_iv(c, k, m, ns, si, d_sxyz, iv, lr);
   FarArgs a;
   a.k = k; a.ns = ns; a.sf = sf; a.si = si; a.iv = iv; a.rhoT = rhoT; a.partial = partial;
   a.err = c->d_err;

@@ -163,15 +163,13 @@ __device__ __forceinline__ NearBox near_box(int4 si, const MeshConst& k) {
   return b;
 }
 
-// Near region of a station: the prisms of its near box whose centre lies
-// closer than near_q half-diagonals by the lower bound
-//   d^2 >= sum over axes of (max(|index offset| - 1/2, 0) * cell edge)^2
-// (the station is somewhere in its home cell).  Everything outside the
-// region is at least that far away, so the far-field expansion holds there.
-// In each box column the region's layers are one interval; the interval of
-// every (station, box column) is computed once, in double, by
-// launch_mesh_near_iv, and every kernel that splits near from far pairs
-// reads the same intervals (lo > hi: the column has no near prism).
+// Near region of a station: the prisms whose centre lies closer to the
+// station than near_q half-diagonals (all of them inside the near box).
+// Everything outside the region is at least that far away, so the far-field
+// expansion holds there.  In each box column the region's layers are one
+// interval; the interval of every (station, box column) is computed once, in
+// double, by launch_mesh_near_iv, and every kernel that splits near from far
+// pairs reads the same intervals (lo > hi: the column has no near prism).
 __device__ __forceinline__ int near_slot(const NearBox& b, int ix, int iy) {
   return (ix - b.x0) + (b.x1 - b.x0 + 1) * (iy - b.y0);
 }
@@ -188,11 +186,7 @@ void launch_mesh_station_prep(ztm_ctx* c, const MeshDesc& m, double L0, int ns,
 // padded layers zero.  nmodels > 1: model-major blocks of ncols*nzp floats.
 void launch_mesh_transpose(ztm_ctx* c, const MeshConst& k, int nmodels, const double* rho,
                            float* rhoT);
-// Near box in double (or float) with vertex sharing: for each station, the
-// sum over box vertices of Phi(vertex - station) times the signed triple
-// difference of the density over the (up to 8) box prisms around the vertex.
-// One warp per station.  out[s] = that sum (metres x density, without G).
 // Near-region intervals: iv[s*nslots + slot] (layers lo..hi) and the
 // station's overall layer range lr[s] = (lmin, lmax) (lmin > lmax: none).
-void launch_mesh_near_iv(ztm_ctx* c, const MeshConst& k, int ns, const int4* si, short2* iv,
-                         int2* lr);
+void launch_mesh_near_iv(ztm_ctx* c, const MeshConst& k, const MeshDesc& m, int ns,
+                         const int4* si, const double* sxyz, short2* iv, int2* lr);
