@@ -258,7 +258,11 @@ __global__ void __launch_bounds__(IF_TS, 8)
     iface_far_fwd(IConst k, int ns, const IStation* __restrict__ sf, const int2* __restrict__ si,
                   const float4* __restrict__ cf, const uint32_t* __restrict__ mask,
                   const int* __restrict__ anynear, int chunk_len, double* __restrict__ partial) {
-  __shared__ float4 s_c[IF_TILE + 2];
+  // the tile's columns, one array per field so that a column pair is one
+  // 8-byte load per field (weight, top depth, thickness, -ix, -iy)
+  __shared__ __align__(8) float s_w[IF_TILE + 2];
+  __shared__ __align__(8) float s_top[IF_TILE + 2];
+  __shared__ __align__(8) float s_th[IF_TILE + 2];
   __shared__ __align__(8) float s_nx[IF_TILE + 2];  // -ix of the tile's columns
   __shared__ __align__(8) float s_ny[IF_TILE + 2];  // -iy
   const int s = blockIdx.x * IF_TS + threadIdx.x;
@@ -288,7 +292,10 @@ __global__ void __launch_bounds__(IF_TS, 8)
     for (int q = threadIdx.x; q < IF_TILE + 2; q += IF_TS) {
       const int c = t0 + q;
       const bool ok = c < c1;
-      s_c[q] = ok ? cf[c] : make_float4(0.f, 0.f, 0.f, 0.f);
+      const float4 cq = ok ? cf[c] : make_float4(0.f, 0.f, 0.f, 0.f);
+      s_w[q] = cq.x;
+      s_top[q] = cq.y;
+      s_th[q] = cq.z;
       // a padding column sits on the station column (finite values; dropped)
       s_nx[q] = ok ? -(float)(c % k.nx) : -(float)hi.x;
       s_ny[q] = ok ? -(float)(c / k.nx) : -(float)hi.y;
@@ -299,15 +306,14 @@ __global__ void __launch_bounds__(IF_TS, 8)
     float2 g = make_float2(0.f, 0.f);  // plain sums over 32 columns, Kahan across
     for (int q = 0; q < cnt; q += 2) {
       // columns q and q+1 (the second is dropped past the end of the tile)
-      const float4 A = s_c[q], B = s_c[q + 1];
       const float2 nx2 = *reinterpret_cast<const float2*>(s_nx + q);
       const float2 ny2 = *reinterpret_cast<const float2*>(s_ny + q);
       const float2 X = __ffma2_rn(__fadd2_rn(hx2, nx2), dxn2, ex2);
       const float2 Y = __ffma2_rn(__fadd2_rn(hy2, ny2), dyn2, ey2);
       const float2 X2 = __fmul2_rn(X, X), Y2 = __fmul2_rn(Y, Y), rh = __fadd2_rn(X2, Y2);
-      const float2 ut = __fadd2_rn(zs2, make_float2(A.y, B.y));
+      const float2 ut = __fadd2_rn(zs2, *reinterpret_cast<const float2*>(s_top + q));
       const float2 rt2 = __ffma2_rn(ut, ut, rh);
-      const float2 th = make_float2(A.z, B.z);
+      const float2 th = *reinterpret_cast<const float2*>(s_th + q);
       float2 itop, u;
       // second order when every lane's pairs are far enough (warp-uniform)
       const bool t2 = __all_sync(__activemask(), fminf(rt2.x, rt2.y) >= k.rt2_t2);
@@ -319,7 +325,7 @@ __global__ void __launch_bounds__(IF_TS, 8)
         u = t2 ? col_unit2<true>(X2, Y2, rh, ut, rt2, th, k, &itop)
                : col_unit2<false>(X2, Y2, rh, ut, rt2, th, k, &itop);
       }
-      float2 v = __fmul2_rn(make_float2(A.x, B.x), u);
+      float2 v = __fmul2_rn(*reinterpret_cast<const float2*>(s_w + q), u);
       if (warp_near) {
         // near columns contribute through the double path: select, which
         // also drops a NaN

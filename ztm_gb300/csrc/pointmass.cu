@@ -120,10 +120,13 @@ __global__ void __launch_bounds__(PM_TS)
 // Float path in two steps.
 //
 // 1. Node list (pm_nodes_count / pm_nodes_scan / pm_nodes_write): the
-//    selected nodes, in order, as float4 (-i, -j, -k, w) in grid units, built
-//    once per call (O(nodes), memory bound).  A block covers PM_NB nodes;
+//    selected nodes, in order, in grid units, built once per call (O(nodes),
+//    memory bound), stored by pairs: nodes 2p and 2p+1 as the two float4
+//    (-i0, -i1, -j0, -j1), (-k0, -k1, w0, w1), so that each packed operand of
+//    the gather is one register pair as loaded.  A block covers PM_NB nodes;
 //    the blocks' counts are scanned so that each block writes its nodes at
-//    its offset in node order.
+//    its offset in node order; an odd count is padded with a zero mass far
+//    away (pm_nodes_pad).
 // 2. Gather (pm_gather_f32_kernel): a thread owns a station; the compacted
 //    nodes stream through shared memory in tiles of PM_TILE (coalesced float4
 //    loads, the next tile's loads in flight while the current one is
@@ -241,7 +244,14 @@ __global__ void __launch_bounds__(PM_NT)
     __syncthreads();
     int wbase = 0;
     for (int w = 0; w < warp; w++) wbase += s_w[w];
-    if (sel) nodes[s_base + wbase + below] = v;
+    if (sel) {  // pair layout: component c of lane L of pair p at 8p + 2c + L
+      const int pos = s_base + wbase + below;
+      float* f = reinterpret_cast<float*>(nodes) + 8 * (size_t)(pos >> 1) + (pos & 1);
+      f[0] = v.x;
+      f[2] = v.y;
+      f[4] = v.z;
+      f[6] = v.w;
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
       int tot = 0;
@@ -249,6 +259,18 @@ __global__ void __launch_bounds__(PM_NT)
       s_base += tot;
     }
     __syncthreads();
+  }
+}
+
+// An odd node count: the second lane of the last pair is a zero mass far away.
+__global__ void pm_nodes_pad(const int* __restrict__ total, float4* __restrict__ nodes) {
+  const int m = *total;
+  if (m & 1) {
+    float* f = reinterpret_cast<float*>(nodes) + 8 * (size_t)(m >> 1) + 1;
+    f[0] = -1.0e18f;
+    f[2] = 0.f;
+    f[4] = 0.f;
+    f[6] = 0.f;
   }
 }
 
@@ -271,33 +293,34 @@ __global__ void __launch_bounds__(PM_TS)
   const long long n1 = min(M, n0 + chunk_len);
   const float2 I0 = make_float2(i0, i0), J0 = make_float2(j0, j0), K0 = make_float2(k0, k0);
   Kahan acc;
-  // this thread's two nodes of the next tile (zero mass far away past the end)
-  const float4 pad = make_float4(-1.0e18f, 0.f, 0.f, 0.f);
-  float4 na = pad, nb = pad;
-  if (n0 + threadIdx.x < n1) na = nodes[n0 + threadIdx.x];
-  if (n0 + PM_TS + threadIdx.x < n1) nb = nodes[n0 + PM_TS + threadIdx.x];
+  // this thread's two float4 of the next tile (float4 j holds half of pair
+  // j / 2; pairs past the end are zero masses far away)
+  auto load = [&](long long j) {
+    if (2 * (j >> 1) < n1) return nodes[j];
+    return (j & 1) ? make_float4(0.f, 0.f, 0.f, 0.f) : make_float4(-1.0e18f, -1.0e18f, 0.f, 0.f);
+  };
+  float4 na = load(n0 + threadIdx.x), nb = load(n0 + PM_TS + threadIdx.x);
   for (long long t0 = n0; t0 < n1; t0 += PM_TILE) {
     __syncthreads();  // the previous tile is consumed
     tile[threadIdx.x] = na;
     tile[PM_TS + threadIdx.x] = nb;
     __syncthreads();
     const long long t1 = t0 + PM_TILE;
-    na = nb = pad;
-    if (t1 + threadIdx.x < n1) na = nodes[t1 + threadIdx.x];
-    if (t1 + PM_TS + threadIdx.x < n1) nb = nodes[t1 + PM_TS + threadIdx.x];
+    na = load(t1 + threadIdx.x);
+    nb = load(t1 + PM_TS + threadIdx.x);
     if (!active) continue;
     const int cnt = (int)min((long long)PM_TILE, n1 - t0);
     float2 g = make_float2(0.f, 0.f);
     for (int q = 0; q < cnt; q += 2) {  // an odd count reads the zero-mass pad
-      const float4 a = tile[q], b = tile[q + 1];
-      const float2 dx = __fadd2_rn(I0, make_float2(a.x, b.x));
-      const float2 dy = __fadd2_rn(J0, make_float2(a.y, b.y));
-      const float2 dz = __fadd2_rn(K0, make_float2(a.z, b.z));
+      const float4 a = tile[q], b = tile[q + 1];  // nodes q, q + 1 of the tile
+      const float2 dx = __fadd2_rn(I0, make_float2(a.x, a.y));
+      const float2 dy = __fadd2_rn(J0, make_float2(a.z, a.w));
+      const float2 dz = __fadd2_rn(K0, make_float2(b.x, b.y));
       float2 d2 = __fmul2_rn(dz, dz);
       d2 = __ffma2_rn(dy, dy, d2);
       d2 = __ffma2_rn(dx, dx, d2);
       const float2 rs = make_float2(pm_rsqrt_ftz(d2.x), pm_rsqrt_ftz(d2.y));
-      const float2 tw = __fmul2_rn(make_float2(a.w, b.w), dz);
+      const float2 tw = __fmul2_rn(make_float2(b.z, b.w), dz);
       g = __ffma2_rn(__fmul2_rn(tw, __fmul2_rn(rs, rs)), rs, g);
       if ((q & 30) == 30) {  // every 16 nodes
         acc.add(g.x + g.y);
@@ -371,7 +394,7 @@ size_t ztm_pointmass_ws(const PmParams& p, int precision, int num_sms) {
   size_t w = WsCarver::need((size_t)chunks * std::max(p.ns, 1) * sizeof(double));
   if (precision != ZTM_PREC_FP64) {  // the float node list
     const long long nb = std::max(1LL, (p.nnodes + PM_NB - 1) / PM_NB);
-    w += WsCarver::need((size_t)std::max(p.nnodes, 1LL) * sizeof(float4)) +
+    w += WsCarver::need((size_t)(std::max(p.nnodes, 1LL) + 2) * sizeof(float4)) +
          WsCarver::need((size_t)nb * sizeof(int)) + WsCarver::need(sizeof(int));
   }
   return w;
@@ -394,17 +417,18 @@ int ztm_launch_pointmass(ztm_ctx* c, const PmParams& p, const double* d_drho,
     } else {
       const long long nb = (p.nnodes + PM_NB - 1) / PM_NB;
       if (nb > (1LL << 31) - 1) return ztm_fail(c, ZTM_ERR_RANGE, "too many point-mass nodes");
-      float4* nodes = wc.take<float4>((size_t)p.nnodes);
+      float4* nodes = wc.take<float4>((size_t)p.nnodes + 2);  // + the pad of an odd count
       int* counts = wc.take<int>((size_t)nb);
       int* total = wc.take<int>(1);
       pm_nodes_count<<<(unsigned)nb, PM_NT, 0, c->stream>>>(p, d_drho, d_nn, counts, c->d_err);
       pm_nodes_scan<<<1, 1024, 0, c->stream>>>((int)nb, counts, total);
       pm_nodes_write<<<(unsigned)nb, PM_NT, 0, c->stream>>>(p, d_drho, d_nn, counts, nodes);
+      pm_nodes_pad<<<1, 1, 0, c->stream>>>(total, nodes);
       {
         ZtmProf prof_(c, "pointmass");
         pm_gather_f32_kernel<<<grid, PM_TS, 0, c->stream>>>(p, nodes, total, d_surf, len, partial);
       }
-      c->launches += 4;
+      c->launches += 5;
     }
   } else {
     chunks = 0;
