@@ -279,6 +279,24 @@ __device__ __forceinline__ void far_column(const float* col, int lmask, int nz8,
       g = make_float2(0.f, 0.f);
     }
   }
+  // unmasked groups: singly up to a 32-layer boundary, four at a time over
+  // whole 32-layer blocks (one loop test and one compensation per block),
+  // singly after
+  for (; l0 < nz8 && (l0 & 31); l0 += 8, fl += 8.f) {
+    g = far_group<T2, false>(col, l0, fl, Zb, zstep, cp2, c2t, elo, espan, nz, g);
+    if ((l0 & 24) == 24) {
+      acc.add(g.x + g.y);
+      g = make_float2(0.f, 0.f);
+    }
+  }
+  for (; l0 + 32 <= nz8; l0 += 32, fl += 32.f) {
+    g = far_group<T2, false>(col, l0, fl, Zb, zstep, cp2, c2t, elo, espan, nz, g);
+    g = far_group<T2, false>(col, l0 + 8, fl + 8.f, Zb, zstep, cp2, c2t, elo, espan, nz, g);
+    g = far_group<T2, false>(col, l0 + 16, fl + 16.f, Zb, zstep, cp2, c2t, elo, espan, nz, g);
+    g = far_group<T2, false>(col, l0 + 24, fl + 24.f, Zb, zstep, cp2, c2t, elo, espan, nz, g);
+    acc.add(g.x + g.y);
+    g = make_float2(0.f, 0.f);
+  }
   for (; l0 < nz8; l0 += 8, fl += 8.f) {
     g = far_group<T2, false>(col, l0, fl, Zb, zstep, cp2, c2t, elo, espan, nz, g);
     if ((l0 & 24) == 24) {
