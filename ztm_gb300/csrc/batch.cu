@@ -115,6 +115,7 @@ __device__ __forceinline__ void far_column(const float* __restrict__ col, const 
   float2 g[W == 1 ? 1 : W / 2];
 #pragma unroll
   for (int m = 0; m < (W == 1 ? 1 : W / 2); m++) g[m] = make_float2(0.f, 0.f);
+#pragma unroll 4
   for (int l0 = 0; l0 < k.nz; l0 += 8, zf += 8.f) {
     const float Zg = fmaf(zf, k.dzn, ez);
     const float2 zg2 = make_float2(Zg, Zg);

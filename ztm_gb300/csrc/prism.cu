@@ -279,15 +279,29 @@ __device__ __forceinline__ void far_column(const float* col, int lmask, int nz8,
       g = make_float2(0.f, 0.f);
     }
   }
-  // unmasked groups: singly up to a 32-layer boundary, four at a time over
-  // whole 32-layer blocks (one loop test and one compensation per block),
-  // singly after
+  // unmasked groups: singly up to a 32-layer boundary, then eight at a time
+  // over whole 64-layer blocks and four at a time over a 32-layer block (one
+  // loop test per block, one compensation per 32 layers), singly after
   for (; l0 < nz8 && (l0 & 31); l0 += 8, fl += 8.f) {
     g = far_group<T2, false>(col, l0, fl, Zb, zstep, cp2, c2t, elo, espan, nz, g);
     if ((l0 & 24) == 24) {
       acc.add(g.x + g.y);
       g = make_float2(0.f, 0.f);
     }
+  }
+  for (; l0 + 64 <= nz8; l0 += 64, fl += 64.f) {
+    g = far_group<T2, false>(col, l0, fl, Zb, zstep, cp2, c2t, elo, espan, nz, g);
+    g = far_group<T2, false>(col, l0 + 8, fl + 8.f, Zb, zstep, cp2, c2t, elo, espan, nz, g);
+    g = far_group<T2, false>(col, l0 + 16, fl + 16.f, Zb, zstep, cp2, c2t, elo, espan, nz, g);
+    g = far_group<T2, false>(col, l0 + 24, fl + 24.f, Zb, zstep, cp2, c2t, elo, espan, nz, g);
+    acc.add(g.x + g.y);
+    g = far_group<T2, false>(col, l0 + 32, fl + 32.f, Zb, zstep, cp2, c2t, elo, espan, nz,
+                             make_float2(0.f, 0.f));
+    g = far_group<T2, false>(col, l0 + 40, fl + 40.f, Zb, zstep, cp2, c2t, elo, espan, nz, g);
+    g = far_group<T2, false>(col, l0 + 48, fl + 48.f, Zb, zstep, cp2, c2t, elo, espan, nz, g);
+    g = far_group<T2, false>(col, l0 + 56, fl + 56.f, Zb, zstep, cp2, c2t, elo, espan, nz, g);
+    acc.add(g.x + g.y);
+    g = make_float2(0.f, 0.f);
   }
   for (; l0 + 32 <= nz8; l0 += 32, fl += 32.f) {
     g = far_group<T2, false>(col, l0, fl, Zb, zstep, cp2, c2t, elo, espan, nz, g);
