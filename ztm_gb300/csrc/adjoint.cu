@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(ADJ_TS, 6)
         const float4 hf = s_h[q];
         const float X = fmaf(hf.x - fix, k.dxn, f.x);
         const float Y = fmaf(hf.y - fiy, k.dyn, f.y);
-        const ColPoly cp = col_poly(X, Y, fc);
+        const float X2 = X * X, Y2 = Y * Y, rh = X2 + Y2;
         const int4 b = s_b[q];
         bool ncl = ix >= b.x && ix <= b.y && iy >= b.z && iy <= b.w;
         int elo = k.nz;
@@ -116,19 +116,25 @@ __global__ void __launch_bounds__(ADJ_TS, 6)
           }
         }
         const float Zg = fmaf(fl0 - hf.z, k.dzn, f.z);
-        const ColPoly2 cp2 = col_poly2(cp, fc.a1);
         const float2 zg2 = make_float2(Zg, Zg);
         const float2 w2 = make_float2(s_r[q], s_r[q]);
         float2 v[ADJ_LG / 2];
         // the warp's columns all far enough for the second-order form (the
-        // lanes of a warp share the station, so this is mostly uniform)
-        if (__all_sync(__activemask(), cp.rh >= k.rh_t2)) {
-          const float2 c2t = make_float2(cp.C2 - fc.h2, cp.C2 - fc.h2);
+        // lanes of a warp share the station, so this is mostly uniform),
+        // which needs only C2t = a0 - a1 rh of the column polynomial
+        if (__all_sync(__activemask(), rh >= k.rh_t2)) {
+          const float c2 = fmaf(-fc.a1, rh, fmaf(X2, fc.cA, Y2 * fc.cB));
+          const float2 c2t = make_float2(c2, c2);
+          ColPoly2 cp2;
+          cp2.rh = make_float2(rh, rh);
+          cp2.a1 = make_float2(fc.a1, fc.a1);
+          cp2.C2 = cp2.C3 = cp2.C4 = make_float2(0.f, 0.f);  // unused by the form
 #pragma unroll
           for (int j = 0; j < ADJ_LG / 2; j++)
             v[j] = far_unit2_t2(
                 __ffma2_rn(make_float2((float)(2 * j), (float)(2 * j + 1)), dz2, zg2), cp2, c2t);
         } else {
+          const ColPoly2 cp2 = col_poly2(col_poly(X, Y, fc), fc.a1);
 #pragma unroll
           for (int j = 0; j < ADJ_LG / 2; j++)
             v[j] = far_unit2(
