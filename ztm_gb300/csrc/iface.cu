@@ -304,7 +304,7 @@ __global__ void __launch_bounds__(IF_TS, 8)
     if (!active) continue;
     const int cnt = min(IF_TILE, c1 - t0);
     float2 g = make_float2(0.f, 0.f);  // plain sums over 32 columns, Kahan across
-#pragma unroll 2
+#pragma unroll 4
     for (int q = 0; q < cnt; q += 2) {
       // columns q and q+1 (the second is dropped past the end of the tile)
       const float2 nx2 = *reinterpret_cast<const float2*>(s_nx + q);
@@ -467,7 +467,7 @@ __global__ void __launch_bounds__(IF_TS, 8)
     if (!active) continue;
     const int cnt = min(IF_TILE, s1 - t0);
     float2 gr = make_float2(0.f, 0.f), gd = make_float2(0.f, 0.f);  // 32 stations, Kahan across
-#pragma unroll 2
+#pragma unroll 4
     for (int q = 0; q < cnt; q += 2) {
       // stations q and q+1 (the second is dropped past the end of the tile)
       const float2 hx = *reinterpret_cast<const float2*>(s_hx + q);
