@@ -107,7 +107,7 @@ def read_traffic():
     return None
 
 
-def cpu_baseline_prism(mesh, rho, st, nsample=48):
+def cpu_baseline_prism(mesh, rho, st, nsample=224):
     import numpy as np
     import oracle
     idx = np.linspace(0, len(st) - 1, nsample).astype(int)

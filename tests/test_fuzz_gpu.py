@@ -95,3 +95,21 @@ def test_random_interfaces_mixed_vs_double(ctx, seed):
     gr64, gd64 = ctx.interface_adjoint(im, depth, rho, st, r, precision="fp64")
     grm, gdm = ctx.interface_adjoint(im, depth, rho, st, r, precision="mixed")
     assert rel_err(grm, gr64) <= 1e-5 and rel_err(gdm, gd64) <= 1e-5
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_station_order_does_not_change_the_fields(ctx, seed):
+    """The forwards compute the stations in Z order of their home cells, so a
+    permuted station list gives the permuted field.  Only stations that share
+    a home cell can land in other warps, where a warp vote may pick the other
+    far-field form: the tolerance is the second-order form's truncation."""
+    mesh, rho, st, rng = _case(200 + seed)
+    perm = rng.permutation(len(st))
+    out = ctx.prism(mesh, rho, st, precision="mixed")
+    outp = ctx.prism(mesh, rho, st[perm], precision="mixed")
+    assert rel_err(outp, out[perm]) <= 1e-8
+    im, depth, rc, ist, rng = _icase(200 + seed)
+    perm = rng.permutation(len(ist))
+    out = ctx.interface(im, depth, rc, ist, precision="mixed")
+    outp = ctx.interface(im, depth, rc, ist[perm], precision="mixed")
+    assert rel_err(outp, out[perm]) <= 1e-8

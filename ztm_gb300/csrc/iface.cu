@@ -257,7 +257,8 @@ template <bool FACE>
 __global__ void __launch_bounds__(IF_TS, 8)
     iface_far_fwd(IConst k, int ns, const IStation* __restrict__ sf, const int2* __restrict__ si,
                   const float4* __restrict__ cf, const uint32_t* __restrict__ mask,
-                  const int* __restrict__ anynear, int chunk_len, double* __restrict__ partial) {
+                  const int* __restrict__ anynear, const int* __restrict__ perm, int chunk_len,
+                  double* __restrict__ partial) {
   // the tile's columns, one array per field so that a column pair is one
   // 8-byte load per field (weight, top depth, thickness, -ix, -iy)
   __shared__ __align__(8) float s_w[IF_TILE + 2];
@@ -265,8 +266,9 @@ __global__ void __launch_bounds__(IF_TS, 8)
   __shared__ __align__(8) float s_th[IF_TILE + 2];
   __shared__ __align__(8) float s_nx[IF_TILE + 2];  // -ix of the tile's columns
   __shared__ __align__(8) float s_ny[IF_TILE + 2];  // -iy
-  const int s = blockIdx.x * IF_TS + threadIdx.x;
-  const bool active = s < ns;
+  const int slot = blockIdx.x * IF_TS + threadIdx.x;  // stations in Z order
+  const bool active = slot < ns;
+  const int s = active ? perm[slot] : 0;
   IStation st = {0.f, 0.f, 0.f, 0.f};
   int2 hi = make_int2(0, 0);
   bool mine_near = false;
@@ -674,6 +676,8 @@ size_t ztm_iface_ws(const IMeshDesc& m, int ns, int precision, int num_sms) {
   w += 2 * WsCarver::need((size_t)std::max(ns, 1) * 4 * 64);
   // per-station "has a near column" flags (forward and adjoint)
   w += 2 * WsCarver::need((size_t)std::max(ns, 1) * 4);
+  // the forward's station order (and the sort's scratch), twice for slack
+  w += 2 * (WsCarver::need((size_t)std::max(ns, 1) * 4) + ztm_station_order_ws(ns, m.nx, m.ny));
   (void)precision;
   return w;
 }
@@ -713,6 +717,10 @@ static int iface_forward_impl(ztm_ctx* c, const IMeshDesc& m, const double* d_de
   double* near = wc.take<double>(ns);
   iface_station_prep<<<(ns + 127) / 128, 128, 0, c->stream>>>(m, k.L0, ns, d_sxyz, nullptr, sf,
                                                               si);
+  int* perm = wc.take<int>(ns);
+  if (int rc = ztm_station_order(c, c->stream, ns, reinterpret_cast<const int*>(si), 2, m.nx, m.ny,
+                                 perm, wc))
+    return rc;
   iface_col_prep<<<(unsigned)((nc + 255) / 256), 256, 0, c->stream>>>(m, k.L0, d_depth, d_rho,
                                                                    FACE ? d_vdep : nullptr, cf);
   uint32_t* mask = wc.take<uint32_t>((size_t)ns * k.words);
@@ -731,7 +739,7 @@ static int iface_forward_impl(ztm_ctx* c, const IMeshDesc& m, const double* d_de
   {
     ZtmProf prof_(c, "iface_far");
     iface_far_fwd<FACE><<<dim3(tiles, ch), IF_TS, 0, c->stream>>>(k, ns, sf, si, cf, mask,
-                                                                  anynear, len, partial);
+                                                                  anynear, perm, len, partial);
   }
   ztm_join(c);
   // the column integral is in units of L0 (x dx dy / L0^2), the face

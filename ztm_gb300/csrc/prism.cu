@@ -204,6 +204,7 @@ struct FarArgs {
   const float4* sf;
   const int4* si;
   const short2* iv;  // near-region intervals [station][box column]
+  const int* perm;   // station of each tile slot (Z order of the home cells)
   const float* rhoT;
   double* partial;  // [chunk][ns]
   int* err;
@@ -472,8 +473,9 @@ __global__ void __launch_bounds__(FAR_TS, 7) far_kernel(FarArgs a) {
     }
     const int f = far_index(item);
     const int tile = f % a.tiles, chunk = f / a.tiles;
-    const int s = tile * FAR_TS + threadIdx.x;
-    const bool active = s < a.ns;
+    const int slot = tile * FAR_TS + threadIdx.x;
+    const bool active = slot < a.ns;
+    const int s = active ? a.perm[slot] : 0;
     FarStation t = {0.f, 0.f, 0.f, 0, 0, 0, {1, 0, 1, 0, 1, 0}};
     if (active) {
       const float4 fv = a.sf[s];
@@ -800,7 +802,8 @@ size_t ztm_prism_ws(const MeshDesc& m, int ns, int precision, int num_sms, const
   for (const auto& sh : FAR_SHAPES)
     chunks = std::max(chunks, far_shape(k, ns, num_sms, o, sh[0], sh[1]).chunks);
   return WsCarver::need(sizeof(int)) + WsCarver::need((size_t)k.ncols * k.nzp * 4) +
-         WsCarver::need((size_t)ns * 16) * 2 +
+         WsCarver::need((size_t)ns * 16) * 2 + WsCarver::need((size_t)ns * 4) +
+         ztm_station_order_ws(ns, m.nx, m.ny) +
          WsCarver::need((size_t)ns * 8) + WsCarver::need((size_t)chunks * ns * 8) +
          WsCarver::need((size_t)ns * k.nslots * 4) + WsCarver::need((size_t)ns * 8);
 }
@@ -851,9 +854,14 @@ int ztm_launch_prism(ztm_ctx* c, const MeshDesc& m, const double* d_rho, int ns,
   int2* lr = wc.take<int2>(ns);
   launch_mesh_transpose(c, k, 1, d_rho, rhoT);
   launch_mesh_station_prep(c, m, k.L0, ns, d_sxyz, sf, si);
+  int* perm = wc.take<int>(ns);
+  if (int rc = ztm_station_order(c, c->stream, ns, reinterpret_cast<const int*>(si), 4, m.nx, m.ny,
+                                 perm, wc))
+    return rc;
   launch_mesh_near_iv(c, k, m, ns, si, d_sxyz, iv, lr);
   FarArgs a;
   a.k = k; a.ns = ns; a.sf = sf; a.si = si; a.iv = iv; a.rhoT = rhoT; a.partial = partial;
+  a.perm = perm;
   a.err = c->d_err;
   a.counter = counter;
   a.n_near = (ns + FAR_NEAR_ST - 1) / FAR_NEAR_ST;

@@ -118,6 +118,14 @@ int ztm_pm_setup(ztm_ctx* c, const ztm_grid* g, PmParams* p);
 int ztm_finish(ztm_ctx* c, bool dev, void* host_out, const void* dev_out, size_t bytes,
                const char* what);
 
+// Z-order permutation of the stations by home cell (order.cu): perm[slot]
+// is the station a one-station-per-thread kernel computes in that slot.  si
+// holds `stride` ints per station, the home cell's x and y first, on an
+// nx x ny mesh.  Runs on `stream` (the context's stream or its side stream).
+size_t ztm_station_order_ws(int ns, int nx, int ny);
+int ztm_station_order(ztm_ctx* c, cudaStream_t stream, int ns, const int* si, int stride, int nx,
+                      int ny, int* perm, WsCarver& wc);
+
 struct MeshDesc {
   int nx, ny, nz;
   double x0, y0, zt, dx, dy, dz;
