@@ -43,6 +43,7 @@ struct BJob {
   double far_scale, G5;
   const float4* sf;
   const int4* si;
+  const int* perm;       // station of each tile slot (Z order of the home cells)
   const float* rhoT;     // [group][column][layer][mgw] float densities
   const double* rho;     // nmodels x np (layer-major, as given)
   const double* sxyz;
@@ -176,8 +177,9 @@ __device__ void tile_done(const BJob& J, int tile, int expected, int* s_flag) {
   __syncthreads();
   if (!*s_flag) return;
   __threadfence();
-  const int s = tile * B_TS + threadIdx.x;
-  if (s >= J.ns) return;
+  const int slot = tile * B_TS + threadIdx.x;
+  if (slot >= J.ns) return;
+  const int s = J.perm[slot];
   for (int md = 0; md < J.nmodels; md++) {
     const double* pp = J.partial + (size_t)md * J.chunks * J.ns;
     double f = 0.0;
@@ -198,8 +200,9 @@ __device__ void near_item(const BJob& J, int tile, double* phi_all, int phi_cap,
   const long long plane = (long long)m.nx * m.ny;
   const long long np = plane * m.nz;
   for (int j = warp; j < B_TS; j += B_WARPS) {
-    const int s = tile * B_TS + j;
-    if (s >= J.ns) break;
+    const int slot = tile * B_TS + j;
+    if (slot >= J.ns) break;
+    const int s = J.perm[slot];
     const NearBox b = near_box(J.si[s], J.k);
     const double xs = J.sxyz[3 * s], ys = J.sxyz[3 * s + 1], zs = J.sxyz[3 * s + 2];
     const int nvx = b.x1 - b.x0 + 2, nvy = b.y1 - b.y0 + 2, nvz = b.l1 - b.l0 + 2;
@@ -289,8 +292,9 @@ __global__ void __launch_bounds__(B_TS, 4) batch_kernel(BArgs a) {
     const int c0 = chunk * J.chunk_cols, c1 = min(k.ncols, c0 + J.chunk_cols);
     const int nst = (c1 - c0 + J.sc - 1) / J.sc;
     const int stage_floats = J.sc * k.nzp * J.mgw;
-    const int s = tile * B_TS + threadIdx.x;
-    const bool active = s < J.ns;
+    const int slot = tile * B_TS + threadIdx.x;
+    const bool active = slot < J.ns;
+    const int s = active ? J.perm[slot] : 0;
     float ex = 0.f, ey = 0.f, ez = 0.f;
     int ixs = 0, iys = 0, izs = 0;
     NearBox nb = {1, 0, 1, 0, 1, 0};
@@ -435,6 +439,7 @@ Plan plan(const ztm_job* jobs, int njobs, double near_q, int num_sms, int stage_
     ws += WsCarver::need((size_t)q.nmodels * J.chunks * q.ns * 8);
     ws += WsCarver::need((size_t)q.nmodels * q.ns * 8);
     ws += WsCarver::need((size_t)J.tiles * 4);
+    ws += WsCarver::need((size_t)q.ns * 4) + WsCarver::need(ztm_station_order_ws(q.ns, m.nx, m.ny));
     p.jobs.push_back(J);
   }
   for (auto& J : p.jobs) {
@@ -569,6 +574,7 @@ int batch_run(ztm_ctx* c, const ztm_job* jobs, int njobs, bool dev, double G, do
   double* phi = wc.take<double>(phi_elems);
   std::vector<const double*> rho_d(njobs), xyz_d(njobs);
   std::vector<double*> gz_d(njobs);
+  std::vector<char*> order_ws(njobs);  // each job's station-sort scratch
   for (int j = 0; j < njobs; j++) {
     const ztm_job& q = jobs[j];
     long long np = (long long)q.mesh.nx * q.mesh.ny * q.mesh.nz;
@@ -603,6 +609,8 @@ int batch_run(ztm_ctx* c, const ztm_job* jobs, int njobs, bool dev, double G, do
     J.partial = wc.take<double>((size_t)J.nmodels * J.chunks * J.ns);
     J.near = wc.take<double>((size_t)J.nmodels * J.ns);
     J.done = wc.take<int>(J.tiles);
+    J.perm = wc.take<int>(J.ns);
+    order_ws[j] = wc.take<char>(ztm_station_order_ws(J.ns, J.m.nx, J.m.ny));
   }
   // graph key: shapes and every pointer the graph bakes in
   std::vector<long long> key;
@@ -664,6 +672,10 @@ int batch_run(ztm_ctx* c, const ztm_job* jobs, int njobs, bool dev, double G, do
       }
       launch_mesh_station_prep(c, J.m, J.k.L0, J.ns, J.sxyz, const_cast<float4*>(J.sf),
                                const_cast<int4*>(J.si));
+      WsCarver ow(order_ws[j]);
+      if (!rc)
+        rc = ztm_station_order(c, c->stream, J.ns, reinterpret_cast<const int*>(J.si), 4, J.m.nx,
+                               J.m.ny, const_cast<int*>(J.perm), ow);
       cudaMemsetAsync(J.done, 0, sizeof(int) * J.tiles, c->stream);
     }
     cudaMemsetAsync(counter, 0, sizeof(int) * 16, c->stream);
@@ -673,6 +685,10 @@ int batch_run(ztm_ctx* c, const ztm_job* jobs, int njobs, bool dev, double G, do
     if (ce != cudaSuccess) {
       if (g) cudaGraphDestroy(g);
       return ztm_cuda_check(c, ce, "end graph capture");
+    }
+    if (rc) {  // a station sort failed to enqueue
+      cudaGraphDestroy(g);
+      return rc;
     }
     e.graph = g;
     if ((rc = ztm_cuda_check(c, cudaGraphInstantiate(&e.exec, g, 0), "instantiate batch graph"))) {
@@ -687,7 +703,7 @@ int batch_run(ztm_ctx* c, const ztm_job* jobs, int njobs, bool dev, double G, do
     rc = ztm_cuda_check(c, cudaGraphLaunch(entry->exec, c->stream), "launch batch graph");
   }
   if (rc) return rc;
-  c->launches += 1 + 2LL * njobs;
+  c->launches += 1 + 3LL * njobs;  // per job: transpose, station prep, sort key
   if (dev) return ZTM_OK;
   for (int j = 0; j < njobs; j++) {
     const ztm_job& q = jobs[j];
