@@ -10,7 +10,7 @@
 //   FP64 plain  thread per prism, stations streamed through shared memory,
 //               8-corner closed form in double; station chunks reduced in a
 //               fixed order.
-//   MIXED/FP32  far pairs: thread per (column, group of 16 layers) and
+//   MIXED/FP32  far pairs: thread per (column, group of 32 layers) and
 //               station slice, the column's horizontal offsets and polynomial
 //               computed once per station and the far-field expansion per
 //               layer in float (second order where the whole warp is far
@@ -31,18 +31,18 @@
 namespace {
 
 constexpr int ADJ_TS = 128;
-constexpr int ADJ_LG = 16;     // layers per thread in the far kernel
-constexpr int ADJ_STILE = 256; // stations per shared-memory tile
+constexpr int ADJ_LG = 32;     // layers per thread in the far kernel
+constexpr int ADJ_STILE = 128; // stations per shared-memory tile
 constexpr int ADJ_SGRP = 32;   // stations per float sum
 
 // grid.x covers ncols * ceil(nz/LG) threads.  g[p] = G5*L0*Vn * sum.
-// A thread sums its column's 16 layers over its block's slice of the
+// A thread sums its column's 32 layers over its block's slice of the
 // stations (grid.y): float over 32 stations (packed, two layers per lane
 // pair), then double in shared memory, then one double atomic per layer into
 // g (zeroed before the launch).
 // The per-(station, column) setup (offsets, the horizontal polynomial, the
-// near box test) is shared by the 16 layers.
-__global__ void __launch_bounds__(ADJ_TS, 6)
+// near box test) is shared by the 32 layers.
+__global__ void __launch_bounds__(ADJ_TS, 5)
     adj_far_kernel(MeshConst k, int ns, const float4* __restrict__ sf,
                    const int4* __restrict__ si, const short2* __restrict__ iv,
                    const double* __restrict__ res, double scale, int slice,
