@@ -113,3 +113,23 @@ def test_station_order_does_not_change_the_fields(ctx, seed):
     out = ctx.interface(im, depth, rc, ist, precision="mixed")
     outp = ctx.interface(im, depth, rc, ist[perm], precision="mixed")
     assert rel_err(outp, out[perm]) <= 1e-8
+
+
+def test_stations_sharing_one_home_cell(ctx):
+    """Every station in one cell column (equal sort keys, one near box for
+    all), above and inside the mesh: the mixed forward and adjoint against
+    the double kernels."""
+    rng = np.random.default_rng(77)
+    mesh = ztm_gb300.make_mesh(40, 36, 20, 800.0, 900.0, 400.0)
+    rho = rng.normal(0.0, 250.0, 40 * 36 * 20)
+    ns = 500
+    x = mesh.x0 + 17 * 800.0 + rng.uniform(1.0, 799.0, ns)
+    y = mesh.y0 + 11 * 900.0 + rng.uniform(1.0, 899.0, ns)
+    z = np.where(rng.random(ns) < 0.5, mesh.z_top + rng.uniform(1.0, 2000.0, ns),
+                 mesh.z_top - rng.uniform(1.0, 7999.0, ns))
+    st = np.stack([x, y, z], 1)
+    ref = ctx.prism(mesh, rho, st, precision="fp64")
+    assert rel_err(ctx.prism(mesh, rho, st, precision="mixed"), ref) <= 1e-6
+    r = rng.normal(0.0, 1.0, ns)
+    assert rel_err(ctx.adjoint(mesh, st, r, precision="mixed"),
+                   ctx.adjoint(mesh, st, r, precision="fp64")) <= 1e-6
