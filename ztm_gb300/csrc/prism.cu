@@ -98,13 +98,32 @@ __global__ void __launch_bounds__(NEAR_IV_TS)
       const double hx = (m.x0 + (ix + 0.5) * m.dx) - xs;
       const double hy = (m.y0 + (iy + 0.5) * m.dy) - ys;
       const double h2 = hx * hx + hy * hy;
-      int lo = 1 << 30, hi = -1;
-      for (int l = b.l0; l <= b.l1; l++) {
+      // the predicate, in double; its layers form one interval holding the
+      // layer lc nearest the station's height (the distance is convex in l)
+      auto in = [&](int l) {
         const double hz = (m.zt - (l + 0.5) * m.dz) - zs;
-        if (h2 + hz * hz < k.R2) {  // one interval: the distance is convex in l
-          lo = min(lo, l);
-          hi = l;
+        return h2 + hz * hz < k.R2;
+      };
+      const int lc = clampi((int)floor((m.zt - zs) / m.dz), b.l0, b.l1);
+      int lo = 1 << 30, hi = -1;
+      if (in(lc)) {
+        // the interval's ends located in float, then settled in double
+        const float h2f = (float)h2, r2f = (float)k.R2, czf = (float)(m.zt - zs),
+                    dzf = (float)m.dz;
+        int flo = lc, fhi = lc;
+        for (int l = b.l0; l <= b.l1; l++) {
+          const float hz = fmaf(-((float)l + 0.5f), dzf, czf);
+          if (fmaf(hz, hz, h2f) < r2f) {
+            flo = min(flo, l);
+            fhi = max(fhi, l);
+          }
         }
+        lo = flo;
+        hi = fhi;
+        while (lo < lc && !in(lo)) lo++;
+        while (lo > b.l0 && in(lo - 1)) lo--;
+        while (hi > lc && !in(hi)) hi--;
+        while (hi < b.l1 && in(hi + 1)) hi++;
       }
       if (hi >= 0) {
         out = make_short2((short)lo, (short)hi);
