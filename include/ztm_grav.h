@@ -141,8 +141,9 @@ int ztm_ctx_sync(ztm_ctx* ctx);
  * the summed device time (ms) and launch count of the kernels whose name
  * contains `name` ("" = all), and clears the records.  Kernel names:
  * pointmass, prism_far (the mixed forward's far fields and near regions),
- * prism_f64, prism_list, adjoint_far,
- * adjoint_near, adjoint_f64, iface_far, iface_near, iface_f64, batch, density.
+ * prism_f64, prism_list, adjoint_far (the mixed adjoint's far fields and
+ * near regions), adjoint_f64, iface_far, iface_near, iface_f64, batch,
+ * density.
  * The reference's only timer is a host clock (zmath.cpp:265-268). */
 int ztm_ctx_profile(ztm_ctx* ctx, int enable);
 int ztm_ctx_profile_read(ztm_ctx* ctx, const char* name, double* ms,

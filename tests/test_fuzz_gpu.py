@@ -133,3 +133,18 @@ def test_stations_sharing_one_home_cell(ctx):
     r = rng.normal(0.0, 1.0, ns)
     assert rel_err(ctx.adjoint(mesh, st, r, precision="mixed"),
                    ctx.adjoint(mesh, st, r, precision="fp64")) <= 1e-6
+
+
+def test_many_stations_on_a_small_mesh(ctx):
+    """200,003 stations (1,563 station tiles, 6,251 near items, many equal
+    sort keys) over a 16x12x8 mesh: mixed against the double kernel."""
+    rng = np.random.default_rng(88)
+    mesh = ztm_gb300.make_mesh(16, 12, 8, 700.0, 600.0, 350.0, x0=-2000.0, y0=1000.0)
+    rho = rng.normal(0.0, 250.0, 16 * 12 * 8)
+    ns = 200_003
+    st = np.stack([rng.uniform(-4000.0, 11000.0, ns), rng.uniform(0.0, 9000.0, ns),
+                   rng.uniform(-2500.0, 1500.0, ns)], 1)
+    ref = ctx.prism(mesh, rho, st, precision="fp64")
+    out = ctx.prism(mesh, rho, st, precision="mixed")
+    assert np.all(np.isfinite(out))
+    assert rel_err(out, ref) <= 1e-6

@@ -17,10 +17,13 @@
 //               enough), float sums over 32 stations, double beyond; the
 //               slices meet in g_rho by double atomics.  Near pairs (prisms in
 //               the station's near region): one warp per station computes
-//               Phi once per vertex in shared memory, combines the 8 corners
-//               of each near prism and adds r[s]*U to g_rho with double
-//               atomics.  g_rho is zeroed first; the atomics make the last
-//               bits order-dependent.
+//               Phi once per vertex into its block's slice of a global
+//               scratch, combines the 8 corners of each near prism and adds
+//               r[s]*U to g_rho with double atomics.  Both are items of one
+//               persistent grid's work queue, the near items spread evenly
+//               among the far items, so that the near regions' FP64 work
+//               runs beside the far fields' FP32 work on every SM.  g_rho is
+//               zeroed first; the atomics make the last bits order-dependent.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -35,25 +38,49 @@ constexpr int ADJ_LG = 32;     // layers per thread in the far kernel
 constexpr int ADJ_STILE = 128; // stations per shared-memory tile
 constexpr int ADJ_SGRP = 32;   // stations per float sum
 
-// grid.x covers ncols * ceil(nz/LG) threads.  g[p] = G5*L0*Vn * sum.
-// A thread sums its column's 32 layers over its block's slice of the
-// stations (grid.y): float over 32 stations (packed, two layers per lane
-// pair), then double in shared memory, then one double atomic per layer into
-// g (zeroed before the launch).
-// The per-(station, column) setup (offsets, the horizontal polynomial, the
-// near box test) is shared by the 32 layers.
-__global__ void __launch_bounds__(ADJ_TS, 5)
-    adj_far_kernel(MeshConst k, int ns, const float4* __restrict__ sf,
-                   const int4* __restrict__ si, const short2* __restrict__ iv,
-                   const double* __restrict__ res, double scale, int slice,
-                   double* __restrict__ g) {
-  __shared__ float4 s_f[ADJ_STILE];
-  __shared__ int4 s_b[ADJ_STILE];  // the station's near box columns x0, x1, y0, y1
-  __shared__ float4 s_h[ADJ_STILE];  // the home cell indices as floats (exact)
-  __shared__ float s_r[ADJ_STILE];
-  __shared__ double s_acc[ADJ_LG][ADJ_TS];
+constexpr int ADJ_NEAR_ST = 8;  // stations per near item (two per warp)
+
+struct AdjArgs {
+  MeshConst k;
+  MeshDesc m;
+  int ns;
+  const float4* sf;
+  const int4* si;
+  const short2* iv;   // near-region intervals [station][box column]
+  const int2* lr;     // per-station near layer range
+  const double* sxyz;
+  const double* res;
+  double scale;       // G5 * L0 * Vn: far sums to gradient units
+  double G5;
+  int slice;          // stations per far item (a multiple of ADJ_STILE)
+  int tiles, slices;  // far items: column tiles x station slices
+  int n_near;         // near items (ADJ_NEAR_ST stations each)
+  int cap;            // near-box vertices per warp's scratch
+  double* phi;        // [grid][warps][cap] near-box vertex values
+  int* counter;       // next work item (zeroed before the launch)
+  double* g;
+};
+
+// Shared memory of a far item: a tile of stations and the double sums of
+// each thread's layers.
+struct AdjSmem {
+  float4 f[ADJ_STILE];
+  int4 b[ADJ_STILE];   // the station's near box columns x0, x1, y0, y1
+  float4 h[ADJ_STILE]; // the home cell indices as floats (exact)
+  float r[ADJ_STILE];
+  double acc[ADJ_LG][ADJ_TS];
+};
+
+// Far item (column tile bx, station slice by): thread per (column, group of
+// 32 layers), g[p] += G5*L0*Vn * sum.  A thread sums its column's 32 layers
+// over the slice's stations: float over 32 stations (packed, two layers per
+// lane pair), then double in shared memory, then one double atomic per
+// layer into g.  The per-(station, column) setup (offsets, the horizontal
+// polynomial, the near box test) is shared by the 32 layers.
+__device__ __forceinline__ void adj_far_item(const AdjArgs& a, int bx, int by, AdjSmem& sm) {
+  const MeshConst& k = a.k;
   const int ngroups = (k.nz + ADJ_LG - 1) / ADJ_LG;
-  const long long t = blockIdx.x * (long long)ADJ_TS + threadIdx.x;
+  const long long t = bx * (long long)ADJ_TS + threadIdx.x;
   const bool active = t < (long long)k.ncols * ngroups;
   int c = 0, lg = 0;
   if (active) {
@@ -65,26 +92,26 @@ __global__ void __launch_bounds__(ADJ_TS, 5)
   const float fix = (float)ix, fiy = (float)iy, fl0 = (float)l0;
   const FarCoef fc = k.fc;
 #pragma unroll
-  for (int j = 0; j < ADJ_LG; j++) s_acc[j][threadIdx.x] = 0.0;
+  for (int j = 0; j < ADJ_LG; j++) sm.acc[j][threadIdx.x] = 0.0;
   const float2 dz2 = make_float2(k.dzn, k.dzn);
-  // this block's slice of the stations (grid.y)
-  const int sb = blockIdx.y * slice, se = min(ns, sb + slice);
+  // this item's slice of the stations
+  const int sb = by * a.slice, se = min(a.ns, sb + a.slice);
   for (int s0 = sb; s0 < se; s0 += ADJ_STILE) {
     __syncthreads();
     for (int q = threadIdx.x; q < ADJ_STILE; q += ADJ_TS) {
       const int s = s0 + q;
       if (s < se) {
-        const int4 i = si[s];
+        const int4 i = a.si[s];
         const NearBox b = near_box(i, k);
-        s_f[q] = sf[s];
-        s_b[q] = make_int4(b.x0, b.x1, b.y0, b.y1);
-        s_h[q] = make_float4((float)i.x, (float)i.y, (float)i.z, 0.f);
-        s_r[q] = (float)res[s];
+        sm.f[q] = a.sf[s];
+        sm.b[q] = make_int4(b.x0, b.x1, b.y0, b.y1);
+        sm.h[q] = make_float4((float)i.x, (float)i.y, (float)i.z, 0.f);
+        sm.r[q] = (float)a.res[s];
       } else {
-        s_f[q] = make_float4(0.f, 0.f, 0.f, 0.f);
-        s_b[q] = make_int4(1, 0, 1, 0);
-        s_h[q] = make_float4(0.f, 0.f, 0.f, 0.f);
-        s_r[q] = 0.f;
+        sm.f[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+        sm.b[q] = make_int4(1, 0, 1, 0);
+        sm.h[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+        sm.r[q] = 0.f;
       }
     }
     __syncthreads();
@@ -96,18 +123,18 @@ __global__ void __launch_bounds__(ADJ_TS, 5)
       for (int j = 0; j < ADJ_LG / 2; j++) gs[j] = make_float2(0.f, 0.f);
       const int q1 = min(cnt, q0 + ADJ_SGRP);
       for (int q = q0; q < q1; q++) {
-        const float4 f = s_f[q];
-        const float4 hf = s_h[q];
+        const float4 f = sm.f[q];
+        const float4 hf = sm.h[q];
         const float X = fmaf(hf.x - fix, k.dxn, f.x);
         const float Y = fmaf(hf.y - fiy, k.dyn, f.y);
         const float X2 = X * X, Y2 = Y * Y, rh = X2 + Y2;
-        const int4 b = s_b[q];
+        const int4 b = sm.b[q];
         bool ncl = ix >= b.x && ix <= b.y && iy >= b.z && iy <= b.w;
         int elo = k.nz;
         unsigned espan = 0u;
         if (ncl) {  // the column's near-region layers for this station
           const short2 tv =
-              iv[(size_t)(s0 + q) * k.nslots + (ix - b.x) + (b.y - b.x + 1) * (iy - b.z)];
+              a.iv[(size_t)(s0 + q) * k.nslots + (ix - b.x) + (b.y - b.x + 1) * (iy - b.z)];
           if (tv.x <= tv.y) {
             elo = tv.x;
             espan = (unsigned)(tv.y - tv.x);
@@ -117,7 +144,7 @@ __global__ void __launch_bounds__(ADJ_TS, 5)
         }
         const float Zg = fmaf(fl0 - hf.z, k.dzn, f.z);
         const float2 zg2 = make_float2(Zg, Zg);
-        const float2 w2 = make_float2(s_r[q], s_r[q]);
+        const float2 w2 = make_float2(sm.r[q], sm.r[q]);
         float2 v[ADJ_LG / 2];
         // the warp's columns all far enough for the second-order form (the
         // lanes of a warp share the station, so this is mostly uniform),
@@ -151,12 +178,11 @@ __global__ void __launch_bounds__(ADJ_TS, 5)
 #pragma unroll
         for (int j = 0; j < ADJ_LG / 2; j++) gs[j] = __ffma2_rn(w2, v[j], gs[j]);
       }
-      // the group's float sums into the double accumulators (FP64 pipe,
-      // otherwise idle in this kernel)
+      // the group's float sums into the double accumulators (FP64 pipe)
 #pragma unroll
       for (int j = 0; j < ADJ_LG / 2; j++) {
-        s_acc[2 * j][threadIdx.x] += (double)gs[j].x;
-        s_acc[2 * j + 1][threadIdx.x] += (double)gs[j].y;
+        sm.acc[2 * j][threadIdx.x] += (double)gs[j].x;
+        sm.acc[2 * j + 1][threadIdx.x] += (double)gs[j].y;
       }
     }
   }
@@ -165,38 +191,33 @@ __global__ void __launch_bounds__(ADJ_TS, 5)
 #pragma unroll
   for (int j = 0; j < ADJ_LG; j++) {
     const int l = l0 + j;
-    if (l < k.nz) atomicAdd(&g[c + plane * l], scale * s_acc[j][threadIdx.x]);
+    if (l < k.nz) atomicAdd(&a.g[c + plane * l], a.scale * sm.acc[j][threadIdx.x]);
   }
 }
 
-// Near box, one warp per station: Phi at every box vertex into shared
-// memory, then per box prism the signed 8-corner sum, scaled by r[s], added
-// to g with double atomics.
+// Near region of station s, by one warp: Phi at every vertex of the near
+// box's layer range into the warp's scratch (phi, cap values), then per near
+// prism the signed 8-corner sum, scaled by r[s], added to g with double
+// atomics.
 template <typename T>
-__global__ void adj_near_kernel(MeshConst k, MeshDesc m, int ns, const double* __restrict__ sxyz,
-                                const int4* __restrict__ si, const short2* __restrict__ iv,
-                                const int2* __restrict__ lr, const double* __restrict__ res,
-                                double G5, int nv_cap, double* __restrict__ g) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  T* phi = reinterpret_cast<T*>(smem) + (size_t)warp * nv_cap;
-  const int s = blockIdx.x * (blockDim.x >> 5) + warp;
-  if (s >= ns) return;
-  const double r = res[s];
+__device__ __forceinline__ void adj_near_station(const AdjArgs& a, int s, T* phi, int lane) {
+  const MeshConst& k = a.k;
+  const MeshDesc& m = a.m;
+  const double r = a.res[s];
   if (r == 0.0) return;
-  const int2 L = lr[s];
+  const int2 L = a.lr[s];
   if (L.x > L.y) return;  // no near prism
-  const NearBox b = near_box(si[s], k);
-  const short2* ivs = iv + (size_t)s * k.nslots;
-  const double xs = sxyz[3 * s], ys = sxyz[3 * s + 1], zs = sxyz[3 * s + 2];
+  const NearBox b = near_box(a.si[s], k);
+  const short2* ivs = a.iv + (size_t)s * k.nslots;
+  const double xs = a.sxyz[3 * s], ys = a.sxyz[3 * s + 1], zs = a.sxyz[3 * s + 2];
   const int nvx = b.x1 - b.x0 + 2, nvy = b.y1 - b.y0 + 2, nvz = L.y - L.x + 2;
   const int nv = nvx * nvy * nvz;
-  if (nv > nv_cap) return;  // the host sizes nv_cap for the largest box
+  if (nv > a.cap) return;  // the host sizes cap for the largest box
   for (int v = lane; v < nv; v += 32) {
-    const int a = b.x0 + v % nvx;
-    const int bb = b.y0 + (v / nvx) % nvy;
+    const int ax = b.x0 + v % nvx;
+    const int ay = b.y0 + (v / nvx) % nvy;
     const int cz = L.x + v / (nvx * nvy);
-    phi[v] = ztm_phi<T>((T)((m.x0 + a * m.dx) - xs), (T)((m.y0 + bb * m.dy) - ys),
+    phi[v] = ztm_phi<T>((T)((m.x0 + ax * m.dx) - xs), (T)((m.y0 + ay * m.dy) - ys),
                         (T)((m.zt - cz * m.dz) - zs));
   }
   __syncwarp();
@@ -216,7 +237,42 @@ __global__ void adj_near_kernel(MeshConst k, MeshDesc m, int ns, const double* _
     T u = P(1, 1, 0) - P(0, 1, 0) - P(1, 0, 0) + P(0, 0, 0) - P(1, 1, 1) + P(0, 1, 1) + P(1, 0, 1) -
           P(0, 0, 1);
     const long long p = ix + (long long)m.nx * iy + plane * l;
-    atomicAdd(&g[p], G5 * r * (double)u);
+    atomicAdd(&a.g[p], a.G5 * r * (double)u);
+  }
+  __syncwarp();  // the scratch is rewritten by the warp's next station
+}
+
+// Persistent kernel of the mixed adjoint: tiles x slices far items and
+// n_near near items (ADJ_NEAR_ST stations, a warp per station) taken from a
+// counter, the near items at evenly spaced queue positions.  The grid is the
+// number of blocks resident at once.  T: the near regions' type (double for
+// the mixed method, float for the FP32 method).
+template <typename T>
+__global__ void __launch_bounds__(ADJ_TS, 5) adj_kernel(AdjArgs a) {
+  __shared__ AdjSmem sm;
+  __shared__ int s_item;
+  const int n_far = a.tiles * a.slices;
+  const int n_items = n_far + a.n_near;
+  // queue position i: near iff floor((i+1) n_near / n) > floor(i n_near / n)
+  auto near_before = [&](int i) { return (int)((long long)i * a.n_near / n_items); };
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  T* phi = reinterpret_cast<T*>(a.phi + ((size_t)blockIdx.x * (ADJ_TS / 32) + warp) * a.cap);
+  for (;;) {
+    __syncthreads();  // the previous item is done with s_item and the tiles
+    if (threadIdx.x == 0) s_item = atomicAdd(a.counter, 1);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= n_items) break;
+    const int nb = near_before(item);
+    if (near_before(item + 1) > nb) {
+      for (int j = warp; j < ADJ_NEAR_ST; j += ADJ_TS / 32) {
+        const int s = nb * ADJ_NEAR_ST + j;
+        if (s < a.ns) adj_near_station<T>(a, s, phi, lane);
+      }
+      continue;
+    }
+    const int f = item - nb;
+    adj_far_item(a, f % a.tiles, f / a.tiles, sm);
   }
 }
 
@@ -288,6 +344,21 @@ int near_cap(const MeshConst& k) {
          (std::min(2 * k.wl + 1, k.nz) + 1);
 }
 
+// Blocks of the persistent adjoint kernel resident at once (its grid); the
+// larger of the two near-region types, which sizes the vertex scratch.
+int adj_grid(int num_sms, bool f64) {
+  int occ = 0;
+  const cudaError_t e =
+      f64 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, adj_kernel<double>, ADJ_TS, 0)
+          : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, adj_kernel<float>, ADJ_TS, 0);
+  if (e != cudaSuccess || occ < 1) {
+    cudaGetLastError();
+    occ = 1;
+  }
+  return occ * std::max(num_sms, 1);
+}
+int adj_grid_max(int num_sms) { return std::max(adj_grid(num_sms, true), adj_grid(num_sms, false)); }
+
 }  // namespace
 
 size_t ztm_adjoint_ws(const MeshDesc& m, int ns, int precision, int num_sms, double near_q) {
@@ -300,7 +371,8 @@ size_t ztm_adjoint_ws(const MeshDesc& m, int ns, int precision, int num_sms, dou
   const MeshConst k = make_mesh_const(m, near_q > 0 ? near_q : 6.0);
   return 2 * WsCarver::need((size_t)std::max(ns, 1) * 16) +
          WsCarver::need((size_t)std::max(ns, 1) * k.nslots * 4) +
-         WsCarver::need((size_t)std::max(ns, 1) * 8);
+         WsCarver::need((size_t)std::max(ns, 1) * 8) + WsCarver::need(64) +
+         WsCarver::need((size_t)adj_grid_max(num_sms) * (ADJ_TS / 32) * near_cap(k) * 8);
 }
 
 int ztm_launch_adjoint(ztm_ctx* c, const MeshDesc& m, int ns, const double* d_sxyz,
@@ -337,59 +409,53 @@ int ztm_launch_adjoint(ztm_ctx* c, const MeshDesc& m, int ns, const double* d_sx
   const int ngroups = (k.nz + ADJ_LG - 1) / ADJ_LG;
   const long long threads = (long long)k.ncols * ngroups;
   const double scale = G5 * k.L0 * (double)k.dxn * k.dyn * k.dzn;
-  // station slices (grid.y) so that the grid is many waves of resident
-  // blocks; the slices' sums meet in g by double atomics (g zeroed first)
-  const long long blocks = (threads + ADJ_TS - 1) / ADJ_TS;
-  int occ = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, adj_far_kernel, ADJ_TS, 0) !=
-          cudaSuccess ||
-      occ < 1) {
-    cudaGetLastError();
-    occ = 1;
-  }
-  const long long resident = (long long)occ * c->num_sms;
-  long long slices = std::max(1LL, (8 * resident + blocks - 1) / blocks);
+  const int cap = near_cap(k);
+  if ((size_t)cap * 8 > 200 * 1024)
+    return ztm_fail(c, ZTM_ERR_RANGE, "near_q too large for the adjoint's near box");
+  const bool f64 = precision == ZTM_PREC_MIXED;
+  // station slices so that there are about eight far items per resident
+  // block; the slices' sums meet in g by double atomics (g zeroed first)
+  const long long tiles = (threads + ADJ_TS - 1) / ADJ_TS;
+  const int grid = adj_grid(c->num_sms, f64);
+  long long slices = std::max(1LL, (8LL * grid + tiles - 1) / tiles);
   slices = std::min(slices, std::max(1LL, (long long)(ns + ADJ_STILE - 1) / ADJ_STILE));
-  slices = std::min(slices, 65535LL);
   int slice = (int)((ns + slices - 1) / slices);
   slice = ((slice + ADJ_STILE - 1) / ADJ_STILE) * ADJ_STILE;
   slices = (ns + slice - 1) / slice;
+  if (tiles * slices + (ns + ADJ_NEAR_ST - 1) / ADJ_NEAR_ST > 2147483647LL)
+    return ztm_fail(c, ZTM_ERR_RANGE, "mixed adjoint: too many work items");
+  int* counter = wc.take<int>(16);
+  double* phi = wc.take<double>((size_t)adj_grid_max(c->num_sms) * (ADJ_TS / 32) * cap);
+  AdjArgs a;
+  a.k = k;
+  a.m = m;
+  a.ns = ns;
+  a.sf = sf;
+  a.si = si;
+  a.iv = iv;
+  a.lr = lr;
+  a.sxyz = d_sxyz;
+  a.res = d_res;
+  a.scale = scale;
+  a.G5 = G5;
+  a.slice = slice;
+  a.tiles = (int)tiles;
+  a.slices = (int)slices;
+  a.n_near = (ns + ADJ_NEAR_ST - 1) / ADJ_NEAR_ST;
+  a.cap = cap;
+  a.phi = phi;
+  a.counter = counter;
+  a.g = d_g;
   cudaMemsetAsync(d_g, 0, (size_t)k.ncols * k.nz * sizeof(double), c->stream);
-  const int cap = near_cap(k);
-  const bool f64 = precision == ZTM_PREC_MIXED;
-  const size_t per_warp = (size_t)cap * (f64 ? 8 : 4);
-  if (per_warp > 200 * 1024)
-    return ztm_fail(c, ZTM_ERR_RANGE, "near_q too large for the adjoint's near box");
-  int wpb = (int)std::max<size_t>(1, std::min<size_t>(4, (96 * 1024) / per_warp));
-  size_t smem = per_warp * wpb;
-  // Both kernels add into the zeroed g with double atomics, so the near
-  // regions (FP64 pipe) run on the side stream beside the far field (FMA
-  // pipe); the side stream's priority places their blocks first as far
-  // blocks retire.
-  ztm_fork(c);
-  if (f64) {
-    cudaFuncSetAttribute(adj_near_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)std::max<size_t>(smem, 48 * 1024));
-    {
-      ZtmProf prof_(c, "adjoint_near", c->aux);
-      adj_near_kernel<double><<<(ns + wpb - 1) / wpb, wpb * 32, smem, c->aux>>>(
-          k, m, ns, d_sxyz, si, iv, lr, d_res, G5, cap, d_g);
-    }
-  } else {
-    cudaFuncSetAttribute(adj_near_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)std::max<size_t>(smem, 48 * 1024));
-    {
-      ZtmProf prof_(c, "adjoint_near", c->aux);
-      adj_near_kernel<float><<<(ns + wpb - 1) / wpb, wpb * 32, smem, c->aux>>>(
-          k, m, ns, d_sxyz, si, iv, lr, d_res, G5, cap, d_g);
-    }
-  }
+  cudaMemsetAsync(counter, 0, sizeof(int), c->stream);
+  // far fields (FMA pipe) and near regions (FP64 pipe) in one persistent grid
   {
     ZtmProf prof_(c, "adjoint_far");
-    adj_far_kernel<<<dim3((unsigned)blocks, (unsigned)slices), ADJ_TS, 0, c->stream>>>(
-        k, ns, sf, si, iv, d_res, scale, slice, d_g);
+    if (f64)
+      adj_kernel<double><<<grid, ADJ_TS, 0, c->stream>>>(a);
+    else
+      adj_kernel<float><<<grid, ADJ_TS, 0, c->stream>>>(a);
   }
-  ztm_join(c);
-  c->launches += 2;
+  c->launches += 1;
   return ztm_after_launch(c, "adjoint mixed kernels");
 }
