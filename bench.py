@@ -424,7 +424,7 @@ def other_workloads(ctx):
     ctx.sync()
     res["batched_32_trials_plus_16_meshes"] = {
         "model_pairs": mp, "ms": ms_b, "model_pair_evals_per_s": mp / (ms_b * 1e-3),
-        "launches_per_call": "1 graph: 3 prep kernels and a library station sort per job + 1 persistent kernel",
+        "launches_per_call": "1 graph: 4 prep kernels and a library station sort per job + 1 persistent kernel",
         "rel_err_trial5_vs_single_call": err(outs[0][5], one)}
     # inversion workload: 512x512 columns, 256x256 stations, 20 L-BFGS iterations
     im5, dep5, rho5, st5, start5 = synth.moho_columns_512()

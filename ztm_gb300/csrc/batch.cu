@@ -44,6 +44,8 @@ struct BJob {
   const float4* sf;
   const int4* si;
   const int* perm;       // station of each tile slot (Z order of the home cells)
+  const short2* iv;      // near-region intervals [station][box column]
+  const int2* lr;        // per-station near layer range
   const float* rhoT;     // [group][column][layer][mgw] float densities
   const double* rho;     // nmodels x np (layer-major, as given)
   const double* sxyz;
@@ -189,6 +191,10 @@ __device__ void tile_done(const BJob& J, int tile, int expected, int* s_flag) {
   }
 }
 
+// Near regions of a tile's stations, a warp per station: Phi once per
+// vertex adjacent to a near-region prism into the warp's scratch, then per
+// model the signed triple difference of the region's densities around each
+// vertex times its Phi.
 __device__ void near_item(const BJob& J, int tile, double* phi_all, int phi_cap, int* err) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double* phi = phi_all + (size_t)warp * phi_cap;
@@ -203,35 +209,60 @@ __device__ void near_item(const BJob& J, int tile, double* phi_all, int phi_cap,
     const int slot = tile * B_TS + j;
     if (slot >= J.ns) break;
     const int s = J.perm[slot];
+    const int2 L = J.lr[s];
+    if (L.x > L.y) {  // no near prism
+      for (int md = lane; md < J.nmodels; md += 32) J.near[(size_t)md * J.ns + s] = 0.0;
+      continue;
+    }
     const NearBox b = near_box(J.si[s], J.k);
+    const short2* ivs = J.iv + (size_t)s * J.k.nslots;
     const double xs = J.sxyz[3 * s], ys = J.sxyz[3 * s + 1], zs = J.sxyz[3 * s + 2];
-    const int nvx = b.x1 - b.x0 + 2, nvy = b.y1 - b.y0 + 2, nvz = b.l1 - b.l0 + 2;
+    const int nvx = b.x1 - b.x0 + 2, nvy = b.y1 - b.y0 + 2, nvz = L.y - L.x + 2;
     const int nv = min(nvx * nvy * nvz, J.nv_cap);
+    // the near-region prisms around vertex (a, bb, cz): ix = a - 1 + da,
+    // iy = bb - 1 + db, l = cz - 1 + dc; bit (da, db, dc) set when in the region
+    auto members = [&](int a, int bb, int cz) {
+      unsigned bits = 0u;
+#pragma unroll
+      for (int da = 0; da < 2; da++) {
+        const int ix = a - 1 + da;
+        if (ix < b.x0 || ix > b.x1) continue;
+#pragma unroll
+        for (int db = 0; db < 2; db++) {
+          const int iy = bb - 1 + db;
+          if (iy < b.y0 || iy > b.y1) continue;
+          const short2 t = ivs[near_slot(b, ix, iy)];
+#pragma unroll
+          for (int dc = 0; dc < 2; dc++) {
+            const int l = cz - 1 + dc;
+            if (l >= t.x && l <= t.y) bits |= 1u << (da * 4 + db * 2 + dc);
+          }
+        }
+      }
+      return bits;
+    };
     for (int v = lane; v < nv; v += 32) {
-      const int a = b.x0 + v % nvx, bb = b.y0 + (v / nvx) % nvy, cz = b.l0 + v / (nvx * nvy);
-      phi[v] = ztm_phi<double>((m.x0 + a * m.dx) - xs, (m.y0 + bb * m.dy) - ys,
-                               (m.zt - cz * m.dz) - zs);
+      const int a = b.x0 + v % nvx, bb = b.y0 + (v / nvx) % nvy, cz = L.x + v / (nvx * nvy);
+      phi[v] = members(a, bb, cz) ? ztm_phi<double>((m.x0 + a * m.dx) - xs,
+                                                    (m.y0 + bb * m.dy) - ys,
+                                                    (m.zt - cz * m.dz) - zs)
+                                  : 0.0;
     }
     __syncwarp();
     for (int md = 0; md < J.nmodels; md++) {
       const double* rho = J.rho + (size_t)md * np;
       double acc = 0.0;
       for (int v = lane; v < nv; v += 32) {
-        const int a = b.x0 + v % nvx, bb = b.y0 + (v / nvx) % nvy, cz = b.l0 + v / (nvx * nvy);
+        const int a = b.x0 + v % nvx, bb = b.y0 + (v / nvx) % nvy, cz = L.x + v / (nvx * nvy);
+        const unsigned bits = members(a, bb, cz);
+        if (!bits) continue;
         double D = 0.0;
-        for (int da = 0; da < 2; da++) {
-          const int ix = a - 1 + da;
-          if (ix < b.x0 || ix > b.x1) continue;
-          for (int db = 0; db < 2; db++) {
-            const int iy = bb - 1 + db;
-            if (iy < b.y0 || iy > b.y1) continue;
-            for (int dc = 0; dc < 2; dc++) {
-              const int l = cz - 1 + dc;
-              if (l < b.l0 || l > b.l1) continue;
-              const double r = rho[ix + (long long)m.nx * iy + plane * l];
-              D += ((da == 1) ^ (db == 1) ^ (dc == 0)) ? -r : r;
-            }
-          }
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          if (!(bits & (1u << q))) continue;
+          const int da = q >> 2, db = (q >> 1) & 1, dc = q & 1;
+          const double r = rho[(a - 1 + da) + (long long)m.nx * (bb - 1 + db) + plane * (cz - 1 + dc)];
+          D += ((da == 1) ^ (db == 1) ^ (dc == 0)) ? -r : r;
         }
         acc += D * phi[v];
       }
@@ -344,8 +375,15 @@ __global__ void __launch_bounds__(B_TS, 4) batch_kernel(BArgs a) {
           const float Y = fmaf((float)(iys - iy), k.dyn, ey);
           const ColPoly cp = col_poly(X, Y, fc);
           const bool ncl = ix >= nb.x0 && ix <= nb.x1 && iy >= nb.y0 && iy <= nb.y1;
-          const int elo = ncl ? nb.l0 : k.nz;
-          const unsigned espan = ncl ? (unsigned)(nb.l1 - nb.l0) : 0u;
+          int elo = k.nz;
+          unsigned espan = 0u;
+          if (ncl) {  // the column's near-region layers
+            const short2 tv = J.iv[(size_t)s * k.nslots + near_slot(nb, ix, iy)];
+            if (tv.x <= tv.y) {
+              elo = tv.x;
+              espan = (unsigned)(tv.y - tv.x);
+            }
+          }
           const float* col = rs + q * k.nzp * J.mgw;
           const ColPoly2 cp2 = col_poly2(cp, fc.a1);
           const float2 c2t = make_float2(cp.C2 - fc.h2, cp.C2 - fc.h2);
@@ -440,6 +478,7 @@ Plan plan(const ztm_job* jobs, int njobs, double near_q, int num_sms, int stage_
     ws += WsCarver::need((size_t)q.nmodels * q.ns * 8);
     ws += WsCarver::need((size_t)J.tiles * 4);
     ws += WsCarver::need((size_t)q.ns * 4) + WsCarver::need(ztm_station_order_ws(q.ns, m.nx, m.ny));
+    ws += WsCarver::need((size_t)q.ns * J.k.nslots * 4) + WsCarver::need((size_t)q.ns * 8);
     p.jobs.push_back(J);
   }
   for (auto& J : p.jobs) {
@@ -610,6 +649,8 @@ int batch_run(ztm_ctx* c, const ztm_job* jobs, int njobs, bool dev, double G, do
     J.near = wc.take<double>((size_t)J.nmodels * J.ns);
     J.done = wc.take<int>(J.tiles);
     J.perm = wc.take<int>(J.ns);
+    J.iv = wc.take<short2>((size_t)J.ns * J.k.nslots);
+    J.lr = wc.take<int2>(J.ns);
     order_ws[j] = wc.take<char>(ztm_station_order_ws(J.ns, J.m.nx, J.m.ny));
   }
   // graph key: shapes and every pointer the graph bakes in
@@ -676,6 +717,8 @@ int batch_run(ztm_ctx* c, const ztm_job* jobs, int njobs, bool dev, double G, do
       if (!rc)
         rc = ztm_station_order(c, c->stream, J.ns, reinterpret_cast<const int*>(J.si), 4, J.m.nx,
                                J.m.ny, const_cast<int*>(J.perm), ow);
+      launch_mesh_near_iv(c, J.k, J.m, J.ns, J.si, J.sxyz, const_cast<short2*>(J.iv),
+                          const_cast<int2*>(J.lr));
       cudaMemsetAsync(J.done, 0, sizeof(int) * J.tiles, c->stream);
     }
     cudaMemsetAsync(counter, 0, sizeof(int) * 16, c->stream);
@@ -703,7 +746,7 @@ int batch_run(ztm_ctx* c, const ztm_job* jobs, int njobs, bool dev, double G, do
     rc = ztm_cuda_check(c, cudaGraphLaunch(entry->exec, c->stream), "launch batch graph");
   }
   if (rc) return rc;
-  c->launches += 1 + 3LL * njobs;  // per job: transpose, station prep, sort key
+  c->launches += 1 + 4LL * njobs;  // per job: transpose, station prep, sort key, near intervals
   if (dev) return ZTM_OK;
   for (int j = 0; j < njobs; j++) {
     const ztm_job& q = jobs[j];
