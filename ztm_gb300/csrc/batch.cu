@@ -61,8 +61,10 @@ struct BArgs {
   long long n_near, n_items;
   int* counter;
   int* err;
-  double* phi;   // [block][warp][phi_cap] near-box vertex values (global scratch)
+  double* phi;   // [block][warp][phi_stride] near-box vertex values and their
+                 // near-prism bits (global scratch)
   int phi_cap;
+  int phi_stride;  // doubles per warp: phi_cap values + phi_cap bytes
 };
 
 // Float densities of a job, model-interleaved: rhoT[((g*ncols + c)*nzp + l)*W
@@ -195,9 +197,11 @@ __device__ void tile_done(const BJob& J, int tile, int expected, int* s_flag) {
 // vertex adjacent to a near-region prism into the warp's scratch, then per
 // model the signed triple difference of the region's densities around each
 // vertex times its Phi.
-__device__ void near_item(const BJob& J, int tile, double* phi_all, int phi_cap, int* err) {
+__device__ void near_item(const BJob& J, int tile, double* phi_all, int phi_cap, int phi_stride,
+                          int* err) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  double* phi = phi_all + (size_t)warp * phi_cap;
+  double* phi = phi_all + (size_t)warp * phi_stride;
+  unsigned char* nbits = reinterpret_cast<unsigned char*>(phi + phi_cap);
   if (J.nv_cap > phi_cap) {  // the host sizes phi_cap as the largest nv_cap
     if (threadIdx.x == 0) atomicOr(err, ZTM_DEVERR_BOUNDS);
     return;
@@ -243,19 +247,20 @@ __device__ void near_item(const BJob& J, int tile, double* phi_all, int phi_cap,
     };
     for (int v = lane; v < nv; v += 32) {
       const int a = b.x0 + v % nvx, bb = b.y0 + (v / nvx) % nvy, cz = L.x + v / (nvx * nvy);
-      phi[v] = members(a, bb, cz) ? ztm_phi<double>((m.x0 + a * m.dx) - xs,
-                                                    (m.y0 + bb * m.dy) - ys,
-                                                    (m.zt - cz * m.dz) - zs)
-                                  : 0.0;
+      const unsigned bits = members(a, bb, cz);
+      nbits[v] = (unsigned char)bits;
+      phi[v] = bits ? ztm_phi<double>((m.x0 + a * m.dx) - xs, (m.y0 + bb * m.dy) - ys,
+                                      (m.zt - cz * m.dz) - zs)
+                    : 0.0;
     }
     __syncwarp();
     for (int md = 0; md < J.nmodels; md++) {
       const double* rho = J.rho + (size_t)md * np;
       double acc = 0.0;
       for (int v = lane; v < nv; v += 32) {
-        const int a = b.x0 + v % nvx, bb = b.y0 + (v / nvx) % nvy, cz = L.x + v / (nvx * nvy);
-        const unsigned bits = members(a, bb, cz);
+        const unsigned bits = nbits[v];
         if (!bits) continue;
+        const int a = b.x0 + v % nvx, bb = b.y0 + (v / nvx) % nvy, cz = L.x + v / (nvx * nvy);
         double D = 0.0;
 #pragma unroll
         for (int q = 0; q < 8; q++) {
@@ -278,8 +283,8 @@ __global__ void __launch_bounds__(B_TS, 4) batch_kernel(BArgs a) {
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
   float* stage = reinterpret_cast<float*>(smem_raw + 128);
   // near-box vertex values: this block's slice of the global scratch
-  // (grid x warps x phi_cap doubles, sized from the same grid on the host)
-  double* phi = a.phi + (size_t)blockIdx.x * B_WARPS * a.phi_cap;
+  // (grid x warps x phi_stride doubles, sized from the same grid on the host)
+  double* phi = a.phi + (size_t)blockIdx.x * B_WARPS * a.phi_stride;
   __shared__ long long s_item;
   __shared__ int s_flag, s_lm;
   // compensated sums of each thread's models (16 KB): in registers they
@@ -305,7 +310,7 @@ __global__ void __launch_bounds__(B_TS, 4) batch_kernel(BArgs a) {
       while (j + 1 < a.njobs && a.jobs[j + 1].near_base <= item) j++;
       const BJob& J = a.jobs[j];
       const int tile = (int)(item - J.near_base);
-      near_item(J, tile, phi, a.phi_cap, a.err);
+      near_item(J, tile, phi, a.phi_cap, a.phi_stride, a.err);
       __syncthreads();
       tile_done(J, tile, J.chunks * J.mgroups + 1, &s_flag);
       continue;
@@ -604,7 +609,9 @@ int batch_run(ztm_ctx* c, const ztm_job* jobs, int njobs, bool dev, double G, do
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, B_TS, p.smem);
   per_sm = std::max(1, per_sm);
   const long long grid = std::min<long long>((long long)per_sm * c->num_sms, p.n_items);
-  const size_t phi_elems = (size_t)grid * B_WARPS * std::max(p.phi_cap, 1);
+  const int phi_cap = std::max(p.phi_cap, 1);
+  const int phi_stride = phi_cap + (phi_cap + 7) / 8;
+  const size_t phi_elems = (size_t)grid * B_WARPS * phi_stride;
   int rc = ztm_ws_reserve(c, p.ws_bytes + stage_bytes + WsCarver::need(phi_elems * 8) + 8192);
   if (rc) return rc;
   WsCarver wc(c->ws);
@@ -689,7 +696,8 @@ int batch_run(ztm_ctx* c, const ztm_job* jobs, int njobs, bool dev, double G, do
     }
     BArgs args;
     args.phi = phi;
-    args.phi_cap = std::max(p.phi_cap, 1);
+    args.phi_cap = phi_cap;
+    args.phi_stride = phi_stride;
     args.jobs = d_jobs;
     args.njobs = njobs;
     args.n_near = p.n_near;
