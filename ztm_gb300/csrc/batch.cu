@@ -61,10 +61,10 @@ struct BArgs {
   long long n_near, n_items;
   int* counter;
   int* err;
-  double* phi;   // [block][warp][phi_stride] near-box vertex values and their
-                 // near-prism bits (global scratch)
+  double* phi;   // [block][warp][phi_stride] near-box vertex values and the
+                 // near prisms' unit responses (global scratch)
   int phi_cap;
-  int phi_stride;  // doubles per warp: phi_cap values + phi_cap bytes
+  int phi_stride;  // doubles per warp: 2 phi_cap
 };
 
 // Float densities of a job, model-interleaved: rhoT[((g*ncols + c)*nzp + l)*W
@@ -194,14 +194,15 @@ __device__ void tile_done(const BJob& J, int tile, int expected, int* s_flag) {
 }
 
 // Near regions of a tile's stations, a warp per station: Phi once per
-// vertex adjacent to a near-region prism into the warp's scratch, then per
-// model the signed triple difference of the region's densities around each
-// vertex times its Phi.
+// vertex next to a near-region prism into the warp's scratch, then each near
+// prism's unit response U (the signed sum of Phi over its 8 corners, in
+// double), then per model sum_p rho_p U_p: one multiply-add per near prism
+// and model.
 __device__ void near_item(const BJob& J, int tile, double* phi_all, int phi_cap, int phi_stride,
                           int* err) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double* phi = phi_all + (size_t)warp * phi_stride;
-  unsigned char* nbits = reinterpret_cast<unsigned char*>(phi + phi_cap);
+  double* U = phi + phi_cap;
   if (J.nv_cap > phi_cap) {  // the host sizes phi_cap as the largest nv_cap
     if (threadIdx.x == 0) atomicOr(err, ZTM_DEVERR_BOUNDS);
     return;
@@ -223,10 +224,8 @@ __device__ void near_item(const BJob& J, int tile, double* phi_all, int phi_cap,
     const double xs = J.sxyz[3 * s], ys = J.sxyz[3 * s + 1], zs = J.sxyz[3 * s + 2];
     const int nvx = b.x1 - b.x0 + 2, nvy = b.y1 - b.y0 + 2, nvz = L.y - L.x + 2;
     const int nv = min(nvx * nvy * nvz, J.nv_cap);
-    // the near-region prisms around vertex (a, bb, cz): ix = a - 1 + da,
-    // iy = bb - 1 + db, l = cz - 1 + dc; bit (da, db, dc) set when in the region
-    auto members = [&](int a, int bb, int cz) {
-      unsigned bits = 0u;
+    // is one of the (up to 8) prisms around vertex (a, bb, cz) in the region
+    auto touches = [&](int a, int bb, int cz) {
 #pragma unroll
       for (int da = 0; da < 2; da++) {
         const int ix = a - 1 + da;
@@ -236,40 +235,46 @@ __device__ void near_item(const BJob& J, int tile, double* phi_all, int phi_cap,
           const int iy = bb - 1 + db;
           if (iy < b.y0 || iy > b.y1) continue;
           const short2 t = ivs[near_slot(b, ix, iy)];
-#pragma unroll
-          for (int dc = 0; dc < 2; dc++) {
-            const int l = cz - 1 + dc;
-            if (l >= t.x && l <= t.y) bits |= 1u << (da * 4 + db * 2 + dc);
-          }
+          if (t.x <= t.y && t.x <= cz && cz - 1 <= t.y) return true;  // layer cz - 1 or cz
         }
       }
-      return bits;
+      return false;
     };
     for (int v = lane; v < nv; v += 32) {
       const int a = b.x0 + v % nvx, bb = b.y0 + (v / nvx) % nvy, cz = L.x + v / (nvx * nvy);
-      const unsigned bits = members(a, bb, cz);
-      nbits[v] = (unsigned char)bits;
-      phi[v] = bits ? ztm_phi<double>((m.x0 + a * m.dx) - xs, (m.y0 + bb * m.dy) - ys,
-                                      (m.zt - cz * m.dz) - zs)
-                    : 0.0;
+      phi[v] = touches(a, bb, cz) ? ztm_phi<double>((m.x0 + a * m.dx) - xs,
+                                                    (m.y0 + bb * m.dy) - ys,
+                                                    (m.zt - cz * m.dz) - zs)
+                                  : 0.0;
+    }
+    __syncwarp();
+    // unit responses: vertices x lower qx (-), upper qx+1 (+); z: layer top
+    // index qz (+), bottom qz+1 (-); zero outside the region
+    const int bx = nvx - 1, by = nvy - 1, bz = nvz - 1;
+    const int nbp = bx * by * bz;  // < nv
+    for (int q = lane; q < nbp; q += 32) {
+      const int qx = q % bx, qy = (q / bx) % by, qz = q / (bx * by);
+      const short2 t = ivs[near_slot(b, b.x0 + qx, b.y0 + qy)];
+      const int l = L.x + qz;
+      double u = 0.0;
+      if (l >= t.x && l <= t.y) {
+        auto P = [&](int dx_, int dy_, int dz_) {
+          return phi[(qx + dx_) + nvx * ((qy + dy_) + nvy * (qz + dz_))];
+        };
+        u = P(1, 1, 0) - P(0, 1, 0) - P(1, 0, 0) + P(0, 0, 0) - P(1, 1, 1) + P(0, 1, 1) +
+            P(1, 0, 1) - P(0, 0, 1);
+      }
+      U[q] = u;
     }
     __syncwarp();
     for (int md = 0; md < J.nmodels; md++) {
       const double* rho = J.rho + (size_t)md * np;
       double acc = 0.0;
-      for (int v = lane; v < nv; v += 32) {
-        const unsigned bits = nbits[v];
-        if (!bits) continue;
-        const int a = b.x0 + v % nvx, bb = b.y0 + (v / nvx) % nvy, cz = L.x + v / (nvx * nvy);
-        double D = 0.0;
-#pragma unroll
-        for (int q = 0; q < 8; q++) {
-          if (!(bits & (1u << q))) continue;
-          const int da = q >> 2, db = (q >> 1) & 1, dc = q & 1;
-          const double r = rho[(a - 1 + da) + (long long)m.nx * (bb - 1 + db) + plane * (cz - 1 + dc)];
-          D += ((da == 1) ^ (db == 1) ^ (dc == 0)) ? -r : r;
-        }
-        acc += D * phi[v];
+      for (int q = lane; q < nbp; q += 32) {
+        const double u = U[q];
+        if (u == 0.0) continue;
+        const int qx = q % bx, qy = (q / bx) % by, qz = q / (bx * by);
+        acc = fma(rho[(b.x0 + qx) + (long long)m.nx * (b.y0 + qy) + plane * (L.x + qz)], u, acc);
       }
       acc = warp_sum_d(acc);
       if (lane == 0) J.near[(size_t)md * J.ns + s] = acc;
@@ -610,7 +615,7 @@ int batch_run(ztm_ctx* c, const ztm_job* jobs, int njobs, bool dev, double G, do
   per_sm = std::max(1, per_sm);
   const long long grid = std::min<long long>((long long)per_sm * c->num_sms, p.n_items);
   const int phi_cap = std::max(p.phi_cap, 1);
-  const int phi_stride = phi_cap + (phi_cap + 7) / 8;
+  const int phi_stride = 2 * phi_cap;
   const size_t phi_elems = (size_t)grid * B_WARPS * phi_stride;
   int rc = ztm_ws_reserve(c, p.ws_bytes + stage_bytes + WsCarver::need(phi_elems * 8) + 8192);
   if (rc) return rc;
