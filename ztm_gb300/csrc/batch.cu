@@ -116,7 +116,7 @@ __device__ __forceinline__ void far_column(const float* __restrict__ col, const 
                                            float* kc) {
   const float2 dz2 = make_float2(k.dzn, k.dzn);
   float zf = (float)(-izs);  // (l0 - izs), exact, stepped by 8
-  // plain float sums over up to 32 layers per model, compensated across
+  // plain float sums over up to 64 layers per model, compensated across
   float2 g[W == 1 ? 1 : W / 2];
 #pragma unroll
   for (int m = 0; m < (W == 1 ? 1 : W / 2); m++) g[m] = make_float2(0.f, 0.f);
@@ -136,7 +136,7 @@ __device__ __forceinline__ void far_column(const float* __restrict__ col, const 
         if ((lb < Lm && (unsigned)(lb - elo) <= espan) || lb >= k.nz) K2[j].y = 0.f;
       }
     }
-    const bool flush = ((l0 >> 3) & 3) == 3 || l0 + 8 >= k.nz;
+    const bool flush = ((l0 >> 3) & 7) == 7 || l0 + 8 >= k.nz;
     if constexpr (W == 1) {
       const float4 ra = *reinterpret_cast<const float4*>(col + l0);
       const float4 rb = *reinterpret_cast<const float4*>(col + l0 + 4);
