@@ -121,7 +121,7 @@ def cpu_baseline_prism(mesh, rho, st, nsample=224):
 
 
 def pointmass_mapping(mesh, rho, st):
-    """Config-2 geometry on the reference's point-mass grid: node-centred
+    """The 256x256x64 draped mesh on the reference's point-mass grid: node-centred
     cells, h = 1 km horizontally, fv = 2 (0.5 km layers), g/cc, grid units;
     the 66.7 constant assumes h = 10 km, so scale = h/10."""
     import numpy as np

@@ -1,7 +1,8 @@
 """CPU oracle of the gravity path - TEST INFRASTRUCTURE ONLY.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may
-import this package, and only as the checker (or the timed CPU baseline).
+import this package, and only to check results against (or as the timed
+CPU baseline).
 The product library never calls it; there is no CPU fallback.
 
 Contents (oracle.c):

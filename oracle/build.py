@@ -1,4 +1,4 @@
-"""Build recipe of the oracle (checker infrastructure, never shipped):
+"""Build recipe of the oracle (test infrastructure, never shipped):
 
   oracle/_build/liboracle.so   the C restatement (oracle.c), gcc, -ffp-contract=off
   oracle/_build/libref_runner.so  driver-API loader of the reference GF kernel

@@ -1,7 +1,8 @@
 /*
  * oracle.c - CPU oracle of the gravity path.  TEST INFRASTRUCTURE ONLY: the
- * tests, the smoke check and the bench's CPU-baseline leg load it as the
- * checker; the product library never links it and has no CPU fallback.
+ * tests, the smoke check and the bench's CPU-baseline leg load it to check
+ * results against; the product library never links it and has no CPU
+ * fallback.
  *
  * Point-mass model (the reference's algorithm):
  *   ora_pointmass_tfm  restates the CPU gravity lambda of TFM.cpp:95-99 with

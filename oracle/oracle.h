@@ -1,6 +1,6 @@
 /*
- * oracle.h - CPU restatement of ZTM's gravity path, used ONLY as the checker
- * by the tests, the smoke check and the bench's CPU baseline.  Nothing in the
+ * oracle.h - CPU restatement of ZTM's gravity path, used ONLY as the oracle
+ * of the tests, the smoke check and the bench's CPU baseline.  Nothing in the
  * product library links or calls it.
  *
  * Parity pins: the point-mass functions restate TFM.cpp:95-99 (double) and

@@ -1,7 +1,7 @@
 // ref_gf_runner.cpp - loads the reference GF kernel (compiled unchanged from
 // GFM_GPU.cu into oracle/_ref/gf_ref.cubin) with the CUDA driver API and runs
 // it the way GFM_GPU.cu:28-32 does: zeroed g, one launch of GF<<<N/ii, ii>>>
-// with ii = (di-1)*fh+1.  Checker / baseline infrastructure only.
+// with ii = (di-1)*fh+1.  Test and baseline infrastructure only.
 #include <cuda.h>
 #include <stdio.h>
 #include <string.h>
