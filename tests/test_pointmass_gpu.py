@@ -83,3 +83,34 @@ def test_reference_gf_kernel_agrees(ctx):
     assert rel_err(gf, ref) <= 5e-5
     ours = ctx.pointmass(g, drho, surf, precision="fp32")
     assert rel_err(ours, ref) <= TOL32
+
+
+@pytest.mark.parametrize("dims", [(31, 29, 17, 1, 2, 5), (9, 7, 5, 2, 3, 1), (5, 5, 2, 1, 1, 0),
+                                  (40, 3, 9, 1, 2, 1)])
+def test_fp32_dims_and_node_lists(ctx, dims):
+    """The float path by node columns: grids with fh, fv > 1, thin grids, and
+    explicit node lists (a node listed twice counts twice, as in the loop of
+    TFM.cpp:96-98)."""
+    di, dj, dk, fh, fv, bfr = dims
+    g = ztm_gb300.make_grid(di, dj, dk, fh, fv, bfr)
+    drho, surf = tfm_like_inputs(di, dj, dk, fh, fv, seed=di + 1)
+    ref = oracle.pointmass_tfm(g, drho, surf)
+    assert rel_err(ctx.pointmass(g, drho, surf, precision="fp32"), ref) <= TOL32
+    nn = np.nonzero(np.abs(drho) > 0.05)[0].astype(np.int32)
+    nn2 = np.concatenate([nn, nn[::3]])
+    ref2 = oracle.pointmass_tfm(g, drho, surf, nn=nn2)
+    assert rel_err(ctx.pointmass(g, drho, surf, nn=nn2, precision="fp32"), ref2) <= TOL32
+
+
+def test_bad_node_index_on_device_is_reported(ctx):
+    """A node index outside the grid passed in device memory is skipped on
+    the device and reported as a range error at the call's end."""
+    torch = pytest.importorskip("torch")
+    g = ztm_gb300.make_grid(21, 19, 9, 1, 2, 3)
+    drho, surf = tfm_like_inputs(21, 19, 9, seed=9)
+    nn = np.nonzero(np.abs(drho) > 0.05)[0].astype(np.int32)
+    nn[len(nn) // 2] = drho.size + 7
+    with pytest.raises(ztm_gb300.GravityError):
+        ctx.pointmass(g, torch.tensor(drho, device="cuda"), torch.tensor(surf, device="cuda"),
+                      nn=torch.tensor(nn, device="cuda"), precision="fp32")
+        ctx.sync()

@@ -117,7 +117,8 @@ __global__ void __launch_bounds__(PM_TS)
   if (active) partial[(long long)blockIdx.y * p.ns + s] = F64 ? acc64 : acc32.value();
 }
 
-// Float path in two steps.
+// Float path by a node list, for grids too deep for the column path below
+// (more than 2 * PM_CT levels), in two steps.
 //
 // 1. Node list (pm_nodes_count / pm_nodes_scan / pm_nodes_write): the
 //    selected nodes, in order, in grid units, built once per call (O(nodes),
@@ -332,6 +333,140 @@ __global__ void __launch_bounds__(PM_TS)
   if (active) partial[(long long)blockIdx.y * p.ns + s] = acc.value();
 }
 
+// Float path by node columns (the context entry points).
+//
+// A run of nodes that shares its horizontal offset needs X^2 + Y^2 once: per
+// node pair the gather then forms only Z, r^2, the rsqrt, the weight and the
+// product (six packed operations against ten with every node's offsets).  So
+// the selected nodes are laid out column by column (fine-grid column
+// c = ni + nj*ii, k ascending), each column's run padded to whole pairs:
+// 1. pm_cols_count: thread per column, its selected nodes (the threshold, or
+//    each node's multiplicity in nn, pm_nn_mark) -> pairs per column;
+// 2. pm_nodes_scan over the columns -> each column's first pair and the
+//    total;
+// 3. pm_cols_write: thread per column, pairs (-k_a, -k_b, w_a, w_b), an odd
+//    run closed by a zero mass far away;
+// 4. pm_gather_cols_kernel: station tile x column chunk; the pairs of
+//    cg_cols columns at a time in shared memory (at most PM_CT pairs), a
+//    thread owns a station and forms each column's X^2 + Y^2 once.  Plain
+//    float sums over 32 nodes, Kahan across.
+constexpr int PM_CT = 512;  // pairs per shared-memory tile of the column gather
+
+// Multiplicity of each node in the nn list (a node listed twice counts
+// twice, as in the reference's loop); bad entries are recorded in err.
+__global__ void pm_nn_mark(PmParams p, const int* __restrict__ nn, int* __restrict__ mult,
+                           int* __restrict__ err) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= p.nnodes) return;
+  const long long n = nn[t];
+  if (n < 0 || n >= p.N) {
+    atomicOr(err, ZTM_DEVERR_BOUNDS);
+    return;
+  }
+  atomicAdd(&mult[n], 1);
+}
+
+// Float weight of node n, 0 when it is not selected.
+__device__ __forceinline__ float pm_col_weight(const PmParams& p, const double* __restrict__ drho,
+                                               const int* __restrict__ mult, long long n) {
+  const double w = drho[n];
+  if (mult) {
+    const int m = mult[n];
+    return m ? (float)(w * m) : 0.f;
+  }
+  return fabsf((float)w) > (float)p.thr ? (float)w : 0.f;
+}
+
+__global__ void pm_cols_count(PmParams p, const double* __restrict__ drho,
+                              const int* __restrict__ mult, int* __restrict__ counts) {
+  const long long ncols = (long long)p.ii * p.jj;
+  const long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (c >= ncols) return;
+  int cnt = 0;
+  for (int k = 0; k < p.kk; k++)
+    if (pm_col_weight(p, drho, mult, c + k * ncols) != 0.f) cnt++;
+  counts[c] = (cnt + 1) >> 1;
+}
+
+__global__ void pm_cols_write(PmParams p, const double* __restrict__ drho,
+                              const int* __restrict__ mult, const int* __restrict__ offs,
+                              float4* __restrict__ pairs) {
+  const long long ncols = (long long)p.ii * p.jj;
+  const long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (c >= ncols) return;
+  float4* out = pairs + offs[c];
+  int q = 0;
+  float ka = 0.f, wa = 0.f;
+  for (int k = 0; k < p.kk; k++) {
+    const float w = pm_col_weight(p, drho, mult, c + k * ncols);
+    if (w == 0.f) continue;
+    const float kz = -(float)(k * (1.0 / p.fv));  // -k in grid units (TFM.cpp:97)
+    if (q & 1)
+      out[q >> 1] = make_float4(ka, kz, wa, w);
+    else {
+      ka = kz;
+      wa = w;
+    }
+    q++;
+  }
+  if (q & 1) out[q >> 1] = make_float4(ka, -1.0e18f, wa, 0.f);
+}
+
+__global__ void __launch_bounds__(PM_TS)
+    pm_gather_cols_kernel(PmParams p, const float4* __restrict__ pairs,
+                          const int* __restrict__ offs, const double* __restrict__ surf,
+                          int cg_cols, int chunk_cols, double* __restrict__ partial) {
+  __shared__ float4 tile[PM_CT];
+  __shared__ int s_off[PM_CT + 1];
+  const int s = blockIdx.x * PM_TS + threadIdx.x;
+  const bool active = s < p.ns;
+  float i0 = 0.f, j0 = 0.f, k0 = 0.f;
+  if (active) {
+    const int si = p.bfr + s % p.ni, sj = p.bfr + s / p.ni;
+    i0 = (float)si;
+    j0 = (float)sj;
+    k0 = (float)surf[si + sj * p.di];
+  }
+  const float2 K0 = make_float2(k0, k0);
+  const int ncols = p.ii * p.jj;
+  const int c0 = blockIdx.y * chunk_cols, c1 = min(ncols, c0 + chunk_cols);
+  Kahan acc;
+  for (int cg = c0; cg < c1; cg += cg_cols) {
+    const int ce = min(c1, cg + cg_cols);
+    __syncthreads();  // the previous group is consumed
+    for (int q = threadIdx.x; q <= ce - cg; q += PM_TS) s_off[q] = offs[cg + q];
+    __syncthreads();
+    const int p0 = s_off[0], npair = s_off[ce - cg] - p0;  // <= PM_CT (host)
+    for (int q = threadIdx.x; q < npair; q += PM_TS) tile[q] = pairs[p0 + q];
+    __syncthreads();
+    if (!active) continue;
+    for (int c = cg; c < ce; c++) {
+      const int a = s_off[c - cg] - p0, b = s_off[c - cg + 1] - p0;
+      if (a == b) continue;
+      const int ni = c % p.ii, nj = c / p.ii;
+      const float X = i0 + (-(float)(ni * (1.0 / p.fh)));
+      const float Y = j0 + (-(float)(nj * (1.0 / p.fh)));
+      const float rh = fmaf(X, X, Y * Y);
+      const float2 rh2 = make_float2(rh, rh);
+      for (int qa = a; qa < b; qa += 16) {
+        const int qb = min(b, qa + 16);
+        float2 g = make_float2(0.f, 0.f);
+#pragma unroll 4
+        for (int q = qa; q < qb; q++) {
+          const float4 v = tile[q];  // nodes (-k_a, -k_b, w_a, w_b)
+          const float2 dz = __fadd2_rn(K0, make_float2(v.x, v.y));
+          const float2 d2 = __ffma2_rn(dz, dz, rh2);
+          const float2 rs = make_float2(pm_rsqrt_ftz(d2.x), pm_rsqrt_ftz(d2.y));
+          const float2 tw = __fmul2_rn(make_float2(v.z, v.w), dz);
+          g = __ffma2_rn(__fmul2_rn(tw, __fmul2_rn(rs, rs)), rs, g);
+        }
+        acc.add(g.x + g.y);
+      }
+    }
+  }
+  if (active) partial[(long long)blockIdx.y * p.ns + s] = acc.value();
+}
+
 // G[m] = factor * sum_chunks partial for interior m, 0 elsewhere.
 __global__ void pm_finalize_kernel(PmParams p, int nchunks,
                                    const double* __restrict__ partial,
@@ -349,12 +484,15 @@ __global__ void pm_finalize_kernel(PmParams p, int nchunks,
 }
 
 // Resident blocks per SM of the gather kernel that a call runs (the float
-// path of the context entry points is the compacted-list kernel).
-int pm_occupancy(int precision, bool compacted) {
+// path of the context entry points is the column kernel, or the compacted
+// list for very deep grids).
+int pm_occupancy(int precision, bool compacted, bool cols = false) {
   int occ = 0;
   cudaError_t e;
   if (precision == ZTM_PREC_FP64)
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pm_gather_kernel<true>, PM_TS, 0);
+  else if (cols)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pm_gather_cols_kernel, PM_TS, 0);
   else if (compacted)
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pm_gather_f32_kernel, PM_TS, 0);
   else
@@ -385,9 +523,37 @@ void pm_shape(const PmParams& p, int num_sms, int occ, int* tiles, int* chunks, 
   *clen = len;
 }
 
+// The column path: a column's run fits one shared-memory tile.
+bool pm_use_cols(const PmParams& p) { return (p.kk + 1) / 2 <= PM_CT; }
+
+// Column gather shape: station tiles x column chunks of whole column groups
+// (cg_cols columns, at most PM_CT pairs), about four waves of resident blocks.
+void pm_cols_shape(const PmParams& p, int num_sms, int* tiles, int* chunks, int* chunk_cols,
+                   int* cg_cols) {
+  const int occ = pm_occupancy(ZTM_PREC_FP32, true, true);
+  *tiles = std::max(1, (p.ns + PM_TS - 1) / PM_TS);
+  const long long ncols = (long long)p.ii * p.jj;
+  *cg_cols = std::max(1, PM_CT / std::max(1, (p.kk + 1) / 2));
+  const long long want = std::max(1LL, (4LL * occ * std::max(num_sms, 1) + *tiles - 1) / *tiles);
+  const long long groups = (ncols + *cg_cols - 1) / *cg_cols;
+  const long long ch = std::max(1LL, std::min(std::min(want, groups), 65535LL));
+  const long long per = (groups + ch - 1) / ch;  // groups per chunk
+  *chunk_cols = (int)(per * *cg_cols);
+  *chunks = (int)((ncols + *chunk_cols - 1) / *chunk_cols);
+}
+
 }  // namespace
 
 size_t ztm_pointmass_ws(const PmParams& p, int precision, int num_sms) {
+  if (precision != ZTM_PREC_FP64 && pm_use_cols(p)) {  // the float node columns
+    int ct, cc, ccols, cg;
+    pm_cols_shape(p, num_sms, &ct, &cc, &ccols, &cg);
+    const long long ncols = (long long)p.ii * p.jj;
+    return WsCarver::need((size_t)cc * std::max(p.ns, 1) * sizeof(double)) +
+           WsCarver::need((size_t)(ncols + 1) * sizeof(int)) +
+           WsCarver::need((size_t)((p.N + ncols) / 2 + 2) * sizeof(float4)) +
+           WsCarver::need((size_t)p.N * sizeof(int));  // nn multiplicities
+  }
   int tiles, chunks;
   long long len;
   pm_shape(p, num_sms, pm_occupancy(precision, true), &tiles, &chunks, &len);
@@ -403,9 +569,13 @@ size_t ztm_pointmass_ws(const PmParams& p, int precision, int num_sms) {
 int ztm_launch_pointmass(ztm_ctx* c, const PmParams& p, const double* d_drho,
                          const int* d_nn, const double* d_surf, double* d_G,
                          double scale, int precision, WsCarver& wc) {
-  int tiles, chunks;
-  long long len;
-  pm_shape(p, c->num_sms, pm_occupancy(precision, true), &tiles, &chunks, &len);
+  const bool cols = precision != ZTM_PREC_FP64 && pm_use_cols(p);
+  int tiles, chunks, chunk_cols = 0, cg_cols = 0;
+  long long len = 0;
+  if (cols)
+    pm_cols_shape(p, c->num_sms, &tiles, &chunks, &chunk_cols, &cg_cols);
+  else
+    pm_shape(p, c->num_sms, pm_occupancy(precision, true), &tiles, &chunks, &len);
   double* partial = wc.take<double>((size_t)chunks * std::max(p.ns, 1));
   if (p.ns > 0 && p.nnodes > 0) {
     dim3 grid(tiles, chunks);
@@ -414,6 +584,28 @@ int ztm_launch_pointmass(ztm_ctx* c, const PmParams& p, const double* d_drho,
       pm_gather_kernel<true><<<grid, PM_TS, 0, c->stream>>>(p, d_drho, d_nn, d_surf, len, partial,
                                                             c->d_err);
       c->launches++;
+    } else if (cols) {
+      const long long ncols = (long long)p.ii * p.jj;
+      int* offs = wc.take<int>((size_t)ncols + 1);
+      float4* pairs = wc.take<float4>((size_t)((p.N + ncols) / 2 + 2));
+      int* mult = nullptr;
+      if (d_nn) {  // the listed nodes, with their multiplicities
+        mult = wc.take<int>((size_t)p.N);
+        cudaMemsetAsync(mult, 0, (size_t)p.N * sizeof(int), c->stream);
+        pm_nn_mark<<<(unsigned)((p.nnodes + 255) / 256), 256, 0, c->stream>>>(p, d_nn, mult,
+                                                                             c->d_err);
+        c->launches++;
+      }
+      const unsigned cb = (unsigned)((ncols + 255) / 256);
+      pm_cols_count<<<cb, 256, 0, c->stream>>>(p, d_drho, mult, offs);
+      pm_nodes_scan<<<1, 1024, 0, c->stream>>>((int)ncols, offs, offs + ncols);
+      pm_cols_write<<<cb, 256, 0, c->stream>>>(p, d_drho, mult, offs, pairs);
+      {
+        ZtmProf prof_(c, "pointmass");
+        pm_gather_cols_kernel<<<grid, PM_TS, 0, c->stream>>>(p, pairs, offs, d_surf, cg_cols,
+                                                            chunk_cols, partial);
+      }
+      c->launches += 4;
     } else {
       const long long nb = (p.nnodes + PM_NB - 1) / PM_NB;
       if (nb > (1LL << 31) - 1) return ztm_fail(c, ZTM_ERR_RANGE, "too many point-mass nodes");
