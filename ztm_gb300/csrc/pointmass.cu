@@ -377,11 +377,16 @@ __device__ __forceinline__ float pm_col_weight(const PmParams& p, const double* 
   return fabsf((float)w) > (float)p.thr ? (float)w : 0.f;
 }
 
+// pairs per column, and the column's (-i, -j) in grid units (TFM.cpp:97; in
+// double once per column, so that the gather runs no FP64 instruction)
 __global__ void pm_cols_count(PmParams p, const double* __restrict__ drho,
-                              const int* __restrict__ mult, int* __restrict__ counts) {
+                              const int* __restrict__ mult, int* __restrict__ counts,
+                              float2* __restrict__ colxy) {
   const long long ncols = (long long)p.ii * p.jj;
   const long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (c >= ncols) return;
+  const int ni = (int)(c % p.ii), nj = (int)(c / p.ii);
+  colxy[c] = make_float2(-(float)(ni * (1.0 / p.fh)), -(float)(nj * (1.0 / p.fh)));
   int cnt = 0;
   for (int k = 0; k < p.kk; k++)
     if (pm_col_weight(p, drho, mult, c + k * ncols) != 0.f) cnt++;
@@ -414,10 +419,12 @@ __global__ void pm_cols_write(PmParams p, const double* __restrict__ drho,
 
 __global__ void __launch_bounds__(PM_TS)
     pm_gather_cols_kernel(PmParams p, const float4* __restrict__ pairs,
-                          const int* __restrict__ offs, const double* __restrict__ surf,
-                          int cg_cols, int chunk_cols, double* __restrict__ partial) {
+                          const int* __restrict__ offs, const float2* __restrict__ colxy,
+                          const double* __restrict__ surf, int cg_cols, int chunk_cols,
+                          double* __restrict__ partial) {
   __shared__ float4 tile[PM_CT];
   __shared__ int s_off[PM_CT + 1];
+  __shared__ float2 s_xy[PM_CT];
   const int s = blockIdx.x * PM_TS + threadIdx.x;
   const bool active = s < p.ns;
   float i0 = 0.f, j0 = 0.f, k0 = 0.f;
@@ -434,7 +441,10 @@ __global__ void __launch_bounds__(PM_TS)
   for (int cg = c0; cg < c1; cg += cg_cols) {
     const int ce = min(c1, cg + cg_cols);
     __syncthreads();  // the previous group is consumed
-    for (int q = threadIdx.x; q <= ce - cg; q += PM_TS) s_off[q] = offs[cg + q];
+    for (int q = threadIdx.x; q <= ce - cg; q += PM_TS) {
+      s_off[q] = offs[cg + q];
+      if (q < ce - cg) s_xy[q] = colxy[cg + q];
+    }
     __syncthreads();
     const int p0 = s_off[0], npair = s_off[ce - cg] - p0;  // <= PM_CT (host)
     for (int q = threadIdx.x; q < npair; q += PM_TS) tile[q] = pairs[p0 + q];
@@ -443,9 +453,8 @@ __global__ void __launch_bounds__(PM_TS)
     for (int c = cg; c < ce; c++) {
       const int a = s_off[c - cg] - p0, b = s_off[c - cg + 1] - p0;
       if (a == b) continue;
-      const int ni = c % p.ii, nj = c / p.ii;
-      const float X = i0 + (-(float)(ni * (1.0 / p.fh)));
-      const float Y = j0 + (-(float)(nj * (1.0 / p.fh)));
+      const float2 xy = s_xy[c - cg];
+      const float X = i0 + xy.x, Y = j0 + xy.y;
       const float rh = fmaf(X, X, Y * Y);
       const float2 rh2 = make_float2(rh, rh);
       for (int qa = a; qa < b; qa += 16) {
@@ -551,6 +560,7 @@ size_t ztm_pointmass_ws(const PmParams& p, int precision, int num_sms) {
     const long long ncols = (long long)p.ii * p.jj;
     return WsCarver::need((size_t)cc * std::max(p.ns, 1) * sizeof(double)) +
            WsCarver::need((size_t)(ncols + 1) * sizeof(int)) +
+           WsCarver::need((size_t)ncols * sizeof(float2)) +
            WsCarver::need((size_t)((p.N + ncols) / 2 + 2) * sizeof(float4)) +
            WsCarver::need((size_t)p.N * sizeof(int));  // nn multiplicities
   }
@@ -587,6 +597,7 @@ int ztm_launch_pointmass(ztm_ctx* c, const PmParams& p, const double* d_drho,
     } else if (cols) {
       const long long ncols = (long long)p.ii * p.jj;
       int* offs = wc.take<int>((size_t)ncols + 1);
+      float2* colxy = wc.take<float2>((size_t)ncols);
       float4* pairs = wc.take<float4>((size_t)((p.N + ncols) / 2 + 2));
       int* mult = nullptr;
       if (d_nn) {  // the listed nodes, with their multiplicities
@@ -597,13 +608,13 @@ int ztm_launch_pointmass(ztm_ctx* c, const PmParams& p, const double* d_drho,
         c->launches++;
       }
       const unsigned cb = (unsigned)((ncols + 255) / 256);
-      pm_cols_count<<<cb, 256, 0, c->stream>>>(p, d_drho, mult, offs);
+      pm_cols_count<<<cb, 256, 0, c->stream>>>(p, d_drho, mult, offs, colxy);
       pm_nodes_scan<<<1, 1024, 0, c->stream>>>((int)ncols, offs, offs + ncols);
       pm_cols_write<<<cb, 256, 0, c->stream>>>(p, d_drho, mult, offs, pairs);
       {
         ZtmProf prof_(c, "pointmass");
-        pm_gather_cols_kernel<<<grid, PM_TS, 0, c->stream>>>(p, pairs, offs, d_surf, cg_cols,
-                                                            chunk_cols, partial);
+        pm_gather_cols_kernel<<<grid, PM_TS, 0, c->stream>>>(p, pairs, offs, colxy, d_surf,
+                                                            cg_cols, chunk_cols, partial);
       }
       c->launches += 4;
     } else {
