@@ -14,7 +14,7 @@
 //               station slice, the column's horizontal offsets and polynomial
 //               computed once per station and the far-field expansion per
 //               layer in float (second order where the whole warp is far
-//               enough), float sums over 32 stations, double beyond; the
+//               enough), float sums over 32 stations, compensated beyond; the
 //               slices meet in g_rho by double atomics.  Near pairs (prisms in
 //               the station's near region): one warp per station computes
 //               Phi once per vertex into its block's slice of a global
@@ -68,13 +68,22 @@ struct AdjSmem {
   int4 b[ADJ_STILE];   // the station's near box columns x0, x1, y0, y1
   float4 h[ADJ_STILE]; // the home cell indices as floats (exact)
   float r[ADJ_STILE];
-  double acc[ADJ_LG][ADJ_TS];
+  float2 acc[ADJ_LG][ADJ_TS];  // compensated float sums (sum, compensation)
 };
+
+// Compensated float add of x into k = (sum, compensation).
+__device__ __forceinline__ void kahan2(float2& k, float x) {
+  const float y = x - k.y;
+  const float t = k.x + y;
+  k.y = (t - k.x) - y;
+  k.x = t;
+}
 
 // Far item (column tile bx, station slice by): thread per (column, group of
 // 32 layers), g[p] += G5*L0*Vn * sum.  A thread sums its column's 32 layers
 // over the slice's stations: float over 32 stations (packed, two layers per
-// lane pair), then double in shared memory, then one double atomic per
+// lane pair), then compensated float sums in shared memory (no FP64
+// instruction per group: GB300's FP64 pipe is slow), then one double atomic per
 // layer into g.  The per-(station, column) setup (offsets, the horizontal
 // polynomial, the near box test) is shared by the 32 layers.
 __device__ __forceinline__ void adj_far_item(const AdjArgs& a, int bx, int by, AdjSmem& sm) {
@@ -92,7 +101,7 @@ __device__ __forceinline__ void adj_far_item(const AdjArgs& a, int bx, int by, A
   const float fix = (float)ix, fiy = (float)iy, fl0 = (float)l0;
   const FarCoef fc = k.fc;
 #pragma unroll
-  for (int j = 0; j < ADJ_LG; j++) sm.acc[j][threadIdx.x] = 0.0;
+  for (int j = 0; j < ADJ_LG; j++) sm.acc[j][threadIdx.x] = make_float2(0.f, 0.f);
   const float2 dz2 = make_float2(k.dzn, k.dzn);
   // this item's slice of the stations
   const int sb = by * a.slice, se = min(a.ns, sb + a.slice);
@@ -178,11 +187,11 @@ __device__ __forceinline__ void adj_far_item(const AdjArgs& a, int bx, int by, A
 #pragma unroll
         for (int j = 0; j < ADJ_LG / 2; j++) gs[j] = __ffma2_rn(w2, v[j], gs[j]);
       }
-      // the group's float sums into the double accumulators (FP64 pipe)
+      // the group's float sums into the compensated accumulators
 #pragma unroll
       for (int j = 0; j < ADJ_LG / 2; j++) {
-        sm.acc[2 * j][threadIdx.x] += (double)gs[j].x;
-        sm.acc[2 * j + 1][threadIdx.x] += (double)gs[j].y;
+        kahan2(sm.acc[2 * j][threadIdx.x], gs[j].x);
+        kahan2(sm.acc[2 * j + 1][threadIdx.x], gs[j].y);
       }
     }
   }
@@ -191,7 +200,10 @@ __device__ __forceinline__ void adj_far_item(const AdjArgs& a, int bx, int by, A
 #pragma unroll
   for (int j = 0; j < ADJ_LG; j++) {
     const int l = l0 + j;
-    if (l < k.nz) atomicAdd(&a.g[c + plane * l], a.scale * sm.acc[j][threadIdx.x]);
+    if (l < k.nz) {
+      const float2 kc = sm.acc[j][threadIdx.x];
+      atomicAdd(&a.g[c + plane * l], a.scale * ((double)kc.x - (double)kc.y));
+    }
   }
 }
 
