@@ -28,6 +28,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "prism_common.cuh"
 #include "ztm_internal.cuh"
@@ -37,6 +38,10 @@ namespace {
 constexpr int IF_TS = 128;
 constexpr int IF_TILE = 256;
 constexpr int IF_NEAR_WPB = 4;
+constexpr int IF_SUB = 32;       // columns per second-order test in the forward
+constexpr float IF_FAR = 1.0e6f; // -index of a padding column (far away)
+// the forward's tile load: each warp loads whole blocks of IF_SUB columns
+static_assert(IF_SUB == 32 && IF_TILE % IF_TS == 0 && IF_TS % 32 == 0, "tile load layout");
 
 struct IConst {
   int nx, ny, ncols, w;  // w: near window half width (columns)
@@ -266,6 +271,7 @@ __global__ void __launch_bounds__(IF_TS, 8)
   __shared__ __align__(8) float s_th[IF_TILE + 2];
   __shared__ __align__(8) float s_nx[IF_TILE + 2];  // -ix of the tile's columns
   __shared__ __align__(8) float s_ny[IF_TILE + 2];  // -iy
+  __shared__ float s_tmin[IF_TILE / IF_SUB];         // shallowest top per column block
   const int slot = blockIdx.x * IF_TS + threadIdx.x;  // stations in Z order
   const bool active = slot < ns;
   const int s = active ? perm[slot] : 0;
@@ -298,56 +304,78 @@ __global__ void __launch_bounds__(IF_TS, 8)
       s_w[q] = cq.x;
       s_top[q] = cq.y;
       s_th[q] = cq.z;
-      // a padding column sits on the station column (finite values; dropped)
-      s_nx[q] = ok ? -(float)(c % k.nx) : -(float)hi.x;
-      s_ny[q] = ok ? -(float)(c / k.nx) : -(float)hi.y;
+      // a padding column has zero weight and lies far away: its terms are
+      // finite and add zero
+      s_nx[q] = ok ? -(float)(c % k.nx) : IF_FAR;
+      s_ny[q] = ok ? -(float)(c / k.nx) : IF_FAR;
+      // the shallowest top of each block of IF_SUB columns (a warp loads one)
+      if (q < IF_TILE) {
+        float t = ok ? cq.y : 3.0e38f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t = fminf(t, __shfl_xor_sync(0xffffffffu, t, o));
+        if ((q & (IF_SUB - 1)) == 0) s_tmin[q / IF_SUB] = t;
+      }
     }
     __syncthreads();
     if (!active) continue;
     const int cnt = min(IF_TILE, c1 - t0);
-    float2 g = make_float2(0.f, 0.f);  // plain sums over 32 columns, Kahan across
+    for (int q0 = 0; q0 < cnt; q0 += IF_SUB) {
+      const int qe = min(cnt, q0 + IF_SUB);
+      // second order for the whole block when every station of the warp is
+      // far enough from every column of it: a lower bound of the squared
+      // distance to a column top from the block's column and row ranges
+      const int ca = t0 + q0, cb = t0 + qe - 1;
+      const int ya = ca / k.nx, yb = cb / k.nx;
+      const int xa = ya == yb ? ca % k.nx : 0, xb = ya == yb ? cb % k.nx : k.nx - 1;
+      auto gap = [](float lo, float hi) {  // min |v| for v between lo and hi
+        return (lo <= 0.f && hi >= 0.f) ? 0.f : fminf(fabsf(lo), fabsf(hi));
+      };
+      const float gx = gap(fmaf((float)(hi.x - xb), k.dxn, st.ex), fmaf((float)(hi.x - xa), k.dxn, st.ex));
+      const float gy = gap(fmaf((float)(hi.y - yb), k.dyn, st.ey), fmaf((float)(hi.y - ya), k.dyn, st.ey));
+      const float gz = fmaxf(0.f, st.zs + s_tmin[q0 / IF_SUB]);
+      const bool t2 = __all_sync(__activemask(), fmaf(gz, gz, fmaf(gx, gx, gy * gy)) >= k.rt2_t2);
+      auto run = [&](auto t2c) {
+        constexpr bool T2 = decltype(t2c)::value;
+        float2 g = make_float2(0.f, 0.f);  // plain sums over IF_SUB columns, Kahan across
 #pragma unroll 4
-    for (int q = 0; q < cnt; q += 2) {
-      // columns q and q+1 (the second is dropped past the end of the tile)
-      const float2 nx2 = *reinterpret_cast<const float2*>(s_nx + q);
-      const float2 ny2 = *reinterpret_cast<const float2*>(s_ny + q);
-      const float2 X = __ffma2_rn(__fadd2_rn(hx2, nx2), dxn2, ex2);
-      const float2 Y = __ffma2_rn(__fadd2_rn(hy2, ny2), dyn2, ey2);
-      const float2 X2 = __fmul2_rn(X, X), Y2 = __fmul2_rn(Y, Y), rh = __fadd2_rn(X2, Y2);
-      const float2 ut = __fadd2_rn(zs2, *reinterpret_cast<const float2*>(s_top + q));
-      const float2 rt2 = __ffma2_rn(ut, ut, rh);
-      const float2 th = *reinterpret_cast<const float2*>(s_th + q);
-      float2 itop, u;
-      // second order when every lane's pairs are far enough (warp-uniform)
-      const bool t2 = __all_sync(__activemask(), fminf(rt2.x, rt2.y) >= k.rt2_t2);
-      if (FACE) {
-        itop = make_float2(rsqrt_ftz(rt2.x), rsqrt_ftz(rt2.y));
-        u = t2 ? face_unit_far2<true>(X2, Y2, ut, itop, k.face)
-               : face_unit_far2<false>(X2, Y2, ut, itop, k.face);
-      } else {
-        u = t2 ? col_unit2<true>(X2, Y2, rh, ut, rt2, th, k, &itop)
-               : col_unit2<false>(X2, Y2, rh, ut, rt2, th, k, &itop);
-      }
-      float2 v = __fmul2_rn(*reinterpret_cast<const float2*>(s_w + q), u);
-      if (warp_near) {
-        // near columns contribute through the double path: select, which
-        // also drops a NaN
-        const int ixa = -(int)nx2.x, iya = -(int)ny2.x, ixb = -(int)nx2.y, iyb = -(int)ny2.y;
-        if (ixa >= wx0 && ixa <= wx1 && iya >= wy0 && iya <= wy1 &&
-            near_bit(mask, s, ixa - wx0 + wbw * (iya - wy0), k))
-          v.x = 0.f;
-        if (ixb >= wx0 && ixb <= wx1 && iyb >= wy0 && iyb <= wy1 &&
-            near_bit(mask, s, ixb - wx0 + wbw * (iyb - wy0), k))
-          v.y = 0.f;
-      }
-      if (q + 1 >= cnt) v.y = 0.f;  // the padding column
-      g = __fadd2_rn(g, v);
-      if ((q & 30) == 30) {
+        for (int q = q0; q < qe; q += 2) {
+          // columns q and q+1 (past the end of the tile: a padding column)
+          const float2 nx2 = *reinterpret_cast<const float2*>(s_nx + q);
+          const float2 ny2 = *reinterpret_cast<const float2*>(s_ny + q);
+          const float2 X = __ffma2_rn(__fadd2_rn(hx2, nx2), dxn2, ex2);
+          const float2 Y = __ffma2_rn(__fadd2_rn(hy2, ny2), dyn2, ey2);
+          const float2 X2 = __fmul2_rn(X, X), Y2 = __fmul2_rn(Y, Y), rh = __fadd2_rn(X2, Y2);
+          const float2 ut = __fadd2_rn(zs2, *reinterpret_cast<const float2*>(s_top + q));
+          const float2 rt2 = __ffma2_rn(ut, ut, rh);
+          const float2 th = *reinterpret_cast<const float2*>(s_th + q);
+          float2 itop, u;
+          if (FACE) {
+            itop = make_float2(rsqrt_ftz(rt2.x), rsqrt_ftz(rt2.y));
+            u = face_unit_far2<T2>(X2, Y2, ut, itop, k.face);
+          } else {
+            u = col_unit2<T2>(X2, Y2, rh, ut, rt2, th, k, &itop);
+          }
+          float2 v = __fmul2_rn(*reinterpret_cast<const float2*>(s_w + q), u);
+          if (warp_near) {
+            // near columns contribute through the double path: select, which
+            // also drops a NaN
+            const int ixa = -(int)nx2.x, iya = -(int)ny2.x, ixb = -(int)nx2.y, iyb = -(int)ny2.y;
+            if (ixa >= wx0 && ixa <= wx1 && iya >= wy0 && iya <= wy1 &&
+                near_bit(mask, s, ixa - wx0 + wbw * (iya - wy0), k))
+              v.x = 0.f;
+            if (ixb >= wx0 && ixb <= wx1 && iyb >= wy0 && iyb <= wy1 &&
+                near_bit(mask, s, ixb - wx0 + wbw * (iyb - wy0), k))
+              v.y = 0.f;
+          }
+          g = __fadd2_rn(g, v);
+        }
         acc.add(g.x + g.y);
-        g = make_float2(0.f, 0.f);
-      }
+      };
+      if (t2)
+        run(std::true_type{});
+      else
+        run(std::false_type{});
     }
-    acc.add(g.x + g.y);
   }
   if (active) partial[(size_t)blockIdx.y * ns + s] = acc.value();
 }
