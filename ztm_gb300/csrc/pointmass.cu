@@ -476,6 +476,97 @@ __global__ void __launch_bounds__(PM_TS)
   if (active) partial[(long long)blockIdx.y * p.ns + s] = acc.value();
 }
 
+// Double path by node columns: the same layout one node per entry,
+// (-k, w) in double, each column's (-i, -j) in double; per node the gather
+// forms Z, r^2 = Z^2 + (X^2 + Y^2), the rsqrt and the product in double.
+__device__ __forceinline__ double pm_col_weight64(const PmParams& p,
+                                                  const double* __restrict__ drho,
+                                                  const int* __restrict__ mult, long long n) {
+  const double w = drho[n];
+  if (mult) {
+    const int m = mult[n];
+    return m ? w * m : 0.0;
+  }
+  return fabs(w) > p.thr ? w : 0.0;
+}
+
+__global__ void pm_cols_count64(PmParams p, const double* __restrict__ drho,
+                                const int* __restrict__ mult, int* __restrict__ counts,
+                                double2* __restrict__ colxy) {
+  const long long ncols = (long long)p.ii * p.jj;
+  const long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (c >= ncols) return;
+  const long long ni = c % p.ii, nj = c / p.ii;
+  colxy[c] = make_double2(-(ni * (1.0 / p.fh)), -(nj * (1.0 / p.fh)));
+  int cnt = 0;
+  for (int k = 0; k < p.kk; k++)
+    if (pm_col_weight64(p, drho, mult, c + k * ncols) != 0.0) cnt++;
+  counts[c] = cnt;
+}
+
+__global__ void pm_cols_write64(PmParams p, const double* __restrict__ drho,
+                                const int* __restrict__ mult, const int* __restrict__ offs,
+                                double2* __restrict__ nodes) {
+  const long long ncols = (long long)p.ii * p.jj;
+  const long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (c >= ncols) return;
+  double2* out = nodes + offs[c];
+  int q = 0;
+  for (int k = 0; k < p.kk; k++) {
+    const double w = pm_col_weight64(p, drho, mult, c + k * ncols);
+    if (w != 0.0) out[q++] = make_double2(-(k * (1.0 / p.fv)), w);
+  }
+}
+
+__global__ void __launch_bounds__(PM_TS)
+    pm_gather_cols64_kernel(PmParams p, const double2* __restrict__ nodes,
+                            const int* __restrict__ offs, const double2* __restrict__ colxy,
+                            const double* __restrict__ surf, int cg_cols, int chunk_cols,
+                            double* __restrict__ partial) {
+  __shared__ double2 tile[PM_CT];
+  __shared__ int s_off[PM_CT + 1];
+  __shared__ double2 s_xy[PM_CT];
+  const int s = blockIdx.x * PM_TS + threadIdx.x;
+  const bool active = s < p.ns;
+  double i0 = 0.0, j0 = 0.0, k0 = 0.0;
+  if (active) {
+    const int si = p.bfr + s % p.ni, sj = p.bfr + s / p.ni;
+    i0 = (double)si;
+    j0 = (double)sj;
+    k0 = surf[si + sj * p.di];
+  }
+  const int ncols = p.ii * p.jj;
+  const int c0 = blockIdx.y * chunk_cols, c1 = min(ncols, c0 + chunk_cols);
+  double acc = 0.0;
+  for (int cg = c0; cg < c1; cg += cg_cols) {
+    const int ce = min(c1, cg + cg_cols);
+    __syncthreads();  // the previous group is consumed
+    for (int q = threadIdx.x; q <= ce - cg; q += PM_TS) {
+      s_off[q] = offs[cg + q];
+      if (q < ce - cg) s_xy[q] = colxy[cg + q];
+    }
+    __syncthreads();
+    const int p0 = s_off[0], nnode = s_off[ce - cg] - p0;  // <= PM_CT (host)
+    for (int q = threadIdx.x; q < nnode; q += PM_TS) tile[q] = nodes[p0 + q];
+    __syncthreads();
+    if (!active) continue;
+    for (int c = cg; c < ce; c++) {
+      const int a = s_off[c - cg] - p0, b = s_off[c - cg + 1] - p0;
+      const double2 xy = s_xy[c - cg];
+      const double X = i0 + xy.x, Y = j0 + xy.y;
+      const double rh = X * X + Y * Y;
+#pragma unroll 4
+      for (int q = a; q < b; q++) {
+        const double2 v = tile[q];  // (-k, w)
+        const double dz = k0 + v.x;
+        const double rs = rsqrt(dz * dz + rh);
+        acc += v.y * dz * (rs * rs * rs);
+      }
+    }
+  }
+  if (active) partial[(long long)blockIdx.y * p.ns + s] = acc;
+}
+
 // G[m] = factor * sum_chunks partial for interior m, 0 elsewhere.
 __global__ void pm_finalize_kernel(PmParams p, int nchunks,
                                    const double* __restrict__ partial,
@@ -498,7 +589,9 @@ __global__ void pm_finalize_kernel(PmParams p, int nchunks,
 int pm_occupancy(int precision, bool compacted, bool cols = false) {
   int occ = 0;
   cudaError_t e;
-  if (precision == ZTM_PREC_FP64)
+  if (precision == ZTM_PREC_FP64 && cols)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pm_gather_cols64_kernel, PM_TS, 0);
+  else if (precision == ZTM_PREC_FP64)
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pm_gather_kernel<true>, PM_TS, 0);
   else if (cols)
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pm_gather_cols_kernel, PM_TS, 0);
@@ -532,17 +625,19 @@ void pm_shape(const PmParams& p, int num_sms, int occ, int* tiles, int* chunks, 
   *clen = len;
 }
 
+// Entries of one column's run: node pairs (float) or nodes (double).
+int pm_col_entries(const PmParams& p, bool f64) { return f64 ? p.kk : (p.kk + 1) / 2; }
 // The column path: a column's run fits one shared-memory tile.
-bool pm_use_cols(const PmParams& p) { return (p.kk + 1) / 2 <= PM_CT; }
+bool pm_use_cols(const PmParams& p, bool f64 = false) { return pm_col_entries(p, f64) <= PM_CT; }
 
 // Column gather shape: station tiles x column chunks of whole column groups
 // (cg_cols columns, at most PM_CT pairs), about four waves of resident blocks.
-void pm_cols_shape(const PmParams& p, int num_sms, int* tiles, int* chunks, int* chunk_cols,
-                   int* cg_cols) {
-  const int occ = pm_occupancy(ZTM_PREC_FP32, true, true);
+void pm_cols_shape(const PmParams& p, int num_sms, bool f64, int* tiles, int* chunks,
+                   int* chunk_cols, int* cg_cols) {
+  const int occ = pm_occupancy(f64 ? ZTM_PREC_FP64 : ZTM_PREC_FP32, true, true);
   *tiles = std::max(1, (p.ns + PM_TS - 1) / PM_TS);
   const long long ncols = (long long)p.ii * p.jj;
-  *cg_cols = std::max(1, PM_CT / std::max(1, (p.kk + 1) / 2));
+  *cg_cols = std::max(1, PM_CT / std::max(1, pm_col_entries(p, f64)));
   const long long want = std::max(1LL, (4LL * occ * std::max(num_sms, 1) + *tiles - 1) / *tiles);
   const long long groups = (ncols + *cg_cols - 1) / *cg_cols;
   const long long ch = std::max(1LL, std::min(std::min(want, groups), 65535LL));
@@ -554,14 +649,15 @@ void pm_cols_shape(const PmParams& p, int num_sms, int* tiles, int* chunks, int*
 }  // namespace
 
 size_t ztm_pointmass_ws(const PmParams& p, int precision, int num_sms) {
-  if (precision != ZTM_PREC_FP64 && pm_use_cols(p)) {  // the float node columns
+  const bool f64 = precision == ZTM_PREC_FP64;
+  if (pm_use_cols(p, f64)) {  // the node columns
     int ct, cc, ccols, cg;
-    pm_cols_shape(p, num_sms, &ct, &cc, &ccols, &cg);
+    pm_cols_shape(p, num_sms, f64, &ct, &cc, &ccols, &cg);
     const long long ncols = (long long)p.ii * p.jj;
+    const size_t entries = f64 ? (size_t)p.N + 2 : (size_t)((p.N + ncols) / 2 + 2);
     return WsCarver::need((size_t)cc * std::max(p.ns, 1) * sizeof(double)) +
            WsCarver::need((size_t)(ncols + 1) * sizeof(int)) +
-           WsCarver::need((size_t)ncols * sizeof(float2)) +
-           WsCarver::need((size_t)((p.N + ncols) / 2 + 2) * sizeof(float4)) +
+           WsCarver::need((size_t)ncols * 16) + WsCarver::need(entries * 16) +
            WsCarver::need((size_t)p.N * sizeof(int));  // nn multiplicities
   }
   int tiles, chunks;
@@ -579,17 +675,41 @@ size_t ztm_pointmass_ws(const PmParams& p, int precision, int num_sms) {
 int ztm_launch_pointmass(ztm_ctx* c, const PmParams& p, const double* d_drho,
                          const int* d_nn, const double* d_surf, double* d_G,
                          double scale, int precision, WsCarver& wc) {
-  const bool cols = precision != ZTM_PREC_FP64 && pm_use_cols(p);
+  const bool f64 = precision == ZTM_PREC_FP64;
+  const bool cols = pm_use_cols(p, f64);
   int tiles, chunks, chunk_cols = 0, cg_cols = 0;
   long long len = 0;
   if (cols)
-    pm_cols_shape(p, c->num_sms, &tiles, &chunks, &chunk_cols, &cg_cols);
+    pm_cols_shape(p, c->num_sms, f64, &tiles, &chunks, &chunk_cols, &cg_cols);
   else
     pm_shape(p, c->num_sms, pm_occupancy(precision, true), &tiles, &chunks, &len);
   double* partial = wc.take<double>((size_t)chunks * std::max(p.ns, 1));
   if (p.ns > 0 && p.nnodes > 0) {
     dim3 grid(tiles, chunks);
-    if (precision == ZTM_PREC_FP64) {
+    if (cols && f64) {
+      const long long ncols = (long long)p.ii * p.jj;
+      int* offs = wc.take<int>((size_t)ncols + 1);
+      double2* colxy = wc.take<double2>((size_t)ncols);
+      double2* nodes = wc.take<double2>((size_t)p.N + 2);
+      int* mult = nullptr;
+      if (d_nn) {  // the listed nodes, with their multiplicities
+        mult = wc.take<int>((size_t)p.N);
+        cudaMemsetAsync(mult, 0, (size_t)p.N * sizeof(int), c->stream);
+        pm_nn_mark<<<(unsigned)((p.nnodes + 255) / 256), 256, 0, c->stream>>>(p, d_nn, mult,
+                                                                             c->d_err);
+        c->launches++;
+      }
+      const unsigned cb = (unsigned)((ncols + 255) / 256);
+      pm_cols_count64<<<cb, 256, 0, c->stream>>>(p, d_drho, mult, offs, colxy);
+      pm_nodes_scan<<<1, 1024, 0, c->stream>>>((int)ncols, offs, offs + ncols);
+      pm_cols_write64<<<cb, 256, 0, c->stream>>>(p, d_drho, mult, offs, nodes);
+      {
+        ZtmProf prof_(c, "pointmass");
+        pm_gather_cols64_kernel<<<grid, PM_TS, 0, c->stream>>>(p, nodes, offs, colxy, d_surf,
+                                                              cg_cols, chunk_cols, partial);
+      }
+      c->launches += 4;
+    } else if (precision == ZTM_PREC_FP64) {
       ZtmProf prof_(c, "pointmass");
       pm_gather_kernel<true><<<grid, PM_TS, 0, c->stream>>>(p, d_drho, d_nn, d_surf, len, partial,
                                                             c->d_err);
