@@ -342,6 +342,64 @@ __device__ __forceinline__ void far_column(const float* col, int lmask, int nz8,
   acc.add(g.x + g.y);
 }
 
+// Two columns A and B, eight layers l0..l0+7, second-order form, no mask:
+// one Z per layer pair serves both columns.
+__device__ __forceinline__ float2 far_group_pair(const float* colA, const float* colB, int l0,
+                                                 float fl, const float2 (&Zb)[4], float2 zstep,
+                                                 const ColPoly2& cpA, float2 c2tA,
+                                                 const ColPoly2& cpB, float2 c2tB, float2 g) {
+  const float4 raA = *reinterpret_cast<const float4*>(colA + l0);
+  const float4 rbA = *reinterpret_cast<const float4*>(colA + l0 + 4);
+  const float4 raB = *reinterpret_cast<const float4*>(colB + l0);
+  const float4 rbB = *reinterpret_cast<const float4*>(colB + l0 + 4);
+  const float2 l2 = make_float2(fl, fl);
+  float2 vA[4], vB[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    const float2 Z = __ffma2_rn(l2, zstep, Zb[j]);
+    vA[j] = far_unit2_t2(Z, cpA, c2tA);
+    vB[j] = far_unit2_t2(Z, cpB, c2tB);
+  }
+  g = __ffma2_rn(make_float2(raA.x, raA.y), vA[0], g);
+  g = __ffma2_rn(make_float2(raB.x, raB.y), vB[0], g);
+  g = __ffma2_rn(make_float2(raA.z, raA.w), vA[1], g);
+  g = __ffma2_rn(make_float2(raB.z, raB.w), vB[1], g);
+  g = __ffma2_rn(make_float2(rbA.x, rbA.y), vA[2], g);
+  g = __ffma2_rn(make_float2(rbB.x, rbB.y), vB[2], g);
+  g = __ffma2_rn(make_float2(rbA.z, rbA.w), vA[3], g);
+  return __ffma2_rn(make_float2(rbB.z, rbB.w), vB[3], g);
+}
+
+// All layers of two columns (nz a multiple of 8): plain float sums over 16
+// layers of both (32 terms), compensated across.
+__device__ __forceinline__ void far_column_pair(const float* colA, const float* colB, int nz,
+                                                const float2 (&Zb)[4], float2 zstep,
+                                                const ColPoly2& cpA, float2 c2tA,
+                                                const ColPoly2& cpB, float2 c2tB, Kahan& acc) {
+  int l0 = 0;
+  float fl = 0.f;
+  const float2 z0 = make_float2(0.f, 0.f);
+  for (; l0 + 64 <= nz; l0 += 64, fl += 64.f) {
+#pragma unroll
+    for (int h = 0; h < 4; h++) {
+      float2 g = far_group_pair(colA, colB, l0 + 16 * h, fl + 16.f * h, Zb, zstep, cpA, c2tA,
+                                cpB, c2tB, z0);
+      g = far_group_pair(colA, colB, l0 + 16 * h + 8, fl + 16.f * h + 8.f, Zb, zstep, cpA, c2tA,
+                         cpB, c2tB, g);
+      acc.add(g.x + g.y);
+    }
+  }
+  for (; l0 + 16 <= nz; l0 += 16, fl += 16.f) {
+    float2 g = far_group_pair(colA, colB, l0, fl, Zb, zstep, cpA, c2tA, cpB, c2tB, z0);
+    g = far_group_pair(colA, colB, l0 + 8, fl + 8.f, Zb, zstep, cpA, c2tA, cpB, c2tB, g);
+    acc.add(g.x + g.y);
+  }
+  if (l0 < nz) {
+    const float2 g = far_group_pair(colA, colB, l0, fl, Zb, zstep, cpA, c2tA, cpB, c2tB, z0);
+    acc.add(g.x + g.y);
+  }
+}
+
 // One shared-memory stage (ncol columns starting at column cs) against this
 // thread's station; adds to acc.  Every lane runs the loop (inactive lanes
 // on dummy data) for the warp votes.
@@ -359,6 +417,42 @@ __device__ __forceinline__ void far_stage(const FarArgs& a, const MeshConst& k, 
   const int lm8 = min((Lm + 7) & ~7, nz8);
   int ix = cs % k.nx, iy = cs / k.nx;
   for (int q = 0; q < ncol; q++) {
+    // two unmasked second-order columns at once where the warp allows it
+    if (nz8 == k.nz && q + 1 < ncol) {
+      int ix1 = ix + 1, iy1 = iy;
+      if (ix1 == k.nx) {
+        ix1 = 0;
+        ++iy1;
+      }
+      const float XA = fmaf((float)(t.ixs - ix), k.dxn, t.ex);
+      const float YA = fmaf((float)(t.iys - iy), k.dyn, t.ey);
+      const float XB = fmaf((float)(t.ixs - ix1), k.dxn, t.ex);
+      const float YB = fmaf((float)(t.iys - iy1), k.dyn, t.ey);
+      const float XA2 = XA * XA, YA2 = YA * YA, rhA = XA2 + YA2;
+      const float XB2 = XB * XB, YB2 = YB * YB, rhB = XB2 + YB2;
+      const bool nclA = ix >= t.nb.x0 && ix <= t.nb.x1 && iy >= t.nb.y0 && iy <= t.nb.y1;
+      const bool nclB = ix1 >= t.nb.x0 && ix1 <= t.nb.x1 && iy1 >= t.nb.y0 && iy1 <= t.nb.y1;
+      const bool unmasked = lm8 == 0 || !__any_sync(0xffffffffu, nclA || nclB);
+      if (unmasked && __all_sync(0xffffffffu, fminf(rhA, rhB) >= k.rh_t2)) {
+        const float cA = fmaf(-fc.a1, rhA, fmaf(XA2, fc.cA, YA2 * fc.cB));
+        const float cB = fmaf(-fc.a1, rhB, fmaf(XB2, fc.cA, YB2 * fc.cB));
+        ColPoly2 cpA, cpB;
+        cpA.rh = make_float2(rhA, rhA);
+        cpB.rh = make_float2(rhB, rhB);
+        cpA.a1 = cpB.a1 = make_float2(fc.a1, fc.a1);
+        cpA.C2 = cpA.C3 = cpA.C4 = cpB.C2 = cpB.C3 = cpB.C4 = make_float2(0.f, 0.f);
+        far_column_pair(rs + q * k.nzp, rs + (q + 1) * k.nzp, k.nz, Zb, zstep, cpA,
+                        make_float2(cA, cA), cpB, make_float2(cB, cB), acc);
+        q++;
+        ix = ix1 + 1;
+        iy = iy1;
+        if (ix == k.nx) {
+          ix = 0;
+          ++iy;
+        }
+        continue;
+      }
+    }
     const float X = fmaf((float)(t.ixs - ix), k.dxn, t.ex);
     const float Y = fmaf((float)(t.iys - iy), k.dyn, t.ey);
     const float X2 = X * X, Y2 = Y * Y, rh = X2 + Y2;
@@ -410,7 +504,7 @@ __device__ __forceinline__ void far_stage(const FarArgs& a, const MeshConst& k, 
 // The density of a far item's columns streams through two shared-memory
 // stages by 1-D bulk copies; the next far item's first stage is copied while
 // the current item's last stage (or a near item) is processed.
-__global__ void __launch_bounds__(FAR_TS, 7) far_kernel(FarArgs a) {
+__global__ void __launch_bounds__(FAR_TS, 6) far_kernel(FarArgs a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
   float* stage = reinterpret_cast<float*>(smem_raw + 128);
