@@ -35,7 +35,7 @@ namespace {
 
 constexpr int ADJ_TS = 128;
 constexpr int ADJ_LG = 32;     // layers per thread in the far kernel
-constexpr int ADJ_STILE = 128; // stations per shared-memory tile
+constexpr int ADJ_STILE = 64;  // stations per shared-memory tile
 constexpr int ADJ_SGRP = 32;   // stations per float sum
 
 constexpr int ADJ_NEAR_ST = 8;  // stations per near item (two per warp)
@@ -68,6 +68,7 @@ struct AdjSmem {
   int4 b[ADJ_STILE];   // the station's near box columns x0, x1, y0, y1
   float4 h[ADJ_STILE]; // the home cell indices as floats (exact)
   float r[ADJ_STILE];
+  float4 z[ADJ_STILE][ADJ_LG / 4];  // the station's Z at the item's 32 layers
   float2 acc[ADJ_LG][ADJ_TS];  // compensated float sums (sum, compensation)
 };
 
@@ -88,21 +89,19 @@ __device__ __forceinline__ void kahan2(float2& k, float x) {
 // polynomial, the near box test) is shared by the 32 layers.
 __device__ __forceinline__ void adj_far_item(const AdjArgs& a, int bx, int by, AdjSmem& sm) {
   const MeshConst& k = a.k;
-  const int ngroups = (k.nz + ADJ_LG - 1) / ADJ_LG;
-  const long long t = bx * (long long)ADJ_TS + threadIdx.x;
-  const bool active = t < (long long)k.ncols * ngroups;
-  int c = 0, lg = 0;
-  if (active) {
-    lg = (int)(t / k.ncols);
-    c = (int)(t % k.ncols);
-  }
+  // column tiles of one layer group each: a block's threads share the
+  // group, so a station's Z values are formed once per block (shared memory)
+  const int tpg = (k.ncols + ADJ_TS - 1) / ADJ_TS;  // column tiles per layer group
+  const int lg = bx / tpg;
+  const int cc = (bx % tpg) * ADJ_TS + threadIdx.x;
+  const bool active = cc < k.ncols;
+  const int c = active ? cc : 0;
   const int ix = c % k.nx, iy = c / k.nx;
   const int l0 = lg * ADJ_LG;
   const float fix = (float)ix, fiy = (float)iy, fl0 = (float)l0;
   const FarCoef fc = k.fc;
 #pragma unroll
   for (int j = 0; j < ADJ_LG; j++) sm.acc[j][threadIdx.x] = make_float2(0.f, 0.f);
-  const float2 dz2 = make_float2(k.dzn, k.dzn);
   // this item's slice of the stations
   const int sb = by * a.slice, se = min(a.ns, sb + a.slice);
   for (int s0 = sb; s0 < se; s0 += ADJ_STILE) {
@@ -116,11 +115,18 @@ __device__ __forceinline__ void adj_far_item(const AdjArgs& a, int bx, int by, A
         sm.b[q] = make_int4(b.x0, b.x1, b.y0, b.y1);
         sm.h[q] = make_float4((float)i.x, (float)i.y, (float)i.z, 0.f);
         sm.r[q] = (float)a.res[s];
+        const float zg = fmaf(fl0 - (float)i.z, k.dzn, a.sf[s].z);
+#pragma unroll
+        for (int j = 0; j < ADJ_LG / 4; j++)
+          sm.z[q][j] = make_float4(fmaf((float)(4 * j), k.dzn, zg), fmaf((float)(4 * j + 1), k.dzn, zg),
+                                   fmaf((float)(4 * j + 2), k.dzn, zg), fmaf((float)(4 * j + 3), k.dzn, zg));
       } else {
         sm.f[q] = make_float4(0.f, 0.f, 0.f, 0.f);
         sm.b[q] = make_int4(1, 0, 1, 0);
         sm.h[q] = make_float4(0.f, 0.f, 0.f, 0.f);
         sm.r[q] = 0.f;
+#pragma unroll
+        for (int j = 0; j < ADJ_LG / 4; j++) sm.z[q][j] = make_float4(1.f, 1.f, 1.f, 1.f);
       }
     }
     __syncthreads();
@@ -151,8 +157,11 @@ __device__ __forceinline__ void adj_far_item(const AdjArgs& a, int bx, int by, A
             ncl = false;
           }
         }
-        const float Zg = fmaf(fl0 - hf.z, k.dzn, f.z);
-        const float2 zg2 = make_float2(Zg, Zg);
+        // Z of layers l0 + 2j, l0 + 2j + 1
+        auto zof = [&](int j) {
+          const float4 z4 = sm.z[q][j >> 1];
+          return (j & 1) ? make_float2(z4.z, z4.w) : make_float2(z4.x, z4.y);
+        };
         const float2 w2 = make_float2(sm.r[q], sm.r[q]);
         float2 v[ADJ_LG / 2];
         // the warp's columns all far enough for the second-order form (the
@@ -166,15 +175,11 @@ __device__ __forceinline__ void adj_far_item(const AdjArgs& a, int bx, int by, A
           cp2.a1 = make_float2(fc.a1, fc.a1);
           cp2.C2 = cp2.C3 = cp2.C4 = make_float2(0.f, 0.f);  // unused by the form
 #pragma unroll
-          for (int j = 0; j < ADJ_LG / 2; j++)
-            v[j] = far_unit2_t2(
-                __ffma2_rn(make_float2((float)(2 * j), (float)(2 * j + 1)), dz2, zg2), cp2, c2t);
+          for (int j = 0; j < ADJ_LG / 2; j++) v[j] = far_unit2_t2(zof(j), cp2, c2t);
         } else {
           const ColPoly2 cp2 = col_poly2(col_poly(X, Y, fc), fc.a1);
 #pragma unroll
-          for (int j = 0; j < ADJ_LG / 2; j++)
-            v[j] = far_unit2(
-                __ffma2_rn(make_float2((float)(2 * j), (float)(2 * j + 1)), dz2, zg2), cp2);
+          for (int j = 0; j < ADJ_LG / 2; j++) v[j] = far_unit2(zof(j), cp2);
         }
         if (ncl || l0 + ADJ_LG > k.nz) {
 #pragma unroll
@@ -419,7 +424,6 @@ int ztm_launch_adjoint(ztm_ctx* c, const MeshDesc& m, int ns, const double* d_sx
   launch_mesh_station_prep(c, m, k.L0, ns, d_sxyz, sf, si);
   launch_mesh_near_iv(c, k, m, ns, si, d_sxyz, iv, lr);
   const int ngroups = (k.nz + ADJ_LG - 1) / ADJ_LG;
-  const long long threads = (long long)k.ncols * ngroups;
   const double scale = G5 * k.L0 * (double)k.dxn * k.dyn * k.dzn;
   const int cap = near_cap(k);
   if ((size_t)cap * 8 > 200 * 1024)
@@ -427,7 +431,7 @@ int ztm_launch_adjoint(ztm_ctx* c, const MeshDesc& m, int ns, const double* d_sx
   const bool f64 = precision == ZTM_PREC_MIXED;
   // station slices so that there are about eight far items per resident
   // block; the slices' sums meet in g by double atomics (g zeroed first)
-  const long long tiles = (threads + ADJ_TS - 1) / ADJ_TS;
+  const long long tiles = (long long)((k.ncols + ADJ_TS - 1) / ADJ_TS) * ngroups;
   const int grid = adj_grid(c->num_sms, f64);
   long long slices = std::max(1LL, (8LL * grid + tiles - 1) / tiles);
   slices = std::min(slices, std::max(1LL, (long long)(ns + ADJ_STILE - 1) / ADJ_STILE));
