@@ -515,8 +515,10 @@ void destroy_entry(ZtmGraphEntry& e) {
 }
 
 // Launch shapes the autotuner tries: {stage KB per model group, log2 of the
-// pairs per far item}.  The first is the default.
-constexpr int BATCH_SHAPES[][2] = {{16, 24}, {8, 24}, {32, 24}, {16, 23}, {16, 25},
+// pairs per far item}.  The first is the default (32 trial models on the
+// 256x256x64 mesh plus 16 regional meshes: 2^23 pairs 223 ms, 2^24 225 ms,
+// 2^25 229 ms, 2^22 223 ms with twice the partial sums).
+constexpr int BATCH_SHAPES[][2] = {{16, 23}, {8, 24}, {32, 24}, {16, 24}, {16, 25},
                                    {8, 23}, {32, 25}};
 
 int batch_run(ztm_ctx* c, const ztm_job* jobs, int njobs, bool dev, double G, double nq,
