@@ -158,8 +158,11 @@ int ztm_measure_peak(ztm_ctx* ctx, int kind, double* value);
  * (g/cc), surf di*dj station heights (grid units), G receives di*dj values
  * in mGal: interior stations get the sum, the rest are set to 0 (as the GPU
  * branch returns them, TFM.cpp:94).  If nn is non-NULL only the n_nn listed
- * nodes contribute (the CPU branch's list, TFM.cpp:89,97); otherwise nodes
- * with |drho| > grid->threshold.  precision: ZTM_PREC_FP64 or _FP32. */
+ * nodes contribute (the CPU branch's list, TFM.cpp:89,97; a node listed
+ * twice counts twice, as in that loop); otherwise nodes with
+ * |drho| > grid->threshold.  An nn entry outside the grid fails the call
+ * (ZTM_ERR_RANGE; with device pointers it is skipped on the device and
+ * reported at the call's end).  precision: ZTM_PREC_FP64 or _FP32. */
 int ztm_gfm_pointmass(ztm_ctx* ctx, const ztm_grid* grid, const double* drho,
                       const int* nn, long long n_nn, const double* surf,
                       double* G, int precision, int flags);
