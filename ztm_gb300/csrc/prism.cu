@@ -12,14 +12,17 @@
 //   FP64 plain  every pair with the 8-corner closed form in double.  One
 //               thread per station, prisms streamed through shared memory,
 //               per-chunk partials reduced in a fixed order.
-//   MIXED       pairs outside a per-station near box (every prism whose
+//   MIXED       pairs outside a station's near region (every prism whose
 //               centre is >= near_q half-diagonals away) use the 4th-order
-//               far-field expansion in float, Kahan-summed per thread; the
-//               near box is summed in double with vertex sharing (one Phi per
-//               box vertex instead of 8 per prism); partials and the final
-//               per-station sum are double.  The density of a block's columns
-//               is staged in shared memory by 1-D TMA bulk copies, double
-//               buffered on mbarriers.
+//               far-field expansion in float (second order beyond 48
+//               half-diagonals), two layers per packed instruction and two
+//               neighbouring columns per pass where the warp allows it,
+//               Kahan-summed per thread; the near region is summed in double
+//               with vertex sharing (one Phi per vertex instead of 8 per
+//               prism); partials and the final per-station sum are double.
+//               Stations are taken in Z order of their home cells.  The
+//               density of a block's columns is staged in shared memory by
+//               1-D TMA bulk copies, double buffered on mbarriers.
 //   FP32        as MIXED with the near box also in float.
 #include <cuda_runtime.h>
 #include <math.h>
