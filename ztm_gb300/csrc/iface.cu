@@ -38,6 +38,9 @@ namespace {
 constexpr int IF_TS = 128;
 constexpr int IF_TILE = 256;
 constexpr int IF_NEAR_WPB = 4;
+// forward blocks per SM to aim for (waves x residency): the Moho forward
+// took 1.75 ms at 8 (under one wave), 1.6 at 24, 1.55 at 48
+constexpr int IF_FWD_PER_SM = 48;
 constexpr int IF_SUB = 32;       // columns per second-order test in the forward
 constexpr float IF_FAR = 1.0e6f; // -index of a padding column (far away)
 // the forward's tile load: each warp loads whole blocks of IF_SUB columns
@@ -658,8 +661,8 @@ __global__ void residual_kernel(int ns, const double* __restrict__ gz,
   if (threadIdx.x == 0) *misfit = 0.5 * red[0];
 }
 
-int chunks_for(long long units, int tiles, int num_sms, int minlen, int* len) {
-  long long want = std::max(1LL, (8LL * std::max(num_sms, 1)) / std::max(tiles, 1));
+int chunks_for(long long units, int tiles, int num_sms, int minlen, int* len, int per_sm = 8) {
+  long long want = std::max(1LL, ((long long)per_sm * std::max(num_sms, 1)) / std::max(tiles, 1));
   long long ch = std::min<long long>(want, std::max(1LL, units / minlen));
   ch = std::max(1LL, std::min(ch, 65535LL));
   *len = (int)((units + ch - 1) / ch);
@@ -667,8 +670,9 @@ int chunks_for(long long units, int tiles, int num_sms, int minlen, int* len) {
   return (int)((units + *len - 1) / *len);
 }
 
-// Station slices of the mixed adjoint: about three waves of blocks of
-// column tiles x slices, slices of at least one shared-memory tile.
+// Station slices of the mixed adjoint: about twelve waves of blocks of
+// column tiles x slices (blocks finish unevenly; three waves left the end of
+// the launch half idle), slices of at least one shared-memory tile.
 int iface_adj_chunks(int ns, long long nc, int num_sms, int* len) {
   int occ = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, iface_far_adj, IF_TS, 0) != cudaSuccess ||
@@ -677,7 +681,7 @@ int iface_adj_chunks(int ns, long long nc, int num_sms, int* len) {
     occ = 1;
   }
   const long long tiles = std::max(1LL, (nc + IF_TS - 1) / IF_TS);
-  long long ch = std::max(1LL, 3LL * occ * std::max(num_sms, 1) / tiles);
+  long long ch = std::max(1LL, 12LL * occ * std::max(num_sms, 1) / tiles);
   ch = std::min(ch, std::max(1LL, (long long)(ns + IF_TILE - 1) / IF_TILE));
   ch = std::min(ch, 65535LL);
   *len = (int)((std::max(ns, 1) + ch - 1) / ch);
@@ -691,6 +695,8 @@ size_t ztm_iface_ws(const IMeshDesc& m, int ns, int precision, int num_sms) {
   int len;
   int tiles = std::max(1, (ns + 63) / 64);
   int ch = chunks_for(nc, tiles, num_sms, 64, &len);
+  ch = std::max(ch, chunks_for(nc, std::max(1, (ns + IF_TS - 1) / IF_TS), num_sms, IF_TILE, &len,
+                               IF_FWD_PER_SM));
   int cha = chunks_for(std::max(ns, 1), (int)((nc + IF_TS - 1) / IF_TS), num_sms, 32, &len);
   size_t w = WsCarver::need((size_t)ch * std::max(ns, 1) * 8) * 2;  // forward partials (x2 slack)
   w += WsCarver::need((size_t)cha * nc * 8) * 2;                    // double adjoint partials
@@ -762,7 +768,7 @@ static int iface_forward_impl(ztm_ctx* c, const IMeshDesc& m, const double* d_de
         k, m, ns, d_sxyz, si, d_depth, d_rho, d_vdep, mask, near);
   }
   int tiles = std::max(1, (ns + IF_TS - 1) / IF_TS), len;
-  int ch = chunks_for(nc, tiles, c->num_sms, IF_TILE, &len);
+  int ch = chunks_for(nc, tiles, c->num_sms, IF_TILE, &len, IF_FWD_PER_SM);
   double* partial = wc.take<double>((size_t)ch * ns);
   {
     ZtmProf prof_(c, "iface_far");
