@@ -631,14 +631,16 @@ int pm_col_entries(const PmParams& p, bool f64) { return f64 ? p.kk : (p.kk + 1)
 bool pm_use_cols(const PmParams& p, bool f64 = false) { return pm_col_entries(p, f64) <= PM_CT; }
 
 // Column gather shape: station tiles x column chunks of whole column groups
-// (cg_cols columns, at most PM_CT pairs), about four waves of resident blocks.
+// (cg_cols columns, at most PM_CT pairs), about sixteen waves of resident
+// blocks (62.4 ms at four waves, 61.2 at eight, 60.7 at sixteen on the
+// 256x256x65-node grid).
 void pm_cols_shape(const PmParams& p, int num_sms, bool f64, int* tiles, int* chunks,
                    int* chunk_cols, int* cg_cols) {
   const int occ = pm_occupancy(f64 ? ZTM_PREC_FP64 : ZTM_PREC_FP32, true, true);
   *tiles = std::max(1, (p.ns + PM_TS - 1) / PM_TS);
   const long long ncols = (long long)p.ii * p.jj;
   *cg_cols = std::max(1, PM_CT / std::max(1, pm_col_entries(p, f64)));
-  const long long want = std::max(1LL, (4LL * occ * std::max(num_sms, 1) + *tiles - 1) / *tiles);
+  const long long want = std::max(1LL, (16LL * occ * std::max(num_sms, 1) + *tiles - 1) / *tiles);
   const long long groups = (ncols + *cg_cols - 1) / *cg_cols;
   const long long ch = std::max(1LL, std::min(std::min(want, groups), 65535LL));
   const long long per = (groups + ch - 1) / ch;  // groups per chunk
