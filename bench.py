@@ -15,9 +15,10 @@ through the public API with pinned host buffers (H2D of density and
 stations and D2H of gz inside the timed region), the roofline of the
 dominant kernel against the measured FP32 FMA issue peak, and the CPU
 baseline (the double-precision oracle on the host cores, bounded sample).
-The reference arm times the reference's own gravity algorithm
-(TFM.cpp:95-99, point mass in double, restated in oracle/) on the host
-cores, on the same geometry, on a bounded station sample.
+The reference arm times the reference's own CPU gravity code (the lambda
+of TFM.cpp:95-99, point mass in double, compiled from TFM.cpp by
+oracle/build.py) on the host cores, on the same geometry, on a bounded
+sample of station rows and nodes.
 """
 import argparse
 import json
@@ -120,60 +121,58 @@ def cpu_baseline_prism(mesh, rho, st, nsample=224):
                       % (nsample, len(st), mesh.nx * mesh.ny * mesh.nz), "seconds": dt}
 
 
-def pointmass_mapping(mesh, rho, st):
-    """The 256x256x64 draped mesh on the reference's point-mass grid: node-centred
-    cells, h = 1 km horizontally, fv = 2 (0.5 km layers), g/cc, grid units;
-    the 66.7 constant assumes h = 10 km, so scale = h/10."""
-    import numpy as np
-    import ztm_gb300
-    nx, ny, nz = mesh.nx, mesh.ny, mesh.nz
-    kk = nz + 1 if nz % 2 == 0 else nz  # (dk-1)*fv+1 must hold every layer
-    dk = (kk - 1) // 2 + 1
-    g = ztm_gb300.make_grid(nx, ny, dk, 1, 2, 0, threshold=0.001, scale=mesh.dx / 10000.0)
-    drho = np.zeros(nx * ny * kk)
-    r = rho.reshape(nz, ny, nx) / 1000.0  # layer 0 on top -> highest k
-    for l in range(nz):
-        K = (kk - 1) - l - (kk - nz)
-        drho[K * nx * ny:(K + 1) * nx * ny] = r[l].ravel()
-    # node k (grid units of h) of the top layer centre: (kk-1-(kk-nz))/2
-    ktop = ((kk - 1) - (kk - nz)) / 2.0
-    surf = np.full(nx * ny, ktop + 0.25 + 1.0)
-    for x, y, z in st:
-        i, j = int(x // mesh.dx), int(y // mesh.dy)
-        surf[i + nx * j] = ktop + (z / 1000.0 + 0.25) / (mesh.dx / 1000.0)
-    return g, drho, surf
-
-
 def run_reference(args, rank):
-    """The reference's CPU algorithm (TFM.cpp:95-99) on the host cores."""
+    """The reference's own CPU gravity code (TFM.cpp:95-99: the GFM lambda,
+    cut verbatim out of TFM.cpp and compiled with g++ -O3 into
+    oracle/_ref/libref_tfm.so) on the host cores, one std::thread per
+    station row as TFM.cpp:99 launches it, on the same geometry mapped onto
+    its node grid.  A step is a bounded sample: as many station rows as the
+    host has cores, each over every 16th selected node (the per-pair work is
+    that of the full sum)."""
     if rank != 0:
         return 0
     import numpy as np
     import oracle
     from ztm_gb300 import synth
     mesh, rho, st = synth.draped_mesh_256x256x64()
-    g, drho, surf = pointmass_mapping(mesh, rho, st)
-    ns_sample = int(os.environ.get("ZTM_REF_SAMPLE", "128"))
-    nn = np.nonzero(np.abs(drho) > g.threshold)[0].astype(np.int32)
+    g, drho, surf = synth.pointmass_grid_of_mesh(mesh, rho, st)
+    nn_all = np.nonzero(np.abs(drho) > g.threshold)[0].astype(np.int32)
+    stride = int(os.environ.get("ZTM_REF_NODE_STRIDE", "16"))
+    nn = np.ascontiguousarray(nn_all[::stride])
+    rows = max(1, min(g.dj, os.cpu_count() or 1))
+    if oracle.ref_tfm_available():
+        kind, algo = "reference", ("the reference's own GFM lambda (TFM.cpp:95-99, point mass in "
+                                   "double) cut verbatim out of TFM.cpp and compiled with g++ -O3 "
+                                   "(oracle/_ref/libref_tfm.so); one thread per station row")
+
+        def sample():
+            oracle.ref_tfm_rows(g, drho, surf, 0, rows, nn=nn)
+    else:  # no reference sources and no generated harness: the restatement
+        kind, algo = "port", ("TFM.cpp:95-99 restated operation for operation in oracle/oracle.c "
+                              "(bit-identical to the compiled lambda where both exist)")
+
+        def sample():
+            oracle.pointmass_tfm_sample(g, drho, surf, 0, rows * g.di, nn=nn, nthreads=rows)
     times = []
     for it in range(args.warmup + args.steps):
         t0 = time.perf_counter()
-        oracle.pointmass_tfm_sample(g, drho, surf, 0, ns_sample, nn=nn)
+        sample()
         dt = time.perf_counter() - t0
         if it >= args.warmup:
             times.append(dt)
-    pairs = ns_sample * nn.size
+    pairs = rows * g.di * nn.size
     value = pairs * len(times) / sum(times)
+    smp = ("%d station rows x %d stations x %d of the %d selected nodes (every %dth) per step"
+           % (rows, g.di, nn.size, nn_all.size, stride))
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": config_dict(args.gpus),
-            "algorithm": "point mass in double, TFM.cpp:95-99 (the reference's CPU gravity path), "
-                         "restated in oracle/oracle.c; same geometry as our arm, node-centred",
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": oracle.NTHREADS, "kind": "port",
-                             "sample": "%d of %d stations x %d nodes per step"
-                                       % (ns_sample, mesh.nx * mesh.ny, nn.size)},
+            "algorithm": algo + "; same geometry as our arm on the reference's node grid "
+                                "(h = 1 km, fv = 2)",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": rows, "kind": kind,
+                             "sample": smp},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -316,6 +315,7 @@ def extras(ctx, mesh, rho, st, d_rho, d_st, gz_mixed):
     import numpy as np
     import torch
     import oracle
+    from ztm_gb300 import synth
     out = {}
     np_ = mesh.nx * mesh.ny * mesh.nz
     stream = torch.cuda.ExternalStream(ctx.stream)
@@ -347,7 +347,7 @@ def extras(ctx, mesh, rho, st, d_rho, d_st, gz_mixed):
                        "ms": msa, "what": "d misfit / d rho, all pairs, mixed"}
     # the reference's own point-mass model on the same geometry (its grid,
     # every node as a station): our float and double gathers
-    g, drho, surf = pointmass_mapping(mesh, rho, st)
+    g, drho, surf = synth.pointmass_grid_of_mesh(mesh, rho, st)
     nodes32 = int(np.count_nonzero(np.abs(drho.astype(np.float32)) > 0.001))
     nodes64 = int(np.count_nonzero(np.abs(drho) > 0.001))
     dd, dsf = torch.tensor(drho, device="cuda"), torch.tensor(surf, device="cuda")
@@ -479,7 +479,7 @@ def run_workload(args, local_rank):
         step = lambda: ctx.batch(djobs)
     elif args.workload == "pointmass":
         mesh, rho, st = synth.draped_mesh_256x256x64()
-        g, drho, surf = pointmass_mapping(mesh, rho, st)
+        g, drho, surf = synth.pointmass_grid_of_mesh(mesh, rho, st)
         dd, dsf = d(drho), d(surf)
         units = int(np.count_nonzero(np.abs(drho.astype(np.float32)) > 0.001)) * mesh.nx * mesh.ny
         what = ("the reference's point-mass model (float) on the 256x256x64 draped-mesh geometry, its grid: "

@@ -11,6 +11,9 @@ Contents (oracle.c):
   prism_* / face  published closed form (no reference implementation)
   ref_gf          the reference GF kernel itself (compiled unchanged into
                   oracle/_ref/gf_ref.cubin) run on a GPU through the driver API
+  ref_tfm         the reference's CPU gravity lambda itself (TFM.cpp:95-99 cut
+                  verbatim out of TFM.cpp into oracle/_ref/tfm_gfm.cpp and
+                  compiled with g++), all interior rows or a range of rows
 """
 import ctypes
 import os
@@ -21,6 +24,7 @@ from . import build as _build
 
 _lib = None
 _runner = None
+_tfm = None
 NTHREADS = max(1, os.cpu_count() or 1)
 
 
@@ -223,3 +227,58 @@ def ref_gf(grid, rho32, s32, reps=1):
     if rc != 0:
         raise RuntimeError("reference GF run failed with code %d" % rc)
     return g, ms.value
+
+
+# ---- the reference's CPU lambda itself (TFM.cpp:95-99) -------------------
+def ref_tfm_available():
+    _build.build()
+    return os.path.exists(_build.TFM_LIB)
+
+
+def _tfm_lib():
+    global _tfm
+    if _tfm is None:
+        if not ref_tfm_available():
+            raise RuntimeError("oracle/_ref/libref_tfm.so is not built (no reference TFM.cpp and "
+                               "no generated harness)")
+        t = ctypes.CDLL(_build.TFM_LIB)
+        P = ctypes.c_void_p
+        I = ctypes.c_int
+        LL = ctypes.c_longlong
+        t.ref_tfm_gfm.argtypes = [I, I, I, I, I, I, P, LL, P, LL, P, P]
+        t.ref_tfm_gfm.restype = None
+        t.ref_tfm_gfm_rows.argtypes = [I, I, I, I, I, I, P, LL, P, LL, P, P, I, I]
+        t.ref_tfm_gfm_rows.restype = None
+        _tfm = t
+    return _tfm
+
+
+def _tfm_args(grid, drho, surf, nn):
+    drho = _f64(drho)
+    surf = _f64(surf)
+    if nn is None:
+        nn = np.nonzero(np.abs(drho) > grid.threshold)[0]
+    nn = np.ascontiguousarray(nn, dtype=np.int32)
+    return drho, surf, nn
+
+
+def ref_tfm(grid, drho, surf, nn=None):
+    """G (di*dj) from the reference's own compiled lambda, every interior
+    row on its own thread, as TFM.cpp:99 launches it; non-interior 0."""
+    t = _tfm_lib()
+    drho, surf, nn = _tfm_args(grid, drho, surf, nn)
+    G = np.zeros(grid.di * grid.dj)
+    t.ref_tfm_gfm(grid.di, grid.dj, grid.dk, grid.fh, grid.fv, grid.bfr, _p(drho), drho.size,
+                  _p(nn), nn.size, _p(surf), _p(G))
+    return G * grid.scale if grid.scale != 1.0 else G
+
+
+def ref_tfm_rows(grid, drho, surf, row_lo, row_hi, nn=None):
+    """The reference lambda on station rows j0 in [row_lo, row_hi) only (one
+    thread per row); returns (G, nodes summed).  Unscaled (grid units)."""
+    t = _tfm_lib()
+    drho, surf, nn = _tfm_args(grid, drho, surf, nn)
+    G = np.zeros(grid.di * grid.dj)
+    t.ref_tfm_gfm_rows(grid.di, grid.dj, grid.dk, grid.fh, grid.fv, grid.bfr, _p(drho), drho.size,
+                       _p(nn), nn.size, _p(surf), _p(G), int(row_lo), int(row_hi))
+    return G, nn.size

@@ -3,10 +3,19 @@
   oracle/_build/liboracle.so   the C restatement (oracle.c), gcc, -ffp-contract=off
   oracle/_build/libref_runner.so  driver-API loader of the reference GF kernel
   oracle/_ref/gf_ref.cubin     the reference GFM_GPU.cu kernel compiled UNCHANGED
-                               from the reference sources (only where they exist;
-                               the GPU host reuses the image built here)
+                               from the reference sources
+  oracle/_ref/tfm_gfm.cpp      the reference's CPU gravity lambda (TFM.cpp:95-99)
+                               cut VERBATIM out of TFM.cpp into a small C
+                               harness (generated, never committed)
+  oracle/_ref/libref_tfm.so    that harness compiled with g++
+
+The reference directory is ZTM_REFERENCE_DIR (default: the read-only copy
+this repository was built beside).  Where it is absent (the GPU host), the
+generated harness source that travels in oracle/_ref/ is compiled there; the
+cubin is GPU code and is used as it is.
 """
 import os
+import re
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -15,7 +24,11 @@ REF = os.path.join(HERE, "_ref")
 LIB = os.path.join(BUILD, "liboracle.so")
 RUNNER = os.path.join(BUILD, "libref_runner.so")
 CUBIN = os.path.join(REF, "gf_ref.cubin")
-REF_GFM = "/root/reference/GFM_GPU.cu"
+TFM_SRC = os.path.join(REF, "tfm_gfm.cpp")
+TFM_LIB = os.path.join(REF, "libref_tfm.so")
+REF_DIR = os.environ.get("ZTM_REFERENCE_DIR", "/root/reference")
+REF_GFM = os.path.join(REF_DIR, "GFM_GPU.cu")
+REF_TFM = os.path.join(REF_DIR, "TFM.cpp")
 
 
 def _run(cmd):
@@ -26,6 +39,98 @@ def _run(cmd):
 
 def _stale(t, deps):
     return not os.path.exists(t) or any(os.path.getmtime(d) > os.path.getmtime(t) for d in deps)
+
+
+# The harness around the reference lambda.  The lambda captures by reference
+# exactly the names FM::FM has in scope at TFM.cpp:95 (di, dj, bfr, ii, jj, fh,
+# fv, surf, G, nn, drho; zmath.cpp:19-21 supplies vec, ivec and thread), so the
+# harness declares those and nothing else.
+_HARNESS_HEAD = """\
+// GENERATED by oracle/build.py from the reference's TFM.cpp -- not committed.
+// The lines marked VERBATIM are copied unchanged from TFM.cpp (line numbers
+// in the markers); everything else is the harness that gives them their
+// scope.  Test and baseline infrastructure only.
+#include <math.h>
+#include <thread>
+#include <vector>
+typedef std::vector<double> vec;  // zmath.cpp:19
+typedef std::vector<int> ivec;    // zmath.cpp:19
+using std::thread;                // zmath.cpp:21
+
+// G (di*dj) from drho (N fine-grid nodes), nn (n_nn indices) and surf (di*dj),
+// through TFM.cpp:95-99 as written: one std::thread per interior station row.
+extern "C" void ref_tfm_gfm(int di, int dj, int dk, int fh, int fv, int bfr, const double* drho_p,
+                            long long N, const int* nn_p, long long n_nn, const double* surf_p,
+                            double* G_p) {
+  int ii = (di - 1) * fh + 1, jj = (dj - 1) * fh + 1;  // TFM.cpp:83
+  (void)dk;
+  vec drho(drho_p, drho_p + N), surf(surf_p, surf_p + (long long)di * dj);
+  vec G(G_p, G_p + (long long)di * dj);
+  ivec nn(nn_p, nn_p + n_nn);
+"""
+
+_HARNESS_ROWS = """\
+  for (long long m = 0; m < (long long)di * dj; m++) G_p[m] = G[m];
+}
+
+// The same lambda for the interior rows j0 in [row_lo, row_hi) only, one
+// std::thread per row (the reference's own threading): a bounded sample of
+// the full call for timing.  Rows outside the range are left as passed in.
+extern "C" void ref_tfm_gfm_rows(int di, int dj, int dk, int fh, int fv, int bfr,
+                                 const double* drho_p, long long N, const int* nn_p,
+                                 long long n_nn, const double* surf_p, double* G_p, int row_lo,
+                                 int row_hi) {
+  int ii = (di - 1) * fh + 1, jj = (dj - 1) * fh + 1;  // TFM.cpp:83
+  (void)dk;
+  vec drho(drho_p, drho_p + N), surf(surf_p, surf_p + (long long)di * dj);
+  vec G(G_p, G_p + (long long)di * dj);
+  ivec nn(nn_p, nn_p + n_nn);
+"""
+
+_HARNESS_TAIL = """\
+  std::vector<thread> rows;
+  for (int j0 = row_lo; j0 < row_hi; j0++)
+    if (j0 >= bfr && j0 < dj - bfr) rows.emplace_back(GFM, j0);
+  for (auto& t : rows) t.join();
+  for (long long m = 0; m < (long long)di * dj; m++) G_p[m] = G[m];
+}
+"""
+
+
+def extract_tfm_lambda(tfm_path=REF_TFM):
+    """The CPU gravity branch of FM::FM (TFM.cpp:95-99), verbatim: the thread
+    array, the three lines of the GFM lambda, and the launch/join line.
+    Returns (thread_decl, lambda_lines, launch, first_line_number)."""
+    lines = open(tfm_path, encoding="latin-1").read().split("\n")
+    start = next(i for i, l in enumerate(lines) if "auto GFM=[&](int j0)" in l)
+    end = next(i for i in range(start, len(lines)) if "}}};" in lines[i])
+    lam = [lines[i].strip() for i in range(start, end + 1)]
+    decl_line = lines[start - 1]
+    m = re.search(r"thread GR\[dj-2\*bfr\];", decl_line)
+    if not m:
+        raise RuntimeError("TFM.cpp: no thread array before the GFM lambda")
+    launch_line = lines[end + 1]
+    m2 = re.search(r"for\(int j=0;j<dj-2\*bfr;j\+\+\)\{GR\[j\]=thread\(GFM,j\+bfr\);\} "
+                   r"for\(auto&w:GR\)\{w\.join\(\);\}", launch_line)
+    if not m2:
+        raise RuntimeError("TFM.cpp: no launch line after the GFM lambda")
+    return m.group(0), lam, m2.group(0), start + 1
+
+
+def write_tfm_harness(tfm_path=REF_TFM, out=TFM_SRC):
+    decl, lam, launch, first = extract_tfm_lambda(tfm_path)
+    n0, n1 = first - 1, first + len(lam)
+    body = ["  // VERBATIM TFM.cpp:%d (from 'thread GR')" % n0, "  " + decl]
+    body.append("  // VERBATIM TFM.cpp:%d-%d" % (first, first + len(lam) - 1))
+    body += ["  " + l for l in lam]
+    body += ["  // VERBATIM TFM.cpp:%d (up to the join)" % n1, "  " + launch]
+    rows = ["  // VERBATIM TFM.cpp:%d-%d" % (first, first + len(lam) - 1)] + ["  " + l for l in lam]
+    src = (_HARNESS_HEAD + "\n".join(body) + "\n" + _HARNESS_ROWS + "\n".join(rows) + "\n" +
+           _HARNESS_TAIL)
+    os.makedirs(os.path.dirname(out), exist_ok=True)
+    with open(out, "w") as f:
+        f.write(src)
+    return out
 
 
 def build(force=False):
@@ -48,6 +153,13 @@ def build(force=False):
         if force or _stale(CUBIN, [wrap, REF_GFM]):
             _run(["nvcc", "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3",
                   '-DZTM_REF_GFM="%s"' % REF_GFM, "-o", CUBIN, wrap])
+    if os.path.exists(REF_TFM) and (force or _stale(TFM_SRC, [REF_TFM, __file__])):
+        write_tfm_harness()
+    if os.path.exists(TFM_SRC) and (force or _stale(TFM_LIB, [TFM_SRC])):
+        # the reference builds with g++ -O3 (TFM.cpp:11); contraction is
+        # switched off so that x86 and Arm hosts round alike
+        _run(["g++", "-O3", "-std=c++14", "-ffp-contract=off", "-fPIC", "-shared", "-pthread",
+              "-o", TFM_LIB, TFM_SRC])
     return LIB
 
 

@@ -57,6 +57,35 @@ def test_tfm_threshold_selects_like_nn():
                           oracle.pointmass_tfm(g, drho, surf, nn=nn))
 
 
+@pytest.mark.skipif(not oracle.ref_tfm_available(), reason="reference TFM.cpp lambda not built")
+@pytest.mark.parametrize("dims", [(21, 19, 9, 1, 2, 3), (61, 61, 33, 1, 2, 10), (16, 16, 9, 1, 3, 0),
+                                  (31, 29, 17, 2, 2, 5), (5, 5, 2, 1, 1, 0)])
+def test_restatement_equals_reference_lambda(dims):
+    """The restatement of TFM.cpp:95-99 against the reference's own lambda,
+    cut verbatim out of TFM.cpp and compiled (oracle/build.py): bit for bit,
+    with the threshold list and with a list holding duplicates."""
+    di, dj, dk, fh, fv, bfr = dims
+    g = ztm_gb300.make_grid(di, dj, dk, fh, fv, bfr)
+    drho, surf = tfm_like_inputs(di, dj, dk, fh, fv, seed=di + dk)
+    assert np.array_equal(oracle.ref_tfm(g, drho, surf), oracle.pointmass_tfm(g, drho, surf))
+    nn = np.nonzero(np.abs(drho) > 0.05)[0].astype(np.int32)
+    nn = np.concatenate([nn, nn[::5]])
+    assert np.array_equal(oracle.ref_tfm(g, drho, surf, nn=nn),
+                          oracle.pointmass_tfm(g, drho, surf, nn=nn))
+
+
+@pytest.mark.skipif(not oracle.ref_tfm_available(), reason="reference TFM.cpp lambda not built")
+def test_reference_lambda_rows_sample_matches_full():
+    """The row-range entry (the bench's bounded sample) is the same lambda."""
+    g = ztm_gb300.make_grid(31, 29, 17, 1, 2, 5)
+    drho, surf = tfm_like_inputs(31, 29, 17, seed=9)
+    full = oracle.ref_tfm(g, drho, surf).reshape(29, 31)
+    part, _ = oracle.ref_tfm_rows(g, drho, surf, 7, 12)
+    part = part.reshape(29, 31)
+    assert np.array_equal(part[7:12], full[7:12])
+    assert np.all(part[:7] == 0) and np.all(part[12:] == 0)
+
+
 @pytest.mark.parametrize("name", sorted(f for f in os.listdir(os.path.join(HERE, "golden"))
                                         if f.startswith("gf_") and f.endswith(".npz")))
 def test_golden_reference_gf_outputs(name):

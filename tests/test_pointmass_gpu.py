@@ -1,11 +1,13 @@
 """Point-mass model (the reference's algorithm) on the GPU against the
-oracle restatement of TFM.cpp:95-99 and against the reference GF kernel."""
+reference's own CPU lambda (TFM.cpp:95-99 compiled from TFM.cpp), the oracle
+restatement of it, and the reference GF kernel."""
 import numpy as np
 import pytest
 
 import oracle
 import ztm_gb300
 from helpers import rel_err, tfm_like_inputs
+from ztm_gb300 import synth
 
 pytestmark = pytest.mark.gpu
 
@@ -114,3 +116,40 @@ def test_bad_node_index_on_device_is_reported(ctx):
         ctx.pointmass(g, torch.tensor(drho, device="cuda"), torch.tensor(surf, device="cuda"),
                       nn=torch.tensor(nn, device="cuda"), precision="fp32")
         ctx.sync()
+
+
+needs_ref_tfm = pytest.mark.skipif(not oracle.ref_tfm_available(),
+                                   reason="reference TFM.cpp lambda not built")
+
+
+@needs_ref_tfm
+@pytest.mark.parametrize("dims", [(16, 16, 9, 1, 3, 0), (31, 29, 17, 1, 2, 5),
+                                  (61, 61, 33, 1, 2, 10), (21, 19, 9, 2, 2, 3)])
+def test_fp64_matches_reference_lambda(ctx, dims):
+    """The double path against the reference's own compiled lambda (the
+    golden dims of tests/golden and TFM's 61x61x33), with its threshold list
+    and with an explicit list holding duplicates."""
+    di, dj, dk, fh, fv, bfr = dims
+    g = ztm_gb300.make_grid(di, dj, dk, fh, fv, bfr)
+    drho, surf = tfm_like_inputs(di, dj, dk, fh, fv, seed=3 * di + dk)
+    ref = oracle.ref_tfm(g, drho, surf)
+    assert rel_err(ctx.pointmass(g, drho, surf, precision="fp64"), ref) <= TOL64
+    nn = np.nonzero(np.abs(drho) > 0.05)[0].astype(np.int32)
+    nn = np.concatenate([nn, nn[::4]])
+    ref = oracle.ref_tfm(g, drho, surf, nn=nn)
+    assert rel_err(ctx.pointmass(g, drho, surf, nn=nn, precision="fp64"), ref) <= TOL64
+
+
+@needs_ref_tfm
+def test_fp64_plain_mesh_on_reference_grid(ctx):
+    """The 64x64x32 plain mesh (2x2x1 km cells) on the reference's node grid
+    (h = 2 km, fv = 2, every node a station): the double path against the
+    compiled reference lambda, normwise and per station (stations whose
+    field is not near a zero crossing)."""
+    mesh, rho, st = synth.plain_mesh_64x64x32()
+    g, drho, surf = synth.pointmass_grid_of_mesh(mesh, rho, st)
+    ref = oracle.ref_tfm(g, drho, surf)
+    out = ctx.pointmass(g, drho, surf, precision="fp64")
+    assert rel_err(out, ref) <= TOL64
+    big = np.abs(ref) > 1e-3 * np.abs(ref).max()
+    assert np.max(np.abs(out - ref)[big] / np.abs(ref)[big]) <= 1e-10

@@ -81,3 +81,30 @@ def test_shim_reference_default_dims_short_input(tmp_path):
                                drho.astype(np.float32).astype(np.float64),
                                surf.astype(np.float32).astype(np.float64))
     assert rel_err(g, ref) <= 1e-5
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+def test_shim_threshold_is_gf_float_rule(tmp_path, prec):
+    """GF selects fabs(rho) > .001f on the float values of R.dat
+    (GFM_GPU.cu:19): nodes stored as exactly 0.001f (whose double value is
+    just above 0.001) and -0.001f contribute nothing, in either precision."""
+    dims = (21, 19, 9, 1, 2, 3)
+    drho, surf = tfm_like_inputs(*dims[:3], seed=4)
+    r32 = drho.astype(np.float32)
+    at = np.nonzero(r32 != 0)[0][::7]
+    r32[at[::2]] = np.float32(0.001)
+    r32[at[1::2]] = np.float32(-0.001)
+    r32.tofile(os.path.join(tmp_path, "R.dat"))
+    surf.astype(np.float32).tofile(os.path.join(tmp_path, "S.dat"))
+    r = run_shim(tmp_path, dims, {"ZTM_GFM_PRECISION": prec})
+    assert r.returncode == 0, r.stderr
+    g = np.fromfile(os.path.join(tmp_path, "G.dat"), dtype=np.float32)
+    grid = ztm_gb300.make_grid(*dims)
+    r64 = r32.astype(np.float64)
+    nn = np.nonzero(np.abs(r32) > np.float32(0.001))[0]
+    ref = oracle.pointmass_tfm(grid, r64, surf.astype(np.float32).astype(np.float64), nn=nn)
+    assert rel_err(g, ref) <= 1e-5
+    # the double threshold would have counted the 0.001f nodes (6e-3 here)
+    wrong = oracle.pointmass_tfm(grid, r64, surf.astype(np.float32).astype(np.float64))
+    assert rel_err(wrong, ref) > 1e-3

@@ -8,9 +8,13 @@
 // ("di,dj,dk,fh,fv,bfr"), else from <dir>/GFM.cfg (same six integers), else
 // the reference defaults 61,61,35,1,2,10 (GFM_GPU.cu:24).  <dir> is
 // ZTM_GFM_DIR or /dev/shm.  ZTM_GFM_PRECISION=fp64 selects the double
-// kernel (default fp32, the reference's arithmetic).  A short R.dat is
-// zero-filled (the reference leaves that tail uninitialised).  Exit status:
+// kernel (default fp32, the reference's arithmetic).  Nodes are selected by
+// GF's own test on the float values of R.dat, fabs(rho) > .001f
+// (GFM_GPU.cu:19), in both precisions, so that a node at exactly 0.001f is
+// left out as the reference leaves it out.  A short R.dat is zero-filled (the
+// reference leaves that tail uninitialised).  Exit status:
 // 0 on success, 1 on a file error, 2 on a library error.
+#include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -68,6 +72,9 @@ int main() {
     return 1;
   }
   std::vector<double> drho(r32.begin(), r32.end()), surf(s32.begin(), s32.end()), G(M);
+  std::vector<int> nn;  // GF's selection, GFM_GPU.cu:19, on the float values
+  for (long long n = 0; n < N; n++)
+    if (fabsf(r32[n]) > .001f) nn.push_back((int)n);
   const char* prec = getenv("ZTM_GFM_PRECISION");
   int p = (prec && !strcmp(prec, "fp64")) ? ZTM_PREC_FP64 : ZTM_PREC_FP32;
   ztm_ctx* ctx = nullptr;
@@ -76,7 +83,8 @@ int main() {
     fprintf(stderr, "GFM: no CUDA device (status %d)\n", rc);
     return 2;
   }
-  rc = ztm_gfm_pointmass(ctx, &g, drho.data(), nullptr, 0, surf.data(), G.data(), p, 0);
+  rc = ztm_gfm_pointmass(ctx, &g, drho.data(), nn.data(), (long long)nn.size(), surf.data(),
+                         G.data(), p, 0);
   if (rc != ZTM_OK) {
     fprintf(stderr, "GFM: %s\n", ztm_last_error(ctx));
     ztm_ctx_destroy(ctx);

@@ -10,7 +10,7 @@ standardised.  Fractal topography: spectral synthesis with power
 """
 import numpy as np
 
-from .gfm import make_imesh, make_mesh
+from .gfm import make_grid, make_imesh, make_mesh
 
 
 def gaussian_field(shape, spacing, corr, rng):
@@ -141,3 +141,28 @@ def line_search_batch(seed=4, n_trials=32, n_regional=16):
 def moho_columns_512(seed=5):
     """Interface inversion: 512x512 columns of 0.5 km, 256x256 stations."""
     return moho_columns(seed=seed, n=512, ns_side=256, cell=500.0)
+
+
+def pointmass_grid_of_mesh(mesh, rho, st):
+    """A prism mesh with 2:1 horizontal:vertical cells (configs 1 and 2) on
+    the reference's point-mass grid (TFM.cpp:83): node-centred cells,
+    fh = 1, fv = 2 (a layer is half a grid unit), bfr = 0, densities in g/cc
+    with layer 0 at the highest k, and every node a station: the stations of
+    `st` at their heights over their home cells, the other nodes one grid
+    unit above the top layer.  The 66.7 constant of TFM.cpp:98 assumes a
+    10 km spacing, so scale = dx / 10 km.  Returns (grid, drho, surf)."""
+    nx, ny, nz = mesh.nx, mesh.ny, mesh.nz
+    kk = nz + 1 if nz % 2 == 0 else nz  # (dk-1)*fv+1 must hold every layer
+    dk = (kk - 1) // 2 + 1
+    g = make_grid(nx, ny, dk, 1, 2, 0, threshold=0.001, scale=mesh.dx / 10000.0)
+    drho = np.zeros(nx * ny * kk)
+    r = np.asarray(rho).reshape(nz, ny, nx) / 1000.0
+    for l in range(nz):
+        K = (kk - 1) - l - (kk - nz)
+        drho[K * nx * ny:(K + 1) * nx * ny] = r[l].ravel()
+    ktop = ((kk - 1) - (kk - nz)) / 2.0  # grid k of the top layer's centre
+    surf = np.full(nx * ny, ktop + 0.25 + 1.0)  # the top face is half a layer above
+    for x, y, z in st:
+        i, j = int(x // mesh.dx), int(y // mesh.dy)
+        surf[i + nx * j] = ktop + 0.25 + (z - mesh.z_top) / mesh.dx
+    return g, drho, surf
