@@ -177,11 +177,16 @@ int ztm_gfm_pointmass(ztm_ctx* ctx, const ztm_grid* grid, const double* drho,
  * cudaMalloc/cudaFree: the scratch is a fixed 4 MiB array reserved in each
  * GPU that loads the library.  Limits: at most 524,256 interior stations
  * (ZTM_ERR_RANGE beyond); all nodes with |drho| > grid->threshold contribute
- * (no nn list).  Every call on a device shares that array, so calls that can
- * overlap on one GPU race: serialise them on one stream.  The first call on
- * each device looks the array up (cudaGetSymbolAddress); make it before any
- * stream capture starts.  Returns ZTM_OK, ZTM_ERR_ARG, ZTM_ERR_RANGE,
- * ZTM_ERR_NODEV or ZTM_ERR_CUDA. */
+ * (no nn list).  It runs the full-grid gather (nodes in grid order), not the
+ * node-column gather of ztm_gfm_pointmass, whose column layout needs a
+ * workspace, so it is slower than that entry on large grids.  Every call on
+ * a device shares that array, so calls that can overlap on one GPU race:
+ * serialise them on one stream.  The first call on each device (and the
+ * first after a cudaDeviceReset) looks the array up (cudaGetSymbolAddress);
+ * make it before any stream capture starts.  A CUDA error already pending
+ * when the call starts is left pending and reported as ZTM_ERR_CUDA.
+ * Returns ZTM_OK, ZTM_ERR_ARG, ZTM_ERR_RANGE, ZTM_ERR_NODEV or
+ * ZTM_ERR_CUDA. */
 int ztm_gfm_pointmass_noalloc(const ztm_grid* grid, const double* drho,
                               const double* surf, double* G, int precision,
                               void* stream);

@@ -12,6 +12,7 @@
 // sum stays in registers, and a split over node chunks writes per-chunk
 // partials that a second kernel adds in a fixed order.  No atomics, so the
 // result is bitwise reproducible.
+#include <cuda.h>  // CUcontext / CUresult types of the two driver calls below
 #include <cuda_runtime.h>
 #include <math.h>
 
@@ -774,9 +775,12 @@ int ztm_launch_pointmass(ztm_ctx* c, const PmParams& p, const double* d_drho,
 // while a stream is being captured into a CUDA graph (cudaMalloc is not
 // allowed there), or a real-time inversion loop that must not pay for, or
 // risk, an allocation inside its iterations.  For them
-// ztm_gfm_pointmass_noalloc runs the same gather kernels as
-// ztm_gfm_pointmass with all of its scratch (the per-chunk partial sums and
-// the error word) in the fixed array below.  It needs no context, does no
+// ztm_gfm_pointmass_noalloc computes the same sum as ztm_gfm_pointmass with
+// the full-grid gather pm_gather_kernel (nodes in grid order, the threshold
+// applied on the fly; not the node-column gather of the context entry points,
+// which needs a workspace for its column layout, so its rates are those of
+// pm_gather_kernel) and keeps all of its scratch (the per-chunk partial sums
+// and the error word) in the fixed array below.  It needs no context, does no
 // host<->device staging, and calls no cudaMalloc, cudaFree or allocating
 // library routine.
 //
@@ -790,14 +794,50 @@ int ztm_launch_pointmass(ztm_ctx* c, const PmParams& p, const double* d_drho,
 //     give wrong results; serialise them on one stream;
 //   * the first call on each device looks up the array's device address
 //     (cudaGetSymbolAddress, which may load the module onto the device); make
-//     that first call before any stream capture begins.
+//     that first call before any stream capture begins.  The address is kept
+//     per device and CUDA context: after a cudaDeviceReset the next call looks
+//     it up again (that call is then a first call).
 #define ZTM_NOALLOC_SCRATCH_BYTES (4u << 20)
 static __device__ __align__(256) unsigned char g_pm_scratch[ZTM_NOALLOC_SCRATCH_BYTES];
 
 namespace {
 constexpr int NOALLOC_MAX_DEVICES = 64;
 std::mutex g_noalloc_mu;
-void* g_noalloc_addr[NOALLOC_MAX_DEVICES] = {};
+struct NoallocSlot {
+  unsigned long long ctx_id = 0;  // the CUDA context the address belongs to
+  void* addr = nullptr;
+};
+NoallocSlot g_noalloc[NOALLOC_MAX_DEVICES];
+
+typedef CUresult (*PfnCtxGetCurrent)(CUcontext*);
+typedef CUresult (*PfnCtxGetId)(CUcontext, unsigned long long*);
+
+// Unique id of the calling thread's current CUDA context, 0 when there is
+// none yet (or the driver cannot say).  The driver functions are reached
+// through the runtime, so the library does not link libcuda itself.
+unsigned long long current_ctx_id() {
+  static PfnCtxGetCurrent get_cur = nullptr;
+  static PfnCtxGetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = q1;
+    void *f1 = nullptr, *f2 = nullptr;
+    const cudaError_t e1 =
+        cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1);
+    const cudaError_t e2 =
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2);
+    if (e1 == cudaSuccess && e2 == cudaSuccess && q1 == cudaDriverEntryPointSuccess &&
+        q2 == cudaDriverEntryPointSuccess) {
+      get_cur = reinterpret_cast<PfnCtxGetCurrent>(f1);
+      get_id = reinterpret_cast<PfnCtxGetId>(f2);
+    }
+  });
+  if (!get_cur || !get_id) return 0;
+  CUcontext c = nullptr;
+  unsigned long long id = 0;
+  if (get_cur(&c) != CUDA_SUCCESS || !c || get_id(c, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
 }  // namespace
 
 extern "C" int ztm_gfm_pointmass_noalloc(const ztm_grid* g, const double* drho,
@@ -805,6 +845,9 @@ extern "C" int ztm_gfm_pointmass_noalloc(const ztm_grid* g, const double* drho,
                                          void* stream) {
   if (!g || !drho || !surf || !G) return ZTM_ERR_ARG;
   if (precision != ZTM_PREC_FP64 && precision != ZTM_PREC_FP32) return ZTM_ERR_ARG;
+  // an error left pending by the caller's earlier work is not this call's:
+  // report it without clearing it, so that its owner still sees it
+  if (cudaPeekAtLastError() != cudaSuccess) return ZTM_ERR_CUDA;
   if (g->di < 1 || g->dj < 1 || g->dk < 1 || g->fh < 1 || g->fv < 1 || g->bfr < 0 ||
       !(g->threshold >= 0) || !isfinite(g->scale))
     return ZTM_ERR_ARG;
@@ -834,20 +877,23 @@ extern "C" int ztm_gfm_pointmass_noalloc(const ztm_grid* g, const double* drho,
   const long long cap = (ZTM_NOALLOC_SCRATCH_BYTES - 256) / sizeof(double);
   if (p.ns > cap) return ZTM_ERR_RANGE;  // more interior stations than the array holds
 
-  // one-time set-up per device: the host-side name of the array is not a
-  // device address; ask the runtime for the address on this device
+  // set-up once per device and context: the host-side name of the array is
+  // not a device address; ask the runtime for the address on this device
   void* base = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_addr[dev]) {
+    NoallocSlot& slot = g_noalloc[dev];
+    const unsigned long long id = current_ctx_id();
+    if (!slot.addr || id == 0 || id != slot.ctx_id) {
       void* a = nullptr;
       if (cudaGetSymbolAddress(&a, g_pm_scratch) != cudaSuccess || !a) {
-        cudaGetLastError();
+        cudaGetLastError();  // raised here (none was pending at entry)
         return ZTM_ERR_CUDA;
       }
-      g_noalloc_addr[dev] = a;
+      slot.addr = a;
+      slot.ctx_id = current_ctx_id();  // the lookup made the context current
     }
-    base = g_noalloc_addr[dev];
+    base = slot.addr;
   }
   int* err = reinterpret_cast<int*>(base);
   double* partial = reinterpret_cast<double*>(static_cast<char*>(base) + 256);
@@ -880,6 +926,7 @@ extern "C" int ztm_gfm_pointmass_noalloc(const ztm_grid* g, const double* drho,
   const double factor = g->scale * 66.7 / ((double)p.fh * p.fh * p.fv);
   const int M = p.di * p.dj;
   pm_finalize_kernel<<<(M + 255) / 256, 256, 0, s>>>(p, chunks, partial, factor, G);
+  // a launch error here is this call's own (none was pending at entry)
   if (cudaGetLastError() != cudaSuccess) return ZTM_ERR_CUDA;
   return ZTM_OK;
 }

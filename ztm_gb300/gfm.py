@@ -47,9 +47,6 @@ class _Args:
         self.keep = []
         self.gctx = gctx
 
-    def _record(self, t):
-        pass
-
     def _kind(self, dev):
         if self.device is None:
             self.device = dev
@@ -70,7 +67,6 @@ class _Args:
                 raise ValueError("%s has %d elements, expected %d" % (name, x.numel(), n))
             self._kind(True)
             self.keep.append(x)
-            self._record(x)
             return ctypes.c_void_p(x.data_ptr())
         a = np.ascontiguousarray(x, dtype=dtype)
         if n is not None and a.size != n:
@@ -84,7 +80,6 @@ class _Args:
             import torch
             t = torch.empty(n, dtype=torch.float64, device=like.device if like is not None else "cuda")
             self.keep.append(t)
-            self._record(t)
             return t, ctypes.c_void_p(t.data_ptr())
         a = np.empty(n, dtype=np.float64)
         self.keep.append(a)
@@ -363,7 +358,6 @@ class GravityContext:
             import torch
             mt = torch.zeros(1, dtype=torch.float64, device=depth.device)
             a.keep.append(mt)
-            a._record(mt)
             pmis = ctypes.c_void_p(mt.data_ptr())
         else:
             pmis = ctypes.cast(ctypes.pointer(mis), ctypes.c_void_p)
