@@ -1,5 +1,5 @@
 """The reference arm of bench.py runs on the CPU and prints the contract's
-JSON line (checked here with a tiny station sample)."""
+JSON line (checked here with a small node sample)."""
 import json
 import os
 import subprocess
@@ -9,7 +9,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def test_reference_arm_json_line():
-    env = dict(os.environ, ZTM_REF_SAMPLE="4")
+    env = dict(os.environ, ZTM_REF_NODE_STRIDE="256")
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
                         "--steps", "1", "--warmup", "0"], capture_output=True, text=True,
                        env=env, timeout=600)
@@ -22,4 +22,8 @@ def test_reference_arm_json_line():
         assert k in d, k
     assert d["impl"] == "reference" and d["value"] > 0
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
-    assert d["cpu_baseline"]["kind"] == "port"
+    # the reference's own lambda where it was built (TFM.cpp present or its
+    # generated harness shipped), else the restatement
+    import oracle
+    want = "reference" if oracle.ref_tfm_available() else "port"
+    assert d["cpu_baseline"]["kind"] == want
