@@ -485,6 +485,17 @@ def run_workload(args, local_rank):
         what = ("the reference's point-mass model (float) on the 256x256x64 draped-mesh geometry, its grid: "
                 "every node a station (pairs of selected nodes x stations)")
         step = lambda: ctx.pointmass(g, dd, dsf, precision="fp32")
+    elif args.workload in ("pointmass_adjoint", "pointmass_adjoint64"):
+        mesh, rho, st = synth.draped_mesh_256x256x64()
+        g, drho, surf = synth.pointmass_grid_of_mesh(mesh, rho, st)
+        dd, dsf = d(drho), d(surf)
+        dw = d(np.random.default_rng(0).normal(0, 1, g.di * g.dj))
+        prec = "fp64" if args.workload.endswith("64") else "fp32"
+        sel = np.abs(drho) > 0.001
+        units = int(np.count_nonzero(sel)) * g.di * g.dj
+        what = ("transposed point-mass sum (%s) on the 256x256x64 draped-mesh geometry, its grid: "
+                "selected nodes x stations" % prec)
+        step = lambda: ctx.pointmass_adjoint(g, dsf, dw, drho=dd, precision=prec)
     else:
         raise SystemExit("unknown workload " + args.workload)
     for _ in range(args.warmup):
@@ -512,7 +523,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quick", action="store_true", help="skip side measurements")
     ap.add_argument("--workload", default="forward",
-                    choices=["forward", "adjoint", "interface", "batch", "pointmass"],
+                    choices=["forward", "adjoint", "interface", "batch", "pointmass",
+                             "pointmass_adjoint", "pointmass_adjoint64"],
                     help="forward (the headline) or another workload as the timed step")
     args = ap.parse_args()
     rank, local_rank, world = dist_env()

@@ -167,6 +167,33 @@ int ztm_gfm_pointmass(ztm_ctx* ctx, const ztm_grid* grid, const double* drho,
                       const int* nn, long long n_nn, const double* surf,
                       double* G, int precision, int flags);
 
+/* Adjoint (transposed sum) of ztm_gfm_pointmass: for every fine-grid node
+ * n, g_drho[n] = sum over interior stations m of w[m] * dG[m]/d drho[n]
+ *             = scale * 66.7/(fh^2 fv) * sum_m w[m] (k0_m - k_n) / r_mn^3,
+ * i.e. J^T w for the station weights w (di*dj values; the interior ones are
+ * read).  Node selection, as in the forward: with nn, only the listed nodes
+ * (times their multiplicity; 0 elsewhere); else, with drho, the nodes with
+ * |drho| > grid->threshold; with neither, every node.  No counterpart in the
+ * reference: its optimiser builds these derivatives by finite differences of
+ * whole forward runs (TFM.cpp:124-135).  precision: ZTM_PREC_FP64 or _FP32. */
+int ztm_gfm_pointmass_adjoint(ztm_ctx* ctx, const ztm_grid* grid, const double* drho,
+                              const int* nn, long long n_nn, const double* surf,
+                              const double* w, double* g_drho, int precision, int flags);
+
+/* The gravity part of the reference misfit, TFM.cpp:101-103, with its
+ * gradient: G = the point-mass forward (as ztm_gfm_pointmass, same node
+ * selection), res[t] = GD[m]/gsig - (G[m] + g0)/gsig over the bfr interior
+ * in TFM's order (i0 outer, j0 inner: t = (i0-bfr)*(dj-2bfr) + (j0-bfr)),
+ * *ssq = sum res^2 (the gravity terms of FM::ssq), and, if asked for,
+ * g_drho = d ssq / d drho (N values, by the adjoint above) and
+ * *g_g0 = d ssq / d g0.  res, G, g_drho, g_g0 may be NULL.  With
+ * ZTM_FLAG_DEVICE_PTRS every array and ssq / g_g0 are device pointers. */
+int ztm_gfm_pointmass_misfit(ztm_ctx* ctx, const ztm_grid* grid, const double* drho,
+                             const int* nn, long long n_nn, const double* surf,
+                             const double* GD, double g0, double gsig, double* ssq,
+                             double* res, double* G, double* g_drho, double* g_g0,
+                             int precision, int flags);
+
 /* Allocation-free point-mass forward.  No counterpart in the reference.
  * For callers that cannot allocate device memory at the time of the call
  * (a host that fixes the GPU memory budget up front, work issued while a
@@ -218,6 +245,24 @@ int ztm_gfm_pointmass_model(ztm_ctx* ctx, const ztm_density_params* p,
                             const double* M, const double* v,
                             const double* surf, double* G, int precision,
                             int flags);
+
+/* TFM.cpp:83-103 with its gradient: the density builder, the point-mass
+ * forward over the nodes it selects, the misfit of ztm_gfm_pointmass_misfit,
+ * and, when any of g_M, g_v, g_par is non-NULL, one adjoint pass chained back
+ * through the builder: g_M (di*dj) = d ssq / d M, g_v (di*dj*dk) =
+ * d ssq / d v, g_par[0..3] = d ssq / d (vm, ro, dr, g0), with ro as the loop
+ * uses it (TFM.cpp:84 takes ro = -B[...], so d ssq / d B = -g_par[1]).  The
+ * builder's node selection is held fixed (the derivative a small finite-
+ * difference step sees).  One forward and one adjoint replace the gravity
+ * columns of the finite-difference Jacobian of TFM.cpp:124-135 (vm, ro, dr,
+ * g0 and, through the rendered Moho M, the Moho nodes; the natural-neighbour
+ * rendering of the nodes into M, NNI.cpp, stays with the caller). */
+int ztm_gfm_pointmass_model_misfit(ztm_ctx* ctx, const ztm_density_params* p,
+                                   const ztm_grid* grid, const double* sea, const double* M,
+                                   const double* v, const double* surf, const double* GD,
+                                   double g0, double gsig, double* ssq, double* res, double* G,
+                                   double* g_M, double* g_v, double* g_par, int precision,
+                                   int flags);
 
 /* ---- prism mode -------------------------------------------------------- */
 /* gz[s] = sum over all prisms of the closed-form attraction of prism p at

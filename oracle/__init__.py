@@ -40,6 +40,7 @@ def _load():
         lib.ora_pointmass_tfm.argtypes = [I, I, I, I, I, I, P, P, L, P, P, I]
         lib.ora_pointmass_tfm_range.argtypes = [I, I, I, I, I, I, P, P, L, P, P, L, L, I]
         lib.ora_pointmass_gf.argtypes = [I, I, I, I, I, I, P, L, P, P]
+        lib.ora_pointmass_adjoint.argtypes = [I, I, I, I, I, I, P, L, P, P, P, I]
         lib.ora_phi.argtypes = [D, D, D]
         lib.ora_phi.restype = D
         lib.ora_prism_unit.argtypes = [D] * 9
@@ -102,6 +103,27 @@ def pointmass_tfm_sample(grid, drho, surf, s_lo, s_hi, nn=None, nthreads=None):
                                 _p(nn), nn.size, _p(surf), _p(G), s_lo, s_hi,
                                 nthreads or NTHREADS)
     return G, nn.size
+
+
+def pointmass_adjoint(grid, surf, w, nn=None, drho=None, nthreads=None):
+    """Transpose of TFM.cpp:96-98 (grid units, times grid.scale like the
+    forward): g[n] = sum over interior stations m of w[m] * dG[m]/d drho[n]
+    for the nodes of nn (with multiplicity), or of |drho| > threshold when
+    nn is None and drho is given, or every node."""
+    lib = _load()
+    surf = _f64(surf)
+    w = _f64(w)
+    ii = (grid.di - 1) * grid.fh + 1
+    jj = (grid.dj - 1) * grid.fh + 1
+    kk = (grid.dk - 1) * grid.fv + 1
+    N = ii * jj * kk
+    if nn is None:
+        nn = np.nonzero(np.abs(_f64(drho)) > grid.threshold)[0] if drho is not None else np.arange(N)
+    nn = np.ascontiguousarray(nn, dtype=np.int32)
+    g = np.zeros(N)
+    lib.ora_pointmass_adjoint(grid.di, grid.dj, grid.dk, grid.fh, grid.fv, grid.bfr, _p(nn), nn.size,
+                              _p(surf), _p(w), _p(g), nthreads or NTHREADS)
+    return g * grid.scale if grid.scale != 1.0 else g
 
 
 def pointmass_gf(grid, rho32, s32, nthreads_total=None):

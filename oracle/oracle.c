@@ -13,6 +13,10 @@
  *                      threads split the stations evenly (same arithmetic per
  *                      station), so that a bounded sample of stations still
  *                      uses every core.
+ *   ora_pointmass_adjoint  the transpose of that sum (no counterpart in the
+ *                      reference, whose optimiser differentiates by finite
+ *                      differences, TFM.cpp:124-135): per node, the weighted
+ *                      sum over stations of the same per-pair term.
  *   ora_pointmass_gf   restates the GF kernel of GFM_GPU.cu:16-22 in float,
  *                      with the kernel's own index math (ii=di*fh, :17) and a
  *                      sequential (thread-order) summation in place of the
@@ -143,6 +147,56 @@ void ora_pointmass_tfm(int di, int dj, int dk, int fh, int fv, int bfr,
                        const double* drho, const int* nn, long n_nn,
                        const double* surf, double* G, int nthreads) {
   ora_pointmass_tfm_range(di, dj, dk, fh, fv, bfr, drho, nn, n_nn, surf, G, 0, -1, nthreads);
+}
+
+/* Transpose of the TFM.cpp:96-98 sum: for every entry q of the node list,
+ * gq = sum over interior stations (j0 outer, i0 inner, as the lambda's rows
+ * and columns) of w[m] * 66.7*(k0-k)/pow(r^2,1.5)/(fh*fh*fv); the entries are
+ * then added into g[nn[q]] in list order (a node listed twice gets it twice),
+ * so that sum_m w[m] G[m] = sum_n g[n] drho[n] for the forward over the same
+ * list. */
+typedef struct {
+  int di, dj, fh, fv, bfr, ii, jj;
+  const int* nn;
+  const double* surf;
+  const double* w;
+  double* gq;
+} pma_args;
+
+static void pma_entries(long lo, long hi, void* p) {
+  pma_args* a = (pma_args*)p;
+  const int fh = a->fh, fv = a->fv, ii = a->ii, jj = a->jj;
+  for (long q = lo; q < hi; q++) {
+    int n = a->nn[q];
+    double i = (n % ii) / (1. * fh), j = ((n / ii) % jj) / (1. * fh), k = (n / (ii * jj)) / (1. * fv);
+    double g = 0;
+    for (int j0 = a->bfr; j0 < a->dj - a->bfr; j0++)
+      for (int i0 = a->bfr; i0 < a->di - a->bfr; i0++) {
+        int m = i0 + j0 * a->di;
+        double k0 = a->surf[m];
+        g += a->w[m] * (66.7 * (k0 - k) /
+                        pow((i0 - i) * (i0 - i) + (j0 - j) * (j0 - j) + (k0 - k) * (k0 - k), 1.5)) /
+             (fh * fh * fv);
+      }
+    a->gq[q] = g;
+  }
+}
+
+void ora_pointmass_adjoint(int di, int dj, int dk, int fh, int fv, int bfr, const int* nn,
+                           long n_nn, const double* surf, const double* w, double* g, int nthreads) {
+  long N = (long)((di - 1) * fh + 1) * ((dj - 1) * fh + 1) * ((dk - 1) * fv + 1);
+  memset(g, 0, sizeof(double) * N);
+  if (di - 2 * bfr <= 0 || dj - 2 * bfr <= 0 || n_nn <= 0) return;
+  pma_args a;
+  a.di = di; a.dj = dj; a.fh = fh; a.fv = fv; a.bfr = bfr;
+  a.ii = (di - 1) * fh + 1;
+  a.jj = (dj - 1) * fh + 1;
+  a.nn = nn; a.surf = surf; a.w = w;
+  a.gq = (double*)malloc(sizeof(double) * n_nn);
+  if (!a.gq) return;
+  parallel_for(n_nn, nthreads, pma_entries, &a);
+  for (long q = 0; q < n_nn; q++) g[nn[q]] += a.gq[q];
+  free(a.gq);
 }
 
 void ora_pointmass_gf(int bfr, int di, int dj, int dk, int fh, int fv,

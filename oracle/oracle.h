@@ -26,6 +26,9 @@ void ora_pointmass_tfm_range(int di, int dj, int dk, int fh, int fv, int bfr,
                              const double* drho, const int* nn, long n_nn,
                              const double* surf, double* G, long s_lo, long s_hi,
                              int nthreads);
+void ora_pointmass_adjoint(int di, int dj, int dk, int fh, int fv, int bfr, const int* nn,
+                           long n_nn, const double* surf, const double* w, double* g,
+                           int nthreads);
 void ora_pointmass_gf(int bfr, int di, int dj, int dk, int fh, int fv,
                       const float* rho, long nthreads_total, const float* s,
                       float* g);

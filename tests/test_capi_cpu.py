@@ -40,6 +40,13 @@ def test_null_and_bad_arguments_do_not_crash():
     assert lib.ztm_ctx_sync(None) == _lib.ERR_ARG
     assert lib.ztm_gfm_pointmass_model(None, None, None, None, None, None, None, None, 0,
                                        0) == _lib.ERR_ARG
+    assert lib.ztm_gfm_pointmass_adjoint(None, None, None, None, 0, None, None, None, 0,
+                                         0) == _lib.ERR_ARG
+    assert lib.ztm_gfm_pointmass_misfit(None, None, None, None, 0, None, None, 0.0, 1.0, None,
+                                        None, None, None, None, 0, 0) == _lib.ERR_ARG
+    assert lib.ztm_gfm_pointmass_model_misfit(None, None, None, None, None, None, None, None, 0.0,
+                                              1.0, None, None, None, None, None, None, 0,
+                                              0) == _lib.ERR_ARG
     lib.ztm_ctx_destroy(None)
 
 

@@ -31,7 +31,8 @@ EXPORTS = (
     "ztm_gfm_interface", "ztm_gfm_interface_adjoint", "ztm_gfm_interface_misfit",
     "ztm_gfm_batch", "ztm_ctx_profile", "ztm_ctx_profile_read", "ztm_measure_peak",
     "ztm_invert_interface", "ztm_gfm_pointmass_noalloc", "ztm_density_build",
-    "ztm_gfm_pointmass_model", "ztm_gfm_interface_jvp",
+    "ztm_gfm_pointmass_model", "ztm_gfm_interface_jvp", "ztm_gfm_pointmass_adjoint",
+    "ztm_gfm_pointmass_misfit", "ztm_gfm_pointmass_model_misfit",
 )
 
 
@@ -102,6 +103,14 @@ _SIGS = {
                                ctypes.POINTER(_LL), _I]),
     "ztm_gfm_pointmass_model": (_I, [_P, ctypes.POINTER(DensityParams), ctypes.POINTER(Grid),
                                      _P, _P, _P, _P, _P, _I, _I]),
+    "ztm_gfm_pointmass_adjoint": (_I, [_P, ctypes.POINTER(Grid), _P, _P, _LL, _P, _P, _P, _I, _I]),
+    "ztm_gfm_pointmass_misfit": (_I, [_P, ctypes.POINTER(Grid), _P, _P, _LL, _P, _P,
+                                      ctypes.c_double, ctypes.c_double, _P, _P, _P, _P, _P, _I,
+                                      _I]),
+    "ztm_gfm_pointmass_model_misfit": (_I, [_P, ctypes.POINTER(DensityParams),
+                                            ctypes.POINTER(Grid), _P, _P, _P, _P, _P,
+                                            ctypes.c_double, ctypes.c_double, _P, _P, _P, _P, _P,
+                                            _P, _I, _I]),
     "ztm_ctx_profile": (_I, [_P, _I]),
     "ztm_ctx_profile_read": (_I, [_P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double),
                                   ctypes.POINTER(_LL)]),

@@ -20,6 +20,8 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <algorithm>
+
 #include "ztm_internal.cuh"
 
 namespace {
@@ -106,6 +108,133 @@ __global__ void density_kernel(DensArgs a, const double* __restrict__ sea,
   }
   const unsigned b = __ballot_sync(0xffffffffu, sel);
   if ((threadIdx.x & 31) == 0 && b) atomicAdd(count, (unsigned long long)__popc(b));
+}
+
+// ---- derivative of the builder ------------------------------------------
+// drho[n] = r1 - r0 (TFM.cpp:86-89) is piecewise linear in its inputs: with
+// b = dr*(v(i,j,k) - vm) and t = (k - m + li)/(2 li),
+//   ramp(r, k, m) = ro                     if k > m + li,
+//                 = r (1 + t) + ro t       if |k - m| < li,
+//                 = r                      otherwise,
+// so d r1/d b, d r1/d ro, d r1/d m1 (= -(b + ro)/(2 li) in the blend) and
+// d r0/d ro follow branch by branch, with the branch decided exactly as the
+// forward decides it.  The node selection (|r1 - r0| > .001, depth > 10 km)
+// is held fixed, as a finite-difference step that does not cross it sees.
+struct RampGrad {
+  double db, dro, dm;  // d ramp / d r, d ro, d m
+};
+
+__device__ RampGrad ramp_grad(double r, double k, double m, double li, double ro) {
+  RampGrad g = {0.0, 0.0, 0.0};
+  if (k > __dadd_rn(m, li)) {
+    g.dro = 1.0;
+    return g;
+  }
+  const double d = __dadd_rn(k, -m);
+  if (fabs(d) < li) {
+    const double t = __dadd_rn(d, li) / (2 * li);
+    g.db = 1.0 + t;
+    g.dro = t;
+    g.dm = -__dadd_rn(r, ro) / (2 * li);
+    return g;
+  }
+  g.db = 1.0;
+  return g;
+}
+
+// Adds s * d interp2(f, x, y)/d f into gf (the weights of interp2_dev).
+__device__ void interp2_scatter(double* __restrict__ gf, double x, double y, int di, int dj,
+                                double s) {
+  const double ii = fmin(fmax(x, 0.0), (double)(di - 1)), jj = fmin(fmax(y, 0.0), (double)(dj - 1));
+  const int i = (int)ii, j = (int)jj;
+  const double si = ii - i, sj = jj - j;
+  const int i1 = i + 1 < di ? i + 1 : i, j1 = j + 1 < dj ? j + 1 : j;
+  const double w[4] = {(1 - si) * (1 - sj), si * (1 - sj), (1 - si) * sj, si * sj};
+  const int at[4] = {i + j * di, i1 + j * di, i + j1 * di, i1 + j1 * di};
+#pragma unroll
+  for (int q = 0; q < 4; q++)
+    if (w[q] != 0.0) atomicAdd(&gf[at[q]], s * w[q]);
+}
+
+// Adds s * d interp3(f, x, y, z)/d f into gf (the weights of interp3_dev).
+__device__ void interp3_scatter(double* __restrict__ gf, double x, double y, double z, int di,
+                                int dj, int dk, double s) {
+  const double ii = fmin(fmax(x, 0.0), (double)(di - 2)), jj = fmin(fmax(y, 0.0), (double)(dj - 2)),
+               kk = fmin(fmax(z, 0.0), (double)(dk - 2));
+  const int i = (int)ii, j = (int)jj, k = (int)kk;
+  const double si = ii - i, sj = jj - j, sk = kk - k;
+  const long long pl = (long long)di * dj;
+#pragma unroll
+  for (int c = 0; c < 2; c++)
+#pragma unroll
+    for (int b = 0; b < 2; b++)
+#pragma unroll
+      for (int a = 0; a < 2; a++) {
+        const double w = (a ? si : 1 - si) * (b ? sj : 1 - sj) * (c ? sk : 1 - sk);
+        if (w != 0.0) atomicAdd(&gf[(i + a) + (long long)(j + b) * di + (k + c) * pl], s * w);
+      }
+}
+
+// From a[n] = d ssq / d drho[n] (zero off the selection): gM += d ssq / d M,
+// gv += d ssq / d v (both zeroed by the caller), and per block the
+// contributions to d ssq / d (vm, ro, dr).
+constexpr int DENS_T = 256;
+__global__ void __launch_bounds__(DENS_T)
+    density_adjoint_kernel(DensArgs a, const double* __restrict__ sea,
+                           const double* __restrict__ M, const double* __restrict__ v,
+                           const double* __restrict__ adrho, double* __restrict__ gM,
+                           double* __restrict__ gv, double* __restrict__ blk) {
+  __shared__ double s_w[DENS_T / 32][3];
+  const long long n = blockIdx.x * (long long)DENS_T + threadIdx.x;
+  double c_vm = 0.0, c_ro = 0.0, c_dr = 0.0;
+  if (n < a.N) {
+    const double an = adrho[n];
+    if (an != 0.0) {
+      const double i = (n % a.ii) / (1. * a.fh), j = ((n / a.ii) % a.jj) / (1. * a.fh),
+                   k = (n / ((long long)a.ii * a.jj)) / (1. * a.fv), li = 1. / a.fv;
+      const double m0 = __dadd_rn(interp2_dev(sea, i, j, a.di, a.dj), -3.5);
+      const double m1 = interp2_dev(M, i, j, a.di, a.dj);
+      const double vi = interp3_dev(v, i, j, k, a.di, a.dj, a.dk);
+      const double b = __dmul_rn(a.dr, __dadd_rn(vi, -a.vm));
+      const RampGrad g0 = ramp_grad(0.0, k, m0, li, a.ro);
+      const RampGrad g1 = ramp_grad(b, k, m1, li, a.ro);
+      // drho = r1 - r0
+      if (g1.db != 0.0) interp3_scatter(gv, i, j, k, a.di, a.dj, a.dk, an * g1.db * a.dr);
+      if (g1.dm != 0.0) interp2_scatter(gM, i, j, a.di, a.dj, an * g1.dm);
+      c_vm = -an * g1.db * a.dr;
+      c_dr = an * g1.db * (vi - a.vm);
+      c_ro = an * (g1.dro - g0.dro);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    c_vm += __shfl_down_sync(0xffffffffu, c_vm, o);
+    c_ro += __shfl_down_sync(0xffffffffu, c_ro, o);
+    c_dr += __shfl_down_sync(0xffffffffu, c_dr, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    s_w[threadIdx.x >> 5][0] = c_vm;
+    s_w[threadIdx.x >> 5][1] = c_ro;
+    s_w[threadIdx.x >> 5][2] = c_dr;
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    double t = 0.0;
+    for (int q = 0; q < DENS_T / 32; q++) t += s_w[q][threadIdx.x];
+    blk[blockIdx.x * 3LL + threadIdx.x] = t;
+  }
+}
+
+// out[c] = sum over blocks of blk[b*3 + c], in block order (one warp each).
+__global__ void density_adjoint_total(long long nblk, const double* __restrict__ blk,
+                                      double* __restrict__ out) {
+  const int c = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (c >= 3) return;
+  double t = 0.0;
+  for (long long b = lane; b < nblk; b += 32) t += blk[b * 3 + c];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+  if (lane == 0) out[c] = t;
 }
 
 // Checks the parameters and fills the kernel arguments.
@@ -243,4 +372,121 @@ extern "C" int ztm_gfm_pointmass_model(ztm_ctx* c, const ztm_density_params* dp,
   rc = ztm_launch_pointmass(c, p, d_rho, nullptr, (const double*)ps, outG, g->scale, precision, wc);
   if (rc) return rc;
   return ztm_finish(c, dev, G, outG, M2 * 8, "density + point-mass forward");
+}
+
+// TFM.cpp:83-103 with its derivative: the builder, the point-mass forward
+// over the nodes it selects, the gravity misfit of TFM.cpp:101-103, and (when
+// a gradient is asked for) the transposed point-mass sum chained back through
+// the builder to the rendered Moho M, the velocity grid v and (vm, ro, dr),
+// plus d ssq / d g0.  Replaces the gravity columns of the finite-difference
+// Jacobian of TFM.cpp:124-135 (one forward per parameter) by one forward and
+// one adjoint.
+extern "C" int ztm_gfm_pointmass_model_misfit(ztm_ctx* c, const ztm_density_params* dp,
+                                              const ztm_grid* g, const double* sea,
+                                              const double* M, const double* v, const double* surf,
+                                              const double* GD, double g0, double gsig,
+                                              double* ssq, double* res, double* G, double* g_M,
+                                              double* g_v, double* g_par, int precision,
+                                              int flags) {
+  if (!c) return ZTM_ERR_ARG;
+  c->err.clear();
+  if (!dp || !g || !sea || !M || !v || !surf || !GD || !ssq)
+    return ztm_fail(c, ZTM_ERR_ARG, "null argument");
+  if (flags & ~ZTM_FLAG_DEVICE_PTRS) return ztm_fail(c, ZTM_ERR_ARG, "unknown flag");
+  if (precision != ZTM_PREC_FP64 && precision != ZTM_PREC_FP32)
+    return ztm_fail(c, ZTM_ERR_ARG, "point-mass precision must be FP64 or FP32");
+  if (dp->di != g->di || dp->dj != g->dj || dp->dk != g->dk || dp->fh != g->fh || dp->fv != g->fv)
+    return ztm_fail(c, ZTM_ERR_ARG, "density and grid dimensions differ");
+  if (!(gsig > 0) || !isfinite(g0)) return ztm_fail(c, ZTM_ERR_ARG, "gsig must be > 0, g0 finite");
+  const bool dev = (flags & ZTM_FLAG_DEVICE_PTRS) != 0;
+  const bool grad = g_M || g_v || g_par;
+  DensArgs a;
+  int rc = dens_setup(c, dp, &a);
+  if (rc) return rc;
+  PmParams p;
+  if ((rc = ztm_pm_setup(c, g, &p))) return rc;
+  DevRestore restore(c->device);
+  const size_t M2 = (size_t)g->di * g->dj, M3 = M2 * g->dk;
+  const long long nblk = (a.N + DENS_T - 1) / DENS_T;
+  size_t need = dens_ws(a) + WsCarver::need(a.N * 8) + WsCarver::need(8) +
+                4 * WsCarver::need(M2 * 8) + WsCarver::need((size_t)std::max(p.ns, 1) * 8) +
+                WsCarver::need(16) + WsCarver::need(a.N * 8) + WsCarver::need(M2 * 8) +
+                WsCarver::need(M3 * 8) + WsCarver::need((size_t)nblk * 24) + WsCarver::need(32) +
+                ztm_pm_misfit_ws(p) +
+                std::max(ztm_pointmass_ws(p, precision, c->num_sms),
+                         grad ? ztm_pm_adjoint_ws(p, precision, c->num_sms, false) : 0) +
+                4096;
+  if ((rc = ztm_ws_reserve(c, need))) return rc;
+  WsCarver wc(c->ws);
+  double* d_rho = wc.take<double>(a.N);
+  unsigned long long* cnt = wc.take<unsigned long long>(1);
+  double* s_surf = wc.take<double>(M2);
+  double* s_GD = wc.take<double>(M2);
+  double* s_G = wc.take<double>(M2);
+  double* s_w = wc.take<double>(M2);
+  double* s_res = wc.take<double>((size_t)std::max(p.ns, 1));
+  double* s_out = wc.take<double>(2);
+  double* s_a = wc.take<double>(a.N);
+  double* s_gM = wc.take<double>(M2);
+  double* s_gv = wc.take<double>(M3);
+  double* s_blk = wc.take<double>((size_t)nblk * 3);
+  double* s_par = wc.take<double>(4);
+  // dens_run stages sea, M and v in the first three slices of its carver;
+  // they stay there for the builder's adjoint
+  WsCarver dw = wc, q = wc;
+  const double* a_sea = q.take<double>(M2);
+  const double* a_M = q.take<double>(M2);
+  const double* a_v = q.take<double>(M3);
+  if ((rc = dens_run(c, a, sea, M, v, dev, dw, d_rho, cnt))) return rc;
+  const double* pse = dev ? sea : a_sea;
+  const double* pM = dev ? M : a_M;
+  const double* pv = dev ? v : a_v;
+  WsCarver after = dw;  // past the staged sea, M, v
+  const void *ps, *pgd;
+  if ((rc = ztm_stage_in(c, surf, M2 * 8, dev, s_surf, &ps))) return rc;
+  if ((rc = ztm_stage_in(c, GD, M2 * 8, dev, s_GD, &pgd))) return rc;
+  double* oG = (dev && G) ? G : s_G;
+  double* ores = res ? (dev ? res : s_res) : nullptr;
+  {
+    WsCarver t = after;
+    rc = ztm_launch_pointmass(c, p, d_rho, nullptr, (const double*)ps, oG, g->scale, precision, t);
+    if (rc) return rc;
+  }
+  WsCarver t2 = after;
+  rc = ztm_launch_pm_misfit(c, p, oG, (const double*)pgd, g0, gsig, ores, s_w, s_out, t2);
+  if (rc) return rc;
+  if (grad) {
+    WsCarver t3 = t2;
+    rc = ztm_launch_pm_adjoint(c, p, d_rho, nullptr, (const double*)ps, s_w, s_a, g->scale,
+                               precision, t3);
+    if (rc) return rc;
+    double* ogM = (dev && g_M) ? g_M : s_gM;
+    double* ogv = (dev && g_v) ? g_v : s_gv;
+    cudaMemsetAsync(ogM, 0, M2 * 8, c->stream);
+    cudaMemsetAsync(ogv, 0, M3 * 8, c->stream);
+    density_adjoint_kernel<<<(unsigned)nblk, DENS_T, 0, c->stream>>>(a, pse, pM, pv, s_a, ogM, ogv,
+                                                                     s_blk);
+    density_adjoint_total<<<1, 96, 0, c->stream>>>(nblk, s_blk, s_par);
+    cudaMemcpyAsync(s_par + 3, s_out + 1, 8, cudaMemcpyDeviceToDevice, c->stream);
+    c->launches += 2;
+    if (dev && g_par) cudaMemcpyAsync(g_par, s_par, 32, cudaMemcpyDeviceToDevice, c->stream);
+    if (!dev) {
+      if (g_M) cudaMemcpyAsync(g_M, ogM, M2 * 8, cudaMemcpyDeviceToHost, c->stream);
+      if (g_v) cudaMemcpyAsync(g_v, ogv, M3 * 8, cudaMemcpyDeviceToHost, c->stream);
+      if (g_par) cudaMemcpyAsync(g_par, s_par, 32, cudaMemcpyDeviceToHost, c->stream);
+    }
+  }
+  if (dev) {
+    cudaMemcpyAsync(ssq, s_out, 8, cudaMemcpyDeviceToDevice, c->stream);
+    return ztm_finish(c, true, nullptr, nullptr, 0, "density + point-mass misfit");
+  }
+  double h = 0.0;
+  cudaMemcpyAsync(&h, s_out, 8, cudaMemcpyDeviceToHost, c->stream);
+  if (G) cudaMemcpyAsync(G, oG, M2 * 8, cudaMemcpyDeviceToHost, c->stream);
+  if (res && p.ns > 0)
+    cudaMemcpyAsync(res, ores, (size_t)p.ns * 8, cudaMemcpyDeviceToHost, c->stream);
+  rc = ztm_finish(c, false, nullptr, nullptr, 0, "density + point-mass misfit");
+  if (rc) return rc;
+  *ssq = h;
+  return ZTM_OK;
 }

@@ -651,6 +651,10 @@ void pm_cols_shape(const PmParams& p, int num_sms, bool f64, int* tiles, int* ch
 
 }  // namespace
 
+void ztm_scan_ints(cudaStream_t s, int n, int* counts, int* total) {
+  pm_nodes_scan<<<1, 1024, 0, s>>>(n, counts, total);
+}
+
 size_t ztm_pointmass_ws(const PmParams& p, int precision, int num_sms) {
   const bool f64 = precision == ZTM_PREC_FP64;
   if (pm_use_cols(p, f64)) {  // the node columns

@@ -111,6 +111,27 @@ int ztm_launch_pointmass(ztm_ctx* c, const PmParams& p, const double* d_drho,
                          const int* d_nn, const double* d_surf, double* d_G,
                          double scale, int precision, WsCarver& wc);
 size_t ztm_pointmass_ws(const PmParams& p, int precision, int num_sms);
+// Exclusive scan of n ints in place on `s` (one block); *total = their sum.
+void ztm_scan_ints(cudaStream_t s, int n, int* counts, int* total);
+
+// Adjoint of the point-mass forward (pm_adjoint.cu): d_g[n] (all N nodes) =
+// scale*66.7/(fh^2 fv) * mult(n) * sum over interior stations m of
+// d_w[m] (k0-k)/r^3, where mult(n) is n's count in d_nn (p.nnodes entries)
+// when d_nn is given, else 1 where |d_drho[n]| > p.thr when d_drho is given,
+// else 1.  d_w has di*dj entries (the interior ones are read).
+size_t ztm_pm_adjoint_ws(const PmParams& p, int precision, int num_sms, bool list);
+int ztm_launch_pm_adjoint(ztm_ctx* c, const PmParams& p, const double* d_drho, const int* d_nn,
+                          const double* d_surf, const double* d_w, double* d_g, double scale,
+                          int precision, WsCarver& wc);
+// The gravity part of TFM's misfit (TFM.cpp:101-103) from the forward's G:
+// r = (GD - (G + g0)) / gsig over the bfr interior, in TFM's order (i0
+// outer, j0 inner) into d_res (may be null); d_w[m] = -2 r / gsig at the
+// interior stations, 0 elsewhere (the adjoint's weights for d ssq / d G);
+// d_out[0] = ssq = sum r^2, d_out[1] = d ssq / d g0 = -2/gsig sum r.
+size_t ztm_pm_misfit_ws(const PmParams& p);
+int ztm_launch_pm_misfit(ztm_ctx* c, const PmParams& p, const double* d_G, const double* d_GD,
+                         double g0, double gsig, double* d_res, double* d_w, double* d_out,
+                         WsCarver& wc);
 // Checks a point-mass grid and fills p (nnodes = N, every node).
 int ztm_pm_setup(ztm_ctx* c, const ztm_grid* g, PmParams* p);
 // End of a call: launch/device error check; in host mode copy `bytes` of

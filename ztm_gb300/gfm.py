@@ -85,6 +85,22 @@ class _Args:
         self.keep.append(a)
         return a, a.ctypes.data_as(ctypes.c_void_p)
 
+    def scalar(self, like=None):
+        """A one-value output: a ctypes double (host) or a 1-element tensor
+        (device); returns (holder, pointer)."""
+        if self.device:
+            import torch
+            t = torch.zeros(1, dtype=torch.float64, device=like.device if like is not None else "cuda")
+            self.keep.append(t)
+            return t, ctypes.c_void_p(t.data_ptr())
+        v = ctypes.c_double(0.0)
+        self.keep.append(v)
+        return v, ctypes.cast(ctypes.pointer(v), ctypes.c_void_p)
+
+    @staticmethod
+    def value(holder):
+        return holder if not isinstance(holder, ctypes.c_double) else holder.value
+
     @property
     def flags(self):
         return _lib.FLAG_DEVICE_PTRS if self.device else 0
@@ -253,6 +269,90 @@ class GravityContext:
         prec = PRECISIONS[precision] if isinstance(precision, str) else precision
         self._run(a, self._lib.ztm_gfm_pointmass_model, self._h, ctypes.byref(p),
                   ctypes.byref(grid), ps, pm, pv, pf, po, prec, a.flags)
+        return out
+
+    # -- derivatives of the reference model (TFM.cpp:101-103, 124-135) -----
+    def pointmass_adjoint(self, grid, surf, w, nn=None, drho=None, precision="fp64"):
+        """J^T w: g[n] = sum over interior stations of w[m] dG[m]/d drho[n]
+        for the nodes of nn (with multiplicity), else of |drho| > threshold
+        when drho is given, else every node."""
+        ii = (grid.di - 1) * grid.fh + 1
+        jj = (grid.dj - 1) * grid.fh + 1
+        kk = (grid.dk - 1) * grid.fv + 1
+        a = _Args(self)
+        ps = a.arr(surf, grid.di * grid.dj, name="surf")
+        pw = a.arr(w, grid.di * grid.dj, name="w")
+        pd = a.arr(drho, ii * jj * kk, name="drho") if drho is not None else None
+        pn, n_nn = None, 0
+        if nn is not None:
+            pn = a.arr(nn, None, dtype=np.int32, name="nn")
+            n_nn = int(nn.numel() if _is_torch_cuda(nn) else np.asarray(nn).size)
+        out, po = a.out(ii * jj * kk, surf)
+        prec = PRECISIONS[precision] if isinstance(precision, str) else precision
+        self._run(a, self._lib.ztm_gfm_pointmass_adjoint, self._h, ctypes.byref(grid), pd, pn,
+                  n_nn, ps, pw, po, prec, a.flags)
+        return out
+
+    def pointmass_misfit(self, grid, drho, surf, GD, g0=0.0, gsig=1.0, nn=None,
+                         precision="fp64", gradient=True):
+        """The gravity misfit of TFM.cpp:101-103.  Returns (ssq, res, G,
+        g_drho, g_g0): res in TFM's order (i0 outer, j0 inner over the bfr
+        interior), g_drho = d ssq / d drho and g_g0 = d ssq / d g0 (None
+        without gradient)."""
+        ii = (grid.di - 1) * grid.fh + 1
+        jj = (grid.dj - 1) * grid.fh + 1
+        kk = (grid.dk - 1) * grid.fv + 1
+        ns = max(0, grid.di - 2 * grid.bfr) * max(0, grid.dj - 2 * grid.bfr)
+        a = _Args(self)
+        pd = a.arr(drho, ii * jj * kk, name="drho")
+        ps = a.arr(surf, grid.di * grid.dj, name="surf")
+        pgd = a.arr(GD, grid.di * grid.dj, name="GD")
+        pn, n_nn = None, 0
+        if nn is not None:
+            pn = a.arr(nn, None, dtype=np.int32, name="nn")
+            n_nn = int(nn.numel() if _is_torch_cuda(nn) else np.asarray(nn).size)
+        res, pres = a.out(max(ns, 1), drho)
+        G, pG = a.out(grid.di * grid.dj, drho)
+        g, pg = a.out(ii * jj * kk, drho) if gradient else (None, None)
+        ssq, pssq = a.scalar(drho)
+        g0h, pg0 = a.scalar(drho) if gradient else (None, None)
+        prec = PRECISIONS[precision] if isinstance(precision, str) else precision
+        self._run(a, self._lib.ztm_gfm_pointmass_misfit, self._h, ctypes.byref(grid), pd, pn, n_nn,
+                  ps, pgd, float(g0), float(gsig), pssq, pres, pG, pg, pg0, prec, a.flags)
+        return (a.value(ssq), res[:ns], G, g, a.value(g0h) if gradient else None)
+
+    def pointmass_model_misfit(self, grid, sea, M, v, surf, GD, vm, ro, dr, rc, g0=0.0, gsig=1.0,
+                               precision="fp64", gradient=True):
+        """TFM.cpp:83-103 with the gradient chained through the density
+        builder.  Returns a dict: ssq, res, G and, with gradient, g_M
+        (d ssq / d M), g_v (d ssq / d v) and g_par (d ssq / d (vm, ro, dr, g0))."""
+        p = _lib.DensityParams(grid.di, grid.dj, grid.dk, grid.fh, grid.fv, vm, ro, dr,
+                               (ctypes.c_double * 10)(*rc))
+        ns = max(0, grid.di - 2 * grid.bfr) * max(0, grid.dj - 2 * grid.bfr)
+        M2 = grid.di * grid.dj
+        a = _Args(self)
+        pse = a.arr(sea, M2, name="sea")
+        pm = a.arr(M, M2, name="M")
+        pv = a.arr(v, M2 * grid.dk, name="v")
+        pf = a.arr(surf, M2, name="surf")
+        pgd = a.arr(GD, M2, name="GD")
+        res, pres = a.out(max(ns, 1), sea)
+        G, pG = a.out(M2, sea)
+        if gradient:
+            gM, pgM = a.out(M2, sea)
+            gv, pgv = a.out(M2 * grid.dk, sea)
+            gp, pgp = a.out(4, sea)
+        else:
+            gM = gv = gp = None
+            pgM = pgv = pgp = None
+        ssq, pssq = a.scalar(sea)
+        prec = PRECISIONS[precision] if isinstance(precision, str) else precision
+        self._run(a, self._lib.ztm_gfm_pointmass_model_misfit, self._h, ctypes.byref(p),
+                  ctypes.byref(grid), pse, pm, pv, pf, pgd, float(g0), float(gsig), pssq, pres, pG,
+                  pgM, pgv, pgp, prec, a.flags)
+        out = {"ssq": a.value(ssq), "res": res[:ns], "G": G}
+        if gradient:
+            out.update(g_M=gM, g_v=gv, g_par=gp)
         return out
 
     # -- prism mesh -----------------------------------------------------
