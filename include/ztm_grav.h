@@ -148,6 +148,24 @@ int ztm_ctx_sync(ztm_ctx* ctx);
 int ztm_ctx_profile(ztm_ctx* ctx, int enable);
 int ztm_ctx_profile_read(ztm_ctx* ctx, const char* name, double* ms,
                          long long* count);
+/* Form counters of the mixed prism forward.  While enabled, the forward runs
+ * a counting variant of its far kernel (the same arithmetic plus one counter
+ * update per column and thread) that adds up the (station, prism) slots it
+ * evaluates in each form of the far-field expansion.  ztm_ctx_form_counts
+ * waits for the stream and returns, then clears: counts[0] slots in the
+ * fourth-order form, [1] second order, [2] second order by column pairs
+ * (slots include the near-region layers a masked group evaluates and drops,
+ * and the padding of nz to a multiple of 8), [3] closed-form corner-function
+ * evaluations (Phi) of the near regions.  These are the numerators of the
+ * executed-flop roofline; the reference has no counterpart. */
+int ztm_ctx_count_forms(ztm_ctx* ctx, int enable);
+int ztm_ctx_form_counts(ztm_ctx* ctx, long long* counts);
+/* Test hook of the timeout path: bounds the copy-arrival waits of the mixed
+ * prism forward's far kernel at `iterations` spins (0 restores the default,
+ * 2^24).  A wait that gives up makes its block record a timeout, wait (with
+ * the full limit) for the copies it has in flight and stop; the call returns
+ * ZTM_ERR_TIMEOUT and the context stays usable. */
+int ztm_ctx_set_wait_limit(ztm_ctx* ctx, unsigned int iterations);
 /* Issue-rate micro-benchmarks of the device, the denominators of the
  * compute roofline: kind 0 = FP32 FMA (TFLOP/s, 2 flops per FMA), 1 = FP64
  * FMA (TFLOP/s), 2 = float rsqrt on the special-function unit (Gop/s). */

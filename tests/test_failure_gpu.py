@@ -1,0 +1,39 @@
+"""Failure handling on the GPU without a GPU fault.
+
+Every copy-arrival wait of the mixed forward's far kernel is bounded; a wait
+that gives up makes its block record a timeout in the context's error word,
+wait (with the full bound) for the copies it still has in flight, and stop.
+The test hook ztm_ctx_set_wait_limit shortens the bound to a single
+non-blocking test of each stage, so that the waits give up before the copies
+land: the call must return ZTM_ERR_TIMEOUT, and the next call on the same
+context, with the default bound, must run normally.  Nothing here faults,
+traps or hangs the GPU: the copies land as usual and are waited for."""
+import numpy as np
+import pytest
+
+import oracle
+import ztm_gb300
+from helpers import awkward_stations, rel_err, small_mesh
+
+pytestmark = pytest.mark.gpu
+
+
+def test_timeout_is_reported_and_the_context_recovers(ctx):
+    mesh, rho = small_mesh(96, 80, 24, seed=4)
+    st = awkward_stations(mesh, n_random=300)
+    ref = oracle.prism_mesh(mesh, rho, st)
+    ctx.set_wait_limit(1)
+    try:
+        with pytest.raises(ztm_gb300.GravityError) as e:
+            ctx.prism(mesh, rho, st, precision="mixed")
+        assert e.value.code == ztm_gb300.ERR_TIMEOUT
+    finally:
+        ctx.set_wait_limit(0)
+    out = ctx.prism(mesh, rho, st, precision="mixed")
+    assert rel_err(out, ref) <= 1e-6
+    # the error word was cleared: a device-pointer call reports nothing stale
+    torch = pytest.importorskip("torch")
+    out = ctx.prism(mesh, torch.tensor(rho, device="cuda"), torch.tensor(st, device="cuda"),
+                    precision="mixed")
+    ctx.sync()
+    assert rel_err(out.cpu().numpy(), ref) <= 1e-6

@@ -161,3 +161,25 @@ def test_draped_mesh_256_linearity_and_batch(ctx):
     ref = ctx.prism(mesh, trials[1], st, precision="mixed")
     assert rel_err(out[1], ref) <= 1e-6
     assert rel_err(out[0], a) <= 1e-6
+
+
+@pytest.mark.parametrize("shape", [(40, 36, 16), (96, 80, 20)])
+def test_form_counts_cover_every_slot(ctx, shape):
+    """The counting variant of the far kernel (the numerators of the
+    executed-flop roofline) gives the same field to the bit, and its slots
+    add up to every station x column x padded layer; the near regions'
+    corner evaluations are counted where stations sit on the mesh."""
+    mesh, rho = small_mesh(*shape, seed=5)
+    st = awkward_stations(mesh, n_random=200)
+    gz = ctx.prism(mesh, rho, st, precision="mixed")
+    ctx.count_forms(True)
+    try:
+        gz_c = ctx.prism(mesh, rho, st, precision="mixed")
+        counts = ctx.form_counts()
+    finally:
+        ctx.count_forms(False)
+    assert np.array_equal(gz, gz_c)
+    nzp = (mesh.nz + 7) // 8 * 8
+    assert counts[0] + counts[1] + counts[2] == len(st) * mesh.nx * mesh.ny * nzp
+    assert counts[3] > 0
+    assert ctx.form_counts() == (0, 0, 0, 0)  # read clears

@@ -155,7 +155,8 @@ __device__ __forceinline__ void near_station(const MeshConst& k, const MeshDesc&
                                              const short2* __restrict__ iv,
                                              const int2* __restrict__ lr,
                                              const double* __restrict__ rho,
-                                             double* __restrict__ out, int lane) {
+                                             double* __restrict__ out, int lane,
+                                             unsigned* nphi = nullptr) {
   const NearBox b = near_box(si[s], k);
   const int2 L = lr[s];
   if (L.x > L.y) {  // no near prism
@@ -201,6 +202,7 @@ __device__ __forceinline__ void near_station(const MeshConst& k, const MeshDesc&
       const T y = (T)((m.y0 + bb * m.dy) - ys);
       const T z = (T)((m.zt - cz * m.dz) - zs);
       acc += (T)D * ztm_phi<T>(x, y, z);
+      if (nphi) ++*nphi;
     }
   }
   double tot = warp_sum_d((double)acc);
@@ -230,6 +232,9 @@ struct FarArgs {
   const float* rhoT;
   double* partial;  // [chunk][ns]
   int* err;
+  unsigned poll_limit;        // test hook, 0 = off: thread 0 polls each stage at most
+                              // this many times and the block follows its verdict
+  unsigned long long* forms;  // counting variant: the four form counters
 };
 
 __device__ __forceinline__ float far_pair(float rho, float Z, float rh, float a0, float h0,
@@ -406,9 +411,12 @@ __device__ __forceinline__ void far_column_pair(const float* colA, const float* 
 // One shared-memory stage (ncol columns starting at column cs) against this
 // thread's station; adds to acc.  Every lane runs the loop (inactive lanes
 // on dummy data) for the warp votes.
+// COUNT: add the (station, prism) slots this thread evaluates to cnt by
+// form: [0] fourth order, [1] second order, [2] second order by column pairs.
+template <bool COUNT>
 __device__ __forceinline__ void far_stage(const FarArgs& a, const MeshConst& k, const FarCoef& fc,
                                           const FarStation& t, int s, int Lm, const float* rs,
-                                          int cs, int ncol, Kahan& acc) {
+                                          int cs, int ncol, Kahan& acc, unsigned (&cnt)[3]) {
   const float2 zstep = make_float2(k.dzn, k.dzn);
   // Z of layers 2j, 2j+1 of a group at l0 = 0; a group at l0 adds l0 dz
   float2 Zb[4];
@@ -446,6 +454,7 @@ __device__ __forceinline__ void far_stage(const FarArgs& a, const MeshConst& k, 
         cpA.C2 = cpA.C3 = cpA.C4 = cpB.C2 = cpB.C3 = cpB.C4 = make_float2(0.f, 0.f);
         far_column_pair(rs + q * k.nzp, rs + (q + 1) * k.nzp, k.nz, Zb, zstep, cpA,
                         make_float2(cA, cA), cpB, make_float2(cB, cB), acc);
+        if (COUNT) cnt[2] += 2 * k.nz;
         q++;
         ix = ix1 + 1;
         iy = iy1;
@@ -483,10 +492,12 @@ __device__ __forceinline__ void far_stage(const FarArgs& a, const MeshConst& k, 
       cp2.C2 = cp2.C3 = cp2.C4 = make_float2(0.f, 0.f);  // unused by the form
       far_column<true>(col, lmask, nz8, k.nz, Zb, zstep, cp2, make_float2(c2t, c2t), elo, espan,
                        acc);
+      if (COUNT) cnt[1] += k.nzp;
     } else {
       const ColPoly2 cp2 = col_poly2(col_poly(X, Y, fc), fc.a1);
       far_column<false>(col, lmask, nz8, k.nz, Zb, zstep, cp2, make_float2(0.f, 0.f), elo, espan,
                         acc);
+      if (COUNT) cnt[0] += k.nzp;
     }
     if (++ix == k.nx) {
       ix = 0;
@@ -507,13 +518,18 @@ __device__ __forceinline__ void far_stage(const FarArgs& a, const MeshConst& k, 
 // The density of a far item's columns streams through two shared-memory
 // stages by 1-D bulk copies; the next far item's first stage is copied while
 // the current item's last stage (or a near item) is processed.
+// COUNT: the counting variant (ztm_ctx_count_forms): the same work, with the
+// evaluated slots of each form (and the near regions' Phi evaluations) added
+// to a.forms at the end.
+template <bool COUNT>
 __global__ void __launch_bounds__(FAR_TS, 6) far_kernel(FarArgs a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
   float* stage = reinterpret_cast<float*>(smem_raw + 128);
   __shared__ int s_lm;
   __shared__ int s_item[2];
-  __shared__ int s_to[2];  // a copy wait gave up (by stage parity)
+  __shared__ int s_to[2];    // a copy wait gave up (by stage parity)
+  __shared__ int s_poll[2];  // test hook: thread 0 saw the stage land (by stage parity)
   const MeshConst& k = a.k;
   const int stage_floats = a.sc * k.nzp;
   const int n_far = a.tiles * a.chunks;
@@ -562,6 +578,7 @@ __global__ void __launch_bounds__(FAR_TS, 6) far_kernel(FarArgs a) {
   bool timed_out = false;
   int par = 0;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  unsigned cnt[3] = {0u, 0u, 0u}, nphi = 0u;
   for (;;) {
     const int item = s_item[par];
     if (item >= n_items) break;
@@ -578,9 +595,11 @@ __global__ void __launch_bounds__(FAR_TS, 6) far_kernel(FarArgs a) {
         const int s = s0 + j;
         if (s >= a.ns) break;
         if (a.near_f64)
-          near_station<double>(k, a.m, s, a.sxyz, a.si, a.iv, a.lr, a.rho, a.near, lane);
+          near_station<double>(k, a.m, s, a.sxyz, a.si, a.iv, a.lr, a.rho, a.near, lane,
+                               COUNT ? &nphi : nullptr);
         else
-          near_station<float>(k, a.m, s, a.sxyz, a.si, a.iv, a.lr, a.rho, a.near, lane);
+          near_station<float>(k, a.m, s, a.sxyz, a.si, a.iv, a.lr, a.rho, a.near, lane,
+                              COUNT ? &nphi : nullptr);
       }
       if (threadIdx.x == 0) s_item[par] = nxt < n_items ? atomicAdd(a.counter, 1) : n_items;
       __syncthreads();
@@ -623,10 +642,26 @@ __global__ void __launch_bounds__(FAR_TS, 6) far_kernel(FarArgs a) {
       // the stage; the block leaves together after the stage's barrier (the
       // flags alternate by stage, so a flag raised in the next stage cannot
       // be read by a thread still finishing this one)
-      if (mbar_wait(&bar[seq & 1], (seq >> 1) & 1)) {
+      bool landed;
+      if (a.poll_limit) {
+        // test hook of the timeout path: one verdict for the whole block, so
+        // that no warp splits around the stage's votes
+        if (threadIdx.x == 0) s_poll[seq & 1] = mbar_poll(&bar[seq & 1], (seq >> 1) & 1, a.poll_limit);
+        __syncthreads();
+        landed = s_poll[seq & 1] && mbar_wait(&bar[seq & 1], (seq >> 1) & 1);
+      } else {
+        landed = mbar_wait(&bar[seq & 1], (seq >> 1) & 1);
+      }
+      if (landed) {
         int cs;
         const int ncol = stage_cols(f, st, &cs);
-        far_stage(a, k, fc, t, s, Lm, stage + (seq & 1) * stage_floats, cs, ncol, acc);
+        unsigned c3[3] = {0u, 0u, 0u};
+        far_stage<COUNT>(a, k, fc, t, s, Lm, stage + (seq & 1) * stage_floats, cs, ncol, acc, c3);
+        if (COUNT && active) {
+          cnt[0] += c3[0];
+          cnt[1] += c3[1];
+          cnt[2] += c3[2];
+        }
       } else {
         s_to[seq & 1] = 1;
       }
@@ -647,8 +682,17 @@ __global__ void __launch_bounds__(FAR_TS, 6) far_kernel(FarArgs a) {
   if (timed_out && threadIdx.x == 0) {
     atomicOr(a.err, ZTM_DEVERR_TIMEOUT);
     // let copies already in flight land before the block's shared memory is
-    // released (bounded as well)
+    // released (bounded by the full limit, whatever a.poll_limit says)
     for (int q = seq; q < issued; q++) mbar_wait(&bar[q & 1], (q >> 1) & 1);
+  }
+  if (COUNT) {
+    unsigned long long v[4] = {cnt[0], cnt[1], cnt[2], nphi};
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v[j] += __shfl_down_sync(0xffffffffu, v[j], o);
+      if (lane == 0 && v[j]) atomicAdd(&a.forms[j], v[j]);
+    }
   }
 }
 
@@ -821,11 +865,13 @@ FarShape far_shape(const MeshConst& k, int ns, int num_sms, const ztm_opts* o, i
   f.smem = 128 + 2 * (size_t)sc * k.nzp * 4;
   // stages above the default 48 KB need the opt-in (very deep meshes)
   if (f.smem > 48 * 1024 &&
-      cudaFuncSetAttribute(far_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)f.smem) != cudaSuccess)
+      (cudaFuncSetAttribute(far_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)f.smem) != cudaSuccess ||
+       cudaFuncSetAttribute(far_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)f.smem) != cudaSuccess))
     cudaGetLastError();
   int occ = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, far_kernel, FAR_TS, f.smem) !=
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, far_kernel<false>, FAR_TS, f.smem) !=
           cudaSuccess ||
       occ < 1) {
     cudaGetLastError();
@@ -987,13 +1033,18 @@ int ztm_launch_prism(ztm_ctx* c, const MeshDesc& m, const double* d_rho, int ns,
   a.rho = d_rho;
   a.lr = lr;
   a.near = near;
+  a.poll_limit = c->stage_wait_limit;
+  a.forms = c->d_forms;
   auto launch_far = [&](const FarShape& t) {
     a.tiles = t.tiles;
     a.chunks = t.chunks;
     a.chunk_cols = t.chunk_cols;
     a.sc = t.sc;
     cudaMemsetAsync(counter, 0, sizeof(int), c->stream);
-    far_kernel<<<t.grid, FAR_TS, t.smem, c->stream>>>(a);
+    if (c->count_forms && c->d_forms)
+      far_kernel<true><<<t.grid, FAR_TS, t.smem, c->stream>>>(a);
+    else
+      far_kernel<false><<<t.grid, FAR_TS, t.smem, c->stream>>>(a);
     c->launches++;
   };
   if (o && (o->flags & ZTM_FLAG_AUTOTUNE) && !(o->chunk > 0) && it == c->tuned.end()) {

@@ -278,6 +278,7 @@ void ztm_ctx_destroy(ztm_ctx* c) {
   for (auto e : c->prof_pool) cudaEventDestroy(e);
   if (c->ws) cudaFree(c->ws);
   if (c->d_err) cudaFree(c->d_err);
+  if (c->d_forms) cudaFree(c->d_forms);
   if (c->aux) {
     cudaStreamSynchronize(c->aux);
     cudaStreamDestroy(c->aux);
@@ -299,6 +300,46 @@ int ztm_ctx_set_stream(ztm_ctx* c, void* stream) {
 void* ztm_ctx_stream(ztm_ctx* c) { return c ? (void*)c->stream : nullptr; }
 
 long long ztm_ctx_launches(const ztm_ctx* c) { return c ? c->launches : -1; }
+
+int ztm_ctx_set_wait_limit(ztm_ctx* c, unsigned int iterations) {
+  if (!c) return ZTM_ERR_ARG;
+  c->stage_wait_limit = iterations;
+  return ZTM_OK;
+}
+
+int ztm_ctx_count_forms(ztm_ctx* c, int enable) {
+  if (!c) return ZTM_ERR_ARG;
+  c->err.clear();
+  if (enable && !c->d_forms) {
+    DeviceGuard g(c->device);
+    if (cudaMalloc((void**)&c->d_forms, 4 * sizeof(unsigned long long)) != cudaSuccess) {
+      cudaGetLastError();
+      c->d_forms = nullptr;
+      return ztm_fail(c, ZTM_ERR_ALLOC, "form counters");
+    }
+    if (cudaMemsetAsync(c->d_forms, 0, 4 * sizeof(unsigned long long), c->stream) != cudaSuccess)
+      return ztm_fail(c, ZTM_ERR_CUDA, "form counters");
+  }
+  c->count_forms = enable != 0;
+  return ZTM_OK;
+}
+
+int ztm_ctx_form_counts(ztm_ctx* c, long long* counts) {
+  if (!c || !counts) return ZTM_ERR_ARG;
+  c->err.clear();
+  for (int j = 0; j < 4; j++) counts[j] = 0;
+  if (!c->d_forms) return ZTM_OK;
+  DeviceGuard g(c->device);
+  unsigned long long h[4] = {0, 0, 0, 0};
+  int rc = ztm_cuda_check(c, cudaMemcpyAsync(h, c->d_forms, sizeof h, cudaMemcpyDeviceToHost,
+                                             c->stream),
+                          "read form counters");
+  if (!rc) rc = ztm_cuda_check(c, cudaStreamSynchronize(c->stream), "read form counters");
+  if (rc) return rc;
+  cudaMemsetAsync(c->d_forms, 0, sizeof h, c->stream);
+  for (int j = 0; j < 4; j++) counts[j] = (long long)h[j];
+  return ZTM_OK;
+}
 
 int ztm_ctx_sync(ztm_ctx* c) {
   if (!c) return ZTM_ERR_ARG;

@@ -49,6 +49,12 @@ struct ztm_ctx {
   std::vector<char> batch_table;
   // launch shapes chosen by the autotuner, keyed by workload shape
   std::map<std::vector<long long>, std::vector<int>> tuned;
+  // spin limit of the far kernel's copy-arrival waits (0: ZTM_WAIT_LIMIT);
+  // a test hook for the timeout path, ztm_ctx_set_wait_limit
+  unsigned stage_wait_limit = 0;
+  // evaluation-form counters of the mixed forward (ztm_ctx_count_forms)
+  bool count_forms = false;
+  unsigned long long* d_forms = nullptr;  // 4 counters on the device
   // tracing: events around compute kernels while enabled
   bool prof = false;
   std::vector<ZtmProfRec> prof_recs;
@@ -296,14 +302,33 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src,
       "l"(src), "r"(bytes), "r"(smem_u32(bar))
       : "memory");
 }
-// Bounded wait on phase `parity`; returns false if the limit ran out.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// Bounded wait on phase `parity`; returns false if `limit` spins ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
+                                          uint32_t limit = ZTM_WAIT_LIMIT) {
   uint32_t a = smem_u32(bar);
-  for (uint32_t it = 0; it < ZTM_WAIT_LIMIT; ++it) {
+  for (uint32_t it = 0; it < limit; ++it) {
     uint32_t ok;
     asm volatile(
         "{\n .reg .pred p;\n"
         " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+// Non-blocking test of phase `parity`, up to `limit` times; false if the phase
+// was not seen complete (the timeout path's test hook).
+__device__ __forceinline__ bool mbar_poll(uint64_t* bar, uint32_t parity, uint32_t limit) {
+  uint32_t a = smem_u32(bar);
+  for (uint32_t it = 0; it < limit; ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n"
+        " mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
         " selp.u32 %0, 1, 0, p;\n}"
         : "=r"(ok)
         : "r"(a), "r"(parity)

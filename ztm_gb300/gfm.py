@@ -213,6 +213,21 @@ class GravityContext:
                                                    ctypes.byref(n)))
         return ms.value, n.value
 
+    def count_forms(self, enable=True):
+        """Run the mixed forward's counting far kernel while enabled."""
+        self._check(self._lib.ztm_ctx_count_forms(self._h, 1 if enable else 0))
+
+    def form_counts(self):
+        """(fourth-order slots, second-order slots, column-pair slots, near
+        Phi evaluations) since the last read; clears them."""
+        out = (ctypes.c_longlong * 4)()
+        self._check(self._lib.ztm_ctx_form_counts(self._h, out))
+        return tuple(int(v) for v in out)
+
+    def set_wait_limit(self, iterations):
+        """Test hook: spin limit of the far kernel's copy waits (0: default)."""
+        self._check(self._lib.ztm_ctx_set_wait_limit(self._h, int(iterations)))
+
     def measure_peak(self, kind):
         """kind 'fp32' / 'fp64' (TFLOP/s of FMA) or 'rsqrt' (Gop/s)."""
         k = {"fp32": 0, "fp64": 1, "rsqrt": 2}[kind]
