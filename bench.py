@@ -36,11 +36,24 @@ METRIC = "prism·station gz evals/s and gradient evals/s; mixed vs FP64 at ≤1e
 UNIT = "evals/s"
 WORKLOAD = ("mixed-precision prism forward, 256x256x64 prisms (1x1x0.5 km), 128x128 stations "
             "draped on fractal topography 0-3 km")
-# executed float flops per (station, prism) pair in the far-field kernel
-# (FMA = 2; the rsqrt on the special-function unit is not counted): Z 2,
-# r^2 2, 1/r^2 1, Horner in 1/r^2 8, Z*s 1, 1/r^3 1, product 1, density FMA 2,
-# and per 8-layer group 7 (group Z, layer counter, Kahan add) -> 19
-FLOPS_PER_PAIR = 19
+# Executed float flops per evaluated (station, prism) slot of the far kernel,
+# by form (FMA = 2; the rsqrt on the special-function unit is not a flop),
+# counted from prism_common.cuh / prism.cu per lane of the packed operations:
+#   fourth order (far_unit2): Z 2, r^2 2, u 1, Horner 4 FMA 8, three products 3,
+#     density accumulate 2 -> 18
+#   second order (far_unit2_t2): Z 2, r^2 2, u 1, two FMA 4, three products 3,
+#     accumulate 2 -> 14
+#   column pairs: second order with one Z for two columns -> 13
+# plus the compensation step per 32 slots (an add and a 4-operation Kahan
+# update: 5/32).  The slot counts come from the counting variant of the same
+# kernel, run once per bench (ztm_ctx_count_forms), so that the numerator is
+# the work this launch executes.
+FLOPS_PER_SLOT = {"fourth_order": 18 + 5 / 32, "second_order": 14 + 5 / 32,
+                  "column_pairs": 13 + 5 / 32}
+# DRAM bytes of one far_kernel launch on this workload, ncu
+# dram__bytes_read.sum + dram__bytes_write.sum (the capture and its command
+# are in profiles/prism_far_256x256x64_draped.md)
+FAR_TRAFFIC_BYTES = 26.4e6
 L2_BYTES = 129 * 2 ** 20
 
 
@@ -92,20 +105,6 @@ class ClockSampler:
         os.unlink(self.path)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
                 "reasons": sorted(reasons), "samples": len(sm)}
-
-
-def read_traffic():
-    """DRAM bytes per far-kernel launch from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "prism_far_256x256x64_draped.md")
-    if not os.path.exists(p):
-        return None
-    for line in open(p):
-        if line.strip().startswith("traffic_bytes_per_launch:"):
-            try:
-                return float(line.split(":", 1)[1])
-            except ValueError:
-                return None
-    return None
 
 
 def cpu_baseline_prism(mesh, rho, st, nsample=224):
@@ -212,7 +211,12 @@ def run_ours(args, rank, local_rank, world):
 
     for _ in range(args.warmup):
         step()
+    # one untimed step of the counting variant: the slots of each form
+    ctx.count_forms(True)
+    step()
     ctx.sync()
+    forms = ctx.form_counts()
+    ctx.count_forms(False)
     torch.cuda.synchronize()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
@@ -280,7 +284,9 @@ def run_ours(args, rank, local_rank, world):
 
     peak32 = ctx.measure_peak("fp32")
     far_avg = far_ms / max(far_n, 1)
-    achieved = FLOPS_PER_PAIR * pairs / (far_avg * 1e-3) / 1e12
+    slots = dict(zip(("fourth_order", "second_order", "column_pairs"), forms[:3]))
+    flops = sum(slots[f] * FLOPS_PER_SLOT[f] for f in slots)
+    achieved = flops / (far_avg * 1e-3) / 1e12
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
@@ -288,11 +294,16 @@ def run_ours(args, rank, local_rank, world):
             "gpu_launches": launches,
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak32,
                          "unit": "TFLOP/s", "frac": achieved / peak32 if peak32 else None,
-                         "traffic": read_traffic(),
+                         "traffic": FAR_TRAFFIC_BYTES,
                          "kernel": "far_kernel: far fields (FMA pipe) and near regions "
                                    "(FP64 pipe) in one persistent grid",
-                         "flops_per_pair": FLOPS_PER_PAIR, "pairs_per_launch": pairs,
-                         "kernel_ms": far_avg,
+                         "flops_per_launch": flops, "slots_per_launch": slots,
+                         "flops_per_slot": FLOPS_PER_SLOT,
+                         "near_phi_per_launch": forms[3],
+                         "pairs_per_launch": pairs, "kernel_ms": far_avg,
+                         "algorithmic_bytes_per_launch": np_ * 4 + len(st) * 32,
+                         "traffic_source": "ncu dram bytes read + written, one launch "
+                                           "(profiles/prism_far_256x256x64_draped.md)",
                          "peak_source": "measured FP32 FMA issue rate on this GPU "
                                         "(ztm_measure_peak; MEASURED_PEAKS.json has only HBM "
                                         "and bf16 tensor peaks, neither bounds this kernel)"},
@@ -308,68 +319,100 @@ def run_ours(args, rank, local_rank, world):
     return 0
 
 
+def _median_ms(ctx, fn, n):
+    """Median device time of n replays of fn (one warm-up call first), CUDA
+    events on the context's stream around each replay."""
+    import torch
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    out = fn()
+    ctx.sync()
+    ms = []
+    for _ in range(n):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = fn()
+        e1.record(stream)
+        ctx.sync()
+        ms.append(e0.elapsed_time(e1))
+    return statistics.median(ms), out
+
+
+FIELD_FIXTURE = os.path.join(ROOT, "tests", "golden", "prism_256x256x64_draped_fp64.npz")
+
+
+def full_field_accuracy(rho, st, gz_mixed):
+    """The mixed field at every station against the committed double field
+    of the same inputs (tests/golden/make_prism_field.py: the CPU oracle,
+    every prism at every station)."""
+    import numpy as np
+    if not os.path.exists(FIELD_FIXTURE):
+        return None
+    z = np.load(FIELD_FIXTURE)
+    same = (abs(float(np.sum(rho)) - float(z["rho_sum"])) <= 1e-9 * float(z["rho_abs_sum"]) and
+            np.allclose(rho[::9973], z["rho_sample"], rtol=0, atol=1e-9) and
+            np.allclose(np.sum(st, axis=0), z["st_sum"], rtol=1e-12))
+    if not same:
+        return {"error": "inputs differ from the fixture's fingerprint"}
+    ref = z["gz"]
+    err = np.abs(gz_mixed - ref)
+    rel = err / np.abs(ref)
+    return {"stations": int(ref.size), "normwise_rel_err": float(err.max() / np.abs(ref).max()),
+            "max_station_rel_err": float(rel.max()), "p99_station_rel_err":
+            float(np.percentile(rel, 99)), "reference": "double-precision CPU oracle, all stations"}
+
+
 def extras(ctx, mesh, rho, st, d_rho, d_st, gz_mixed):
-    """Side measurements: plain FP64 kernel rate and the mixed error on a
-    station subset, gradient evals/s, and the reference GF kernel on the
-    same geometry."""
+    """Side measurements: the mixed field against the double field at every
+    station, the plain FP64 kernel's rate, gradient evals/s of the adjoint,
+    the reference's point-mass model on the same geometry (ours and the
+    reference GF kernel itself).  Rates are medians of replays."""
     import numpy as np
     import torch
     import oracle
     from ztm_gb300 import synth
     out = {}
     np_ = mesh.nx * mesh.ny * mesh.nz
-    stream = torch.cuda.ExternalStream(ctx.stream)
+    acc = full_field_accuracy(rho, st, gz_mixed)
+    if acc is not None:
+        out["accuracy_full_field"] = acc
     sub = np.arange(0, len(st), len(st) // 64)[:64]
     ds = torch.tensor(st[sub], device="cuda")
-    ctx.prism(mesh, d_rho, ds, precision="fp64")
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    ref = ctx.prism(mesh, d_rho, ds, precision="fp64")
-    e1.record(stream)
-    ctx.sync()
-    ms64 = e0.elapsed_time(e1)
+    ms64, ref = _median_ms(ctx, lambda: ctx.prism(mesh, d_rho, ds, precision="fp64"), 5)
     r = ref.cpu().numpy()
     m = gz_mixed[sub]
     out["fp64_plain"] = {"value": np_ * len(sub) / (ms64 * 1e-3), "unit": UNIT,
-                         "sample": "%d stations x all prisms" % len(sub)}
+                         "sample": "%d stations x all prisms, median of 5" % len(sub)}
     out["accuracy"] = {"normwise_rel_err_vs_fp64": float(np.max(np.abs(m - r)) / np.max(np.abs(r))),
                        "max_station_rel_err": float(np.max(np.abs(m - r) / np.abs(r))),
-                       "stations_checked": len(sub)}
+                       "stations_checked": len(sub), "reference": "the plain FP64 GPU kernel"}
     # gradient evals/s: adjoint of the same forward (d misfit / d rho)
     res = torch.tensor(np.random.default_rng(0).normal(0, 1, len(st)), device="cuda")
-    ctx.adjoint(mesh, d_st, res, precision="mixed")
-    e0.record(stream)
-    ctx.adjoint(mesh, d_st, res, precision="mixed")
-    e1.record(stream)
-    ctx.sync()
-    msa = e0.elapsed_time(e1)
+    msa, _ = _median_ms(ctx, lambda: ctx.adjoint(mesh, d_st, res, precision="mixed"), 10)
     out["gradient"] = {"value": np_ * len(st) / (msa * 1e-3), "unit": "gradient evals/s",
-                       "ms": msa, "what": "d misfit / d rho, all pairs, mixed"}
+                       "ms": msa, "what": "d misfit / d rho, all pairs, mixed, median of 10"}
     # the reference's own point-mass model on the same geometry (its grid,
-    # every node as a station): our float and double gathers
+    # every node as a station): our float and double gathers and adjoints
     g, drho, surf = synth.pointmass_grid_of_mesh(mesh, rho, st)
     nodes32 = int(np.count_nonzero(np.abs(drho.astype(np.float32)) > 0.001))
     nodes64 = int(np.count_nonzero(np.abs(drho) > 0.001))
     dd, dsf = torch.tensor(drho, device="cuda"), torch.tensor(surf, device="cuda")
+    dw = torch.tensor(np.random.default_rng(1).normal(0, 1, g.di * g.dj), device="cuda")
     pm = {}
-    for prec, nodes in (("fp32", nodes32), ("fp64", nodes64)):
-        ctx.pointmass(g, dd, dsf, precision=prec)
-        e0.record(stream)
-        ctx.pointmass(g, dd, dsf, precision=prec)
-        e1.record(stream)
-        ctx.sync()
-        ms = e0.elapsed_time(e1)
+    for prec, nodes, n in (("fp32", nodes32, 10), ("fp64", nodes64, 3)):
+        ms, _ = _median_ms(ctx, lambda: ctx.pointmass(g, dd, dsf, precision=prec), n)
+        msj, _ = _median_ms(ctx, lambda: ctx.pointmass_adjoint(g, dsf, dw, drho=dd,
+                                                               precision=prec), n)
         pm[prec] = {"value": nodes * mesh.nx * mesh.ny / (ms * 1e-3), "unit": "point-mass pairs/s",
-                    "ms": ms}
+                    "ms": ms, "adjoint_value": nodes64 * mesh.nx * mesh.ny / (msj * 1e-3),
+                    "adjoint_ms": msj, "replays": n}
     out["pointmass_gpu"] = pm
     if oracle.ref_gf_available():
         gf, ms = oracle.ref_gf(g, drho.astype(np.float32), surf.astype(np.float32), reps=3)
-        nodes = int(np.count_nonzero(np.abs(drho.astype(np.float32)) > 0.001))
         out["reference_gf_gpu"] = {
-            "value": nodes * mesh.nx * mesh.ny / (ms * 1e-3), "unit": "point-mass pairs/s",
+            "value": nodes32 * mesh.nx * mesh.ny / (ms * 1e-3), "unit": "point-mass pairs/s",
             "ms": ms, "what": "reference GF kernel (GFM_GPU.cu:16-22) compiled unchanged for "
-                              "sm_103a, same geometry on its grid (%d stations x %d nodes)"
-                              % (mesh.nx * mesh.ny, nodes)}
+                              "sm_103a, same geometry on its grid (%d stations x %d nodes), mean "
+                              "of 3 launches" % (mesh.nx * mesh.ny, nodes32)}
     return out
 
 
