@@ -160,12 +160,14 @@ int ztm_ctx_profile_read(ztm_ctx* ctx, const char* name, double* ms,
  * executed-flop roofline; the reference has no counterpart. */
 int ztm_ctx_count_forms(ztm_ctx* ctx, int enable);
 int ztm_ctx_form_counts(ztm_ctx* ctx, long long* counts);
-/* Test hook of the timeout path: bounds the copy-arrival waits of the mixed
- * prism forward's far kernel at `iterations` spins (0 restores the default,
- * 2^24).  A wait that gives up makes its block record a timeout, wait (with
- * the full limit) for the copies it has in flight and stop; the call returns
- * ZTM_ERR_TIMEOUT and the context stays usable. */
-int ztm_ctx_set_wait_limit(ztm_ctx* ctx, unsigned int iterations);
+/* Test hook of the timeout path (no GPU fault involved).  With polls > 0,
+ * every copy-arrival wait of the mixed prism forward's far kernel waits
+ * instead on a barrier that nothing completes and gives up after `polls`
+ * tests; each block then records a timeout, waits (with the full bound) for
+ * the copies it has in flight and stops, and the call returns
+ * ZTM_ERR_TIMEOUT.  polls = 0 switches the hook off; the context stays
+ * usable throughout. */
+int ztm_ctx_test_timeout(ztm_ctx* ctx, unsigned int polls);
 /* Issue-rate micro-benchmarks of the device, the denominators of the
  * compute roofline: kind 0 = FP32 FMA (TFLOP/s, 2 flops per FMA), 1 = FP64
  * FMA (TFLOP/s), 2 = float rsqrt on the special-function unit (Gop/s). */

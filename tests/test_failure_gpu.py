@@ -3,11 +3,12 @@
 Every copy-arrival wait of the mixed forward's far kernel is bounded; a wait
 that gives up makes its block record a timeout in the context's error word,
 wait (with the full bound) for the copies it still has in flight, and stop.
-The test hook ztm_ctx_set_wait_limit shortens the bound to a single
-non-blocking test of each stage, so that the waits give up before the copies
-land: the call must return ZTM_ERR_TIMEOUT, and the next call on the same
-context, with the default bound, must run normally.  Nothing here faults,
-traps or hangs the GPU: the copies land as usual and are waited for."""
+The test hook ztm_ctx_test_timeout points each stage wait at a barrier that
+nothing completes, with a bound of a few tests, so that the waits run out:
+the call must return ZTM_ERR_TIMEOUT, and the next call on the same context,
+without the hook, must run normally.  Nothing here faults, traps or hangs
+the GPU: the density copies land as usual and each block waits for its own
+before it stops."""
 import numpy as np
 import pytest
 
@@ -22,13 +23,13 @@ def test_timeout_is_reported_and_the_context_recovers(ctx):
     mesh, rho = small_mesh(96, 80, 24, seed=4)
     st = awkward_stations(mesh, n_random=300)
     ref = oracle.prism_mesh(mesh, rho, st)
-    ctx.set_wait_limit(1)
+    ctx.test_timeout(4)
     try:
         with pytest.raises(ztm_gb300.GravityError) as e:
             ctx.prism(mesh, rho, st, precision="mixed")
         assert e.value.code == ztm_gb300.ERR_TIMEOUT
     finally:
-        ctx.set_wait_limit(0)
+        ctx.test_timeout(0)
     out = ctx.prism(mesh, rho, st, precision="mixed")
     assert rel_err(out, ref) <= 1e-6
     # the error word was cleared: a device-pointer call reports nothing stale

@@ -33,7 +33,7 @@ EXPORTS = (
     "ztm_invert_interface", "ztm_gfm_pointmass_noalloc", "ztm_density_build",
     "ztm_gfm_pointmass_model", "ztm_gfm_interface_jvp", "ztm_gfm_pointmass_adjoint",
     "ztm_gfm_pointmass_misfit", "ztm_gfm_pointmass_model_misfit", "ztm_ctx_count_forms",
-    "ztm_ctx_form_counts", "ztm_ctx_set_wait_limit",
+    "ztm_ctx_form_counts", "ztm_ctx_test_timeout",
 )
 
 
@@ -114,7 +114,7 @@ _SIGS = {
                                             _P, _I, _I]),
     "ztm_ctx_count_forms": (_I, [_P, _I]),
     "ztm_ctx_form_counts": (_I, [_P, ctypes.POINTER(_LL)]),
-    "ztm_ctx_set_wait_limit": (_I, [_P, ctypes.c_uint]),
+    "ztm_ctx_test_timeout": (_I, [_P, ctypes.c_uint]),
     "ztm_ctx_profile": (_I, [_P, _I]),
     "ztm_ctx_profile_read": (_I, [_P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double),
                                   ctypes.POINTER(_LL)]),

@@ -7,7 +7,8 @@
 // parameter by a full forward run (TFM.cpp:124-135); this is what replaces
 // those gravity columns.
 //
-//   FP64 plain  thread per prism, stations streamed through shared memory,
+//   FP64 plain  thread per mesh vertex (the station-weighted corner function
+//               Psi(v), vertex sharing), stations streamed through shared memory,
 //               8-corner closed form in double; station chunks reduced in a
 //               fixed order.
 //   MIXED/FP32  far pairs: thread per (column, group of 32 layers) and
@@ -294,24 +295,26 @@ __global__ void __launch_bounds__(ADJ_TS, 5) adj_kernel(AdjArgs a) {
 }
 
 // ---- plain double ---------------------------------------------------------
+// By vertices, as the plain forward: Psi(v) = sum_s resid_s Phi(v - station_s)
+// once per mesh vertex (thread per vertex, stations streamed through shared
+// memory, per-chunk partials), then g[p] = G * sum over the eight corners of
+// p of s_x s_y s_z Psi(corner), s = +1 at the upper and -1 at the lower limit
+// of each axis -- the corner form of the prism integral with the station sum
+// taken first.  (nx+1)(ny+1)(nz+1) Phi per station instead of 8 nx ny nz.
 __global__ void __launch_bounds__(ADJ_TS)
     adj_f64_kernel(MeshDesc m, int ns, const double* __restrict__ sxyz,
                    const double* __restrict__ res, int chunk_len, double* __restrict__ partial) {
   __shared__ double s_st[4 * 128];
-  const long long np = (long long)m.nx * m.ny * m.nz;
-  const long long p = blockIdx.x * (long long)ADJ_TS + threadIdx.x;
-  const bool active = p < np;
-  const long long plane = (long long)m.nx * m.ny;
-  int ix = 0, iy = 0, l = 0;
+  const long long nvx = m.nx + 1, nvy = m.ny + 1, nv = nvx * nvy * (m.nz + 1);
+  const long long v = blockIdx.x * (long long)ADJ_TS + threadIdx.x;
+  const bool active = v < nv;
+  double xv = 0.0, yv = 0.0, zv = 0.0;
   if (active) {
-    l = (int)(p / plane);
-    long long rem = p - (long long)l * plane;
-    iy = (int)(rem / m.nx);
-    ix = (int)(rem % m.nx);
+    const int a = (int)(v % nvx), b = (int)((v / nvx) % nvy), c = (int)(v / (nvx * nvy));
+    xv = m.x0 + a * m.dx;  // the corner coordinates the corner form uses
+    yv = m.y0 + b * m.dy;
+    zv = m.zt - c * m.dz;
   }
-  const double xa = m.x0 + ix * m.dx, xb = m.x0 + (ix + 1) * m.dx;
-  const double ya = m.y0 + iy * m.dy, yb = m.y0 + (iy + 1) * m.dy;
-  const double za = m.zt - (l + 1) * m.dz, zb = m.zt - l * m.dz;
   const int s0 = blockIdx.y * chunk_len, s1 = min(ns, s0 + chunk_len);
   double acc = 0.0;
   for (int t0 = s0; t0 < s1; t0 += 128) {
@@ -330,24 +333,41 @@ __global__ void __launch_bounds__(ADJ_TS)
     for (int q = 0; q < cnt; q++) {
       const double r = s_st[4 * q + 3];
       if (r == 0.0) continue;
-      const double xs = s_st[4 * q], ys = s_st[4 * q + 1], zs = s_st[4 * q + 2];
-      acc += r * ztm_prism_unit<double>(xa - xs, xb - xs, ya - ys, yb - ys, za - zs, zb - zs);
+      acc += r * ztm_phi<double>(xv - s_st[4 * q], yv - s_st[4 * q + 1], zv - s_st[4 * q + 2]);
     }
   }
-  if (active) partial[(size_t)blockIdx.y * np + p] = acc;
+  if (active) partial[(size_t)blockIdx.y * nv + v] = acc;
 }
 
-__global__ void adj_f64_finalize(long long np, int nchunks, const double* __restrict__ partial,
+__global__ void adj_f64_finalize(MeshDesc m, int nchunks, const double* __restrict__ partial,
                                  double G5, double* __restrict__ g) {
-  long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long np = (long long)m.nx * m.ny * m.nz;
+  const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (p >= np) return;
+  const long long nvx = m.nx + 1, nvy = m.ny + 1, nv = nvx * nvy * (m.nz + 1);
+  const long long plane = (long long)m.nx * m.ny;
+  const int l = (int)(p / plane);
+  const long long rem = p - (long long)l * plane;
+  const int iy = (int)(rem / m.nx), ix = (int)(rem % m.nx);
   double a = 0.0;
-  for (int c = 0; c < nchunks; c++) a += partial[(size_t)c * np + p];
+#pragma unroll
+  for (int dc = 0; dc < 2; dc++)      // c = l: top (+), c = l + 1: bottom (-)
+#pragma unroll
+    for (int db = 0; db < 2; db++)    // b = iy: lower (-), b = iy + 1: upper (+)
+#pragma unroll
+      for (int da = 0; da < 2; da++) {
+        const long long v = (ix + da) + nvx * ((iy + db) + nvy * (long long)(l + dc));
+        double psi = 0.0;
+        for (int c = 0; c < nchunks; c++) psi += partial[(size_t)c * nv + v];
+        const bool neg = (da == 0) ^ (db == 0) ^ (dc == 1);
+        a += neg ? -psi : psi;
+      }
   g[p] = G5 * a;
 }
 
-int adj_f64_chunks(long long np, int ns, int num_sms, int* len) {
-  long long blocks = (np + ADJ_TS - 1) / ADJ_TS;
+// Station chunks of the plain double adjoint over nv vertices.
+int adj_f64_chunks(long long nv, int ns, int num_sms, int* len) {
+  long long blocks = (nv + ADJ_TS - 1) / ADJ_TS;
   long long want = std::max(1LL, (8LL * std::max(num_sms, 1)) / std::max(blocks, 1LL));
   long long ch = std::min<long long>(std::min(want, (long long)std::max(1, ns / 32)), 65535);
   ch = std::max(1LL, ch);
@@ -381,9 +401,10 @@ int adj_grid_max(int num_sms) { return std::max(adj_grid(num_sms, true), adj_gri
 size_t ztm_adjoint_ws(const MeshDesc& m, int ns, int precision, int num_sms, double near_q) {
   long long np = (long long)m.nx * m.ny * m.nz;
   if (precision == ZTM_PREC_FP64) {
+    const long long nv = (long long)(m.nx + 1) * (m.ny + 1) * (m.nz + 1);
     int len;
-    int ch = adj_f64_chunks(np, std::max(ns, 1), num_sms, &len);
-    return WsCarver::need((size_t)ch * np * 8);
+    int ch = adj_f64_chunks(nv, std::max(ns, 1), num_sms, &len);
+    return WsCarver::need((size_t)ch * nv * 8);
   }
   const MeshConst k = make_mesh_const(m, near_q > 0 ? near_q : 6.0);
   return 2 * WsCarver::need((size_t)std::max(ns, 1) * 16) +
@@ -402,15 +423,17 @@ int ztm_launch_adjoint(ztm_ctx* c, const MeshDesc& m, int ns, const double* d_sx
     return ztm_after_launch(c, "adjoint (no stations)");
   }
   if (precision == ZTM_PREC_FP64) {
+    const long long nv = (long long)(m.nx + 1) * (m.ny + 1) * (m.nz + 1);
+    if (nv > (1LL << 31) - 1) return ztm_fail(c, ZTM_ERR_RANGE, "mesh has more than 2^31-1 vertices");
     int len;
-    int ch = adj_f64_chunks(np, ns, c->num_sms, &len);
-    double* partial = wc.take<double>((size_t)ch * np);
-    dim3 grid((unsigned)((np + ADJ_TS - 1) / ADJ_TS), ch);
+    int ch = adj_f64_chunks(nv, ns, c->num_sms, &len);
+    double* partial = wc.take<double>((size_t)ch * nv);
+    dim3 grid((unsigned)((nv + ADJ_TS - 1) / ADJ_TS), ch);
     {
       ZtmProf prof_(c, "adjoint_f64");
       adj_f64_kernel<<<grid, ADJ_TS, 0, c->stream>>>(m, ns, d_sxyz, d_res, len, partial);
     }
-    adj_f64_finalize<<<(unsigned)((np + 255) / 256), 256, 0, c->stream>>>(np, ch, partial, G5, d_g);
+    adj_f64_finalize<<<(unsigned)((np + 255) / 256), 256, 0, c->stream>>>(m, ch, partial, G5, d_g);
     c->launches += 2;
     return ztm_after_launch(c, "adjoint FP64 kernels");
   }

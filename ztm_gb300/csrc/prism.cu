@@ -9,9 +9,11 @@
 // below reproduces.
 //
 // Three methods:
-//   FP64 plain  every pair with the 8-corner closed form in double.  One
-//               thread per station, prisms streamed through shared memory,
-//               per-chunk partials reduced in a fixed order.
+//   FP64 plain  every pair with the 8-corner closed form in double, the
+//               corner function taken once per mesh vertex and station
+//               (vertex sharing).  One thread per station, vertices streamed
+//               through shared memory, per-chunk partials reduced in a fixed
+//               order.
 //   MIXED       pairs outside a station's near region (every prism whose
 //               centre is >= near_q half-diagonals away) use the 4th-order
 //               far-field expansion in float (second order beyond 48
@@ -232,8 +234,8 @@ struct FarArgs {
   const float* rhoT;
   double* partial;  // [chunk][ns]
   int* err;
-  unsigned poll_limit;        // test hook, 0 = off: thread 0 polls each stage at most
-                              // this many times and the block follows its verdict
+  unsigned poll_limit;        // test hook, 0 = off: each stage wait polls a barrier
+                              // that nothing completes this many times and gives up
   unsigned long long* forms;  // counting variant: the four form counters
 };
 
@@ -566,6 +568,7 @@ __global__ void __launch_bounds__(FAR_TS, 6) far_kernel(FarArgs a) {
     s_to[0] = s_to[1] = 0;
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
+    mbar_init(&bar[2], 1);  // the timeout hook's barrier: nothing ever arrives on it
     fence_mbar_init();
     const int first = atomicAdd(a.counter, 1);
     s_item[0] = first;
@@ -644,9 +647,11 @@ __global__ void __launch_bounds__(FAR_TS, 6) far_kernel(FarArgs a) {
       // be read by a thread still finishing this one)
       bool landed;
       if (a.poll_limit) {
-        // test hook of the timeout path: one verdict for the whole block, so
-        // that no warp splits around the stage's votes
-        if (threadIdx.x == 0) s_poll[seq & 1] = mbar_poll(&bar[seq & 1], (seq >> 1) & 1, a.poll_limit);
+        // test hook of the timeout path: thread 0 waits, with a short bound,
+        // on a barrier that no copy completes, so the wait runs out; one
+        // verdict for the whole block, so that no warp splits around the
+        // stage's votes.  The copies in flight are waited for below.
+        if (threadIdx.x == 0) s_poll[seq & 1] = mbar_poll(&bar[2], 0, a.poll_limit);
         __syncthreads();
         landed = s_poll[seq & 1] && mbar_wait(&bar[seq & 1], (seq >> 1) & 1);
       } else {
@@ -710,12 +715,53 @@ __global__ void finalize_kernel(int ns, int nchunks, const double* __restrict__ 
 }
 
 // ---------------------------------------------------------------------------
-// plain double, every pair with the closed form
+// plain double, every pair with the closed form, by vertices.
+//
+// sum_p rho_p * sum_{corners of p} s_x s_y s_z Phi(corner - station) takes
+// each mesh vertex's Phi once per station: gz = sum_v D(v) Phi(v - station),
+// with D(v) the sum over the (up to) eight prisms around v of rho_p times
+// s_x s_y s_z, s = +1 where v is the prism's upper limit along that axis and
+// -1 where it is the lower.  (nx+1)(ny+1)(nz+1) Phi per station instead of
+// 8 nx ny nz; each Phi is evaluated at the same double coordinates as the
+// corner form evaluates it.  D is formed once per call (vertex_weight_kernel).
+__global__ void vertex_weight_kernel(MeshDesc m, const double* __restrict__ rho,
+                                     double* __restrict__ D) {
+  const long long nvx = m.nx + 1, nvy = m.ny + 1, nv = nvx * nvy * (m.nz + 1);
+  const long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  const int a = (int)(v % nvx), b = (int)((v / nvx) % nvy), c = (int)(v / (nvx * nvy));
+  const long long plane = (long long)m.nx * m.ny;
+  double d = 0.0;
+#pragma unroll
+  for (int dc = 0; dc < 2; dc++) {
+    const int l = c - 1 + dc;  // l = c - 1: v is its bottom (-); l = c: its top (+)
+    if (l < 0 || l >= m.nz) continue;
+#pragma unroll
+    for (int db = 0; db < 2; db++) {
+      const int iy = b - 1 + db;  // iy = b - 1: v is its upper y limit (+)
+      if (iy < 0 || iy >= m.ny) continue;
+#pragma unroll
+      for (int da = 0; da < 2; da++) {
+        const int ix = a - 1 + da;
+        if (ix < 0 || ix >= m.nx) continue;
+        const double r = rho[ix + (long long)m.nx * iy + plane * l];
+        const bool neg = (da == 1) ^ (db == 1) ^ (dc == 0);
+        d += neg ? -r : r;
+      }
+    }
+  }
+  D[v] = d;
+}
+
+struct __align__(16) Vtx {
+  double x, y, z, d;
+};
+
 __global__ void __launch_bounds__(F64_TS)
     mesh_f64_kernel(MeshDesc m, int ns, const double* __restrict__ sxyz,
-                    const double* __restrict__ rho, long long chunk_len,
+                    const double* __restrict__ D, long long chunk_len,
                     double* __restrict__ partial) {
-  __shared__ double tile[256];
+  __shared__ Vtx tile[256];
   const int s = blockIdx.x * F64_TS + threadIdx.x;
   const bool active = s < ns;
   double xs = 0, ys = 0, zs = 0;
@@ -724,28 +770,32 @@ __global__ void __launch_bounds__(F64_TS)
     ys = sxyz[3 * s + 1];
     zs = sxyz[3 * s + 2];
   }
-  const long long np = (long long)m.nx * m.ny * m.nz;
-  const long long p0 = (long long)blockIdx.y * chunk_len;
-  const long long p1 = min(np, p0 + chunk_len);
-  const long long plane = (long long)m.nx * m.ny;
+  const long long nvx = m.nx + 1, nvy = m.ny + 1, nv = nvx * nvy * (m.nz + 1);
+  const long long v0 = (long long)blockIdx.y * chunk_len;
+  const long long v1 = min(nv, v0 + chunk_len);
   double acc = 0.0;
-  for (long long t0 = p0; t0 < p1; t0 += 256) {
+  for (long long t0 = v0; t0 < v1; t0 += 256) {
     __syncthreads();
-    for (int q = threadIdx.x; q < 256; q += F64_TS) tile[q] = (t0 + q < p1) ? rho[t0 + q] : 0.0;
+    for (int q = threadIdx.x; q < 256; q += F64_TS) {
+      const long long v = t0 + q;
+      Vtx w = {0.0, 0.0, 0.0, 0.0};
+      if (v < v1) {
+        const int a = (int)(v % nvx), b = (int)((v / nvx) % nvy), c = (int)(v / (nvx * nvy));
+        // corner minus station as the corner form writes it: (x0 + a dx) - xs
+        w.x = m.x0 + a * m.dx;
+        w.y = m.y0 + b * m.dy;
+        w.z = m.zt - c * m.dz;
+        w.d = D[v];
+      }
+      tile[q] = w;
+    }
     __syncthreads();
-    const int cnt = (int)min(256LL, p1 - t0);
+    const int cnt = (int)min(256LL, v1 - t0);
     if (!active) continue;
     for (int q = 0; q < cnt; q++) {
-      const double r = tile[q];
-      if (r == 0.0) continue;  // uniform: all lanes read prism q
-      const long long p = t0 + q;
-      const int l = (int)(p / plane);
-      const long long rem = p - (long long)l * plane;
-      const int iy = (int)(rem / m.nx), ix = (int)(rem % m.nx);
-      const double xa = (m.x0 + ix * m.dx) - xs, xb = (m.x0 + (ix + 1) * m.dx) - xs;
-      const double ya = (m.y0 + iy * m.dy) - ys, yb = (m.y0 + (iy + 1) * m.dy) - ys;
-      const double za = (m.zt - (l + 1) * m.dz) - zs, zb = (m.zt - l * m.dz) - zs;
-      acc += r * ztm_prism_unit<double>(xa, xb, ya, yb, za, zb);
+      const Vtx w = tile[q];
+      if (w.d == 0.0) continue;  // uniform: all lanes read vertex q
+      acc += w.d * ztm_phi<double>(w.x - xs, w.y - ys, w.z - zs);
     }
   }
   if (active) partial[(size_t)blockIdx.y * ns + s] = acc;
@@ -953,10 +1003,11 @@ void launch_mesh_near_iv(ztm_ctx* c, const MeshConst& k, const MeshDesc& m, int 
 
 size_t ztm_prism_ws(const MeshDesc& m, int ns, int precision, int num_sms, const ztm_opts* o) {
   if (precision == ZTM_PREC_FP64) {
-    long long np = (long long)m.nx * m.ny * m.nz, len;
+    const long long nv = (long long)(m.nx + 1) * (m.ny + 1) * (m.nz + 1);
+    long long len;
     int tiles = std::max(1, (ns + F64_TS - 1) / F64_TS);
-    long long ch = f64_chunks(np, tiles, num_sms, &len);
-    return WsCarver::need((size_t)ch * ns * 8);
+    long long ch = f64_chunks(nv, tiles, num_sms, &len);
+    return WsCarver::need((size_t)ch * ns * 8) + WsCarver::need((size_t)nv * 8);
   }
   double nq = (o && o->near_q > 0) ? o->near_q : 6.0;
   MeshConst k = make_mesh_const(m, nq);
@@ -975,18 +1026,22 @@ int ztm_launch_prism(ztm_ctx* c, const MeshDesc& m, const double* d_rho, int ns,
                      const ztm_opts* o, WsCarver& wc) {
   const double G5 = G * 1.0e5;
   if (precision == ZTM_PREC_FP64) {
-    long long np = (long long)m.nx * m.ny * m.nz, len;
+    const long long nv = (long long)(m.nx + 1) * (m.ny + 1) * (m.nz + 1);
+    if (nv > (1LL << 31) - 1) return ztm_fail(c, ZTM_ERR_RANGE, "mesh has more than 2^31-1 vertices");
+    long long len;
     int tiles = std::max(1, (ns + F64_TS - 1) / F64_TS);
-    long long ch = f64_chunks(np, tiles, c->num_sms, &len);
+    long long ch = f64_chunks(nv, tiles, c->num_sms, &len);
     double* partial = wc.take<double>((size_t)ch * ns);
+    double* D = wc.take<double>((size_t)nv);
+    vertex_weight_kernel<<<(unsigned)((nv + 255) / 256), 256, 0, c->stream>>>(m, d_rho, D);
     {
       ZtmProf prof_(c, "prism_f64");
-      mesh_f64_kernel<<<dim3(tiles, (unsigned)ch), F64_TS, 0, c->stream>>>(m, ns, d_sxyz, d_rho, len,
+      mesh_f64_kernel<<<dim3(tiles, (unsigned)ch), F64_TS, 0, c->stream>>>(m, ns, d_sxyz, D, len,
                                                                            partial);
     }
     finalize_kernel<<<(ns + 255) / 256, 256, 0, c->stream>>>(ns, (int)ch, partial, 1.0, nullptr,
                                                              G5, d_gz);
-    c->launches += 2;
+    c->launches += 3;
     return ztm_after_launch(c, "prism FP64 kernels");
   }
   const double nq = (o && o->near_q > 0) ? o->near_q : 6.0;

@@ -301,9 +301,9 @@ void* ztm_ctx_stream(ztm_ctx* c) { return c ? (void*)c->stream : nullptr; }
 
 long long ztm_ctx_launches(const ztm_ctx* c) { return c ? c->launches : -1; }
 
-int ztm_ctx_set_wait_limit(ztm_ctx* c, unsigned int iterations) {
+int ztm_ctx_test_timeout(ztm_ctx* c, unsigned int polls) {
   if (!c) return ZTM_ERR_ARG;
-  c->stage_wait_limit = iterations;
+  c->stage_wait_limit = polls;
   return ZTM_OK;
 }
 

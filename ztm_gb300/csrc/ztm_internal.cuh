@@ -49,8 +49,8 @@ struct ztm_ctx {
   std::vector<char> batch_table;
   // launch shapes chosen by the autotuner, keyed by workload shape
   std::map<std::vector<long long>, std::vector<int>> tuned;
-  // spin limit of the far kernel's copy-arrival waits (0: ZTM_WAIT_LIMIT);
-  // a test hook for the timeout path, ztm_ctx_set_wait_limit
+  // timeout-path test hook (ztm_ctx_test_timeout): polls of the far
+  // kernel's redirected stage wait, 0 = off
   unsigned stage_wait_limit = 0;
   // evaluation-form counters of the mixed forward (ztm_ctx_count_forms)
   bool count_forms = false;

@@ -224,9 +224,10 @@ class GravityContext:
         self._check(self._lib.ztm_ctx_form_counts(self._h, out))
         return tuple(int(v) for v in out)
 
-    def set_wait_limit(self, iterations):
-        """Test hook: spin limit of the far kernel's copy waits (0: default)."""
-        self._check(self._lib.ztm_ctx_set_wait_limit(self._h, int(iterations)))
+    def test_timeout(self, polls):
+        """Test hook of the timeout path: polls > 0 makes the far kernel's
+        stage waits run out (on a barrier nothing completes); 0: off."""
+        self._check(self._lib.ztm_ctx_test_timeout(self._h, int(polls)))
 
     def measure_peak(self, kind):
         """kind 'fp32' / 'fp64' (TFLOP/s of FMA) or 'rsqrt' (Gop/s)."""
