@@ -486,6 +486,57 @@ def other_workloads(ctx):
     return res
 
 
+def inversion_study(ctx, fp64_iterations=3):
+    """The interface inversion workload (512x512 columns of 0.5 km, 256x256
+    stations, lambda = 1e-2) against double precision: data from the plain
+    double forward of the true Moho plus 0.05 mGal noise; the mixed L-BFGS
+    run of 20 iterations; its final model's misfit re-evaluated with the
+    double forward; and the first iterations of the same inversion run in
+    plain double beside it (each double evaluation is a full forward and
+    adjoint over 1.7e10 pairs).  Prints one JSON line."""
+    import numpy as np
+    from ztm_gb300 import synth
+    im, dep, rho, st, start = synth.moho_columns_512()
+    t0 = time.perf_counter()
+    data = ctx.interface(im, dep, rho, st, precision="fp64")
+    t_data = time.perf_counter() - t0
+    data = data + np.random.default_rng(5).normal(0, 0.05, len(st))
+    t0 = time.perf_counter()
+    dm, hm, nm = ctx.invert_interface(im, start, rho, st, data, lam=1e-2, iterations=20,
+                                      precision="mixed")
+    t_mixed = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    mis64_final = 0.5 * float(np.sum((ctx.interface(im, dm, rho, st, precision="fp64") - data) ** 2))
+    t_check = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    dd, hd, nd = ctx.invert_interface(im, start, rho, st, data, lam=1e-2,
+                                      iterations=fp64_iterations, precision="fp64")
+    t_fp64 = time.perf_counter() - t0
+    k = min(len(hd), len(hm))
+    noise_floor = 0.5 * len(st) * 0.05 ** 2
+    line = {"workload": "inversion", "what": __doc_line__(inversion_study),
+            "columns": im.nx * im.ny, "stations": len(st), "lambda": 1e-2,
+            "data": "plain double forward of the true model + N(0, 0.05 mGal)",
+            "mixed": {"iterations": nm, "seconds": t_mixed, "misfit": [float(x) for x in hm],
+                      "mean_abs_depth_error_m": float(np.abs(dm - dep).mean())},
+            "final_model_misfit_fp64": mis64_final,
+            "final_model_misfit_mixed": float(hm[-1]),
+            "final_misfit_rel_diff": abs(mis64_final - float(hm[-1])) / mis64_final,
+            "fp64": {"iterations": nd, "seconds": t_fp64, "misfit": [float(x) for x in hd],
+                     "mean_abs_depth_error_m": float(np.abs(dd - dep).mean())},
+            "trajectory_max_rel_diff_first_%d" % k:
+                float(np.max(np.abs(np.asarray(hm[:k]) - np.asarray(hd[:k])) / np.asarray(hd[:k]))),
+            "noise_floor_misfit": noise_floor,
+            "start_mean_abs_depth_error_m": float(np.abs(start - dep).mean()),
+            "seconds_fp64_forward": t_data, "seconds_fp64_check": t_check}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def __doc_line__(f):
+    return " ".join(f.__doc__.split())
+
+
 def run_workload(args, local_rank):
     """The other workloads as the timed step (side measurements and ncu
     targets; the default forward workload is the headline)."""
@@ -539,6 +590,8 @@ def run_workload(args, local_rank):
         what = ("transposed point-mass sum (%s) on the 256x256x64 draped-mesh geometry, its grid: "
                 "selected nodes x stations" % prec)
         step = lambda: ctx.pointmass_adjoint(g, dsf, dw, drho=dd, precision=prec)
+    elif args.workload == "inversion":
+        return inversion_study(ctx)
     else:
         raise SystemExit("unknown workload " + args.workload)
     for _ in range(args.warmup):
@@ -567,7 +620,7 @@ def main():
     ap.add_argument("--quick", action="store_true", help="skip side measurements")
     ap.add_argument("--workload", default="forward",
                     choices=["forward", "adjoint", "interface", "batch", "pointmass",
-                             "pointmass_adjoint", "pointmass_adjoint64"],
+                             "pointmass_adjoint", "pointmass_adjoint64", "inversion"],
                     help="forward (the headline) or another workload as the timed step")
     args = ap.parse_args()
     rank, local_rank, world = dist_env()

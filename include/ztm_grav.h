@@ -355,6 +355,19 @@ int ztm_invert_interface(ztm_ctx* ctx, const ztm_imesh* mesh, double* depth,
                          const double* data, double lambda, int iterations,
                          const ztm_opts* opt, double* history, int* n_done);
 
+/* The same inversion by Gauss-Newton: each iteration solves
+ * (J^T J + lambda L) step = -gradient with at most cg_iterations conjugate-
+ * gradient steps, each one ztm_gfm_interface_jvp (J v) and one depth adjoint
+ * (J^T w), J never formed, then takes the projected step with a
+ * backtracking line search.  Same objective, units, bounds, history and
+ * n_done as ztm_invert_interface.  The reference's damped Gauss-Newton
+ * (TFM.cpp:155-167) forms J^T J from a finite-difference Jacobian. */
+int ztm_invert_interface_gn(ztm_ctx* ctx, const ztm_imesh* mesh, double* depth,
+                            const double* rho_col, int ns, const double* sxyz,
+                            const double* data, double lambda, int iterations,
+                            int cg_iterations, const ztm_opts* opt, double* history,
+                            int* n_done);
+
 /* ---- batched ----------------------------------------------------------- */
 /* Evaluates every job (trial models of a line search, independent regional
  * meshes of uneven size) in one persistent launch, replayed from a CUDA

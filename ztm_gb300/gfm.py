@@ -485,8 +485,9 @@ class GravityContext:
         return misfit, gz, g_rho, g_dep
 
     def invert_interface(self, imesh, depth0, rho_col, stations, data, lam=1e-2, iterations=20,
-                         precision="mixed", G=None, near_q=None):
-        """L-BFGS inversion of the column tops (host arrays).  Returns
+                         precision="mixed", G=None, near_q=None, method="lbfgs", cg_iterations=10):
+        """Inversion of the column tops (host arrays) by L-BFGS (method
+        "lbfgs") or Gauss-Newton with CG inner solves ("gn").  Returns
         (depth, data-misfit history, iterations taken)."""
         nc = imesh.nx * imesh.ny
         ns = _nstations(stations)
@@ -503,10 +504,18 @@ class GravityContext:
         hist = np.zeros(iterations + 1)
         done = ctypes.c_int(0)
         o = _opts(precision, 0, G, near_q)
-        self._check(self._lib.ztm_invert_interface(self._h, ctypes.byref(imesh), pd, pr, ns, px, pdat,
-                                                   float(lam), int(iterations), ctypes.byref(o),
-                                                   hist.ctypes.data_as(ctypes.c_void_p),
-                                                   ctypes.byref(done)))
+        ph = hist.ctypes.data_as(ctypes.c_void_p)
+        if method == "gn":
+            self._check(self._lib.ztm_invert_interface_gn(self._h, ctypes.byref(imesh), pd, pr, ns,
+                                                          px, pdat, float(lam), int(iterations),
+                                                          int(cg_iterations), ctypes.byref(o), ph,
+                                                          ctypes.byref(done)))
+        elif method == "lbfgs":
+            self._check(self._lib.ztm_invert_interface(self._h, ctypes.byref(imesh), pd, pr, ns, px,
+                                                       pdat, float(lam), int(iterations),
+                                                       ctypes.byref(o), ph, ctypes.byref(done)))
+        else:
+            raise ValueError("method must be 'lbfgs' or 'gn'")
         return depth, hist[:done.value + 1], done.value
 
     # -- batched ----------------------------------------------------------
