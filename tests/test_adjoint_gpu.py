@@ -41,7 +41,10 @@ def test_mesh_adjoint_dot_product(ctx):
     for p in ("fp64", "mixed"):
         lhs = np.dot(ctx.adjoint(mesh, st, r, precision=p), rho)
         rhs = np.dot(r, ctx.prism(mesh, rho, st, precision=p))
-        assert lhs == pytest.approx(rhs, rel=1e-6 if p == "mixed" else 1e-11)
+        # double: forward and adjoint sum the cancelling corner terms by
+        # vertices in different orders (1e-10, the double kernels' tolerance
+        # against the oracle)
+        assert lhs == pytest.approx(rhs, rel=1e-6 if p == "mixed" else 1e-10)
 
 
 def iface_case(n=24, seed=0, ns=60):
