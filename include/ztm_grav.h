@@ -368,6 +368,23 @@ int ztm_invert_interface_gn(ztm_ctx* ctx, const ztm_imesh* mesh, double* depth,
                             int cg_iterations, const ztm_opts* opt, double* history,
                             int* n_done);
 
+/* ---- damped Gauss-Newton step (normal equations) ------------------------ */
+/* The trial models of one LMA::fit iteration (TFM.cpp:159-160): JJ = J^T J
+ * (zmath.cpp:260-262 MTM), M = diag(diag(JJ)), A = diag(1/sig^2) and, for
+ * each of the nd damping pairs (d0, d1) in `damping` (nd x 2),
+ *   B[d] = b + inv(JJ + d0 M + d1 A) J^T r
+ * (the reference inverts by Gauss-Jordan with partial pivoting,
+ * zmath.cpp:129-140; here the same elimination runs on the right-hand side,
+ * which gives the same step up to rounding).  J is nrows x ncols, row-major
+ * (J[data][parameter], as Jac returns it), r the nrows residuals y - f, b and
+ * sig ncols values, B nd x ncols; JJ (ncols x ncols) is returned if non-NULL.
+ * A singular system leaves its B row equal to b, as the reference's inv
+ * returns a zero matrix there.  Double precision throughout.  Limits:
+ * ncols <= 32768 and nd*ncols*(ncols+1) < 2^31. */
+int ztm_lm_steps(ztm_ctx* ctx, const double* J, int nrows, int ncols, const double* r,
+                 const double* b, const double* sig, const double* damping, int nd,
+                 double* B, double* JJ, int flags);
+
 /* ---- batched ----------------------------------------------------------- */
 /* Evaluates every job (trial models of a line search, independent regional
  * meshes of uneven size) in one persistent launch, replayed from a CUDA

@@ -25,6 +25,7 @@ from . import build as _build
 _lib = None
 _runner = None
 _tfm = None
+_lm = None
 NTHREADS = max(1, os.cpu_count() or 1)
 
 
@@ -304,3 +305,46 @@ def ref_tfm_rows(grid, drho, surf, row_lo, row_hi, nn=None):
     t.ref_tfm_gfm_rows(grid.di, grid.dj, grid.dk, grid.fh, grid.fv, grid.bfr, _p(drho), drho.size,
                        _p(nn), nn.size, _p(surf), _p(G), int(row_lo), int(row_hi))
     return G, nn.size
+
+
+# ---- the reference's own LM step (zmath.cpp + TFM.cpp:159-160) -----------
+def ref_lm_available():
+    _build.build()
+    return os.path.exists(_build.LM_LIB)
+
+
+def ref_lm_steps(J, r, b, sig, damping):
+    """B (nd x ncols) and JJ from the reference's zmath.cpp (MTM, inv, T and
+    its operators, compiled unchanged) and the two statements of LMA::fit
+    (TFM.cpp:159-160)."""
+    global _lm
+    if _lm is None:
+        if not ref_lm_available():
+            raise RuntimeError("oracle/_ref/libref_lm.so is not built")
+        t = ctypes.CDLL(_build.LM_LIB)
+        P = ctypes.c_void_p
+        I = ctypes.c_int
+        t.ref_lm_steps.argtypes = [P, I, I, P, P, P, P, I, P, P]
+        t.ref_lm_steps.restype = None
+        _lm = t
+    J = _f64(J)
+    nrows, ncols = J.shape
+    r, b, sig = _f64(r), _f64(b), _f64(sig)
+    dm = _f64(damping).reshape(-1, 2)
+    B = np.zeros((dm.shape[0], ncols))
+    JJ = np.zeros((ncols, ncols))
+    _lm.ref_lm_steps(_p(J), nrows, ncols, _p(r), _p(b), _p(sig), _p(dm), dm.shape[0], _p(B), _p(JJ))
+    return B, JJ
+
+
+def lm_steps(J, r, b, sig, damping):
+    """TFM.cpp:159-160 restated in numpy (when the reference sources are
+    absent): JJ = J^T J, B[d] = b + inv(JJ + d0 diag(JJ) + d1 diag(1/sig^2)) J^T r."""
+    J = _f64(J)
+    JJ = J.T @ J
+    g = J.T @ _f64(r)
+    out = []
+    for d0, d1 in _f64(damping).reshape(-1, 2):
+        A = JJ + d0 * np.diag(np.diag(JJ)) + d1 * np.diag(1.0 / _f64(sig) ** 2)
+        out.append(_f64(b) + np.linalg.inv(A) @ g)
+    return np.array(out), JJ

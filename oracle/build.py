@@ -8,6 +8,10 @@
                                cut VERBATIM out of TFM.cpp into a small C
                                harness (generated, never committed)
   oracle/_ref/libref_tfm.so    that harness compiled with g++
+  oracle/_ref/zmath_lm.cpp     the reference's zmath.cpp VERBATIM, followed by a
+                               harness around the damped Gauss-Newton step of
+                               LMA::fit (TFM.cpp:159-160, cut verbatim)
+  oracle/_ref/libref_lm.so     that file compiled with g++
 
 The reference directory is ZTM_REFERENCE_DIR (default: the read-only copy
 this repository was built beside).  Where it is absent (the GPU host), the
@@ -26,9 +30,12 @@ RUNNER = os.path.join(BUILD, "libref_runner.so")
 CUBIN = os.path.join(REF, "gf_ref.cubin")
 TFM_SRC = os.path.join(REF, "tfm_gfm.cpp")
 TFM_LIB = os.path.join(REF, "libref_tfm.so")
+LM_SRC = os.path.join(REF, "zmath_lm.cpp")
+LM_LIB = os.path.join(REF, "libref_lm.so")
 REF_DIR = os.environ.get("ZTM_REFERENCE_DIR", "/root/reference")
 REF_GFM = os.path.join(REF_DIR, "GFM_GPU.cu")
 REF_TFM = os.path.join(REF_DIR, "TFM.cpp")
+REF_ZMATH = os.path.join(REF_DIR, "zmath.cpp")
 
 
 def _run(cmd):
@@ -133,6 +140,58 @@ def write_tfm_harness(tfm_path=REF_TFM, out=TFM_SRC):
     return out
 
 
+_LM_HARNESS = """
+// ---- harness (GENERATED by oracle/build.py; not part of zmath.cpp) --------
+// The damped Gauss-Newton step of LMA::fit, TFM.cpp:159-160 (the two
+// statements marked VERBATIM), for a given Jacobian J (nrows x ncols,
+// J[data][parameter]), residual r = y - f, parameters b, uncertainties sig
+// and nd damping pairs dm: B[n] = b + inv(JJ + d0 M + d1 A) J^T r.
+struct ZtmLmArgs {
+  vec sig;
+};
+extern "C" void ref_lm_steps(const double* Jp, int nrows, int ncols, const double* rp,
+                             const double* bp, const double* sigp, const double* dmp, int nd,
+                             double* Bout, double* JJout) {
+  mat J(nrows, vec(ncols)), JJ, M, A;
+  for (int i = 0; i < nrows; i++)
+    for (int j = 0; j < ncols; j++) J[i][j] = Jp[(long long)i * ncols + j];
+  vec r(rp, rp + nrows), b(bp, bp + ncols);
+  ZtmLmArgs S;
+  S.sig = vec(sigp, sigp + ncols);
+  mat B(nd);
+  // VERBATIM TFM.cpp:159 (from 'JJ=MTM(J)')
+  %(line159)s
+  // VERBATIM TFM.cpp:160
+  %(line160)s
+  for (int n = 0; n < nd; n++) F(n, vec{dmp[2 * n], dmp[2 * n + 1]});
+  for (int n = 0; n < nd; n++)
+    for (int j = 0; j < ncols; j++) Bout[(long long)n * ncols + j] = B[n][j];
+  if (JJout)
+    for (int i = 0; i < ncols; i++)
+      for (int j = 0; j < ncols; j++) JJout[(long long)i * ncols + j] = JJ[i][j];
+}
+"""
+
+
+def write_lm_harness(zmath_path=REF_ZMATH, tfm_path=REF_TFM, out=LM_SRC):
+    """zmath.cpp verbatim + the LMA step of TFM.cpp:159-160."""
+    zm = open(zmath_path, encoding="latin-1").read()
+    lines = open(tfm_path, encoding="latin-1").read().split("\n")
+    i = next(k for k, l in enumerate(lines) if "JJ=MTM(J); M=diag(diag(JJ)); A=diag(1/(S.sig^2));" in l)
+    m = re.search(r"JJ=MTM\(J\); M=diag\(diag\(JJ\)\); A=diag\(1/\(S\.sig\^2\)\);", lines[i])
+    m2 = re.search(r"auto F=\[&\]\(int n,vec d\)\{B\[n\]=b\+inv\(JJ\+d\[0\]\*M\+d\[1\]\*A\)\*T\(J\)\*r;\};",
+                   lines[i + 1])
+    if not m or not m2:
+        raise RuntimeError("TFM.cpp: LMA step lines not found")
+    src = ("// GENERATED by oracle/build.py: the reference's zmath.cpp, unchanged, then a\n"
+           "// harness.  Test and baseline infrastructure only; never committed.\n" + zm +
+           _LM_HARNESS % {"line159": m.group(0), "line160": m2.group(0)})
+    os.makedirs(os.path.dirname(out), exist_ok=True)
+    with open(out, "w", encoding="latin-1") as f:
+        f.write(src)
+    return out
+
+
 def build(force=False):
     os.makedirs(BUILD, exist_ok=True)
     src = os.path.join(HERE, "oracle.c")
@@ -160,6 +219,12 @@ def build(force=False):
         # switched off so that x86 and Arm hosts round alike
         _run(["g++", "-O3", "-std=c++14", "-ffp-contract=off", "-fPIC", "-shared", "-pthread",
               "-o", TFM_LIB, TFM_SRC])
+    if os.path.exists(REF_ZMATH) and os.path.exists(REF_TFM) and (
+            force or _stale(LM_SRC, [REF_ZMATH, REF_TFM, __file__])):
+        write_lm_harness()
+    if os.path.exists(LM_SRC) and (force or _stale(LM_LIB, [LM_SRC])):
+        _run(["g++", "-O3", "-std=c++14", "-ffp-contract=off", "-fPIC", "-shared", "-pthread",
+              "-w", "-o", LM_LIB, LM_SRC])
     return LIB
 
 

@@ -47,6 +47,8 @@ def test_null_and_bad_arguments_do_not_crash():
     assert lib.ztm_gfm_pointmass_model_misfit(None, None, None, None, None, None, None, None, 0.0,
                                               1.0, None, None, None, None, None, None, 0,
                                               0) == _lib.ERR_ARG
+    assert lib.ztm_lm_steps(None, None, 0, 0, None, None, None, None, 0, None, None,
+                            0) == _lib.ERR_ARG
     lib.ztm_ctx_destroy(None)
 
 

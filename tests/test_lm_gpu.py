@@ -1,0 +1,66 @@
+"""The damped Gauss-Newton step of the reference's optimiser on the GPU
+(ztm_lm_steps) against the reference's own code: zmath.cpp compiled
+unchanged (MTM, inv, T and its operators) with the two statements of
+LMA::fit (TFM.cpp:159-160), or their numpy restatement where the reference
+sources are absent.
+
+TOLERANCES: J^T J 1e-13 (normwise relative: the same sums in another order);
+the trial models 1e-9 (normwise relative over b's change: the reference
+inverts and multiplies, the library eliminates on the right-hand side, and
+the normal equations square the condition number)."""
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def reference(J, r, b, sig, dm):
+    if oracle.ref_lm_available():
+        return oracle.ref_lm_steps(J, r, b, sig, dm)
+    return oracle.lm_steps(J, r, b, sig, dm)
+
+
+def problem(nrows, ncols, seed):
+    rng = np.random.default_rng(seed)
+    J = rng.normal(size=(nrows, ncols)) * rng.uniform(0.1, 10.0, ncols)[None, :]
+    r = rng.normal(size=nrows)
+    b = rng.normal(size=ncols)
+    sig = rng.uniform(0.05, 2.0, ncols)
+    dm = np.array([[0.0, 0.0], [1e-3, 1e-4], [0.1, 1e-2], [1.0, 1.0]])
+    return J, r, b, sig, dm
+
+
+@pytest.mark.parametrize("nrows,ncols", [(400, 60), (2000, 300), (150, 130)])
+def test_lm_steps_match_reference(ctx, nrows, ncols):
+    J, r, b, sig, dm = problem(nrows, ncols, nrows + ncols)
+    Bref, JJref = reference(J, r, b, sig, dm)
+    B, JJ = ctx.lm_steps(J, r, b, sig, dm, return_jtj=True)
+    assert np.max(np.abs(JJ - JJref)) <= 1e-13 * np.max(np.abs(JJref))
+    for d in range(dm.shape[0]):
+        step_ref = Bref[d] - b
+        assert np.max(np.abs((B[d] - b) - step_ref)) <= 1e-9 * np.max(np.abs(step_ref)), d
+
+
+def test_lm_singular_system_keeps_b(ctx):
+    """A parameter the data do not constrain (zero column) and no damping:
+    the reference's inv returns zeros, so the trial is b itself."""
+    J, r, b, sig, _ = problem(300, 40, 7)
+    J[:, 5] = 0.0
+    dm = np.array([[0.0, 0.0], [0.0, 1e-2]])
+    Bref, _ = reference(J, r, b, sig, dm)
+    B = ctx.lm_steps(J, r, b, sig, dm)
+    assert np.array_equal(B[0], b) and np.array_equal(Bref[0], b)
+    step_ref = Bref[1] - b
+    assert np.max(np.abs((B[1] - b) - step_ref)) <= 1e-9 * np.max(np.abs(step_ref))
+
+
+def test_lm_device_pointers(ctx):
+    torch = pytest.importorskip("torch")
+    J, r, b, sig, dm = problem(500, 70, 3)
+    host = ctx.lm_steps(J, r, b, sig, dm)
+    d = lambda a: torch.tensor(np.ascontiguousarray(a), device="cuda")
+    dev = ctx.lm_steps(d(J), d(r), d(b), d(sig), d(dm))
+    ctx.sync()
+    assert np.array_equal(dev.cpu().numpy(), host)

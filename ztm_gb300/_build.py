@@ -18,7 +18,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
                      "-Xcompiler", "-ffp-contract=off"]
 
-SOURCES = ["ztm_capi.cu", "pointmass.cu", "prism.cu", "adjoint.cu", "iface.cu", "batch.cu", "trace.cu", "density.cu", "order.cu", "pm_adjoint.cu"]
+SOURCES = ["ztm_capi.cu", "pointmass.cu", "prism.cu", "adjoint.cu", "iface.cu", "batch.cu", "trace.cu", "density.cu", "order.cu", "pm_adjoint.cu", "lm.cu"]
 HOST_SOURCES = ["invert.cpp"]
 
 

@@ -518,6 +518,29 @@ class GravityContext:
             raise ValueError("method must be 'lbfgs' or 'gn'")
         return depth, hist[:done.value + 1], done.value
 
+    # -- damped Gauss-Newton step (TFM.cpp:159-160) -------------------------
+    def lm_steps(self, J, r, b, sig, damping, return_jtj=False):
+        """The trial models b + inv(J^T J + d0 diag(J^T J) + d1 diag(1/sig^2))
+        J^T r for each damping pair (d0, d1); J is (nrows, ncols).  Returns
+        B (nd, ncols) and, with return_jtj, J^T J."""
+        shape = tuple(J.shape)
+        if len(shape) != 2:
+            raise ValueError("J must be (nrows, ncols)")
+        nrows, ncols = int(shape[0]), int(shape[1])
+        nd = int(damping.shape[0]) if len(tuple(damping.shape)) == 2 else int(damping.shape[0]) // 2
+        a = _Args(self)
+        pJ = a.arr(J, nrows * ncols, name="J")
+        pr = a.arr(r, nrows, name="r")
+        pb = a.arr(b, ncols, name="b")
+        ps = a.arr(sig, ncols, name="sig")
+        pd = a.arr(damping, 2 * nd, name="damping")
+        B, pB = a.out(nd * ncols, J)
+        JJ, pJJ = a.out(ncols * ncols, J) if return_jtj else (None, None)
+        self._run(a, self._lib.ztm_lm_steps, self._h, pJ, nrows, ncols, pr, pb, ps, pd, nd, pB, pJJ,
+                  a.flags)
+        B = B.reshape(nd, ncols)
+        return (B, JJ.reshape(ncols, ncols)) if return_jtj else B
+
     # -- batched ----------------------------------------------------------
     def batch(self, jobs, precision="mixed", G=None, near_q=None, autotune=False):
         """jobs: list of (mesh, rho[nmodels, nprisms], stations[ns, 3]).
