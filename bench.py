@@ -309,7 +309,7 @@ def run_ours(args, rank, local_rank, world):
                                         "and bf16 tensor peaks, neither bounds this kernel)"},
             "kernels_ms": {"far_kernel": far_avg, "step": ms_per_step}}
     if not args.quick:
-        line.update(extras(ctx, mesh, rho, st, d_rho, d_st, gz))
+        line.update(extras(ctx, mesh, rho, st, d_rho, d_st, gz, ms_per_step))
         if world == 1:
             line["cpu_baseline"] = cpu_baseline_prism(mesh, rho, st)
             line["other_workloads"] = other_workloads(ctx)
@@ -361,7 +361,7 @@ def full_field_accuracy(rho, st, gz_mixed):
             float(np.percentile(rel, 99)), "reference": "double-precision CPU oracle, all stations"}
 
 
-def extras(ctx, mesh, rho, st, d_rho, d_st, gz_mixed):
+def extras(ctx, mesh, rho, st, d_rho, d_st, gz_mixed, fwd_ms):
     """Side measurements: the mixed field against the double field at every
     station, the plain FP64 kernel's rate, gradient evals/s of the adjoint,
     the reference's point-mass model on the same geometry (ours and the
@@ -390,6 +390,18 @@ def extras(ctx, mesh, rho, st, d_rho, d_st, gz_mixed):
     msa, _ = _median_ms(ctx, lambda: ctx.adjoint(mesh, d_st, res, precision="mixed"), 10)
     out["gradient"] = {"value": np_ * len(st) / (msa * 1e-3), "unit": "gradient evals/s",
                        "ms": msa, "what": "d misfit / d rho, all pairs, mixed, median of 10"}
+    rs = torch.tensor(np.random.default_rng(0).normal(0, 1, len(sub)), device="cuda")
+    msa64, _ = _median_ms(ctx, lambda: ctx.adjoint(mesh, ds, rs, precision="fp64"), 5)
+    out["fp64_plain_adjoint"] = {"value": np_ * len(sub) / (msa64 * 1e-3),
+                                 "unit": "gradient evals/s",
+                                 "sample": "%d stations x all prisms, median of 5" % len(sub)}
+    pairs = np_ * len(st)
+    t64 = pairs / out["fp64_plain"]["value"] + pairs / out["fp64_plain_adjoint"]["value"]
+    tmx = (fwd_ms + msa) * 1e-3
+    out["forward_plus_adjoint_vs_plain_fp64"] = {
+        "mixed_s": tmx, "fp64_s_at_measured_rates": t64, "speedup": t64 / tmx,
+        "what": "mixed forward (the timed step) + mixed adjoint against the plain double forward "
+                "+ adjoint of the same pairs at their measured rates (vertex-shared double kernels)"}
     # the reference's own point-mass model on the same geometry (its grid,
     # every node as a station): our float and double gathers and adjoints
     g, drho, surf = synth.pointmass_grid_of_mesh(mesh, rho, st)
@@ -471,7 +483,7 @@ def other_workloads(ctx):
         "rel_err_trial5_vs_single_call": err(outs[0][5], one)}
     # inversion workload: 512x512 columns, 256x256 stations, 20 L-BFGS iterations
     im5, dep5, rho5, st5, start5 = synth.moho_columns_512()
-    data5 = ctx.interface(im5, d(dep5), d(rho5), d(st5), precision="mixed")
+    data5 = ctx.interface(im5, d(dep5), d(rho5), d(st5), precision="fp64")
     ctx.sync()
     data5 = data5.cpu().numpy() + np.random.default_rng(5).normal(0, 0.05, len(st5))
     t0 = time.perf_counter()
@@ -479,10 +491,21 @@ def other_workloads(ctx):
                                               precision="mixed")
     dt = time.perf_counter() - t0
     res["inversion_512x512_20_iterations"] = {
-        "seconds": dt, "iterations": nit, "misfit_start": float(hist[0]),
+        "method": "L-BFGS", "seconds": dt, "iterations": nit, "misfit_start": float(hist[0]),
         "misfit_end": float(hist[-1]), "pairs_per_forward": im5.nx * im5.ny * len(st5),
         "mean_abs_depth_error_m": {"start": float(np.abs(start5 - dep5).mean()),
                                    "end": float(np.abs(dep_out - dep5).mean())}}
+    t0 = time.perf_counter()
+    dep_gn, hist_gn, nit_gn = ctx.invert_interface(im5, start5, rho5, st5, data5, lam=1e-2,
+                                                   iterations=20, precision="mixed", method="gn",
+                                                   cg_iterations=10)
+    dt = time.perf_counter() - t0
+    res["inversion_512x512_20_iterations_gauss_newton"] = {
+        "method": "Gauss-Newton, 10 CG steps (J v + J^T w) per iteration", "seconds": dt,
+        "iterations": nit_gn, "misfit": [float(x) for x in hist_gn],
+        "noise_floor_misfit": 0.5 * len(st5) * 0.05 ** 2,
+        "mean_abs_depth_error_m": {"start": float(np.abs(start5 - dep5).mean()),
+                                   "end": float(np.abs(dep_gn - dep5).mean())}}
     return res
 
 
