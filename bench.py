@@ -613,6 +613,44 @@ def run_workload(args, local_rank):
         what = ("transposed point-mass sum (%s) on the 256x256x64 draped-mesh geometry, its grid: "
                 "selected nodes x stations" % prec)
         step = lambda: ctx.pointmass_adjoint(g, dsf, dw, drho=dd, precision=prec)
+    elif args.workload == "prism_f64":
+        mesh, rho, st = synth.draped_mesh_256x256x64()
+        sub = st[np.arange(0, len(st), len(st) // 64)[:64]]
+        dr, ds = d(rho), d(sub)
+        units = mesh.nx * mesh.ny * mesh.nz * len(sub)
+        what = ("plain double prism forward (vertex-shared) of the 256x256x64 draped mesh at 64 of "
+                "its stations")
+        step = lambda: ctx.prism(mesh, dr, ds, precision="fp64")
+    elif args.workload in ("pointmass_small", "pointmass64_small", "pointmass_adjoint_small",
+                           "pointmass_adjoint64_small"):
+        # the 128x128 top-left columns and 32 top layers of the draped mesh on
+        # the reference grid: 128x128 stations x 5.4e5 nodes
+        mesh, rho, st = synth.draped_mesh_256x256x64()
+        r3 = rho.reshape(64, 256, 256)[:32, :128, :128]
+        m2 = ztm_gb300.make_mesh(128, 128, 32, mesh.dx, mesh.dy, mesh.dz)
+        st2 = st[(st[:, 0] < 128 * mesh.dx) & (st[:, 1] < 128 * mesh.dy)]
+        g, drho, surf = synth.pointmass_grid_of_mesh(m2, np.ascontiguousarray(r3).ravel(), st2)
+        dd, dsf = d(drho), d(surf)
+        prec = "fp64" if "64" in args.workload else "fp32"
+        units = int(np.count_nonzero(np.abs(drho) > 0.001)) * g.di * g.dj
+        if "adjoint" in args.workload:
+            dw = d(np.random.default_rng(0).normal(0, 1, g.di * g.dj))
+            what = "transposed point-mass sum (%s), 128x128x33-node grid, every node a station" % prec
+            step = lambda: ctx.pointmass_adjoint(g, dsf, dw, drho=dd, precision=prec)
+        else:
+            what = "point-mass forward (%s), 128x128x33-node grid, every node a station" % prec
+            step = lambda: ctx.pointmass(g, dd, dsf, precision=prec)
+    elif args.workload == "lm":
+        rng = np.random.default_rng(0)
+        nrows, ncols, nd = 12000, 2700, 4
+        J = rng.normal(size=(nrows, ncols)) * rng.uniform(0.1, 10.0, ncols)[None, :]
+        dJ, dr_, db = d(J), d(rng.normal(size=nrows)), d(rng.normal(size=ncols))
+        dsig = d(rng.uniform(0.05, 2.0, ncols))
+        dm = d(np.array([[0.0, 0.0], [1e-3, 1e-4], [0.1, 1e-2], [1.0, 1.0]]))
+        units = nrows * ncols * ncols + nd * ncols ** 3  # ~ J^T J and Gauss-Jordan multiply-adds
+        what = ("damped Gauss-Newton trials (TFM.cpp:159-160): J 12000 x 2700, 4 damping pairs "
+                "(J^T J + 4 Gauss-Jordan solves; units: multiply-adds of J^T J and the solves)")
+        step = lambda: ctx.lm_steps(dJ, dr_, db, dsig, dm)
     elif args.workload == "inversion":
         return inversion_study(ctx)
     else:
@@ -643,7 +681,9 @@ def main():
     ap.add_argument("--quick", action="store_true", help="skip side measurements")
     ap.add_argument("--workload", default="forward",
                     choices=["forward", "adjoint", "interface", "batch", "pointmass",
-                             "pointmass_adjoint", "pointmass_adjoint64", "inversion"],
+                             "pointmass_adjoint", "pointmass_adjoint64", "inversion",
+                             "prism_f64", "pointmass_small", "pointmass64_small",
+                             "pointmass_adjoint_small", "pointmass_adjoint64_small", "lm"],
                     help="forward (the headline) or another workload as the timed step")
     args = ap.parse_args()
     rank, local_rank, world = dist_env()

@@ -181,7 +181,7 @@ def central_difference(ctx, g, rc, sea, M, v, surf, GD, which, idx=None, g0=0.3,
             sels.append(selection(ctx, g, sea, Mx, vx, p["vm"], p["ro"], p["dr"], rc))
         if np.array_equal(sels[0], sels[1]):
             return (vals[0] - vals[1]) / (2 * h)
-    pytest.skip("no step keeps the node selection fixed")
+    return None  # every step moved a node across the selection threshold
 
 
 @pytest.mark.parametrize("di,dj,dk", [(21, 19, 13), (61, 61, 33)])
@@ -189,17 +189,31 @@ def test_model_gradient_vs_finite_differences(ctx, di, dj, dk):
     g, rc, sea, M, v, surf, GD = model_case(di, dj, dk, seed=di + 4)
     r = ctx.pointmass_model_misfit(g, sea, M, v, surf, GD, VM, RO, DR, rc, g0=0.3, gsig=0.7)
     gp = r["g_par"]
+    checked = 0
     for k, name in enumerate(("vm", "ro", "dr", "g0")):
         fd = central_difference(ctx, g, rc, sea, M, v, surf, GD, name)
+        if fd is None:
+            continue
         assert abs(gp[k] - fd) <= 1e-5 * abs(fd), (name, gp[k], fd)
+        checked += 1
     # Moho nodes where the gradient is largest (blend zones above selected
     # nodes), and velocity nodes
     for idx in np.argsort(-np.abs(r["g_M"]))[:4]:
         fd = central_difference(ctx, g, rc, sea, M, v, surf, GD, "M", int(idx))
+        if fd is None:
+            continue
         assert abs(r["g_M"][idx] - fd) <= 1e-5 * abs(fd), ("M", idx, r["g_M"][idx], fd)
+        checked += 1
     for idx in np.argsort(-np.abs(r["g_v"]))[:4]:
         fd = central_difference(ctx, g, rc, sea, M, v, surf, GD, "v", int(idx))
+        if fd is None:
+            continue
         assert abs(r["g_v"][idx] - fd) <= 1e-5 * abs(fd), ("v", idx, r["g_v"][idx], fd)
+        checked += 1
+    # a global parameter moves every node's density, so a step can cross the
+    # selection threshold of one of ~1e5 nodes; all but a few entries must be
+    # checkable
+    assert checked >= 9, checked
 
 
 def test_model_misfit_matches_oracle_chain(ctx):
