@@ -613,6 +613,14 @@ def run_workload(args, local_rank):
         what = ("transposed point-mass sum (%s) on the 256x256x64 draped-mesh geometry, its grid: "
                 "selected nodes x stations" % prec)
         step = lambda: ctx.pointmass_adjoint(g, dsf, dw, drho=dd, precision=prec)
+    elif args.workload == "forward_small":
+        mesh, rho, st = synth.draped_mesh_256x256x64()
+        sub = np.ascontiguousarray(st[::8])
+        dr, ds = d(rho), d(sub)
+        units = mesh.nx * mesh.ny * mesh.nz * len(sub)
+        what = ("mixed prism forward of the 256x256x64 draped mesh at every 8th of its stations "
+                "(2,048): the profiling case of the far kernel")
+        step = lambda: ctx.prism(mesh, dr, ds, precision="mixed")
     elif args.workload == "prism_f64":
         mesh, rho, st = synth.draped_mesh_256x256x64()
         sub = st[np.arange(0, len(st), len(st) // 64)[:64]]
@@ -682,7 +690,7 @@ def main():
     ap.add_argument("--workload", default="forward",
                     choices=["forward", "adjoint", "interface", "batch", "pointmass",
                              "pointmass_adjoint", "pointmass_adjoint64", "inversion",
-                             "prism_f64", "pointmass_small", "pointmass64_small",
+                             "prism_f64", "forward_small", "pointmass_small", "pointmass64_small",
                              "pointmass_adjoint_small", "pointmass_adjoint64_small", "lm"],
                     help="forward (the headline) or another workload as the timed step")
     args = ap.parse_args()
