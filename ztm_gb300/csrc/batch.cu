@@ -31,14 +31,14 @@
 namespace {
 
 constexpr int B_TS = 128;   // threads per block = stations per tile
-constexpr int B_MG = 16;    // models per far item
+constexpr int B_MG = 16;    // models per far item (the default variant's)
 constexpr int B_WARPS = B_TS / 32;
 
 struct BJob {
   MeshConst k;
   MeshDesc m;
   int nmodels, ns, tiles, chunks, chunk_cols, sc, mgroups, nv_cap;
-  int mgw;               // models interleaved per group: 1 or B_MG
+  int mgw;               // models interleaved per group: 1 or the variant's MG
   long long near_base, far_base;
   double far_scale, G5;
   const float4* sf;
@@ -283,7 +283,11 @@ __device__ void near_item(const BJob& J, int tile, double* phi_all, int phi_cap,
   }
 }
 
-__global__ void __launch_bounds__(B_TS, 4) batch_kernel(BArgs a) {
+// MG models per far item (the interleave width of a multi-model job), MINB
+// resident blocks per SM asked of the compiler: the kernel variants the
+// autotuner tries (BATCH_VARIANTS).
+template <int MG, int MINB>
+__global__ void __launch_bounds__(B_TS, MINB) batch_kernel(BArgs a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
   float* stage = reinterpret_cast<float*>(smem_raw + 128);
@@ -294,7 +298,7 @@ __global__ void __launch_bounds__(B_TS, 4) batch_kernel(BArgs a) {
   __shared__ int s_flag, s_lm;
   // compensated sums of each thread's models (16 KB): in registers they
   // would cost 32 per thread
-  __shared__ float s_ks[B_MG * B_TS], s_kc[B_MG * B_TS];
+  __shared__ float s_ks[MG * B_TS], s_kc[MG * B_TS];
   float* const ks = s_ks + threadIdx.x;
   float* const kc = s_kc + threadIdx.x;
   if (threadIdx.x == 0) {
@@ -363,7 +367,7 @@ __global__ void __launch_bounds__(B_TS, 4) batch_kernel(BArgs a) {
     const int Lm = min(s_lm, k.nz);
     const FarCoef fc = k.fc;
 #pragma unroll
-    for (int md = 0; md < B_MG; md++) ks[md * B_TS] = kc[md * B_TS] = 0.f;
+    for (int md = 0; md < MG; md++) ks[md * B_TS] = kc[md * B_TS] = 0.f;
     bool timed_out = false;
     for (int st = 0; st < nst; st++) {
       if (threadIdx.x == 0 && st + 1 < nst) issue(st + 1);
@@ -409,10 +413,10 @@ __global__ void __launch_bounds__(B_TS, 4) batch_kernel(BArgs a) {
             }
           } else {
             switch (form) {
-              case 0: far_column<B_MG, false, false>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc); break;
-              case 1: far_column<B_MG, true, false>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc); break;
-              case 2: far_column<B_MG, false, true>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc); break;
-              default: far_column<B_MG, true, true>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc);
+              case 0: far_column<MG, false, false>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc); break;
+              case 1: far_column<MG, true, false>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc); break;
+              case 2: far_column<MG, false, true>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc); break;
+              default: far_column<MG, true, true>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc);
             }
           }
           if (++ix == k.nx) {
@@ -429,7 +433,7 @@ __global__ void __launch_bounds__(B_TS, 4) batch_kernel(BArgs a) {
     }
     if (active) {
 #pragma unroll
-      for (int md = 0; md < B_MG; md++)
+      for (int md = 0; md < MG; md++)
         if (md < mcnt)
           J.partial[((size_t)(m0 + md) * J.chunks + chunk) * J.ns + s] =
               (double)ks[md * B_TS] - (double)kc[md * B_TS];
@@ -447,7 +451,8 @@ struct Plan {
 };
 
 // Shapes only (no pointers): per-job tiles, chunks, stage widths, workspace.
-Plan plan(const ztm_job* jobs, int njobs, double near_q, int num_sms, int stage_kb, int tlog2) {
+Plan plan(const ztm_job* jobs, int njobs, double near_q, int num_sms, int stage_kb, int tlog2,
+          int mg) {
   Plan p;
   size_t ws = 0;
   for (int j = 0; j < njobs; j++) {
@@ -462,7 +467,7 @@ Plan plan(const ztm_job* jobs, int njobs, double near_q, int num_sms, int stage_
     J.nmodels = q.nmodels;
     J.ns = q.ns;
     J.tiles = std::max(1, (q.ns + B_TS - 1) / B_TS);
-    J.mgw = q.nmodels > 1 ? B_MG : 1;
+    J.mgw = q.nmodels > 1 ? mg : 1;
     J.mgroups = (q.nmodels + J.mgw - 1) / J.mgw;
     int sc = std::max(1, (stage_kb * 1024) / (J.k.nzp * 4 * J.mgw));
     sc = std::min(sc, 32);
@@ -514,15 +519,29 @@ void destroy_entry(ZtmGraphEntry& e) {
   e.graph = nullptr;
 }
 
+// Kernel variants: {models per far item, blocks per SM asked of the
+// compiler}.  Variant 0 is the default.
+constexpr int BATCH_VARIANTS[][2] = {{16, 4}, {16, 5}, {8, 6}, {32, 3}};
+using BatchFn = void (*)(BArgs);
+BatchFn batch_fn(int v) {
+  switch (v) {
+    case 1: return batch_kernel<16, 5>;
+    case 2: return batch_kernel<8, 6>;
+    case 3: return batch_kernel<32, 3>;
+    default: return batch_kernel<16, 4>;
+  }
+}
+
 // Launch shapes the autotuner tries: {stage KB per model group, log2 of the
-// pairs per far item}.  The first is the default (32 trial models on the
-// 256x256x64 mesh plus 16 regional meshes: 2^23 pairs 223 ms, 2^24 225 ms,
-// 2^25 229 ms, 2^22 223 ms with twice the partial sums).
-constexpr int BATCH_SHAPES[][2] = {{16, 23}, {8, 24}, {32, 24}, {16, 24}, {16, 25},
-                                   {8, 23}, {32, 25}};
+// pairs per far item, kernel variant}.  The first is the default (32 trial
+// models on the 256x256x64 mesh plus 16 regional meshes: 2^23 pairs 223 ms,
+// 2^24 225 ms, 2^25 229 ms, 2^22 223 ms with twice the partial sums).
+constexpr int BATCH_SHAPES[][3] = {{16, 23, 0}, {8, 24, 0}, {32, 24, 0}, {16, 24, 0}, {16, 25, 0},
+                                   {8, 23, 0},  {32, 25, 0}, {16, 23, 1}, {8, 23, 2}, {16, 23, 2},
+                                   {32, 23, 3}, {16, 24, 3}};
 
 int batch_run(ztm_ctx* c, const ztm_job* jobs, int njobs, bool dev, double G, double nq,
-              int stage_kb, int tlog2);
+              int stage_kb, int tlog2, int variant);
 
 }  // namespace
 
@@ -565,10 +584,11 @@ extern "C" int ztm_gfm_batch(ztm_ctx* c, const ztm_job* jobs, int njobs, const z
     tkey.insert(tkey.end(), {jobs[j].mesh.nx, jobs[j].mesh.ny, jobs[j].mesh.nz,
                              jobs[j].nmodels, jobs[j].ns});
   auto it = c->tuned.find(tkey);
-  int stage_kb = BATCH_SHAPES[0][0], tlog2 = BATCH_SHAPES[0][1];
+  int stage_kb = BATCH_SHAPES[0][0], tlog2 = BATCH_SHAPES[0][1], variant = BATCH_SHAPES[0][2];
   if (it != c->tuned.end()) {
     stage_kb = it->second[0];
     tlog2 = it->second[1];
+    variant = it->second[2];
   } else if (tune) {
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
@@ -576,29 +596,34 @@ extern "C" int ztm_gfm_batch(ztm_ctx* c, const ztm_job* jobs, int njobs, const z
     float best = 1e30f;
     for (const auto& sh : BATCH_SHAPES) {
       cudaEventRecord(e0, c->stream);
-      const int rc = batch_run(c, jobs, njobs, dev, G, nq, sh[0], sh[1]);
+      const int rc = batch_run(c, jobs, njobs, dev, G, nq, sh[0], sh[1], sh[2]);
       cudaEventRecord(e1, c->stream);
       float ms = 0.f;
       if (rc == ZTM_OK && cudaEventSynchronize(e1) == cudaSuccess &&
-          cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess && ms < best) {
-        best = ms;
-        stage_kb = sh[0];
-        tlog2 = sh[1];
+          cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess) {
+        c->tune_log.push_back({sh[0], sh[1], sh[2], (int)(ms * 1000.f)});
+        if (ms < best) {
+          best = ms;
+          stage_kb = sh[0];
+          tlog2 = sh[1];
+          variant = sh[2];
+        }
       }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     c->err.clear();  // a candidate that did not fit is not the call's error
-    c->tuned[tkey] = {stage_kb, tlog2};
+    c->tuned[tkey] = {stage_kb, tlog2, variant};
   }
-  return batch_run(c, jobs, njobs, dev, G, nq, stage_kb, tlog2);
+  return batch_run(c, jobs, njobs, dev, G, nq, stage_kb, tlog2, variant);
 }
 
 namespace {
 
 int batch_run(ztm_ctx* c, const ztm_job* jobs, int njobs, bool dev, double G, double nq,
-              int stage_kb, int tlog2) {
-  Plan p = plan(jobs, njobs, nq, c->num_sms, stage_kb, tlog2);
+              int stage_kb, int tlog2, int variant) {
+  const BatchFn kfn = batch_fn(variant);
+  Plan p = plan(jobs, njobs, nq, c->num_sms, stage_kb, tlog2, BATCH_VARIANTS[variant][0]);
   if (p.smem > 200 * 1024) return ztm_fail(c, ZTM_ERR_RANGE, "near box too large for a batch");
   size_t stage_bytes = 0;
   if (!dev)
@@ -610,10 +635,10 @@ int batch_run(ztm_ctx* c, const ztm_job* jobs, int njobs, bool dev, double G, do
                      WsCarver::need((size_t)q.nmodels * q.ns * 8);
     }
   // persistent grid: as many blocks as fit on the device at once
-  cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)std::max<size_t>(p.smem, 48 * 1024));
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, B_TS, p.smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, B_TS, p.smem);
   per_sm = std::max(1, per_sm);
   const long long grid = std::min<long long>((long long)per_sm * c->num_sms, p.n_items);
   const int phi_cap = std::max(p.phi_cap, 1);
@@ -675,6 +700,7 @@ int batch_run(ztm_ctx* c, const ztm_job* jobs, int njobs, bool dev, double G, do
   key.push_back((long long)(nq * 1e6));
   key.push_back(stage_kb);
   key.push_back(tlog2);
+  key.push_back(variant);
   for (int j = 0; j < njobs; j++) {
     const ztm_job& q = jobs[j];
     key.insert(key.end(), {q.mesh.nx, q.mesh.ny, q.mesh.nz, (long long)(q.mesh.dx * 1e3),
@@ -737,7 +763,7 @@ int batch_run(ztm_ctx* c, const ztm_job* jobs, int njobs, bool dev, double G, do
       cudaMemsetAsync(J.done, 0, sizeof(int) * J.tiles, c->stream);
     }
     cudaMemsetAsync(counter, 0, sizeof(int) * 16, c->stream);
-    batch_kernel<<<(unsigned)grid, B_TS, p.smem, c->stream>>>(args);
+    kfn<<<(unsigned)grid, B_TS, p.smem, c->stream>>>(args);
     cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
     c->launches = launches_before;  // captured launches are counted per replay
     if (ce != cudaSuccess) {

@@ -47,8 +47,10 @@ struct ztm_ctx {
   // batched-launch graph cache and the host copy of the last job table
   std::vector<ZtmGraphEntry> graphs;
   std::vector<char> batch_table;
-  // launch shapes chosen by the autotuner, keyed by workload shape
+  // launch shapes chosen by the autotuner, keyed by workload shape, and the
+  // timings of the candidates it measured ({shape..., microseconds})
   std::map<std::vector<long long>, std::vector<int>> tuned;
+  std::vector<std::vector<int>> tune_log;
   // timeout-path test hook (ztm_ctx_test_timeout): polls of the far
   // kernel's redirected stage wait, 0 = off
   unsigned stage_wait_limit = 0;
