@@ -587,9 +587,15 @@ def run_workload(args, local_rank):
         what = ("forward + adjoint (misfit, d/drho, d/ddepth) of 256x256 Moho columns at "
                 "128x128 stations (gz evals + gradient evals)")
         step = lambda: ctx.interface_misfit(im, d0, dr, dst, data, precision="mixed")
-    elif args.workload == "batch":
+    elif args.workload in ("batch", "batch_tuned"):
         jobs, _ = synth.line_search_batch()
         djobs = [(m_, d(r_), d(s_)) for m_, r_, s_ in jobs]
+        if args.workload == "batch_tuned":  # every candidate shape and variant, timed once
+            ctx.batch(djobs, autotune=True)
+            ctx.sync()
+            print(json.dumps({"batch_tuning": ctx.tuning(),
+                              "columns": ["stage_kb", "log2_pairs_per_item", "variant", "us"]}),
+                  flush=True)
         units = sum(int(r_.shape[0]) * m_.nx * m_.ny * m_.nz * len(s_) for m_, r_, s_ in jobs)
         what = ("32 line-search trials on the 256x256x64 mesh + 16 regional meshes, one "
                 "graph-captured persistent launch (model-pair evals)")
@@ -690,7 +696,7 @@ def main():
     ap.add_argument("--workload", default="forward",
                     choices=["forward", "adjoint", "interface", "batch", "pointmass",
                              "pointmass_adjoint", "pointmass_adjoint64", "inversion",
-                             "prism_f64", "forward_small", "pointmass_small", "pointmass64_small",
+                             "prism_f64", "forward_small", "pointmass_small", "batch_tuned", "pointmass64_small",
                              "pointmass_adjoint_small", "pointmass_adjoint64_small", "lm"],
                     help="forward (the headline) or another workload as the timed step")
     args = ap.parse_args()

@@ -148,6 +148,12 @@ int ztm_ctx_sync(ztm_ctx* ctx);
 int ztm_ctx_profile(ztm_ctx* ctx, int enable);
 int ztm_ctx_profile_read(ztm_ctx* ctx, const char* name, double* ms,
                          long long* count);
+/* The autotuner's record: the candidates it timed since the context was
+ * created (ZTM_FLAG_AUTOTUNE), four ints each -- for a batched launch (stage
+ * KB per model group, log2 of the pairs per far item, kernel variant,
+ * microseconds); writes at most max_rows rows and returns how many it wrote
+ * (negative on a bad argument). */
+int ztm_ctx_tuning(const ztm_ctx* ctx, int* rows, int max_rows);
 /* Form counters of the mixed prism forward.  While enabled, the forward runs
  * a counting variant of its far kernel (the same arithmetic plus one counter
  * update per column and thread) that adds up the (station, prism) slots it

@@ -34,7 +34,7 @@ EXPORTS = (
     "ztm_gfm_pointmass_model", "ztm_gfm_interface_jvp", "ztm_gfm_pointmass_adjoint",
     "ztm_gfm_pointmass_misfit", "ztm_gfm_pointmass_model_misfit", "ztm_ctx_count_forms",
     "ztm_ctx_form_counts", "ztm_ctx_test_timeout", "ztm_invert_interface_gn",
-    "ztm_lm_steps",
+    "ztm_lm_steps", "ztm_ctx_tuning",
 )
 
 
@@ -116,6 +116,7 @@ _SIGS = {
     "ztm_invert_interface_gn": (_I, [_P, ctypes.POINTER(IMesh), _P, _P, _I, _P, _P, ctypes.c_double,
                                      _I, _I, ctypes.POINTER(Opts), _P, ctypes.POINTER(_I)]),
     "ztm_lm_steps": (_I, [_P, _P, _I, _I, _P, _P, _P, _P, _I, _P, _P, _I]),
+    "ztm_ctx_tuning": (_I, [_P, ctypes.POINTER(_I), _I]),
     "ztm_ctx_count_forms": (_I, [_P, _I]),
     "ztm_ctx_form_counts": (_I, [_P, ctypes.POINTER(_LL)]),
     "ztm_ctx_test_timeout": (_I, [_P, ctypes.c_uint]),

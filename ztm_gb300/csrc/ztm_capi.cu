@@ -301,6 +301,17 @@ void* ztm_ctx_stream(ztm_ctx* c) { return c ? (void*)c->stream : nullptr; }
 
 long long ztm_ctx_launches(const ztm_ctx* c) { return c ? c->launches : -1; }
 
+int ztm_ctx_tuning(const ztm_ctx* c, int* rows, int max_rows) {
+  if (!c || max_rows < 0 || (max_rows > 0 && !rows)) return ZTM_ERR_ARG;
+  int n = 0;
+  for (const auto& r : c->tune_log) {
+    if (n >= max_rows) break;
+    for (int j = 0; j < 4; j++) rows[4 * n + j] = j < (int)r.size() ? r[j] : 0;
+    n++;
+  }
+  return n;
+}
+
 int ztm_ctx_test_timeout(ztm_ctx* c, unsigned int polls) {
   if (!c) return ZTM_ERR_ARG;
   c->stage_wait_limit = polls;

@@ -213,6 +213,15 @@ class GravityContext:
                                                    ctypes.byref(n)))
         return ms.value, n.value
 
+    def tuning(self, max_rows=256):
+        """The autotuner's timed candidates: rows of (stage KB, log2 pairs per
+        item, kernel variant, microseconds) for batched launches."""
+        buf = (ctypes.c_int * (4 * max_rows))()
+        n = self._lib.ztm_ctx_tuning(self._h, buf, max_rows)
+        if n < 0:
+            raise GravityError(n, "bad argument")
+        return [tuple(buf[4 * i:4 * i + 4]) for i in range(n)]
+
     def count_forms(self, enable=True):
         """Run the mixed forward's counting far kernel while enabled."""
         self._check(self._lib.ztm_ctx_count_forms(self._h, 1 if enable else 0))
