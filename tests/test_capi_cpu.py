@@ -49,6 +49,7 @@ def test_null_and_bad_arguments_do_not_crash():
                                               0) == _lib.ERR_ARG
     assert lib.ztm_lm_steps(None, None, 0, 0, None, None, None, None, 0, None, None,
                             0) == _lib.ERR_ARG
+    assert lib.ztm_ctx_tuning(None, None, 0) == _lib.ERR_ARG
     lib.ztm_ctx_destroy(None)
 
 
