@@ -10,11 +10,11 @@ import subprocess
 import pytest
 
 import oracle
+from oracle.build import REF_DIR
 from ztm_gb300 import _build, tfm_patch
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 INCLUDE = os.path.join(ROOT, "include")
-REF_DIR = os.environ.get("ZTM_REFERENCE_DIR", "/root/reference")
 
 
 def _have_ref():
