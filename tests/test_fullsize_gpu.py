@@ -131,3 +131,36 @@ def test_line_search_batch_against_double(ctx):
         sub = np.linspace(0, len(s) - 1, 48).astype(int)
         ref = ctx.prism(m, models[0], s[sub], precision="fp64")
         assert rel_err(outs[j][0][sub], ref) <= 1e-6, (j, m.nx, m.ny, m.nz, len(s))
+
+
+def test_draped_mesh_linearity_and_adjoint_identity_full_size(ctx):
+    """Size-independent properties at full size (256x256x64 prisms, 16,384
+    stations), mixed method: the forward is linear in the density
+    (gz(a r1 + b r2) = a gz(r1) + b gz(r2)) and the adjoint is its transpose
+    (<w, F r> = <F^T w, r>), both to the precision target 1e-6."""
+    mesh, rho, st = synth.draped_mesh_256x256x64()
+    rng = np.random.default_rng(21)
+    r2 = rng.normal(0.0, 100.0, rho.size)
+    a, b = 0.7, -1.3
+    g1 = ctx.prism(mesh, rho, st, precision="mixed")
+    g2 = ctx.prism(mesh, r2, st, precision="mixed")
+    g12 = ctx.prism(mesh, a * rho + b * r2, st, precision="mixed")
+    assert rel_err(g12, a * g1 + b * g2) <= 1e-6
+    w = rng.normal(0.0, 1.0, len(st))
+    gt = ctx.adjoint(mesh, st, w, precision="mixed")
+    lhs, rhs = float(np.dot(w, g1)), float(np.dot(gt, rho))
+    assert abs(lhs - rhs) <= 1e-6 * float(np.sum(np.abs(w * g1)))
+
+
+def test_pointmass_model_adjoint_identity_full_size(ctx):
+    """The reference's point-mass model on the 256x256x64 geometry (its node
+    grid, every node a station: 4.1e6 selected nodes x 65,536 stations): the
+    float forward and the float transposed sum satisfy <w, J d> = <J^T w, d>
+    to the float path's 1e-5."""
+    mesh, rho, st = synth.draped_mesh_256x256x64()
+    g, drho, surf = synth.pointmass_grid_of_mesh(mesh, rho, st)
+    w = np.random.default_rng(22).normal(0.0, 1.0, g.di * g.dj)
+    G = ctx.pointmass(g, drho, surf, precision="fp32")
+    gt = ctx.pointmass_adjoint(g, surf, w, drho=drho, precision="fp32")
+    lhs, rhs = float(np.dot(w, G)), float(np.dot(gt, drho))
+    assert abs(lhs - rhs) <= 1e-5 * float(np.sum(np.abs(w * G)))
