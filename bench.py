@@ -481,6 +481,32 @@ def other_workloads(ctx):
         "model_pairs": mp, "ms": ms_b, "model_pair_evals_per_s": mp / (ms_b * 1e-3),
         "launches_per_call": "1 graph: 4 prep kernels and a library station sort per job + 1 persistent kernel",
         "rel_err_trial5_vs_single_call": err(outs[0][5], one)}
+    # the damped Gauss-Newton trials of LMA::fit (TFM.cpp:159-160): the GPU at
+    # the reference's size, and against the reference's own zmath code (the
+    # CPU baseline: MTM, inv and the products, compiled unchanged) at 600
+    # parameters x 3000 data, 4 damping pairs
+    import oracle
+    rng = np.random.default_rng(7)
+    dm = np.array([[0.0, 0.0], [1e-3, 1e-4], [0.1, 1e-2], [1.0, 1.0]])
+    lm = {}
+    for nrows, ncols in ((3000, 600), (12000, 2700)):
+        J = rng.normal(size=(nrows, ncols)) * rng.uniform(0.1, 10.0, ncols)[None, :]
+        r_, b_, sg = rng.normal(size=nrows), rng.normal(size=ncols), rng.uniform(0.05, 2.0, ncols)
+        dJ, dr_, db_, ds_, ddm = d(J), d(r_), d(b_), d(sg), d(dm)
+        ms, B = _timed(ctx, lambda: ctx.lm_steps(dJ, dr_, db_, ds_, ddm), 3)
+        row = {"gpu_ms": ms, "damping_pairs": 4}
+        if ncols == 600 and oracle.ref_lm_available():
+            t0 = time.perf_counter()
+            Bref, _ = oracle.ref_lm_steps(J, r_, b_, sg, dm)
+            row["reference_cpu_s"] = time.perf_counter() - t0
+            row["reference"] = ("zmath.cpp compiled unchanged + TFM.cpp:159-160 (MTM with one "
+                                "thread per column, inv per damping pair on its own thread)")
+            step = Bref - b_[None, :]
+            row["rel_diff_steps"] = float(np.max(np.abs((B.cpu().numpy() - b_[None, :]) - step)) /
+                                          np.max(np.abs(step)))
+            row["speedup"] = row["reference_cpu_s"] / (ms * 1e-3)
+        lm["J_%dx%d" % (nrows, ncols)] = row
+    res["lm_steps"] = lm
     # inversion workload: 512x512 columns, 256x256 stations, 20 L-BFGS iterations
     im5, dep5, rho5, st5, start5 = synth.moho_columns_512()
     data5 = ctx.interface(im5, d(dep5), d(rho5), d(st5), precision="fp64")
