@@ -64,3 +64,22 @@ def test_lm_device_pointers(ctx):
     dev = ctx.lm_steps(d(J), d(r), d(b), d(sig), d(dm))
     ctx.sync()
     assert np.array_equal(dev.cpu().numpy(), host)
+
+
+def test_lm_underdetermined_and_one_parameter(ctx):
+    """Fewer data than parameters: J^T J has rank 20 of 50, and the damping
+    of the uncertainties (d1 > 0) makes the system solvable; and the smallest
+    system, one parameter."""
+    J, r, b, sig, _ = problem(20, 50, 9)
+    dm = np.array([[0.0, 0.5], [0.3, 0.5]])
+    Bref, _ = reference(J, r, b, sig, dm)
+    B = ctx.lm_steps(J, r, b, sig, dm)
+    for d in (0, 1):
+        step_ref = Bref[d] - b
+        assert np.max(np.abs((B[d] - b) - step_ref)) <= 1e-8 * np.max(np.abs(step_ref)), d
+    J1 = np.arange(1.0, 8.0).reshape(7, 1)
+    r1 = np.linspace(-1.0, 1.0, 7) + 0.3
+    B1 = ctx.lm_steps(J1, r1, np.array([2.0]), np.array([0.5]), np.array([[0.1, 0.2]]))
+    jj, jr = float(np.sum(J1 ** 2)), float(np.dot(J1[:, 0], r1))
+    want = 2.0 + jr / (jj + 0.1 * jj + 0.2 / 0.25)
+    assert B1[0, 0] == pytest.approx(want, rel=1e-14)

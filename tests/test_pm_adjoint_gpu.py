@@ -260,3 +260,30 @@ def test_model_misfit_device_pointers(ctx):
     # atomics in the builder's adjoint: the same up to the order of the adds
     for k in ("g_M", "g_v"):
         assert rel_err(dev[k].cpu().numpy(), host[k]) <= 1e-13, k
+
+
+def test_edge_cases_no_interior_and_no_gradient(ctx):
+    """bfr leaving no interior station: the transposed sum is zero and the
+    misfit is zero; the misfit without its gradient returns the same ssq and
+    residual as with it."""
+    g = ztm_gb300.make_grid(8, 8, 4, 1, 2, 4)
+    drho, surf = tfm_like_inputs(8, 8, 4, seed=6)
+    w = np.ones(64)
+    assert np.all(ctx.pointmass_adjoint(g, surf, w, drho=drho) == 0.0)
+    ssq, res, G, gd, g0 = ctx.pointmass_misfit(g, drho, surf, np.ones(64), 0.1, 1.0)
+    assert ssq == 0.0 and res.size == 0 and np.all(G == 0.0) and np.all(gd == 0.0)
+    assert g0 == 0.0
+    g = ztm_gb300.make_grid(21, 19, 9, 1, 2, 3)
+    drho, surf = tfm_like_inputs(21, 19, 9, seed=8)
+    GD = oracle.pointmass_tfm(g, drho, surf) + 0.2
+    a = ctx.pointmass_misfit(g, drho, surf, GD, 0.1, 0.5)
+    b = ctx.pointmass_misfit(g, drho, surf, GD, 0.1, 0.5, gradient=False)
+    assert a[0] == b[0] and np.array_equal(a[1], b[1]) and b[3] is None
+
+
+def test_model_misfit_without_gradient(ctx):
+    g, rc, sea, M, v, surf, GD = model_case(21, 19, 13, seed=12)
+    a = ctx.pointmass_model_misfit(g, sea, M, v, surf, GD, VM, RO, DR, rc, g0=0.3, gsig=0.7)
+    b = ctx.pointmass_model_misfit(g, sea, M, v, surf, GD, VM, RO, DR, rc, g0=0.3, gsig=0.7,
+                                   gradient=False)
+    assert a["ssq"] == b["ssq"] and np.array_equal(a["G"], b["G"]) and "g_M" not in b
