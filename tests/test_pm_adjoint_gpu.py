@@ -287,3 +287,14 @@ def test_model_misfit_without_gradient(ctx):
     b = ctx.pointmass_model_misfit(g, sea, M, v, surf, GD, VM, RO, DR, rc, g0=0.3, gsig=0.7,
                                    gradient=False)
     assert a["ssq"] == b["ssq"] and np.array_equal(a["G"], b["G"]) and "g_M" not in b
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_model_misfit_field_is_the_model_forward(ctx, precision):
+    """The chained call's G is ztm_gfm_pointmass_model's field, bit for bit,
+    so the central differences above are differences of that forward."""
+    g, rc, sea, M, v, surf, GD = model_case(61, 61, 33, seed=5)
+    r = ctx.pointmass_model_misfit(g, sea, M, v, surf, GD, VM, RO, DR, rc, g0=0.3, gsig=0.7,
+                                   precision=precision)
+    G = ctx.pointmass_model(g, sea, M, v, surf, VM, RO, DR, rc, precision=precision)
+    assert np.array_equal(r["G"], G)
