@@ -626,6 +626,20 @@ def run_workload(args, local_rank):
         what = ("32 line-search trials on the 256x256x64 mesh + 16 regional meshes, one "
                 "graph-captured persistent launch (model-pair evals)")
         step = lambda: ctx.batch(djobs)
+    elif args.workload == "batch_trials_small":
+        jobs, _ = synth.line_search_batch(n_regional=0)
+        mesh, trials, st = jobs[0]
+        sub = np.ascontiguousarray(st[::8])
+        djobs = [(mesh, d(trials), d(sub))]
+        ctx.batch(djobs, autotune=True)  # every candidate shape and variant, timed once
+        ctx.sync()
+        print(json.dumps({"batch_tuning": ctx.tuning(),
+                          "columns": ["stage_kb", "log2_pairs_per_item", "variant", "us"]}),
+              flush=True)
+        units = int(trials.shape[0]) * mesh.nx * mesh.ny * mesh.nz * len(sub)
+        what = ("32 line-search trials on the 256x256x64 mesh at every 8th station (2,048), "
+                "the fastest shape: the profiling case of the batched kernel (model-pair evals)")
+        step = lambda: ctx.batch(djobs, autotune=True)
     elif args.workload == "pointmass":
         mesh, rho, st = synth.draped_mesh_256x256x64()
         g, drho, surf = synth.pointmass_grid_of_mesh(mesh, rho, st)
@@ -723,7 +737,8 @@ def main():
                     choices=["forward", "adjoint", "interface", "batch", "pointmass",
                              "pointmass_adjoint", "pointmass_adjoint64", "inversion",
                              "prism_f64", "forward_small", "pointmass_small", "batch_tuned", "pointmass64_small",
-                             "pointmass_adjoint_small", "pointmass_adjoint64_small", "lm"],
+                             "pointmass_adjoint_small", "pointmass_adjoint64_small", "lm",
+                             "batch_trials_small"],
                     help="forward (the headline) or another workload as the timed step")
     args = ap.parse_args()
     rank, local_rank, world = dist_env()

@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "prism_common.cuh"
+#include "tc_tf32.cuh"
 #include "ztm_internal.cuh"
 
 namespace {
@@ -39,6 +40,8 @@ struct BJob {
   MeshDesc m;
   int nmodels, ns, tiles, chunks, chunk_cols, sc, mgroups, nv_cap;
   int mgw;               // models interleaved per group: 1 or the variant's MG
+  int tc, nzt;           // far items on the tensor cores; their layers per column
+                         // (nz rounded up to a multiple of 16)
   long long near_base, far_base;
   double far_scale, G5;
   const float4* sf;
@@ -47,6 +50,7 @@ struct BJob {
   const short2* iv;      // near-region intervals [station][box column]
   const int2* lr;        // per-station near layer range
   const float* rhoT;     // [group][column][layer][mgw] float densities
+  const float* rhoC;     // tensor-core jobs: [group][column][MMA B layout]
   const double* rho;     // nmodels x np (layer-major, as given)
   const double* sxyz;
   double* partial;       // [model][chunk][ns]
@@ -65,6 +69,7 @@ struct BArgs {
                  // near prisms' unit responses (global scratch)
   int phi_cap;
   int phi_stride;  // doubles per warp: 2 phi_cap
+  int drain;       // tensor-core items: k-blocks per accumulation window
 };
 
 // Float densities of a job, model-interleaved: rhoT[((g*ncols + c)*nzp + l)*W
@@ -283,9 +288,117 @@ __device__ void near_item(const BJob& J, int tile, double* phi_all, int phi_cap,
   }
 }
 
+// One far item on the CUDA cores: (job, station tile, column chunk, model
+// group of MG, or one model where the job has one).  Returns false if a
+// stage wait ran out (the caller reports the timeout).
+template <int MG>
+__device__ bool far_item_cc(const BJob& J, int tile, int chunk, int mg, uint64_t* bar,
+                            float* stage, unsigned& uses0, unsigned& uses1, float* ks,
+                            float* kc, int* s_lm) {
+  const MeshConst& k = J.k;
+  const int m0 = mg * J.mgw, mcnt = min(J.mgw, J.nmodels - m0);
+  const int c0 = chunk * J.chunk_cols, c1 = min(k.ncols, c0 + J.chunk_cols);
+  const int nst = (c1 - c0 + J.sc - 1) / J.sc;
+  const int stage_floats = J.sc * k.nzp * J.mgw;
+  const int slot = tile * B_TS + threadIdx.x;
+  const bool active = slot < J.ns;
+  const int s = active ? J.perm[slot] : 0;
+  float ex = 0.f, ey = 0.f, ez = 0.f;
+  int ixs = 0, iys = 0, izs = 0;
+  NearBox nb = {1, 0, 1, 0, 1, 0};
+  if (threadIdx.x == 0) *s_lm = 0;
+  __syncthreads();
+  if (active) {
+    const float4 f = J.sf[s];
+    const int4 i = J.si[s];
+    ex = f.x; ey = f.y; ez = f.z;
+    ixs = i.x; iys = i.y; izs = i.z;
+    nb = near_box(i, k);
+    atomicMax(s_lm, nb.l1 + 1);
+  }
+  auto issue = [&](int st) {
+    const int buf = st & 1;
+    const int cs = c0 + st * J.sc;
+    const int ncol = min(J.sc, c1 - cs);
+    const uint32_t bytes = (uint32_t)ncol * k.nzp * J.mgw * 4u;
+    mbar_expect_tx(&bar[buf], bytes);
+    bulk_g2s(stage + buf * stage_floats,
+             J.rhoT + ((size_t)mg * k.ncols + cs) * k.nzp * J.mgw, bytes, &bar[buf]);
+  };
+  if (threadIdx.x == 0 && nst > 0) issue(0);
+  __syncthreads();
+  const int Lm = min(*s_lm, k.nz);
+  const FarCoef fc = k.fc;
+#pragma unroll
+  for (int md = 0; md < MG; md++) ks[md * B_TS] = kc[md * B_TS] = 0.f;
+  for (int st = 0; st < nst; st++) {
+    if (threadIdx.x == 0 && st + 1 < nst) issue(st + 1);
+    const int buf = st & 1;
+    const unsigned par = (buf ? uses1 : uses0) & 1u;
+    const bool ok = mbar_wait(&bar[buf], par);
+    if (buf) uses1++; else uses0++;
+    if (__syncthreads_or(!ok)) return false;
+    const float* rs = stage + buf * stage_floats;
+    const int cs = c0 + st * J.sc;
+    const int ncol = min(J.sc, c1 - cs);
+    if (active) {
+      int ix = cs % k.nx, iy = cs / k.nx;
+      for (int q = 0; q < ncol; q++) {
+        const float X = fmaf((float)(ixs - ix), k.dxn, ex);
+        const float Y = fmaf((float)(iys - iy), k.dyn, ey);
+        const ColPoly cp = col_poly(X, Y, fc);
+        const bool ncl = ix >= nb.x0 && ix <= nb.x1 && iy >= nb.y0 && iy <= nb.y1;
+        int elo = k.nz;
+        unsigned espan = 0u;
+        if (ncl) {  // the column's near-region layers
+          const short2 tv = J.iv[(size_t)s * k.nslots + near_slot(nb, ix, iy)];
+          if (tv.x <= tv.y) {
+            elo = tv.x;
+            espan = (unsigned)(tv.y - tv.x);
+          }
+        }
+        const float* col = rs + q * k.nzp * J.mgw;
+        const ColPoly2 cp2 = col_poly2(cp, fc.a1);
+        const float2 c2t = make_float2(cp.C2 - fc.h2, cp.C2 - fc.h2);
+        const unsigned am = __activemask();
+        const int form = (__all_sync(am, cp.rh >= k.rh_t2) ? 1 : 0) |
+                         ((__any_sync(am, ncl) || (k.nz & 7)) ? 2 : 0);
+        if (MG == 1 || J.mgw == 1) {
+          switch (form) {
+            case 0: far_column<1, false, false>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc); break;
+            case 1: far_column<1, true, false>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc); break;
+            case 2: far_column<1, false, true>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc); break;
+            default: far_column<1, true, true>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc);
+          }
+        } else {
+          switch (form) {
+            case 0: far_column<MG, false, false>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc); break;
+            case 1: far_column<MG, true, false>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc); break;
+            case 2: far_column<MG, false, true>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc); break;
+            default: far_column<MG, true, true>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc);
+          }
+        }
+        if (++ix == k.nx) {
+          ix = 0;
+          ++iy;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (active) {
+#pragma unroll
+    for (int md = 0; md < MG; md++)
+      if (md < mcnt)
+        J.partial[((size_t)(m0 + md) * J.chunks + chunk) * J.ns + s] =
+            (double)ks[md * B_TS] - (double)kc[md * B_TS];
+  }
+  return true;
+}
+
 // MG models per far item (the interleave width of a multi-model job), MINB
-// resident blocks per SM asked of the compiler: the kernel variants the
-// autotuner tries (BATCH_VARIANTS).
+// resident blocks per SM asked of the compiler: the CUDA-core kernel
+// variants the autotuner tries (BATCH_VARIANTS).
 template <int MG, int MINB>
 __global__ void __launch_bounds__(B_TS, MINB) batch_kernel(BArgs a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -332,114 +445,384 @@ __global__ void __launch_bounds__(B_TS, MINB) batch_kernel(BArgs a) {
     r /= J.tiles;
     const int chunk = (int)(r % J.chunks);
     const int mg = (int)(r / J.chunks);
-    const MeshConst& k = J.k;
-    const int m0 = mg * J.mgw, mcnt = min(J.mgw, J.nmodels - m0);
-    const int c0 = chunk * J.chunk_cols, c1 = min(k.ncols, c0 + J.chunk_cols);
-    const int nst = (c1 - c0 + J.sc - 1) / J.sc;
-    const int stage_floats = J.sc * k.nzp * J.mgw;
-    const int slot = tile * B_TS + threadIdx.x;
-    const bool active = slot < J.ns;
-    const int s = active ? J.perm[slot] : 0;
-    float ex = 0.f, ey = 0.f, ez = 0.f;
-    int ixs = 0, iys = 0, izs = 0;
-    NearBox nb = {1, 0, 1, 0, 1, 0};
-    if (threadIdx.x == 0) s_lm = 0;
-    __syncthreads();
-    if (active) {
-      const float4 f = J.sf[s];
-      const int4 i = J.si[s];
-      ex = f.x; ey = f.y; ez = f.z;
-      ixs = i.x; iys = i.y; izs = i.z;
-      nb = near_box(i, k);
-      atomicMax(&s_lm, nb.l1 + 1);
-    }
-    auto issue = [&](int st) {
-      const int buf = st & 1;
-      const int cs = c0 + st * J.sc;
-      const int ncol = min(J.sc, c1 - cs);
-      const uint32_t bytes = (uint32_t)ncol * k.nzp * J.mgw * 4u;
-      mbar_expect_tx(&bar[buf], bytes);
-      bulk_g2s(stage + buf * stage_floats,
-               J.rhoT + ((size_t)mg * k.ncols + cs) * k.nzp * J.mgw, bytes, &bar[buf]);
-    };
-    if (threadIdx.x == 0 && nst > 0) issue(0);
-    __syncthreads();
-    const int Lm = min(s_lm, k.nz);
-    const FarCoef fc = k.fc;
-#pragma unroll
-    for (int md = 0; md < MG; md++) ks[md * B_TS] = kc[md * B_TS] = 0.f;
-    bool timed_out = false;
-    for (int st = 0; st < nst; st++) {
-      if (threadIdx.x == 0 && st + 1 < nst) issue(st + 1);
-      const int buf = st & 1;
-      const unsigned par = (buf ? uses1 : uses0) & 1u;
-      const bool ok = mbar_wait(&bar[buf], par);
-      if (buf) uses1++; else uses0++;
-      if (__syncthreads_or(!ok)) {
-        timed_out = true;
-        break;
-      }
-      const float* rs = stage + buf * stage_floats;
-      const int cs = c0 + st * J.sc;
-      const int ncol = min(J.sc, c1 - cs);
-      if (active) {
-        int ix = cs % k.nx, iy = cs / k.nx;
-        for (int q = 0; q < ncol; q++) {
-          const float X = fmaf((float)(ixs - ix), k.dxn, ex);
-          const float Y = fmaf((float)(iys - iy), k.dyn, ey);
-          const ColPoly cp = col_poly(X, Y, fc);
-          const bool ncl = ix >= nb.x0 && ix <= nb.x1 && iy >= nb.y0 && iy <= nb.y1;
-          int elo = k.nz;
-          unsigned espan = 0u;
-          if (ncl) {  // the column's near-region layers
-            const short2 tv = J.iv[(size_t)s * k.nslots + near_slot(nb, ix, iy)];
-            if (tv.x <= tv.y) {
-              elo = tv.x;
-              espan = (unsigned)(tv.y - tv.x);
-            }
-          }
-          const float* col = rs + q * k.nzp * J.mgw;
-          const ColPoly2 cp2 = col_poly2(cp, fc.a1);
-          const float2 c2t = make_float2(cp.C2 - fc.h2, cp.C2 - fc.h2);
-          const unsigned am = __activemask();
-          const int form = (__all_sync(am, cp.rh >= k.rh_t2) ? 1 : 0) |
-                           ((__any_sync(am, ncl) || (k.nz & 7)) ? 2 : 0);
-          if (J.mgw == 1) {
-            switch (form) {
-              case 0: far_column<1, false, false>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc); break;
-              case 1: far_column<1, true, false>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc); break;
-              case 2: far_column<1, false, true>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc); break;
-              default: far_column<1, true, true>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc);
-            }
-          } else {
-            switch (form) {
-              case 0: far_column<MG, false, false>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc); break;
-              case 1: far_column<MG, true, false>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc); break;
-              case 2: far_column<MG, false, true>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc); break;
-              default: far_column<MG, true, true>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc);
-            }
-          }
-          if (++ix == k.nx) {
-            ix = 0;
-            ++iy;
-          }
-        }
-      }
-      __syncthreads();
-    }
-    if (timed_out) {
+    if (!far_item_cc<MG>(J, tile, chunk, mg, bar, stage, uses0, uses1, ks, kc, &s_lm)) {
       if (threadIdx.x == 0) atomicOr(a.err, ZTM_DEVERR_TIMEOUT);
       return;
     }
-    if (active) {
+    tile_done(J, tile, J.chunks * J.mgroups + 1, &s_flag);
+  }
+}
+
+// ---- multi-model far items on the tensor cores ----------------------------
+//
+// For a job with many models the far field is a contraction: with K[s][p] the
+// far-field value of (station s, prism p), gz_far[s][m] = sum_p K[s][p]
+// rho_m[p].  A far item of a tensor-core job is (station tile of 128, column
+// chunk, group of TC_MG = 32 models): each thread computes K for its station
+// as in far_column, 16 layers at a time, and writes them to its TMEM lane as
+// TF32 high and low parts (hi = nearest TF32 of K, lo = K - hi); one thread
+// issues per 8 layers (M 128, N 32, K 8 each)
+//   D[:, 0:32]  += A_hi x B_hi
+//   D[:, 32:64] += A_hi x B_lo,  D[:, 32:64] += A_lo x B_hi
+// with B the group's densities split the same way (B_lo is rho - B_hi), so
+// D[:, m] + D[:, 32 + m] carries K rho_m to about 2^-22 of each product (the
+// dropped lo x lo term and the TF32 rounding of the low parts).  The tensor
+// core's FP32 accumulation truncates: every add into an accumulator loses
+// about half a unit in its last place, toward zero.  So the small cross
+// products have their own accumulator, the main one takes one add per 8
+// layers, and every `drain` k-blocks (default 4: 8 adds, a bias of about
+// 2e-7 of the window's sum) the accumulators are read back (tcgen05.ld) and
+// added to the thread's compensated sums in registers.  (Two adds per 8
+// layers and 32 per window measured 1.6e-6 on the 256x256x64 line search.)
+//
+// B comes from HBM ready in the MMA's shared-memory layout (see
+// transpose_models_tc_kernel), one 1-D bulk copy per column into a ring of
+// TC_NS stages, issued two columns ahead.  Synchronisation, per block:
+//   stage[i]  bulk copy of a column landed (thread 0 waits before its MMAs);
+//   mma[b]    tcgen05.commit after the MMAs that read A buffer b: every thread
+//             waits for k-block n - 2 before writing buffer n & 1, and the
+//             drain waits for the last k-block before reading D.  Waiting for
+//             k-block n - 2 also frees the stage of column c - 2 (commits
+//             complete in order), which is the stage the copy issued at the
+//             start of column c fills.
+constexpr int TC_MG = 32;           // models per tensor-core group
+constexpr int TC_N = 2 * TC_MG;     // rows of B: the high parts, then the low parts
+constexpr int TC_NS = 4;            // column stages
+constexpr int TC_KB = 16;           // layers per k-block (two MMA steps of K = 8)
+constexpr uint32_t TC_COLS = 128;   // TMEM columns: D [0, 64), A buffer b at 64 + 32 b
+constexpr uint32_t TC_IDESC = tc_idesc_tf32(128, TC_MG);
+
+// Densities of a tensor-core job in the MMA's B layout, one column after
+// another: per column, per 8 layers (lb), the two K halves (kc: layers
+// +0..3, +4..7) of TC_N rows in groups of 8 (ng), each row 16 bytes (4
+// layers): rhoC[((((g ncols + c) (nzt/8) + lb) 2 + kc) (TC_N/8) + ng) 32 +
+// nr 4 + kk] = part(n) of rho_{g TC_MG + n % TC_MG}(c, 8 lb + 4 kc + kk),
+// n = 8 ng + nr, part 0 (n < TC_MG) the nearest TF32 value h of the density,
+// part 1 the nearest TF32 value of (density - h); zero for padded layers and
+// models.  A column is one contiguous range (one bulk copy), and 8 layers of
+// it are one MMA step's B operand with LBO = TC_N * 16 bytes (kc stride) and
+// SBO = 128 bytes (ng stride).
+__global__ void transpose_models_tc_kernel(MeshConst k, int nmodels, int nzt,
+                                           const double* __restrict__ rho,
+                                           float* __restrict__ rhoC) {
+  const int ngroups = (nmodels + TC_MG - 1) / TC_MG;
+  const long long per_col = (long long)nzt * TC_N;
+  const long long total = (long long)ngroups * k.ncols * per_col;
+  const long long np = (long long)k.ncols * k.nz;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int e = (int)(t % per_col);
+    const long long gc = t / per_col;
+    const int c = (int)(gc % k.ncols), g = (int)(gc / k.ncols);
+    const int kk = e & 3, nr = (e >> 2) & 7;
+    int r = e >> 5;
+    const int ng = r % (TC_N / 8);
+    r /= TC_N / 8;
+    const int kc = r & 1, lb = r >> 1;
+    const int l = lb * 8 + kc * 4 + kk, n = ng * 8 + nr;
+    const int md = g * TC_MG + n % TC_MG;
+    float v = 0.f;
+    if (l < k.nz && md < nmodels) {
+      const double x = rho[(long long)md * np + (long long)l * k.ncols + c];
+      const float h = __uint_as_float(tf32_rna((float)x));
+      v = n < TC_MG ? h : __uint_as_float(tf32_rna((float)(x - (double)h)));
+    }
+    rhoC[t] = v;
+  }
+}
+
+struct TcBars {
+  uint64_t stage[TC_NS];
+  uint64_t mma[2];
+  uint64_t fin;
+};
+
+struct TcState {
+  uint32_t tmem;      // TMEM base of the block
+  unsigned kblk;      // k-blocks committed by the block (uniform)
+  unsigned gcol;      // columns staged by the block (uniform)
+  unsigned issued;    // stage copies issued (thread 0)
+  unsigned waited;    // stage copies waited for (thread 0)
+};
+
+__device__ __forceinline__ void kahan_reg(float& s, float& c, float x) {
+  const float y = x - c;
+  const float t = s + y;
+  c = (t - s) - y;
+  s = t;
+}
+
+// K of 16 layers (l0 .. l0 + 15) of one column for this thread's station,
+// split into TF32 high parts and FP32 remainders.
+template <bool T2, bool MASK>
+__device__ __forceinline__ void tc_kblock(const MeshConst& k, const ColPoly2& cp2, float2 c2t,
+                                          float ez, float zf0, int l0, int Lm, int elo,
+                                          unsigned espan, uint32_t (&hi)[16],
+                                          uint32_t (&lo)[16]) {
+  const float2 dz2 = make_float2(k.dzn, k.dzn);
 #pragma unroll
-      for (int md = 0; md < MG; md++)
-        if (md < mcnt)
-          J.partial[((size_t)(m0 + md) * J.chunks + chunk) * J.ns + s] =
-              (double)ks[md * B_TS] - (double)kc[md * B_TS];
+  for (int h = 0; h < 2; h++) {
+    const float Zg = fmaf(zf0 + 8.f * h, k.dzn, ez);
+    const float2 zg2 = make_float2(Zg, Zg);
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const float2 Z = __ffma2_rn(make_float2((float)(2 * j), (float)(2 * j + 1)), dz2, zg2);
+      float2 K = T2 ? far_unit2_t2(Z, cp2, c2t) : far_unit2(Z, cp2);
+      if (MASK) {
+        const int la = l0 + 8 * h + 2 * j, lb = la + 1;
+        // select: a NaN at a near-region prism is dropped
+        if ((la < Lm && (unsigned)(la - elo) <= espan) || la >= k.nz) K.x = 0.f;
+        if ((lb < Lm && (unsigned)(lb - elo) <= espan) || lb >= k.nz) K.y = 0.f;
+      }
+      const uint32_t hx = tf32_rna(K.x), hy = tf32_rna(K.y);
+      const float2 L = __ffma2_rn(make_float2(-1.f, -1.f),
+                                  make_float2(__uint_as_float(hx), __uint_as_float(hy)), K);
+      hi[8 * h + 2 * j] = hx;
+      hi[8 * h + 2 * j + 1] = hy;
+      lo[8 * h + 2 * j] = __float_as_uint(L.x);
+      lo[8 * h + 2 * j + 1] = __float_as_uint(L.y);
+    }
+  }
+}
+
+// One tensor-core far item.  Returns false if a wait ran out (*s_to set).
+__device__ bool far_item_tc(const BJob& J, int tile, int chunk, int mg, TcState& ts,
+                            TcBars* tb, float* stage, int* s_to, int* s_lm, int drain) {
+  const MeshConst& k = J.k;
+  const int tid = threadIdx.x;
+  const uint32_t lane_off = (uint32_t)(32 * (tid >> 5)) << 16;
+  const int m0 = mg * TC_MG, mcnt = min(TC_MG, J.nmodels - m0);
+  const int c0 = chunk * J.chunk_cols, c1 = min(k.ncols, c0 + J.chunk_cols);
+  const int ncol = c1 - c0;
+  const int nkb = J.nzt / TC_KB;
+  const uint32_t col_floats = (uint32_t)J.nzt * TC_N;
+  const uint32_t col_bytes = col_floats * 4u;
+  const int slot = tile * B_TS + tid;
+  const bool active = slot < J.ns;
+  const int s = active ? J.perm[slot] : 0;
+  float ex = 0.f, ey = 0.f, ez = 0.f;
+  int ixs = 0, iys = 0, izs = 0;
+  NearBox nb = {1, 0, 1, 0, 1, 0};
+  if (tid == 0) *s_lm = 0;
+  __syncthreads();
+  if (active) {
+    const float4 f = J.sf[s];
+    const int4 i = J.si[s];
+    ex = f.x; ey = f.y; ez = f.z;
+    ixs = i.x; iys = i.y; izs = i.z;
+    nb = near_box(i, k);
+    atomicMax(s_lm, nb.l1 + 1);
+  }
+  const unsigned g0 = ts.gcol;
+  auto issue = [&](int q) {  // thread 0: column c0 + q into stage (g0 + q) % TC_NS
+    const unsigned g = g0 + (unsigned)q;
+    uint64_t* bar = &tb->stage[g % TC_NS];
+    mbar_expect_tx(bar, col_bytes);
+    bulk_g2s(stage + (g % TC_NS) * col_floats,
+             J.rhoC + ((size_t)mg * k.ncols + c0 + q) * col_floats, col_bytes, bar);
+    ts.issued = g + 1;
+  };
+  if (tid == 0) {
+    issue(0);
+    if (ncol > 1) issue(1);
+  }
+  __syncthreads();
+  const int Lm = min(*s_lm, k.nz);
+  const FarCoef fc = k.fc;
+  const uint32_t tmem = ts.tmem;
+  float as[TC_MG], ac[TC_MG];
+#pragma unroll
+  for (int m = 0; m < TC_MG; m++) as[m] = ac[m] = 0.f;
+  // add D (the products since the last drain) to the compensated sums
+  auto drain_d = [&](unsigned nl) {
+    if (!mbar_wait(&tb->mma[nl & 1u], (nl >> 1) & 1u)) *s_to = 1;
+    tc_fence_after();
+#pragma unroll
+    for (int h = 0; h < TC_MG / 16; h++) {
+      uint32_t d0[16], d1[16];
+      tmem_ld16(tmem + lane_off + 16 * h, d0);
+      tmem_ld16(tmem + lane_off + TC_MG + 16 * h, d1);
+      tmem_wait_ld();
+#pragma unroll
+      for (int j = 0; j < 16; j++)
+        kahan_reg(as[16 * h + j], ac[16 * h + j], __uint_as_float(d0[j]) + __uint_as_float(d1[j]));
+    }
+  };
+  bool pending = false;  // D holds products not yet drained
+  int ix = c0 % k.nx, iy = c0 / k.nx;
+  for (int q = 0; q < ncol; q++) {
+    const float X = fmaf((float)(ixs - ix), k.dxn, ex);
+    const float Y = fmaf((float)(iys - iy), k.dyn, ey);
+    const ColPoly cp = col_poly(X, Y, fc);
+    const bool ncl = active && ix >= nb.x0 && ix <= nb.x1 && iy >= nb.y0 && iy <= nb.y1;
+    int elo = k.nz;
+    unsigned espan = 0u;
+    if (ncl) {
+      const short2 tv = J.iv[(size_t)s * k.nslots + near_slot(nb, ix, iy)];
+      if (tv.x <= tv.y) {
+        elo = tv.x;
+        espan = (unsigned)(tv.y - tv.x);
+      }
+    }
+    const ColPoly2 cp2 = col_poly2(cp, fc.a1);
+    const float2 c2t = make_float2(cp.C2 - fc.h2, cp.C2 - fc.h2);
+    const int form = (__all_sync(0xffffffffu, !active || cp.rh >= k.rh_t2) ? 1 : 0) |
+                     ((__any_sync(0xffffffffu, ncl) || (k.nz & (TC_KB - 1))) ? 2 : 0);
+    float zf = (float)(-izs);
+    for (int kb = 0; kb < nkb; kb++, zf += (float)TC_KB) {
+      const unsigned n = ts.kblk, b = n & 1u;
+      if (n >= 2) {  // the MMAs that read A buffer b (k-block n - 2) are done
+        if (!mbar_wait(&tb->mma[b], ((n >> 1) - 1u) & 1u)) *s_to = 1;
+        tc_fence_after();
+      }
+      if (tid == 0 && kb == 0 && q + 2 < ncol) issue(q + 2);
+      uint32_t hi[16], lo[16];
+      switch (form) {
+        case 0: tc_kblock<false, false>(k, cp2, c2t, ez, zf, kb * TC_KB, Lm, elo, espan, hi, lo); break;
+        case 1: tc_kblock<true, false>(k, cp2, c2t, ez, zf, kb * TC_KB, Lm, elo, espan, hi, lo); break;
+        case 2: tc_kblock<false, true>(k, cp2, c2t, ez, zf, kb * TC_KB, Lm, elo, espan, hi, lo); break;
+        default: tc_kblock<true, true>(k, cp2, c2t, ez, zf, kb * TC_KB, Lm, elo, espan, hi, lo);
+      }
+      if (!active) {
+#pragma unroll
+        for (int j = 0; j < 16; j++) hi[j] = lo[j] = 0u;
+      }
+      const uint32_t abuf = tmem + 64u + 32u * b;
+      tmem_st16(abuf + lane_off, hi);
+      tmem_st16(abuf + lane_off + 16u, lo);
+      tmem_wait_st();
+      if (tid == 0 && kb == 0) {  // this column's densities in shared memory
+        const unsigned g = g0 + (unsigned)q;
+        if (!mbar_wait(&tb->stage[g % TC_NS], (g / TC_NS) & 1u)) *s_to = 1;
+        ts.waited = g + 1;
+      }
+      const bool first = (q * nkb + kb) % drain == 0;
+      if (first && pending) drain_d(n - 1u);
+      tc_fence_before();
+      __syncthreads();
+      if (*s_to) return false;
+      if (tid == 0) {
+        tc_fence_after();
+        const uint32_t sb = smem_u32(stage + ((g0 + q) % TC_NS) * col_floats) +
+                            (uint32_t)kb * 2u * (8u * TC_N * 4u);
+#pragma unroll
+        for (int st = 0; st < 2; st++) {
+          const uint32_t bh = sb + st * (8u * TC_N * 4u);  // rows 0..31: B_hi
+          const uint32_t bl = bh + (TC_MG / 8) * 128u;     // rows 32..63: B_lo
+          const uint64_t dh = tc_smem_desc(bh, TC_N * 16u, 128u);
+          const uint64_t dl = tc_smem_desc(bl, TC_N * 16u, 128u);
+          const uint32_t acc = (first && st == 0) ? 0u : 1u;
+          tc_mma_ts(tmem, abuf + 8u * st, dh, TC_IDESC, acc);
+          tc_mma_ts(tmem + TC_MG, abuf + 8u * st, dl, TC_IDESC, acc);
+          tc_mma_ts(tmem + TC_MG, abuf + 16u + 8u * st, dh, TC_IDESC, 1u);
+        }
+        tc_commit(&tb->mma[b]);
+      }
+      ts.kblk = n + 1u;
+      pending = true;
+    }
+    if (++ix == k.nx) {
+      ix = 0;
+      ++iy;
+    }
+  }
+  ts.gcol = g0 + (unsigned)ncol;
+  if (pending) drain_d(ts.kblk - 1u);
+  tc_fence_before();
+  __syncthreads();  // every thread has read D before the next item overwrites it
+  if (*s_to) return false;
+  if (active) {
+#pragma unroll
+    for (int md = 0; md < TC_MG; md++)
+      if (md < mcnt)
+        J.partial[((size_t)(m0 + md) * J.chunks + chunk) * J.ns + s] =
+            (double)as[md] - (double)ac[md];
+  }
+  return true;
+}
+
+// The tensor-core variant: multi-model jobs (J.tc) by far_item_tc, one-model
+// jobs by far_item_cc<1>, near items as in batch_kernel.  TMEM (TC_COLS
+// columns) is allocated once per block and freed after the block's last item,
+// once its MMAs and stage copies have completed.
+template <int MINB>
+__global__ void __launch_bounds__(B_TS, MINB) batch_tc_kernel(BArgs a) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
+  float* stage = reinterpret_cast<float*>(smem_raw + 128);
+  double* phi = a.phi + (size_t)blockIdx.x * B_WARPS * a.phi_stride;
+  __shared__ long long s_item;
+  __shared__ int s_flag, s_lm, s_to;
+  __shared__ float s_ks[B_TS], s_kc[B_TS];
+  __shared__ TcBars tb;
+  __shared__ uint32_t s_tmem;
+  float* const ks = s_ks + threadIdx.x;
+  float* const kc = s_kc + threadIdx.x;
+  if ((threadIdx.x >> 5) == 0) {
+    tmem_alloc(&s_tmem, TC_COLS);
+    tmem_relinquish();
+  }
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    for (int i = 0; i < TC_NS; i++) mbar_init(&tb.stage[i], 1);
+    mbar_init(&tb.mma[0], 1);
+    mbar_init(&tb.mma[1], 1);
+    mbar_init(&tb.fin, 1);
+    fence_mbar_init();
+    s_to = 0;
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  TcState ts{s_tmem, 0u, 0u, 0u, 0u};
+  unsigned uses0 = 0, uses1 = 0;
+  bool failed = false;
+  for (long long guard = 0; guard < a.n_items + 1; guard++) {
+    if (threadIdx.x == 0) s_item = atomicAdd(a.counter, 1);
+    __syncthreads();
+    const long long item = s_item;
+    __syncthreads();
+    if (item >= a.n_items) break;
+    if (item < a.n_near) {
+      int j = 0;
+      while (j + 1 < a.njobs && a.jobs[j + 1].near_base <= item) j++;
+      const BJob& J = a.jobs[j];
+      const int tile = (int)(item - J.near_base);
+      near_item(J, tile, phi, a.phi_cap, a.phi_stride, a.err);
+      __syncthreads();
+      tile_done(J, tile, J.chunks * J.mgroups + 1, &s_flag);
+      continue;
+    }
+    int j = 0;
+    while (j + 1 < a.njobs && a.jobs[j + 1].far_base <= item) j++;
+    const BJob& J = a.jobs[j];
+    long long r = item - J.far_base;
+    const int tile = (int)(r % J.tiles);
+    r /= J.tiles;
+    const int chunk = (int)(r % J.chunks);
+    const int mg = (int)(r / J.chunks);
+    const bool ok = J.tc ? far_item_tc(J, tile, chunk, mg, ts, &tb, stage, &s_to, &s_lm, a.drain)
+                         : far_item_cc<1>(J, tile, chunk, mg, bar, stage, uses0, uses1, ks, kc,
+                                          &s_lm);
+    if (!ok) {
+      failed = true;
+      break;
     }
     tile_done(J, tile, J.chunks * J.mgroups + 1, &s_flag);
   }
+  if (failed && threadIdx.x == 0) atomicOr(a.err, ZTM_DEVERR_TIMEOUT);
+  // before TMEM is freed: every MMA of the block complete, every stage copy
+  // landed (bounded waits; a wait that runs out only adds to the error)
+  if (threadIdx.x == 0) tc_commit(&tb.fin);
+  if (!mbar_wait(&tb.fin, 0u) && threadIdx.x == 0) atomicOr(a.err, ZTM_DEVERR_TIMEOUT);
+  if (threadIdx.x == 0)
+    for (unsigned g = ts.waited; g < ts.issued; g++)
+      if (!mbar_wait(&tb.stage[g % TC_NS], (g / TC_NS) & 1u)) atomicOr(a.err, ZTM_DEVERR_TIMEOUT);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if ((threadIdx.x >> 5) == 0) tmem_dealloc(ts.tmem, TC_COLS);
 }
 
 struct Plan {
@@ -451,8 +834,10 @@ struct Plan {
 };
 
 // Shapes only (no pointers): per-job tiles, chunks, stage widths, workspace.
+// tc: multi-model jobs take their far items on the tensor cores (one column
+// per stage, TC_MG models per group; stage_kb is then unused).
 Plan plan(const ztm_job* jobs, int njobs, double near_q, int num_sms, int stage_kb, int tlog2,
-          int mg) {
+          int mg, bool tc) {
   Plan p;
   size_t ws = 0;
   for (int j = 0; j < njobs; j++) {
@@ -467,10 +852,12 @@ Plan plan(const ztm_job* jobs, int njobs, double near_q, int num_sms, int stage_
     J.nmodels = q.nmodels;
     J.ns = q.ns;
     J.tiles = std::max(1, (q.ns + B_TS - 1) / B_TS);
-    J.mgw = q.nmodels > 1 ? mg : 1;
+    J.tc = (tc && q.nmodels > 1) ? 1 : 0;
+    J.nzt = ((m.nz + TC_KB - 1) / TC_KB) * TC_KB;
+    J.mgw = J.tc ? TC_MG : (q.nmodels > 1 ? mg : 1);
     J.mgroups = (q.nmodels + J.mgw - 1) / J.mgw;
     int sc = std::max(1, (stage_kb * 1024) / (J.k.nzp * 4 * J.mgw));
-    sc = std::min(sc, 32);
+    sc = J.tc ? 1 : std::min(sc, 32);
     J.sc = sc;
     // split columns so that a far item holds about 2^tlog2 (station, prism)
     // pairs (each applied to up to 8 models)
@@ -485,9 +872,10 @@ Plan plan(const ztm_job* jobs, int njobs, double near_q, int num_sms, int stage_
     J.nv_cap = (std::min(2 * J.k.wx + 1, m.nx) + 1) * (std::min(2 * J.k.wy + 1, m.ny) + 1) *
                (std::min(2 * J.k.wl + 1, m.nz) + 1);
     J.far_scale = J.k.L0 * (double)J.k.dxn * J.k.dyn * J.k.dzn;
-    p.smem = std::max(p.smem, 128 + (size_t)2 * sc * J.k.nzp * 4 * J.mgw);
+    const size_t col_floats = J.tc ? (size_t)J.nzt * TC_N : (size_t)J.k.nzp * J.mgw;
+    p.smem = std::max(p.smem, 128 + (J.tc ? (size_t)TC_NS : (size_t)2 * sc) * col_floats * 4);
     p.phi_cap = std::max(p.phi_cap, J.nv_cap);
-    ws += WsCarver::need((size_t)J.mgroups * J.mgw * J.k.ncols * J.k.nzp * 4);
+    ws += WsCarver::need((size_t)J.mgroups * J.k.ncols * col_floats * 4);
     ws += WsCarver::need((size_t)q.ns * 16) * 2;
     ws += WsCarver::need((size_t)q.nmodels * J.chunks * q.ns * 8);
     ws += WsCarver::need((size_t)q.nmodels * q.ns * 8);
@@ -506,6 +894,9 @@ Plan plan(const ztm_job* jobs, int njobs, double near_q, int num_sms, int stage_
     far += (long long)J.tiles * J.chunks * J.mgroups;
   }
   p.n_items = far;
+  // tensor-core variant: at least 48 KB of dynamic shared memory per block,
+  // so that no more than 512 / TC_COLS = 4 blocks share an SM's TMEM
+  if (tc) p.smem = std::max<size_t>(p.smem, 48 * 1024);
   ws += WsCarver::need(sizeof(BJob) * njobs) + WsCarver::need(64);
   p.ws_bytes = ws;
   (void)num_sms;
@@ -520,25 +911,30 @@ void destroy_entry(ZtmGraphEntry& e) {
 }
 
 // Kernel variants: {models per far item, blocks per SM asked of the
-// compiler}.  Variant 0 is the default.
-constexpr int BATCH_VARIANTS[][2] = {{16, 4}, {16, 5}, {8, 6}, {32, 3}};
+// compiler, tensor cores}.  Variants 0-3 run every far item on the CUDA
+// cores; variant 4 runs the far items of multi-model jobs on the tensor cores.
+constexpr int BATCH_VARIANTS[][3] = {{16, 4, 0}, {16, 5, 0}, {8, 6, 0}, {32, 3, 0}, {TC_MG, 3, 1}};
+constexpr int BATCH_TC_VARIANT = 4;
 using BatchFn = void (*)(BArgs);
 BatchFn batch_fn(int v) {
   switch (v) {
     case 1: return batch_kernel<16, 5>;
     case 2: return batch_kernel<8, 6>;
     case 3: return batch_kernel<32, 3>;
+    case 4: return batch_tc_kernel<3>;
     default: return batch_kernel<16, 4>;
   }
 }
 
-// Launch shapes the autotuner tries: {stage KB per model group, log2 of the
-// pairs per far item, kernel variant}.  The first is the default (32 trial
-// models on the 256x256x64 mesh plus 16 regional meshes: 2^23 pairs 223 ms,
-// 2^24 225 ms, 2^25 229 ms, 2^22 223 ms with twice the partial sums).
-constexpr int BATCH_SHAPES[][3] = {{16, 23, 0}, {8, 24, 0}, {32, 24, 0}, {16, 24, 0}, {16, 25, 0},
-                                   {8, 23, 0},  {32, 25, 0}, {16, 23, 1}, {8, 23, 2}, {16, 23, 2},
-                                   {32, 23, 3}, {16, 24, 3}};
+// Launch shapes the autotuner tries: {stage KB per model group (for the
+// tensor-core variant: k-blocks per TMEM accumulation window), log2 of the
+// pairs per far item, kernel variant}.  The first is the default.  CUDA-core
+// variant 0 on 32 trial models on the 256x256x64 mesh plus 16 regional
+// meshes: 2^23 pairs 223 ms, 2^24 225 ms, 2^25 229 ms, 2^22 223 ms.
+constexpr int BATCH_SHAPES[][3] = {{4, 23, 4},  {2, 23, 4},  {4, 21, 4},  {4, 24, 4},
+                                   {16, 23, 0}, {8, 24, 0},  {32, 24, 0}, {16, 24, 0},
+                                   {16, 25, 0}, {8, 23, 0},  {32, 25, 0}, {16, 23, 1},
+                                   {8, 23, 2},  {16, 23, 2}, {32, 23, 3}, {16, 24, 3}};
 
 int batch_run(ztm_ctx* c, const ztm_job* jobs, int njobs, bool dev, double G, double nq,
               int stage_kb, int tlog2, int variant);
@@ -620,10 +1016,32 @@ extern "C" int ztm_gfm_batch(ztm_ctx* c, const ztm_job* jobs, int njobs, const z
 
 namespace {
 
+// Blocks of kfn that fit on one SM by registers, shared memory, threads and
+// the block limit (the runtime's occupancy query, done by hand: for kernels
+// that allocate TMEM it answers 1, while the SM runs as many as fit).
+int resident_blocks(ztm_ctx* c, BatchFn kfn, int threads, size_t dyn_smem) {
+  cudaFuncAttributes fa;
+  if (cudaFuncGetAttributes(&fa, kfn) != cudaSuccess) return 1;
+  int regs_sm = 65536, smem_sm = 0, thr_sm = 2048, blk_sm = 32, reserved = 1024;
+  cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, c->device);
+  cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device);
+  cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, c->device);
+  cudaDeviceGetAttribute(&blk_sm, cudaDevAttrMaxBlocksPerMultiprocessor, c->device);
+  cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, c->device);
+  const int warps = (threads + 31) / 32;
+  const int regs_warp = ((fa.numRegs * 32 + 255) / 256) * 256;  // allocated per warp
+  const int by_regs = regs_warp > 0 ? (regs_sm / regs_warp) / warps : blk_sm;
+  const size_t smem_blk = dyn_smem + fa.sharedSizeBytes + (size_t)reserved;
+  const int by_smem = (int)((size_t)smem_sm / std::max<size_t>(smem_blk, 1));
+  const int by_thr = thr_sm / (warps * 32);
+  return std::max(1, std::min(std::min(by_regs, by_smem), std::min(by_thr, blk_sm)));
+}
+
 int batch_run(ztm_ctx* c, const ztm_job* jobs, int njobs, bool dev, double G, double nq,
               int stage_kb, int tlog2, int variant) {
   const BatchFn kfn = batch_fn(variant);
-  Plan p = plan(jobs, njobs, nq, c->num_sms, stage_kb, tlog2, BATCH_VARIANTS[variant][0]);
+  const bool tc = BATCH_VARIANTS[variant][2] != 0;
+  Plan p = plan(jobs, njobs, nq, c->num_sms, stage_kb, tlog2, BATCH_VARIANTS[variant][0], tc);
   if (p.smem > 200 * 1024) return ztm_fail(c, ZTM_ERR_RANGE, "near box too large for a batch");
   size_t stage_bytes = 0;
   if (!dev)
@@ -638,7 +1056,10 @@ int batch_run(ztm_ctx* c, const ztm_job* jobs, int njobs, bool dev, double G, do
   cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)std::max<size_t>(p.smem, 48 * 1024));
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, B_TS, p.smem);
+  if (tc)  // the occupancy query answers 1 for a kernel that allocates TMEM
+    per_sm = std::min<int>(resident_blocks(c, kfn, B_TS, p.smem), 512 / TC_COLS);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, B_TS, p.smem);
   per_sm = std::max(1, per_sm);
   const long long grid = std::min<long long>((long long)per_sm * c->num_sms, p.n_items);
   const int phi_cap = std::max(p.phi_cap, 1);
@@ -678,8 +1099,10 @@ int batch_run(ztm_ctx* c, const ztm_job* jobs, int njobs, bool dev, double G, do
     J.sxyz = xyz_d[j];
     J.gz = gz_d[j];
     J.G5 = G * 1.0e5;
-    float* rhoT = wc.take<float>((size_t)J.mgroups * J.mgw * J.k.ncols * J.k.nzp);
-    J.rhoT = rhoT;
+    float* rhoT = wc.take<float>((size_t)J.mgroups * J.k.ncols *
+                                 (J.tc ? (size_t)J.nzt * TC_N : (size_t)J.k.nzp * J.mgw));
+    J.rhoT = J.tc ? nullptr : rhoT;
+    J.rhoC = J.tc ? rhoT : nullptr;
     float4* sf = wc.take<float4>(J.ns);
     int4* si = wc.take<int4>(J.ns);
     J.sf = sf;
@@ -737,6 +1160,7 @@ int batch_run(ztm_ctx* c, const ztm_job* jobs, int njobs, bool dev, double G, do
     args.n_items = p.n_items;
     args.counter = counter;
     args.err = c->d_err;
+    args.drain = tc ? std::max(1, stage_kb) : 1;
     ZtmGraphEntry e;
     e.key = key;
     cudaGraph_t g = nullptr;
@@ -746,7 +1170,12 @@ int batch_run(ztm_ctx* c, const ztm_job* jobs, int njobs, bool dev, double G, do
       return rc;
     for (int j = 0; j < njobs; j++) {
       BJob& J = p.jobs[j];
-      {
+      if (J.tc) {
+        const long long total = (long long)J.mgroups * J.k.ncols * J.nzt * TC_N;
+        const int blocks = (int)std::min<long long>((total + 255) / 256, 32LL * c->num_sms);
+        transpose_models_tc_kernel<<<std::max(blocks, 1), 256, 0, c->stream>>>(
+            J.k, J.nmodels, J.nzt, J.rho, const_cast<float*>(J.rhoC));
+      } else {
         const long long total = (long long)J.mgroups * J.mgw * J.k.ncols * J.k.nzp;
         const int blocks = (int)std::min<long long>((total + 255) / 256, 32LL * c->num_sms);
         transpose_models_kernel<<<std::max(blocks, 1), 256, 0, c->stream>>>(
