@@ -360,9 +360,12 @@ __device__ bool far_item_cc(const BJob& J, int tile, int chunk, int mg, uint64_t
         const float* col = rs + q * k.nzp * J.mgw;
         const ColPoly2 cp2 = col_poly2(cp, fc.a1);
         const float2 c2t = make_float2(cp.C2 - fc.h2, cp.C2 - fc.h2);
+        // padded layers (l >= nz) need the mask only below the mesh: for a
+        // station with izs < nz their Z is at least half a layer, so K is
+        // finite there and the zero densities add nothing
         const unsigned am = __activemask();
         const int form = (__all_sync(am, cp.rh >= k.rh_t2) ? 1 : 0) |
-                         ((__any_sync(am, ncl) || (k.nz & 7)) ? 2 : 0);
+                         ((__any_sync(am, ncl || ((k.nz & 7) && izs >= k.nz))) ? 2 : 0);
         if (MG == 1 || J.mgw == 1) {
           switch (form) {
             case 0: far_column<1, false, false>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc); break;
@@ -666,8 +669,9 @@ __device__ bool far_item_tc(const BJob& J, int tile, int chunk, int mg, TcState&
     }
     const ColPoly2 cp2 = col_poly2(cp, fc.a1);
     const float2 c2t = make_float2(cp.C2 - fc.h2, cp.C2 - fc.h2);
-    const int form = (__all_sync(0xffffffffu, !active || cp.rh >= k.rh_t2) ? 1 : 0) |
-                     ((__any_sync(0xffffffffu, ncl) || (k.nz & (TC_KB - 1))) ? 2 : 0);
+    const int form =
+        (__all_sync(0xffffffffu, !active || cp.rh >= k.rh_t2) ? 1 : 0) |
+        (__any_sync(0xffffffffu, ncl || (active && (k.nz & (TC_KB - 1)) && izs >= k.nz)) ? 2 : 0);
     float zf = (float)(-izs);
     for (int kb = 0; kb < nkb; kb++, zf += (float)TC_KB) {
       const unsigned n = ts.kblk, b = n & 1u;
