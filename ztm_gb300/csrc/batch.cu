@@ -471,26 +471,33 @@ __global__ void __launch_bounds__(B_TS, MINB) batch_kernel(BArgs a) {
 // D[:, m] + D[:, 32 + m] carries K rho_m to about 2^-22 of each product (the
 // dropped lo x lo term and the TF32 rounding of the low parts).  The tensor
 // core's FP32 accumulation truncates: every add into an accumulator loses
-// about half a unit in its last place, toward zero.  So the small cross
-// products have their own accumulator, the main one takes one add per 8
-// layers, and every `drain` k-blocks (default 4: 8 adds, a bias of about
-// 2e-7 of the window's sum) the accumulators are read back (tcgen05.ld) and
-// added to the thread's compensated sums in registers.  (Two adds per 8
-// layers and 32 per window measured 1.6e-6 on the 256x256x64 line search.)
+// about half a unit in its last place, toward zero.  So the main products
+// D[:, 0:32] take one add per 8 layers, and every `drain` k-blocks (default
+// 4: 8 adds, a bias of about 2e-7 of the window's sum) they are read back
+// (tcgen05.ld) and added to the thread's compensated sums in registers.  The
+// cross products D[:, 32:64] (terms about 2^-11 of the main ones, of random
+// sign) accumulate over the whole item and are read once at its end.  (Two
+// adds into the main accumulator per 8 layers and 32 per window measured
+// 1.6e-6 on the 256x256x64 line search.)
+//
+// On this tensor core an MMA of N <= 64 costs about 47 cycles of issue for
+// K = 8 (N = 256 about 130): the tensor pipe is not the limit here, the
+// threads' K evaluation is, so the block is sized for occupancy (128 TMEM
+// columns and 128 registers a thread: four blocks per SM).
 //
 // B comes from HBM ready in the MMA's shared-memory layout (see
 // transpose_models_tc_kernel), one 1-D bulk copy per column into a ring of
-// TC_NS stages, issued two columns ahead.  Synchronisation, per block:
+// TC_NS stages, issued one column ahead.  Synchronisation, per block:
 //   stage[i]  bulk copy of a column landed (thread 0 waits before its MMAs);
 //   mma[b]    tcgen05.commit after the MMAs that read A buffer b: every thread
 //             waits for k-block n - 2 before writing buffer n & 1, and the
 //             drain waits for the last k-block before reading D.  Waiting for
 //             k-block n - 2 also frees the stage of column c - 2 (commits
-//             complete in order), which is the stage the copy issued at the
-//             start of column c fills.
+//             complete in order, and a column has at least one k-block), which
+//             is the stage the copy issued at the start of column c fills.
 constexpr int TC_MG = 32;           // models per tensor-core group
 constexpr int TC_N = 2 * TC_MG;     // rows of B: the high parts, then the low parts
-constexpr int TC_NS = 4;            // column stages
+constexpr int TC_NS = 3;            // column stages
 constexpr int TC_KB = 16;           // layers per k-block (two MMA steps of K = 8)
 constexpr uint32_t TC_COLS = 128;   // TMEM columns: D [0, 64), A buffer b at 64 + 32 b
 constexpr uint32_t TC_IDESC = tc_idesc_tf32(128, TC_MG);
@@ -577,7 +584,7 @@ __device__ __forceinline__ void tc_kblock(const MeshConst& k, const ColPoly2& cp
         if ((la < Lm && (unsigned)(la - elo) <= espan) || la >= k.nz) K.x = 0.f;
         if ((lb < Lm && (unsigned)(lb - elo) <= espan) || lb >= k.nz) K.y = 0.f;
       }
-      const uint32_t hx = tf32_rna(K.x), hy = tf32_rna(K.y);
+      const uint32_t hx = tf32_round_bits(K.x), hy = tf32_round_bits(K.y);
       const float2 L = __ffma2_rn(make_float2(-1.f, -1.f),
                                   make_float2(__uint_as_float(hx), __uint_as_float(hy)), K);
       hi[8 * h + 2 * j] = hx;
@@ -625,10 +632,7 @@ __device__ bool far_item_tc(const BJob& J, int tile, int chunk, int mg, TcState&
              J.rhoC + ((size_t)mg * k.ncols + c0 + q) * col_floats, col_bytes, bar);
     ts.issued = g + 1;
   };
-  if (tid == 0) {
-    issue(0);
-    if (ncol > 1) issue(1);
-  }
+  if (tid == 0) issue(0);
   __syncthreads();
   const int Lm = min(*s_lm, k.nz);
   const FarCoef fc = k.fc;
@@ -636,19 +640,28 @@ __device__ bool far_item_tc(const BJob& J, int tile, int chunk, int mg, TcState&
   float as[TC_MG], ac[TC_MG];
 #pragma unroll
   for (int m = 0; m < TC_MG; m++) as[m] = ac[m] = 0.f;
-  // add D (the products since the last drain) to the compensated sums
-  auto drain_d = [&](unsigned nl) {
+  // add the main products since the last drain (with cross, the item's cross
+  // products too) to the compensated sums, once k-block nl's MMAs (and so all
+  // before them) have completed
+  auto drain_d = [&](unsigned nl, bool cross) {
     if (!mbar_wait(&tb->mma[nl & 1u], (nl >> 1) & 1u)) *s_to = 1;
     tc_fence_after();
 #pragma unroll
     for (int h = 0; h < TC_MG / 16; h++) {
-      uint32_t d0[16], d1[16];
+      uint32_t d0[16];
       tmem_ld16(tmem + lane_off + 16 * h, d0);
-      tmem_ld16(tmem + lane_off + TC_MG + 16 * h, d1);
       tmem_wait_ld();
+      float v[16];
 #pragma unroll
-      for (int j = 0; j < 16; j++)
-        kahan_reg(as[16 * h + j], ac[16 * h + j], __uint_as_float(d0[j]) + __uint_as_float(d1[j]));
+      for (int j = 0; j < 16; j++) v[j] = __uint_as_float(d0[j]);
+      if (cross) {
+        tmem_ld16(tmem + lane_off + TC_MG + 16 * h, d0);
+        tmem_wait_ld();
+#pragma unroll
+        for (int j = 0; j < 16; j++) v[j] += __uint_as_float(d0[j]);
+      }
+#pragma unroll
+      for (int j = 0; j < 16; j++) kahan_reg(as[16 * h + j], ac[16 * h + j], v[j]);
     }
   };
   bool pending = false;  // D holds products not yet drained
@@ -679,7 +692,7 @@ __device__ bool far_item_tc(const BJob& J, int tile, int chunk, int mg, TcState&
         if (!mbar_wait(&tb->mma[b], ((n >> 1) - 1u) & 1u)) *s_to = 1;
         tc_fence_after();
       }
-      if (tid == 0 && kb == 0 && q + 2 < ncol) issue(q + 2);
+      if (tid == 0 && kb == 0 && q + 1 < ncol) issue(q + 1);
       uint32_t hi[16], lo[16];
       switch (form) {
         case 0: tc_kblock<false, false>(k, cp2, c2t, ez, zf, kb * TC_KB, Lm, elo, espan, hi, lo); break;
@@ -700,8 +713,9 @@ __device__ bool far_item_tc(const BJob& J, int tile, int chunk, int mg, TcState&
         if (!mbar_wait(&tb->stage[g % TC_NS], (g / TC_NS) & 1u)) *s_to = 1;
         ts.waited = g + 1;
       }
-      const bool first = (q * nkb + kb) % drain == 0;
-      if (first && pending) drain_d(n - 1u);
+      const int ki = q * nkb + kb;
+      const bool first = ki % drain == 0;
+      if (first && pending) drain_d(n - 1u, false);
       tc_fence_before();
       __syncthreads();
       if (*s_to) return false;
@@ -715,9 +729,8 @@ __device__ bool far_item_tc(const BJob& J, int tile, int chunk, int mg, TcState&
           const uint32_t bl = bh + (TC_MG / 8) * 128u;     // rows 32..63: B_lo
           const uint64_t dh = tc_smem_desc(bh, TC_N * 16u, 128u);
           const uint64_t dl = tc_smem_desc(bl, TC_N * 16u, 128u);
-          const uint32_t acc = (first && st == 0) ? 0u : 1u;
-          tc_mma_ts(tmem, abuf + 8u * st, dh, TC_IDESC, acc);
-          tc_mma_ts(tmem + TC_MG, abuf + 8u * st, dl, TC_IDESC, acc);
+          tc_mma_ts(tmem, abuf + 8u * st, dh, TC_IDESC, (first && st == 0) ? 0u : 1u);
+          tc_mma_ts(tmem + TC_MG, abuf + 8u * st, dl, TC_IDESC, (ki == 0 && st == 0) ? 0u : 1u);
           tc_mma_ts(tmem + TC_MG, abuf + 16u + 8u * st, dh, TC_IDESC, 1u);
         }
         tc_commit(&tb->mma[b]);
@@ -731,7 +744,7 @@ __device__ bool far_item_tc(const BJob& J, int tile, int chunk, int mg, TcState&
     }
   }
   ts.gcol = g0 + (unsigned)ncol;
-  if (pending) drain_d(ts.kblk - 1u);
+  if (pending) drain_d(ts.kblk - 1u, true);
   tc_fence_before();
   __syncthreads();  // every thread has read D before the next item overwrites it
   if (*s_to) return false;
@@ -917,7 +930,7 @@ void destroy_entry(ZtmGraphEntry& e) {
 // Kernel variants: {models per far item, blocks per SM asked of the
 // compiler, tensor cores}.  Variants 0-3 run every far item on the CUDA
 // cores; variant 4 runs the far items of multi-model jobs on the tensor cores.
-constexpr int BATCH_VARIANTS[][3] = {{16, 4, 0}, {16, 5, 0}, {8, 6, 0}, {32, 3, 0}, {TC_MG, 3, 1}};
+constexpr int BATCH_VARIANTS[][3] = {{16, 4, 0}, {16, 5, 0}, {8, 6, 0}, {32, 3, 0}, {TC_MG, 4, 1}};
 constexpr int BATCH_TC_VARIANT = 4;
 using BatchFn = void (*)(BArgs);
 BatchFn batch_fn(int v) {
@@ -925,7 +938,7 @@ BatchFn batch_fn(int v) {
     case 1: return batch_kernel<16, 5>;
     case 2: return batch_kernel<8, 6>;
     case 3: return batch_kernel<32, 3>;
-    case 4: return batch_tc_kernel<3>;
+    case 4: return batch_tc_kernel<4>;
     default: return batch_kernel<16, 4>;
   }
 }

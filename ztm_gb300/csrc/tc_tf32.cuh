@@ -116,4 +116,11 @@ __device__ __forceinline__ uint32_t tf32_rna(float x) {
   return r;
 }
 
+// The same rounding by integer arithmetic on the bits (add half a TF32 unit,
+// drop the 13 low mantissa bits), for finite x below the largest float:
+// two integer operations.
+__device__ __forceinline__ uint32_t tf32_round_bits(float x) {
+  return (__float_as_uint(x) + 0x1000u) & 0xFFFFE000u;
+}
+
 #endif  // __CUDACC__
