@@ -150,7 +150,8 @@ int ztm_ctx_profile_read(ztm_ctx* ctx, const char* name, double* ms,
                          long long* count);
 /* The autotuner's record: the candidates it timed since the context was
  * created (ZTM_FLAG_AUTOTUNE), four ints each -- for a batched launch (stage
- * KB per model group, log2 of the pairs per far item, kernel variant,
+ * KB per model group, or for the tensor-core variant 4 the 16-layer blocks
+ * per accumulator read-back; log2 of the pairs per far item; kernel variant;
  * microseconds); writes at most max_rows rows and returns how many it wrote
  * (negative on a bad argument). */
 int ztm_ctx_tuning(const ztm_ctx* ctx, int* rows, int max_rows);
