@@ -665,6 +665,7 @@ __device__ bool far_item_tc(const BJob& J, int tile, int chunk, int mg, TcState&
     }
   };
   bool pending = false;  // D holds products not yet drained
+  int win = 0;           // k-blocks into the current accumulation window
   int ix = c0 % k.nx, iy = c0 / k.nx;
   for (int q = 0; q < ncol; q++) {
     const float X = fmaf((float)(ixs - ix), k.dxn, ex);
@@ -700,10 +701,8 @@ __device__ bool far_item_tc(const BJob& J, int tile, int chunk, int mg, TcState&
         case 2: tc_kblock<false, true>(k, cp2, c2t, ez, zf, kb * TC_KB, Lm, elo, espan, hi, lo); break;
         default: tc_kblock<true, true>(k, cp2, c2t, ez, zf, kb * TC_KB, Lm, elo, espan, hi, lo);
       }
-      if (!active) {
-#pragma unroll
-        for (int j = 0; j < 16; j++) hi[j] = lo[j] = 0u;
-      }
+      // (a thread without a station writes whatever it computed: its TMEM
+      // row only reaches its own row of D, which is never read)
       const uint32_t abuf = tmem + 64u + 32u * b;
       tmem_st16(abuf + lane_off, hi);
       tmem_st16(abuf + lane_off + 16u, lo);
@@ -713,8 +712,8 @@ __device__ bool far_item_tc(const BJob& J, int tile, int chunk, int mg, TcState&
         if (!mbar_wait(&tb->stage[g % TC_NS], (g / TC_NS) & 1u)) *s_to = 1;
         ts.waited = g + 1;
       }
-      const int ki = q * nkb + kb;
-      const bool first = ki % drain == 0;
+      const bool first = win == 0;  // the k-block opens an accumulation window
+      if (++win == drain) win = 0;
       if (first && pending) drain_d(n - 1u, false);
       tc_fence_before();
       __syncthreads();
@@ -730,7 +729,7 @@ __device__ bool far_item_tc(const BJob& J, int tile, int chunk, int mg, TcState&
           const uint64_t dh = tc_smem_desc(bh, TC_N * 16u, 128u);
           const uint64_t dl = tc_smem_desc(bl, TC_N * 16u, 128u);
           tc_mma_ts(tmem, abuf + 8u * st, dh, TC_IDESC, (first && st == 0) ? 0u : 1u);
-          tc_mma_ts(tmem + TC_MG, abuf + 8u * st, dl, TC_IDESC, (ki == 0 && st == 0) ? 0u : 1u);
+          tc_mma_ts(tmem + TC_MG, abuf + 8u * st, dl, TC_IDESC, (!pending && st == 0) ? 0u : 1u);
           tc_mma_ts(tmem + TC_MG, abuf + 16u + 8u * st, dh, TC_IDESC, 1u);
         }
         tc_commit(&tb->mma[b]);
