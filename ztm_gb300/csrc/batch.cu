@@ -23,6 +23,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 
 #include "prism_common.cuh"
@@ -686,57 +687,65 @@ __device__ bool far_item_tc(const BJob& J, int tile, int chunk, int mg, TcState&
     const int form =
         (__all_sync(0xffffffffu, !active || cp.rh >= k.rh_t2) ? 1 : 0) |
         (__any_sync(0xffffffffu, ncl || (active && (k.nz & (TC_KB - 1)) && izs >= k.nz)) ? 2 : 0);
-    float zf = (float)(-izs);
-    for (int kb = 0; kb < nkb; kb++, zf += (float)TC_KB) {
-      const unsigned n = ts.kblk, b = n & 1u;
-      if (n >= 2) {  // the MMAs that read A buffer b (k-block n - 2) are done
-        if (!mbar_wait(&tb->mma[b], ((n >> 1) - 1u) & 1u)) *s_to = 1;
-        tc_fence_after();
-      }
-      if (tid == 0 && kb == 0 && q + 1 < ncol) issue(q + 1);
-      uint32_t hi[16], lo[16];
-      switch (form) {
-        case 0: tc_kblock<false, false>(k, cp2, c2t, ez, zf, kb * TC_KB, Lm, elo, espan, hi, lo); break;
-        case 1: tc_kblock<true, false>(k, cp2, c2t, ez, zf, kb * TC_KB, Lm, elo, espan, hi, lo); break;
-        case 2: tc_kblock<false, true>(k, cp2, c2t, ez, zf, kb * TC_KB, Lm, elo, espan, hi, lo); break;
-        default: tc_kblock<true, true>(k, cp2, c2t, ez, zf, kb * TC_KB, Lm, elo, espan, hi, lo);
-      }
-      // (a thread without a station writes whatever it computed: its TMEM
-      // row only reaches its own row of D, which is never read)
-      const uint32_t abuf = tmem + 64u + 32u * b;
-      tmem_st16(abuf + lane_off, hi);
-      tmem_st16(abuf + lane_off + 16u, lo);
-      tmem_wait_st();
-      if (tid == 0 && kb == 0) {  // this column's densities in shared memory
-        const unsigned g = g0 + (unsigned)q;
-        if (!mbar_wait(&tb->stage[g % TC_NS], (g / TC_NS) & 1u)) *s_to = 1;
-        ts.waited = g + 1;
-      }
-      const bool first = win == 0;  // the k-block opens an accumulation window
-      if (++win == drain) win = 0;
-      if (first && pending) drain_d(n - 1u, false);
-      tc_fence_before();
-      __syncthreads();
-      if (*s_to) return false;
-      if (tid == 0) {
-        tc_fence_after();
-        const uint32_t sb = smem_u32(stage + ((g0 + q) % TC_NS) * col_floats) +
-                            (uint32_t)kb * 2u * (8u * TC_N * 4u);
-#pragma unroll
-        for (int st = 0; st < 2; st++) {
-          const uint32_t bh = sb + st * (8u * TC_N * 4u);  // rows 0..31: B_hi
-          const uint32_t bl = bh + (TC_MG / 8) * 128u;     // rows 32..63: B_lo
-          const uint64_t dh = tc_smem_desc(bh, TC_N * 16u, 128u);
-          const uint64_t dl = tc_smem_desc(bl, TC_N * 16u, 128u);
-          tc_mma_ts(tmem, abuf + 8u * st, dh, TC_IDESC, (first && st == 0) ? 0u : 1u);
-          tc_mma_ts(tmem + TC_MG, abuf + 8u * st, dl, TC_IDESC, (!pending && st == 0) ? 0u : 1u);
-          tc_mma_ts(tmem + TC_MG, abuf + 16u + 8u * st, dh, TC_IDESC, 1u);
+    // the column's k-blocks, with the form (a compile-time choice of the
+    // expansion order and of the near/pad mask) fixed for the whole column
+    auto column = [&](auto t2c, auto maskc) {
+      constexpr bool T2 = decltype(t2c)::value, MASK = decltype(maskc)::value;
+      const unsigned g = g0 + (unsigned)q, si = g % TC_NS;
+      // B of the column's first 8 layers; the k-steps follow 2048 bytes
+      // (128 descriptor units) apart, the low parts' rows 512 bytes (32
+      // units) after the high parts'
+      const uint64_t dcol = tc_smem_desc(smem_u32(stage + si * col_floats), TC_N * 16u, 128u);
+      float zf = (float)(-izs);
+      for (int kb = 0; kb < nkb; kb++, zf += (float)TC_KB) {
+        const unsigned n = ts.kblk, b = n & 1u;
+        if (n >= 2) {  // the MMAs that read A buffer b (k-block n - 2) are done
+          if (!mbar_wait(&tb->mma[b], ((n >> 1) - 1u) & 1u)) *s_to = 1;
+          tc_fence_after();
         }
-        tc_commit(&tb->mma[b]);
+        if (tid == 0 && kb == 0 && q + 1 < ncol) issue(q + 1);
+        uint32_t hi[16], lo[16];
+        tc_kblock<T2, MASK>(k, cp2, c2t, ez, zf, kb * TC_KB, Lm, elo, espan, hi, lo);
+        // (a thread without a station writes whatever it computed: its TMEM
+        // row only reaches its own row of D, which is never read)
+        const uint32_t abuf = tmem + 64u + 32u * b;
+        tmem_st16(abuf + lane_off, hi);
+        tmem_st16(abuf + lane_off + 16u, lo);
+        tmem_wait_st();
+        if (tid == 0 && kb == 0) {  // this column's densities in shared memory
+          if (!mbar_wait(&tb->stage[si], (g / TC_NS) & 1u)) *s_to = 1;
+          ts.waited = g + 1;
+        }
+        const bool first = win == 0;  // the k-block opens an accumulation window
+        if (++win == drain) win = 0;
+        if (first && pending) drain_d(n - 1u, false);
+        tc_fence_before();
+        __syncthreads();
+        if (*s_to) return false;
+        if (tid == 0) {
+          tc_fence_after();
+          const uint64_t d = dcol + (uint64_t)(kb * 256);
+          tc_mma_ts(tmem, abuf, d, TC_IDESC, first ? 0u : 1u);
+          tc_mma_ts(tmem + TC_MG, abuf, d + 32u, TC_IDESC, pending ? 1u : 0u);
+          tc_mma_ts(tmem + TC_MG, abuf + 16u, d, TC_IDESC, 1u);
+          tc_mma_ts(tmem, abuf + 8u, d + 128u, TC_IDESC, 1u);
+          tc_mma_ts(tmem + TC_MG, abuf + 8u, d + 160u, TC_IDESC, 1u);
+          tc_mma_ts(tmem + TC_MG, abuf + 24u, d + 128u, TC_IDESC, 1u);
+          tc_commit(&tb->mma[b]);
+        }
+        ts.kblk = n + 1u;
+        pending = true;
       }
-      ts.kblk = n + 1u;
-      pending = true;
+      return true;
+    };
+    bool ok;
+    switch (form) {
+      case 0: ok = column(std::false_type{}, std::false_type{}); break;
+      case 1: ok = column(std::true_type{}, std::false_type{}); break;
+      case 2: ok = column(std::false_type{}, std::true_type{}); break;
+      default: ok = column(std::true_type{}, std::true_type{});
     }
+    if (!ok) return false;
     if (++ix == k.nx) {
       ix = 0;
       ++iy;
