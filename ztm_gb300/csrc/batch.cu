@@ -513,32 +513,44 @@ constexpr uint32_t TC_IDESC = tc_idesc_tf32(128, TC_MG);
 // models.  A column is one contiguous range (one bulk copy), and 8 layers of
 // it are one MMA step's B operand with LBO = TC_N * 16 bytes (kc stride) and
 // SBO = 128 bytes (ng stride).
-__global__ void transpose_models_tc_kernel(MeshConst k, int nmodels, int nzt,
-                                           const double* __restrict__ rho,
-                                           float* __restrict__ rhoC) {
+__global__ void __launch_bounds__(256) transpose_models_tc_kernel(MeshConst k, int nmodels,
+                                                                    int nzt,
+                                                                    const double* __restrict__ rho,
+                                                                    float* __restrict__ rhoC) {
+  // a block per (model group, 8-layer block lb, 16 consecutive columns): the
+  // 32 models x 8 layers x 16 columns are read along the columns (coalesced)
+  // into shared memory, then each column's 8-layer block (64 rows x 8 layers,
+  // 2 KB, contiguous in rhoC) is written by consecutive threads
+  __shared__ double t[TC_MG * 8][17];
+  const int nlb = nzt / 8, ncb = (k.ncols + 15) / 16;
   const int ngroups = (nmodels + TC_MG - 1) / TC_MG;
-  const long long per_col = (long long)nzt * TC_N;
-  const long long total = (long long)ngroups * k.ncols * per_col;
   const long long np = (long long)k.ncols * k.nz;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
-       t += (long long)gridDim.x * blockDim.x) {
-    const int e = (int)(t % per_col);
-    const long long gc = t / per_col;
-    const int c = (int)(gc % k.ncols), g = (int)(gc / k.ncols);
-    const int kk = e & 3, nr = (e >> 2) & 7;
-    int r = e >> 5;
-    const int ng = r % (TC_N / 8);
-    r /= TC_N / 8;
-    const int kc = r & 1, lb = r >> 1;
-    const int l = lb * 8 + kc * 4 + kk, n = ng * 8 + nr;
-    const int md = g * TC_MG + n % TC_MG;
-    float v = 0.f;
-    if (l < k.nz && md < nmodels) {
-      const double x = rho[(long long)md * np + (long long)l * k.ncols + c];
-      const float h = __uint_as_float(tf32_rna((float)x));
-      v = n < TC_MG ? h : __uint_as_float(tf32_rna((float)(x - (double)h)));
+  const long long nblk = (long long)ngroups * nlb * ncb;
+  for (long long blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
+    const int cb = (int)(blk % ncb);
+    const int lb = (int)((blk / ncb) % nlb);
+    const int g = (int)(blk / ((long long)ncb * nlb));
+    const int c0 = cb * 16;
+    __syncthreads();
+    for (int e = threadIdx.x; e < TC_MG * 8 * 16; e += 256) {
+      const int cc = e & 15, row = e >> 4;  // row = m * 8 + layer within the block
+      const int m = row >> 3, l = lb * 8 + (row & 7), md = g * TC_MG + m, c = c0 + cc;
+      double v = 0.0;
+      if (md < nmodels && l < k.nz && c < k.ncols) v = rho[(long long)md * np + (long long)l * k.ncols + c];
+      t[row][cc] = v;
     }
-    rhoC[t] = v;
+    __syncthreads();
+    for (int e = threadIdx.x; e < 16 * 8 * TC_N; e += 256) {
+      const int cc = e / (8 * TC_N), w = e % (8 * TC_N);  // w: position in the column's block
+      const int c = c0 + cc;
+      if (c >= k.ncols) continue;
+      const int kk = w & 3, nr = (w >> 2) & 7, ng = (w >> 5) % (TC_N / 8), kc = (w >> 5) / (TC_N / 8);
+      const int n = ng * 8 + nr, m = n % TC_MG, lw = kc * 4 + kk;
+      const double x = t[m * 8 + lw][cc];
+      const float h = __uint_as_float(tf32_rna((float)x));
+      const float v = n < TC_MG ? h : __uint_as_float(tf32_rna((float)(x - (double)h)));
+      rhoC[(((long long)g * k.ncols + c) * nlb + lb) * (8 * TC_N) + w] = v;
+    }
   }
 }
 
@@ -1196,8 +1208,8 @@ int batch_run(ztm_ctx* c, const ztm_job* jobs, int njobs, bool dev, double G, do
     for (int j = 0; j < njobs; j++) {
       BJob& J = p.jobs[j];
       if (J.tc) {
-        const long long total = (long long)J.mgroups * J.k.ncols * J.nzt * TC_N;
-        const int blocks = (int)std::min<long long>((total + 255) / 256, 32LL * c->num_sms);
+        const long long nblk = (long long)J.mgroups * (J.nzt / 8) * ((J.k.ncols + 15) / 16);
+        const int blocks = (int)std::min<long long>(nblk, 16LL * c->num_sms);
         transpose_models_tc_kernel<<<std::max(blocks, 1), 256, 0, c->stream>>>(
             J.k, J.nmodels, J.nzt, J.rho, const_cast<float*>(J.rhoC));
       } else {
