@@ -59,3 +59,21 @@ def test_batch_autotuned_shape_gives_the_same_field(ctx):
     again = ctx.batch([(mesh, models, st)], autotune=True)[0]
     assert rel_err(tuned, ref) <= 1e-6
     assert np.array_equal(tuned, again)
+
+
+def test_batch_awkward_stations_with_padded_layers(ctx):
+    """Multi-model far items (tensor cores) with 13 layers (padded to 16) and
+    stations on faces, edges and vertices, inside the mesh and below it (one
+    at the centre of the first padding layer under a column, where the
+    padded layer's far-field value would be 0/0 without the mask): every
+    model against its single mixed call."""
+    from helpers import awkward_stations
+    rng = np.random.default_rng(11)
+    mesh, rho = small_mesh(20, 18, 13, seed=12)
+    models = np.stack([rho * (1.0 + 0.07 * k) + rng.normal(0, 3, rho.size) for k in range(5)])
+    st = awkward_stations(mesh, n_random=150, seed=13)
+    out = ctx.batch([(mesh, models, st)])[0]
+    assert np.all(np.isfinite(out))
+    for k in range(models.shape[0]):
+        ref = ctx.prism(mesh, models[k], st, precision="mixed")
+        assert rel_err(out[k], ref) <= 1e-6, k

@@ -220,6 +220,11 @@ __device__ void near_item(const BJob& J, int tile, double* phi_all, int phi_cap,
     const int slot = tile * B_TS + j;
     if (slot >= J.ns) break;
     const int s = J.perm[slot];
+    if (J.nmodels == 1) {  // one model: the forward's vertex pass (Phi only where
+                           // the region's signed density difference is not zero)
+      near_station<double>(J.k, m, s, J.sxyz, J.si, J.iv, J.lr, J.rho, J.near, lane);
+      continue;
+    }
     const int2 L = J.lr[s];
     if (L.x > L.y) {  // no near prism
       for (int md = lane; md < J.nmodels; md += 32) J.near[(size_t)md * J.ns + s] = 0.0;

@@ -174,6 +174,71 @@ __device__ __forceinline__ int near_slot(const NearBox& b, int ix, int iy) {
   return (ix - b.x0) + (b.x1 - b.x0 + 1) * (iy - b.y0);
 }
 
+// Near region of station s in T (double: the mixed method; float: the FP32
+// method), by one warp: Phi once per vertex of the region times the signed
+// triple difference of the region's densities around the vertex; lane 0
+// writes out[s].
+template <typename T>
+__device__ __forceinline__ void near_station(const MeshConst& k, const MeshDesc& m, int s,
+                                             const double* __restrict__ sxyz,
+                                             const int4* __restrict__ si,
+                                             const short2* __restrict__ iv,
+                                             const int2* __restrict__ lr,
+                                             const double* __restrict__ rho,
+                                             double* __restrict__ out, int lane,
+                                             unsigned* nphi = nullptr) {
+  const NearBox b = near_box(si[s], k);
+  const int2 L = lr[s];
+  if (L.x > L.y) {  // no near prism
+    if (lane == 0) out[s] = 0.0;
+    return;
+  }
+  const short2* ivs = iv + (size_t)s * k.nslots;
+  const double xs = sxyz[3 * s], ys = sxyz[3 * s + 1], zs = sxyz[3 * s + 2];
+  const int nvx = b.x1 - b.x0 + 2, nvy = b.y1 - b.y0 + 2, nvz = L.y - L.x + 2;
+  const int nv = nvx * nvy * nvz;
+  const long long plane = (long long)m.nx * m.ny;
+  T acc = T(0);
+  for (int v = lane; v < nv; v += 32) {
+    const int a = b.x0 + v % nvx;
+    const int bb = b.y0 + (v / nvx) % nvy;
+    const int cz = L.x + v / (nvx * nvy);
+    // signed triple difference of the region's density around vertex
+    // (a, bb, cz): prism ix = a-1 has the vertex as its upper x limit (+),
+    // ix = a lower (-); layer l = cz has it as its upper z limit (+), l = cz-1
+    // lower (-).
+    double D = 0.0;
+#pragma unroll
+    for (int da = 0; da < 2; da++) {
+      const int ix = a - 1 + da;
+      if (ix < b.x0 || ix > b.x1) continue;
+#pragma unroll
+      for (int db = 0; db < 2; db++) {
+        const int iy = bb - 1 + db;
+        if (iy < b.y0 || iy > b.y1) continue;
+        const short2 t = ivs[near_slot(b, ix, iy)];
+#pragma unroll
+        for (int dc = 0; dc < 2; dc++) {
+          const int l = cz - 1 + dc;
+          if (l < t.x || l > t.y) continue;
+          const double r = rho[ix + (long long)m.nx * iy + plane * l];
+          const int neg = (da == 1) ^ (db == 1) ^ (dc == 0);
+          D += neg ? -r : r;
+        }
+      }
+    }
+    if (D != 0.0) {
+      const T x = (T)((m.x0 + a * m.dx) - xs);
+      const T y = (T)((m.y0 + bb * m.dy) - ys);
+      const T z = (T)((m.zt - cz * m.dz) - zs);
+      acc += (T)D * ztm_phi<T>(x, y, z);
+      if (nphi) ++*nphi;
+    }
+  }
+  double tot = warp_sum_d((double)acc);
+  if (lane == 0) out[s] = tot;
+}
+
 // ---- host launchers (prism.cu) ------------------------------------------
 MeshConst make_mesh_const(const MeshDesc& m, double near_q);
 // Station-relative integer/float decomposition (computed in double once per
