@@ -168,10 +168,11 @@ int ztm_ctx_tuning(const ztm_ctx* ctx, int* rows, int max_rows);
 int ztm_ctx_count_forms(ztm_ctx* ctx, int enable);
 int ztm_ctx_form_counts(ztm_ctx* ctx, long long* counts);
 /* Test hook of the timeout path (no GPU fault involved).  With polls > 0,
- * every copy-arrival wait of the mixed prism forward's far kernel waits
- * instead on a barrier that nothing completes and gives up after `polls`
- * tests; each block then records a timeout, waits (with the full bound) for
- * the copies it has in flight and stops, and the call returns
+ * every copy-arrival wait of the mixed prism forward's far kernel, and of the
+ * tensor-core far items of the batched launch, waits instead on a barrier
+ * that nothing completes and gives up after `polls` tests; each block then
+ * records a timeout, waits (with the full bound) for the copies and MMAs it
+ * has in flight, frees its tensor memory and stops, and the call returns
  * ZTM_ERR_TIMEOUT.  polls = 0 switches the hook off; the context stays
  * usable throughout. */
 int ztm_ctx_test_timeout(ztm_ctx* ctx, unsigned int polls);

@@ -38,3 +38,26 @@ def test_timeout_is_reported_and_the_context_recovers(ctx):
                     precision="mixed")
     ctx.sync()
     assert rel_err(out.cpu().numpy(), ref) <= 1e-6
+
+
+def test_batched_tensor_core_timeout_frees_the_block_and_recovers(ctx):
+    """The tensor-core far items of the batched launch under the same hook:
+    the stage waits run out, each block waits for its copies and MMAs in
+    flight, frees its tensor memory and stops; the call reports the timeout
+    and the next batched call (hook off, a new graph) gives the field of
+    single calls, so no tensor memory was left allocated."""
+    rng = np.random.default_rng(3)
+    mesh, rho = small_mesh(64, 56, 16, seed=6)
+    models = np.stack([rho * (1.0 + 0.05 * k) + rng.normal(0, 2, rho.size) for k in range(8)])
+    st = awkward_stations(mesh, n_random=400)
+    ctx.test_timeout(4)
+    try:
+        with pytest.raises(ztm_gb300.GravityError) as e:
+            ctx.batch([(mesh, models, st)])
+        assert e.value.code == ztm_gb300.ERR_TIMEOUT
+    finally:
+        ctx.test_timeout(0)
+    out = ctx.batch([(mesh, models, st)])[0]
+    for k in (0, 7):
+        ref = ctx.prism(mesh, models[k], st, precision="mixed")
+        assert rel_err(out[k], ref) <= 1e-6

@@ -71,6 +71,8 @@ struct BArgs {
   int phi_cap;
   int phi_stride;  // doubles per warp: 2 phi_cap
   int drain;       // tensor-core items: k-blocks per accumulation window
+  unsigned poll_limit;  // test hook, 0 = off: the tensor-core items' stage
+                        // waits poll a barrier that nothing completes
 };
 
 // Float densities of a job, model-interleaved: rhoT[((g*ncols + c)*nzp + l)*W
@@ -563,6 +565,7 @@ struct TcBars {
   uint64_t stage[TC_NS];
   uint64_t mma[2];
   uint64_t fin;
+  uint64_t never;  // the timeout hook's barrier: nothing arrives on it
 };
 
 struct TcState {
@@ -615,7 +618,8 @@ __device__ __forceinline__ void tc_kblock(const MeshConst& k, const ColPoly2& cp
 
 // One tensor-core far item.  Returns false if a wait ran out (*s_to set).
 __device__ bool far_item_tc(const BJob& J, int tile, int chunk, int mg, TcState& ts,
-                            TcBars* tb, float* stage, int* s_to, int* s_lm, int drain) {
+                            TcBars* tb, float* stage, int* s_to, int* s_lm, int drain,
+                            unsigned poll_limit) {
   const MeshConst& k = J.k;
   const int tid = threadIdx.x;
   const uint32_t lane_off = (uint32_t)(32 * (tid >> 5)) << 16;
@@ -730,8 +734,13 @@ __device__ bool far_item_tc(const BJob& J, int tile, int chunk, int mg, TcState&
         tmem_st16(abuf + lane_off + 16u, lo);
         tmem_wait_st();
         if (tid == 0 && kb == 0) {  // this column's densities in shared memory
-          if (!mbar_wait(&tb->stage[si], (g / TC_NS) & 1u)) *s_to = 1;
-          ts.waited = g + 1;
+          // (the test hook waits on a barrier that nothing completes, with a
+          // short bound; a copy not waited for is waited for before the
+          // block stops)
+          const bool landed = poll_limit ? mbar_poll(&tb->never, 0u, poll_limit)
+                                         : mbar_wait(&tb->stage[si], (g / TC_NS) & 1u);
+          if (landed) ts.waited = g + 1;
+          else *s_to = 1;
         }
         const bool first = win == 0;  // the k-block opens an accumulation window
         if (++win == drain) win = 0;
@@ -811,6 +820,7 @@ __global__ void __launch_bounds__(B_TS, MINB) batch_tc_kernel(BArgs a) {
     mbar_init(&tb.mma[0], 1);
     mbar_init(&tb.mma[1], 1);
     mbar_init(&tb.fin, 1);
+    mbar_init(&tb.never, 1);
     fence_mbar_init();
     s_to = 0;
   }
@@ -844,7 +854,8 @@ __global__ void __launch_bounds__(B_TS, MINB) batch_tc_kernel(BArgs a) {
     r /= J.tiles;
     const int chunk = (int)(r % J.chunks);
     const int mg = (int)(r / J.chunks);
-    const bool ok = J.tc ? far_item_tc(J, tile, chunk, mg, ts, &tb, stage, &s_to, &s_lm, a.drain)
+    const bool ok = J.tc ? far_item_tc(J, tile, chunk, mg, ts, &tb, stage, &s_to, &s_lm, a.drain,
+                                       a.poll_limit)
                          : far_item_cc<1>(J, tile, chunk, mg, bar, stage, uses0, uses1, ks, kc,
                                           &s_lm);
     if (!ok) {
@@ -1166,6 +1177,7 @@ int batch_run(ztm_ctx* c, const ztm_job* jobs, int njobs, bool dev, double G, do
   key.push_back(stage_kb);
   key.push_back(tlog2);
   key.push_back(variant);
+  key.push_back((long long)c->stage_wait_limit);  // the timeout test hook is baked in
   for (int j = 0; j < njobs; j++) {
     const ztm_job& q = jobs[j];
     key.insert(key.end(), {q.mesh.nx, q.mesh.ny, q.mesh.nz, (long long)(q.mesh.dx * 1e3),
@@ -1203,6 +1215,7 @@ int batch_run(ztm_ctx* c, const ztm_job* jobs, int njobs, bool dev, double G, do
     args.counter = counter;
     args.err = c->d_err;
     args.drain = tc ? std::max(1, stage_kb) : 1;
+    args.poll_limit = tc ? c->stage_wait_limit : 0u;
     ZtmGraphEntry e;
     e.key = key;
     cudaGraph_t g = nullptr;
