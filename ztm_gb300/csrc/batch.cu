@@ -472,26 +472,29 @@ __global__ void __launch_bounds__(B_TS, MINB) batch_kernel(BArgs a) {
 // chunk, group of TC_MG = 32 models): each thread computes K for its station
 // as in far_column, 16 layers at a time, and writes them to its TMEM lane as
 // TF32 high and low parts (hi = nearest TF32 of K, lo = K - hi); one thread
-// issues per 8 layers (M 128, N 32, K 8 each)
-//   D[:, 0:32]  += A_hi x B_hi
-//   D[:, 32:64] += A_hi x B_lo,  D[:, 32:64] += A_lo x B_hi
+// issues per 8 layers two MMAs (M 128, K 8)
+//   D[:, 0:64]  += A_hi x [B_hi | B_lo]   (N 64: D[:, 0:32] += A_hi B_hi,
+//                                          D[:, 32:64] += A_hi B_lo)
+//   D[:, 32:64] += A_lo x B_hi            (N 32)
 // with B the group's densities split the same way (B_lo is rho - B_hi), so
 // D[:, m] + D[:, 32 + m] carries K rho_m to about 2^-22 of each product (the
 // dropped lo x lo term and the TF32 rounding of the low parts).  The tensor
 // core's FP32 accumulation truncates: every add into an accumulator loses
 // about half a unit in its last place, toward zero.  So the main products
 // D[:, 0:32] take one add per 8 layers, and every `drain` k-blocks (default
-// 4: 8 adds, a bias of about 2e-7 of the window's sum) they are read back
-// (tcgen05.ld) and added to the thread's compensated sums in registers.  The
-// cross products D[:, 32:64] (terms about 2^-11 of the main ones, of random
-// sign) accumulate over the whole item and are read once at its end.  (Two
-// adds into the main accumulator per 8 layers and 32 per window measured
-// 1.6e-6 on the 256x256x64 line search.)
+// 4: 8 adds, a bias of about 2e-7 of the window's sum) D is read back
+// (tcgen05.ld) and added to the thread's compensated sums in registers; the
+// cross products D[:, 32:64] (terms about 2^-11 of the main ones) have their
+// own columns.  (Two adds into the main accumulator per 8 layers and 32 per
+// window measured 1.6e-6 on the 256x256x64 line search.)
 //
 // On this tensor core an MMA of N <= 64 costs about 47 cycles of issue for
-// K = 8 (N = 256 about 130): the tensor pipe is not the limit here, the
-// threads' K evaluation is, so the block is sized for occupancy (128 TMEM
-// columns and 128 registers a thread: four blocks per SM).
+// K = 8 (N = 256 about 130), and one MMA's issue-to-mbarrier round trip
+// about 250 cycles: with four blocks sharing the SM's tensor core, the MMAs
+// of a k-block must complete within the next k-block's K evaluation, so
+// fewer and wider MMAs (two, not three, per 8 layers) help.  The block is
+// sized for occupancy (128 TMEM columns and 128 registers a thread: four
+// blocks per SM).
 //
 // B comes from HBM ready in the MMA's shared-memory layout (see
 // transpose_models_tc_kernel), one 1-D bulk copy per column into a ring of
@@ -509,6 +512,7 @@ constexpr int TC_NS = 3;            // column stages
 constexpr int TC_KB = 16;           // layers per k-block (two MMA steps of K = 8)
 constexpr uint32_t TC_COLS = 128;   // TMEM columns: D [0, 64), A buffer b at 64 + 32 b
 constexpr uint32_t TC_IDESC = tc_idesc_tf32(128, TC_MG);
+constexpr uint32_t TC_IDESC64 = tc_idesc_tf32(128, TC_N);
 
 // Densities of a tensor-core job in the MMA's B layout, one column after
 // another: per column, per 8 layers (lb), the two K halves (kc: layers
@@ -662,28 +666,20 @@ __device__ bool far_item_tc(const BJob& J, int tile, int chunk, int mg, TcState&
   float as[TC_MG], ac[TC_MG];
 #pragma unroll
   for (int m = 0; m < TC_MG; m++) as[m] = ac[m] = 0.f;
-  // add the main products since the last drain (with cross, the item's cross
-  // products too) to the compensated sums, once k-block nl's MMAs (and so all
-  // before them) have completed
-  auto drain_d = [&](unsigned nl, bool cross) {
+  // add D (main and cross products since the last drain) to the compensated
+  // sums, once k-block nl's MMAs (and so all before them) have completed
+  auto drain_d = [&](unsigned nl) {
     if (!mbar_wait(&tb->mma[nl & 1u], (nl >> 1) & 1u)) *s_to = 1;
     tc_fence_after();
 #pragma unroll
     for (int h = 0; h < TC_MG / 16; h++) {
-      uint32_t d0[16];
+      uint32_t d0[16], d1[16];
       tmem_ld16(tmem + lane_off + 16 * h, d0);
+      tmem_ld16(tmem + lane_off + TC_MG + 16 * h, d1);
       tmem_wait_ld();
-      float v[16];
 #pragma unroll
-      for (int j = 0; j < 16; j++) v[j] = __uint_as_float(d0[j]);
-      if (cross) {
-        tmem_ld16(tmem + lane_off + TC_MG + 16 * h, d0);
-        tmem_wait_ld();
-#pragma unroll
-        for (int j = 0; j < 16; j++) v[j] += __uint_as_float(d0[j]);
-      }
-#pragma unroll
-      for (int j = 0; j < 16; j++) kahan_reg(as[16 * h + j], ac[16 * h + j], v[j]);
+      for (int j = 0; j < 16; j++)
+        kahan_reg(as[16 * h + j], ac[16 * h + j], __uint_as_float(d0[j]) + __uint_as_float(d1[j]));
     }
   };
   bool pending = false;  // D holds products not yet drained
@@ -744,18 +740,16 @@ __device__ bool far_item_tc(const BJob& J, int tile, int chunk, int mg, TcState&
         }
         const bool first = win == 0;  // the k-block opens an accumulation window
         if (++win == drain) win = 0;
-        if (first && pending) drain_d(n - 1u, false);
+        if (first && pending) drain_d(n - 1u);
         tc_fence_before();
         __syncthreads();
         if (*s_to) return false;
         if (tid == 0) {
           tc_fence_after();
           const uint64_t d = dcol + (uint64_t)(kb * 256);
-          tc_mma_ts(tmem, abuf, d, TC_IDESC, first ? 0u : 1u);
-          tc_mma_ts(tmem + TC_MG, abuf, d + 32u, TC_IDESC, pending ? 1u : 0u);
+          tc_mma_ts(tmem, abuf, d, TC_IDESC64, first ? 0u : 1u);
           tc_mma_ts(tmem + TC_MG, abuf + 16u, d, TC_IDESC, 1u);
-          tc_mma_ts(tmem, abuf + 8u, d + 128u, TC_IDESC, 1u);
-          tc_mma_ts(tmem + TC_MG, abuf + 8u, d + 160u, TC_IDESC, 1u);
+          tc_mma_ts(tmem, abuf + 8u, d + 128u, TC_IDESC64, 1u);
           tc_mma_ts(tmem + TC_MG, abuf + 24u, d + 128u, TC_IDESC, 1u);
           tc_commit(&tb->mma[b]);
         }
@@ -778,7 +772,7 @@ __device__ bool far_item_tc(const BJob& J, int tile, int chunk, int mg, TcState&
     }
   }
   ts.gcol = g0 + (unsigned)ncol;
-  if (pending) drain_d(ts.kblk - 1u, true);
+  if (pending) drain_d(ts.kblk - 1u);
   tc_fence_before();
   __syncthreads();  // every thread has read D before the next item overwrites it
   if (*s_to) return false;
