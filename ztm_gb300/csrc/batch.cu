@@ -10,7 +10,8 @@
 // model).  Independent regional meshes are further jobs.
 //
 // Work items, taken from one global counter by a persistent grid of
-// (resident blocks x SMs):
+// (resident blocks x SMs), the near items spread evenly among the far ones
+// (the FP64 pipe busy beside the FMA pipe and the tensor cores):
 //   near item  (job, station tile): for each station, Phi at the near-box
 //              vertices in double into shared memory once, then per model
 //              the signed triple difference of that model's density.
@@ -64,6 +65,7 @@ struct BArgs {
   const BJob* jobs;
   int njobs;
   long long n_near, n_items;
+  long long near_span;  // queue positions the near items are spread over
   int* counter;
   int* err;
   double* phi;   // [block][warp][phi_stride] near-box vertex values and the
@@ -435,10 +437,18 @@ __global__ void __launch_bounds__(B_TS, MINB) batch_kernel(BArgs a) {
   for (long long guard = 0; guard < a.n_items + 1; guard++) {
     if (threadIdx.x == 0) s_item = atomicAdd(a.counter, 1);
     __syncthreads();
-    const long long item = s_item;
+    const long long pos = s_item;
     __syncthreads();
-    if (item >= a.n_items) break;
-    if (item < a.n_near) {
+    if (pos >= a.n_items) break;
+    // queue position pos < near_span: a near item iff floor((pos+1) n_near /
+    // near_span) > floor(pos n_near / near_span), so that the near items
+    // (double, FP64 pipe) are spread evenly among the first far items (FMA
+    // pipe, tensor cores), none late enough to hold up the end of the launch
+    const long long nb = pos < a.near_span ? pos * a.n_near / a.near_span : a.n_near;
+    const bool is_near = pos < a.near_span && (pos + 1) * a.n_near / a.near_span > nb;
+    // near items are numbered 0 .. n_near - 1, far items n_near .. n_items - 1
+    const long long item = is_near ? nb : a.n_near + (pos - nb);
+    if (is_near) {
       int j = 0;
       while (j + 1 < a.njobs && a.jobs[j + 1].near_base <= item) j++;
       const BJob& J = a.jobs[j];
@@ -827,10 +837,18 @@ __global__ void __launch_bounds__(B_TS, MINB) batch_tc_kernel(BArgs a) {
   for (long long guard = 0; guard < a.n_items + 1; guard++) {
     if (threadIdx.x == 0) s_item = atomicAdd(a.counter, 1);
     __syncthreads();
-    const long long item = s_item;
+    const long long pos = s_item;
     __syncthreads();
-    if (item >= a.n_items) break;
-    if (item < a.n_near) {
+    if (pos >= a.n_items) break;
+    // queue position pos < near_span: a near item iff floor((pos+1) n_near /
+    // near_span) > floor(pos n_near / near_span), so that the near items
+    // (double, FP64 pipe) are spread evenly among the first far items (FMA
+    // pipe, tensor cores), none late enough to hold up the end of the launch
+    const long long nb = pos < a.near_span ? pos * a.n_near / a.near_span : a.n_near;
+    const bool is_near = pos < a.near_span && (pos + 1) * a.n_near / a.near_span > nb;
+    // near items are numbered 0 .. n_near - 1, far items n_near .. n_items - 1
+    const long long item = is_near ? nb : a.n_near + (pos - nb);
+    if (is_near) {
       int j = 0;
       while (j + 1 < a.njobs && a.jobs[j + 1].near_base <= item) j++;
       const BJob& J = a.jobs[j];
@@ -1206,6 +1224,7 @@ int batch_run(ztm_ctx* c, const ztm_job* jobs, int njobs, bool dev, double G, do
     args.njobs = njobs;
     args.n_near = p.n_near;
     args.n_items = p.n_items;
+    args.near_span = std::max<long long>(1, p.n_near + (p.n_items - p.n_near) / 2);
     args.counter = counter;
     args.err = c->d_err;
     args.drain = tc ? std::max(1, stage_kb) : 1;
