@@ -77,3 +77,24 @@ def test_batch_awkward_stations_with_padded_layers(ctx):
     for k in range(models.shape[0]):
         ref = ctx.prism(mesh, models[k], st, precision="mixed")
         assert rel_err(out[k], ref) <= 1e-6, k
+
+
+def test_batch_more_models_than_a_tensor_core_group(ctx):
+    """37 models: two 32-model groups of tensor-core far items, the second
+    with 5 models and 27 zero-padded ones; every model against its single
+    mixed call, and a 2-model job beside it in the same launch."""
+    rng = np.random.default_rng(21)
+    mesh, rho = small_mesh(36, 30, 16, seed=22)
+    models = np.stack([rho * (1.0 + 0.03 * k) + rng.normal(0, 4, rho.size) for k in range(37)])
+    st = np.stack([rng.uniform(mesh.x0 - 3e3, mesh.x0 + 39e3, 140),
+                   rng.uniform(mesh.y0 - 3e3, mesh.y0 + 27e3, 140),
+                   rng.uniform(mesh.z_top + 5.0, mesh.z_top + 2500.0, 140)], 1)
+    mesh2, rho2 = small_mesh(24, 20, 12, seed=23)
+    two = np.stack([rho2, -0.5 * rho2])
+    outs = ctx.batch([(mesh, models, st), (mesh2, two, st)])
+    for k in (0, 17, 31, 32, 36):
+        ref = ctx.prism(mesh, models[k], st, precision="mixed")
+        assert rel_err(outs[0][k], ref) <= 1e-6, k
+    ref2 = ctx.prism(mesh2, rho2, st, precision="mixed")
+    assert rel_err(outs[1][0], ref2) <= 1e-6
+    assert rel_err(outs[1][1], -0.5 * ref2) <= 1e-6
