@@ -99,7 +99,9 @@ typedef struct {
   double G;       /* gravitational constant; 0 selects 6.67e-11, the value
                      that TFM.cpp:98's 66.7 mGal factor bakes in */
   double near_q;  /* mixed mode: pairs closer than near_q prism half-
-                     diagonals are evaluated in double; 0 selects 6 */
+                     diagonals are evaluated in double; 0 selects 4 for
+                     the regular 3-D mesh (sixth-order far field), 6 for
+                     the explicit prism list and the interface columns */
   int tile;       /* reserved, 0 */
   int chunk;      /* prism columns per block; 0 = chosen by the library
                      (from the autotuner's cache when ZTM_FLAG_AUTOTUNE) */
@@ -160,7 +162,7 @@ int ztm_ctx_tuning(const ztm_ctx* ctx, int* rows, int max_rows);
  * update per column and thread) that adds up the (station, prism) slots it
  * evaluates in each form of the far-field expansion.  ztm_ctx_form_counts
  * waits for the stream and returns, then clears: counts[0] slots in the
- * fourth-order form, [1] second order, [2] second order by column pairs
+ * sixth-order form, [1] second order, [2] second order by column pairs
  * (slots include the near-region layers a masked group evaluates and drops,
  * and the padding of nz to a multiple of 8), [3] closed-form corner-function
  * evaluations (Phi) of the near regions.  These are the numerators of the

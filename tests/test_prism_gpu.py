@@ -48,12 +48,12 @@ def test_fp32_mode(ctx):
     assert rel_err(ctx.prism(mesh, rho, st, precision="fp32"), ref) <= TOL32
 
 
-@pytest.mark.parametrize("q", [3.0, 6.0, 10.0])
+@pytest.mark.parametrize("q", [3.0, 4.0, 6.0, 10.0])
 def test_mixed_near_threshold_option(ctx, q):
     mesh, rho = small_mesh(48, 40, 12, seed=5)
     st = awkward_stations(mesh, n_random=30)
     ref = ctx.prism(mesh, rho, st, precision="fp64")
-    tol = TOLMIX if q >= 6 else 1e-4
+    tol = TOLMIX if q >= 4 else 1e-4
     assert rel_err(ctx.prism(mesh, rho, st, precision="mixed", near_q=q), ref) <= tol
 
 

@@ -174,7 +174,7 @@ __device__ __forceinline__ void adj_far_item(const AdjArgs& a, int bx, int by, A
           ColPoly2 cp2;
           cp2.rh = make_float2(rh, rh);
           cp2.a1 = make_float2(fc.a1, fc.a1);
-          cp2.C2 = cp2.C3 = cp2.C4 = make_float2(0.f, 0.f);  // unused by the form
+          cp2.C2 = cp2.C3 = cp2.C4 = cp2.C5 = cp2.C6 = make_float2(0.f, 0.f);  // unused by the form
 #pragma unroll
           for (int j = 0; j < ADJ_LG / 2; j++) v[j] = far_unit2_t2(zof(j), cp2, c2t);
         } else {
@@ -406,7 +406,7 @@ size_t ztm_adjoint_ws(const MeshDesc& m, int ns, int precision, int num_sms, dou
     int ch = adj_f64_chunks(nv, std::max(ns, 1), num_sms, &len);
     return WsCarver::need((size_t)ch * nv * 8);
   }
-  const MeshConst k = make_mesh_const(m, near_q > 0 ? near_q : 6.0);
+  const MeshConst k = make_mesh_const(m, near_q > 0 ? near_q : ZTM_MESH_NEAR_Q);
   return 2 * WsCarver::need((size_t)std::max(ns, 1) * 16) +
          WsCarver::need((size_t)std::max(ns, 1) * k.nslots * 4) +
          WsCarver::need((size_t)std::max(ns, 1) * 8) + WsCarver::need(64) +
@@ -437,7 +437,7 @@ int ztm_launch_adjoint(ztm_ctx* c, const MeshDesc& m, int ns, const double* d_sx
     c->launches += 2;
     return ztm_after_launch(c, "adjoint FP64 kernels");
   }
-  const double nq = (o && o->near_q > 0) ? o->near_q : 6.0;
+  const double nq = (o && o->near_q > 0) ? o->near_q : ZTM_MESH_NEAR_Q;
   MeshConst k = make_mesh_const(m, nq);
   if (m.nz > 32767) return ztm_fail(c, ZTM_ERR_RANGE, "mixed adjoint supports nz <= 32767");
   float4* sf = wc.take<float4>(ns);

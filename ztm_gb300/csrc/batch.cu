@@ -1018,7 +1018,7 @@ extern "C" int ztm_gfm_batch(ztm_ctx* c, const ztm_job* jobs, int njobs, const z
   const bool dev = o && (o->flags & ZTM_FLAG_DEVICE_PTRS);
   const bool tune = o && (o->flags & ZTM_FLAG_AUTOTUNE);
   const double G = (o && o->G > 0) ? o->G : 6.67e-11;
-  const double nq = (o && o->near_q > 0) ? o->near_q : 6.0;
+  const double nq = (o && o->near_q > 0) ? o->near_q : ZTM_MESH_NEAR_Q;
   for (int j = 0; j < njobs; j++) {
     const ztm_job& q = jobs[j];
     if (q.mesh.nx < 1 || q.mesh.ny < 1 || q.mesh.nz < 1 || !(q.mesh.dx > 0) ||

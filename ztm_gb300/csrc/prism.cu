@@ -349,7 +349,7 @@ __device__ __forceinline__ void far_column_pair(const float* colA, const float* 
 // thread's station; adds to acc.  Every lane runs the loop (inactive lanes
 // on dummy data) for the warp votes.
 // COUNT: add the (station, prism) slots this thread evaluates to cnt by
-// form: [0] fourth order, [1] second order, [2] second order by column pairs.
+// form: [0] sixth order, [1] second order, [2] second order by column pairs.
 template <bool COUNT>
 __device__ __forceinline__ void far_stage(const FarArgs& a, const MeshConst& k, const FarCoef& fc,
                                           const FarStation& t, int s, int Lm, const float* rs,
@@ -388,7 +388,8 @@ __device__ __forceinline__ void far_stage(const FarArgs& a, const MeshConst& k, 
         cpA.rh = make_float2(rhA, rhA);
         cpB.rh = make_float2(rhB, rhB);
         cpA.a1 = cpB.a1 = make_float2(fc.a1, fc.a1);
-        cpA.C2 = cpA.C3 = cpA.C4 = cpB.C2 = cpB.C3 = cpB.C4 = make_float2(0.f, 0.f);
+        cpA.C2 = cpA.C3 = cpA.C4 = cpA.C5 = cpA.C6 = make_float2(0.f, 0.f);
+        cpB.C2 = cpB.C3 = cpB.C4 = cpB.C5 = cpB.C6 = make_float2(0.f, 0.f);
         far_column_pair(rs + q * k.nzp, rs + (q + 1) * k.nzp, k.nz, Zb, zstep, cpA,
                         make_float2(cA, cA), cpB, make_float2(cB, cB), acc);
         if (COUNT) cnt[2] += 2 * k.nz;
@@ -426,7 +427,7 @@ __device__ __forceinline__ void far_stage(const FarArgs& a, const MeshConst& k, 
       ColPoly2 cp2;
       cp2.rh = make_float2(rh, rh);
       cp2.a1 = make_float2(fc.a1, fc.a1);
-      cp2.C2 = cp2.C3 = cp2.C4 = make_float2(0.f, 0.f);  // unused by the form
+      cp2.C2 = cp2.C3 = cp2.C4 = cp2.C5 = cp2.C6 = make_float2(0.f, 0.f);  // unused by the form
       far_column<true>(col, lmask, nz8, k.nz, Zb, zstep, cp2, make_float2(c2t, c2t), elo, espan,
                        acc);
       if (COUNT) cnt[1] += k.nzp;
@@ -944,7 +945,7 @@ size_t ztm_prism_ws(const MeshDesc& m, int ns, int precision, int num_sms, const
     long long ch = f64_chunks(nv, tiles, num_sms, &len);
     return WsCarver::need((size_t)ch * ns * 8) + WsCarver::need((size_t)nv * 8);
   }
-  double nq = (o && o->near_q > 0) ? o->near_q : 6.0;
+  double nq = (o && o->near_q > 0) ? o->near_q : ZTM_MESH_NEAR_Q;
   MeshConst k = make_mesh_const(m, nq);
   int chunks = 0;
   for (const auto& sh : FAR_SHAPES)
@@ -979,7 +980,7 @@ int ztm_launch_prism(ztm_ctx* c, const MeshDesc& m, const double* d_rho, int ns,
     c->launches += 3;
     return ztm_after_launch(c, "prism FP64 kernels");
   }
-  const double nq = (o && o->near_q > 0) ? o->near_q : 6.0;
+  const double nq = (o && o->near_q > 0) ? o->near_q : ZTM_MESH_NEAR_Q;
   MeshConst k = make_mesh_const(m, nq);
   if (m.nz > 32767) return ztm_fail(c, ZTM_ERR_RANGE, "mixed prism forward supports nz <= 32767");
   {  // two one-column stages of the far kernel must fit in shared memory

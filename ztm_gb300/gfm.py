@@ -227,7 +227,7 @@ class GravityContext:
         self._check(self._lib.ztm_ctx_count_forms(self._h, 1 if enable else 0))
 
     def form_counts(self):
-        """(fourth-order slots, second-order slots, column-pair slots, near
+        """(sixth-order slots, second-order slots, column-pair slots, near
         Phi evaluations) since the last read; clears them."""
         out = (ctypes.c_longlong * 4)()
         self._check(self._lib.ztm_ctx_form_counts(self._h, out))
