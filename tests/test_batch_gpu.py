@@ -98,3 +98,18 @@ def test_batch_more_models_than_a_tensor_core_group(ctx):
     ref2 = ctx.prism(mesh2, rho2, st, precision="mixed")
     assert rel_err(outs[1][0], ref2) <= 1e-6
     assert rel_err(outs[1][1], -0.5 * ref2) <= 1e-6
+
+
+def test_batch_deep_mesh_runs_on_the_cuda_cores(ctx):
+    """300 layers: the tensor-core items' column stages (768 bytes a layer)
+    would not fit in shared memory, so the launch takes the CUDA-core
+    variant; every model against its single mixed call."""
+    rng = np.random.default_rng(31)
+    mesh, rho = small_mesh(10, 8, 300, seed=32)
+    models = np.stack([rho, 0.5 * rho + rng.normal(0, 3, rho.size), -rho])
+    st = np.stack([rng.uniform(mesh.x0, mesh.x0 + 10e3, 40), rng.uniform(mesh.y0, mesh.y0 + 6.4e3, 40),
+                   rng.uniform(mesh.z_top + 5.0, mesh.z_top + 1500.0, 40)], 1)
+    out = ctx.batch([(mesh, models, st)])[0]
+    for k in range(3):
+        ref = ctx.prism(mesh, models[k], st, precision="mixed")
+        assert rel_err(out[k], ref) <= 1e-6, k

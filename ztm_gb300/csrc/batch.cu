@@ -1000,6 +1000,7 @@ constexpr int BATCH_SHAPES[][3] = {{4, 23, 4},  {2, 23, 4},  {4, 21, 4},  {4, 24
                                    {16, 23, 0}, {8, 24, 0},  {32, 24, 0}, {16, 24, 0},
                                    {16, 25, 0}, {8, 23, 0},  {32, 25, 0}, {16, 23, 1},
                                    {8, 23, 2},  {16, 23, 2}, {32, 23, 3}, {16, 24, 3}};
+constexpr int BATCH_CC_SHAPE = 4;  // the CUDA-core variants' default shape
 
 int batch_run(ztm_ctx* c, const ztm_job* jobs, int njobs, bool dev, double G, double nq,
               int stage_kb, int tlog2, int variant);
@@ -1104,9 +1105,14 @@ int resident_blocks(ztm_ctx* c, BatchFn kfn, int threads, size_t dyn_smem) {
 
 int batch_run(ztm_ctx* c, const ztm_job* jobs, int njobs, bool dev, double G, double nq,
               int stage_kb, int tlog2, int variant) {
-  const BatchFn kfn = batch_fn(variant);
   const bool tc = BATCH_VARIANTS[variant][2] != 0;
   Plan p = plan(jobs, njobs, nq, c->num_sms, stage_kb, tlog2, BATCH_VARIANTS[variant][0], tc);
+  // the tensor-core items stage whole columns (768 bytes a layer in three
+  // stages): a mesh too deep for that runs on the CUDA-core default variant
+  if (tc && p.smem > 200 * 1024)
+    return batch_run(c, jobs, njobs, dev, G, nq, BATCH_SHAPES[BATCH_CC_SHAPE][0],
+                     BATCH_SHAPES[BATCH_CC_SHAPE][1], BATCH_SHAPES[BATCH_CC_SHAPE][2]);
+  const BatchFn kfn = batch_fn(variant);
   if (p.smem > 200 * 1024) return ztm_fail(c, ZTM_ERR_RANGE, "near box too large for a batch");
   size_t stage_bytes = 0;
   if (!dev)
