@@ -701,9 +701,12 @@ def run_workload(args, local_rank):
         dJ, dr_, db = d(J), d(rng.normal(size=nrows)), d(rng.normal(size=ncols))
         dsig = d(rng.uniform(0.05, 2.0, ncols))
         dm = d(np.array([[0.0, 0.0], [1e-3, 1e-4], [0.1, 1e-2], [1.0, 1.0]]))
-        units = nrows * ncols * ncols + nd * ncols ** 3  # ~ J^T J and Gauss-Jordan multiply-adds
+        # units: the multiply-adds of J^T J (full) and of a Gauss-Jordan inversion
+        # per pair (the reference's work); the library factorises by blocked LU
+        units = nrows * ncols * ncols + nd * ncols ** 3
         what = ("damped Gauss-Newton trials (TFM.cpp:159-160): J 12000 x 2700, 4 damping pairs "
-                "(J^T J + 4 Gauss-Jordan solves; units: multiply-adds of J^T J and the solves)")
+                "(J^T J + 4 solves by blocked LU; units: the multiply-adds of J^T J and of the "
+                "reference's Gauss-Jordan inversions)")
         step = lambda: ctx.lm_steps(dJ, dr_, db, dsig, dm)
     elif args.workload == "inversion":
         return inversion_study(ctx)

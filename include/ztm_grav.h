@@ -384,8 +384,9 @@ int ztm_invert_interface_gn(ztm_ctx* ctx, const ztm_imesh* mesh, double* depth,
  * each of the nd damping pairs (d0, d1) in `damping` (nd x 2),
  *   B[d] = b + inv(JJ + d0 M + d1 A) J^T r
  * (the reference inverts by Gauss-Jordan with partial pivoting,
- * zmath.cpp:129-140; here the same elimination runs on the right-hand side,
- * which gives the same step up to rounding).  J is nrows x ncols, row-major
+ * zmath.cpp:129-140; here the system is factorised by blocked LU with the
+ * same pivot rule and the right-hand side attached, which gives the same
+ * step up to rounding).  J is nrows x ncols, row-major
  * (J[data][parameter], as Jac returns it), r the nrows residuals y - f, b and
  * sig ncols values, B nd x ncols; JJ (ncols x ncols) is returned if non-NULL.
  * A singular system leaves its B row equal to b, as the reference's inv
