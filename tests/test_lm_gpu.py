@@ -6,8 +6,8 @@ sources are absent.
 
 TOLERANCES: J^T J 1e-13 (normwise relative: the same sums in another order);
 the trial models 1e-9 (normwise relative over b's change: the reference
-inverts and multiplies, the library eliminates on the right-hand side, and
-the normal equations square the condition number)."""
+inverts and multiplies, the library factorises with the right-hand side
+attached, and the normal equations square the condition number)."""
 import numpy as np
 import pytest
 
@@ -83,3 +83,22 @@ def test_lm_underdetermined_and_one_parameter(ctx):
     jj, jr = float(np.sum(J1 ** 2)), float(np.dot(J1[:, 0], r1))
     want = 2.0 + jr / (jj + 0.1 * jj + 0.2 / 0.25)
     assert B1[0, 0] == pytest.approx(want, rel=1e-14)
+
+
+def test_lm_steps_beyond_the_shared_memory_panel(ctx):
+    """3,520 parameters: more rows than a panel in shared memory holds, so
+    the panels are factorised in global memory (row swaps over whole rows);
+    each step against numpy's solve of the same damped system built from the
+    library's own J^T J."""
+    rng = np.random.default_rng(77)
+    nrows, ncols = 3600, 3520
+    J = rng.normal(size=(nrows, ncols)) * rng.uniform(0.5, 2.0, ncols)[None, :]
+    r, b = rng.normal(size=nrows), rng.normal(size=ncols)
+    sig = rng.uniform(0.5, 2.0, ncols)
+    dm = np.array([[1e-3, 1e-3], [0.1, 1.0]])
+    B, JJ = ctx.lm_steps(J, r, b, sig, dm, return_jtj=True)
+    g = J.T @ r
+    for k, (d0, d1) in enumerate(dm):
+        A = JJ + np.diag(d0 * np.diag(JJ) + d1 / sig ** 2)
+        step = np.linalg.solve(A, g)
+        assert np.max(np.abs((B[k] - b) - step)) <= 1e-9 * np.max(np.abs(step)), k
