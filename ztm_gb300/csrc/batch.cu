@@ -27,6 +27,7 @@
 #include <type_traits>
 #include <vector>
 
+#include "mesh_far.cuh"
 #include "prism_common.cuh"
 #include "tc_tf32.cuh"
 #include "ztm_internal.cuh"
@@ -104,8 +105,8 @@ __global__ void transpose_models_kernel(MeshConst k, int nmodels, int W,
 
 // Far field of one column for every model of the group, W models
 // interleaved in `col` (layer-major, W per layer).  K is computed once per
-// (station, prism) pair; per model two packed FMAs per layer pair (W = 1) or
-// per model pair (W = 8); plain sums over 32 layers, Kahan across groups.
+// (station, prism) pair; two packed FMAs per model pair and layer; plain
+// sums over 64 layers, Kahan across groups.
 // T2: the second-order form (every lane of the warp far enough); MASK: some
 // lane of the warp has the column in its near box, or nz is not a multiple
 // of 8 (both warp-uniform, so the selects are skipped for most columns).
@@ -127,9 +128,10 @@ __device__ __forceinline__ void far_column(const float* __restrict__ col, const 
   const float2 dz2 = make_float2(k.dzn, k.dzn);
   float zf = (float)(-izs);  // (l0 - izs), exact, stepped by 8
   // plain float sums over up to 64 layers per model, compensated across
-  float2 g[W == 1 ? 1 : W / 2];
+  static_assert(W % 4 == 0, "models are read four at a time");
+  float2 g[W / 2];
 #pragma unroll
-  for (int m = 0; m < (W == 1 ? 1 : W / 2); m++) g[m] = make_float2(0.f, 0.f);
+  for (int m = 0; m < W / 2; m++) g[m] = make_float2(0.f, 0.f);
 #pragma unroll 4
   for (int l0 = 0; l0 < k.nz; l0 += 8, zf += 8.f) {
     const float Zg = fmaf(zf, k.dzn, ez);
@@ -147,37 +149,24 @@ __device__ __forceinline__ void far_column(const float* __restrict__ col, const 
       }
     }
     const bool flush = ((l0 >> 3) & 7) == 7 || l0 + 8 >= k.nz;
-    if constexpr (W == 1) {
-      const float4 ra = *reinterpret_cast<const float4*>(col + l0);
-      const float4 rb = *reinterpret_cast<const float4*>(col + l0 + 4);
-      g[0] = __ffma2_rn(K2[0], make_float2(ra.x, ra.y), g[0]);
-      g[0] = __ffma2_rn(K2[1], make_float2(ra.z, ra.w), g[0]);
-      g[0] = __ffma2_rn(K2[2], make_float2(rb.x, rb.y), g[0]);
-      g[0] = __ffma2_rn(K2[3], make_float2(rb.z, rb.w), g[0]);
-      if (flush) {
-        kahan_smem(ks, kc, 0, g[0].x + g[0].y);
-        g[0] = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      const float Kj = (j & 1) ? K2[j >> 1].y : K2[j >> 1].x;
+      const float2 kk = make_float2(Kj, Kj);
+      const float* row = col + (l0 + j) * W;
+#pragma unroll
+      for (int m = 0; m < W / 4; m++) {
+        const float4 r4 = *reinterpret_cast<const float4*>(row + 4 * m);
+        g[2 * m] = __ffma2_rn(kk, make_float2(r4.x, r4.y), g[2 * m]);
+        g[2 * m + 1] = __ffma2_rn(kk, make_float2(r4.z, r4.w), g[2 * m + 1]);
       }
-    } else {
+    }
+    if (flush) {
 #pragma unroll
-      for (int j = 0; j < 8; j++) {
-        const float Kj = (j & 1) ? K2[j >> 1].y : K2[j >> 1].x;
-        const float2 kk = make_float2(Kj, Kj);
-        const float* row = col + (l0 + j) * W;
-#pragma unroll
-        for (int m = 0; m < W / 4; m++) {
-          const float4 r4 = *reinterpret_cast<const float4*>(row + 4 * m);
-          g[2 * m] = __ffma2_rn(kk, make_float2(r4.x, r4.y), g[2 * m]);
-          g[2 * m + 1] = __ffma2_rn(kk, make_float2(r4.z, r4.w), g[2 * m + 1]);
-        }
-      }
-      if (flush) {
-#pragma unroll
-        for (int m = 0; m < W / 2; m++) {
-          kahan_smem(ks, kc, 2 * m, g[m].x);
-          kahan_smem(ks, kc, 2 * m + 1, g[m].y);
-          g[m] = make_float2(0.f, 0.f);
-        }
+      for (int m = 0; m < W / 2; m++) {
+        kahan_smem(ks, kc, 2 * m, g[m].x);
+        kahan_smem(ks, kc, 2 * m + 1, g[m].y);
+        g[m] = make_float2(0.f, 0.f);
       }
     }
   }
@@ -299,8 +288,10 @@ __device__ void near_item(const BJob& J, int tile, double* phi_all, int phi_cap,
 }
 
 // One far item on the CUDA cores: (job, station tile, column chunk, model
-// group of MG, or one model where the job has one).  Returns false if a
-// stage wait ran out (the caller reports the timeout).
+// group of MG, or one model where the job has one: then the mixed forward's
+// own column loop, meshfar::far_stage, with its column pairs and
+// second-order shortcut).  Returns false if a stage wait ran out (the caller
+// reports the timeout).
 template <int MG>
 __device__ bool far_item_cc(const BJob& J, int tile, int chunk, int mg, uint64_t* bar,
                             float* stage, unsigned& uses0, unsigned& uses1, float* ks,
@@ -339,6 +330,9 @@ __device__ bool far_item_cc(const BJob& J, int tile, int chunk, int mg, uint64_t
   __syncthreads();
   const int Lm = min(*s_lm, k.nz);
   const FarCoef fc = k.fc;
+  const bool one = MG == 1 || J.mgw == 1;
+  const meshfar::FarStation t = {ex, ey, ez, ixs, iys, izs, nb};
+  Kahan acc1;  // the one-model sum
 #pragma unroll
   for (int md = 0; md < MG; md++) ks[md * B_TS] = kc[md * B_TS] = 0.f;
   for (int st = 0; st < nst; st++) {
@@ -351,55 +345,53 @@ __device__ bool far_item_cc(const BJob& J, int tile, int chunk, int mg, uint64_t
     const float* rs = stage + buf * stage_floats;
     const int cs = c0 + st * J.sc;
     const int ncol = min(J.sc, c1 - cs);
-    if (active) {
-      int ix = cs % k.nx, iy = cs / k.nx;
-      for (int q = 0; q < ncol; q++) {
-        const float X = fmaf((float)(ixs - ix), k.dxn, ex);
-        const float Y = fmaf((float)(iys - iy), k.dyn, ey);
-        const ColPoly cp = col_poly(X, Y, fc);
-        const bool ncl = ix >= nb.x0 && ix <= nb.x1 && iy >= nb.y0 && iy <= nb.y1;
-        int elo = k.nz;
-        unsigned espan = 0u;
-        if (ncl) {  // the column's near-region layers
-          const short2 tv = J.iv[(size_t)s * k.nslots + near_slot(nb, ix, iy)];
-          if (tv.x <= tv.y) {
-            elo = tv.x;
-            espan = (unsigned)(tv.y - tv.x);
+    if (one) {  // every lane (inactive ones on dummy data) for the warp votes
+      unsigned cnt[3];
+      meshfar::far_stage<false>(J.iv, k, fc, t, s, Lm, rs, cs, ncol, acc1, cnt);
+    } else if constexpr (MG > 1) {
+      if (active) {
+        int ix = cs % k.nx, iy = cs / k.nx;
+        for (int q = 0; q < ncol; q++) {
+          const float X = fmaf((float)(ixs - ix), k.dxn, ex);
+          const float Y = fmaf((float)(iys - iy), k.dyn, ey);
+          const ColPoly cp = col_poly(X, Y, fc);
+          const bool ncl = ix >= nb.x0 && ix <= nb.x1 && iy >= nb.y0 && iy <= nb.y1;
+          int elo = k.nz;
+          unsigned espan = 0u;
+          if (ncl) {  // the column's near-region layers
+            const short2 tv = J.iv[(size_t)s * k.nslots + near_slot(nb, ix, iy)];
+            if (tv.x <= tv.y) {
+              elo = tv.x;
+              espan = (unsigned)(tv.y - tv.x);
+            }
           }
-        }
-        const float* col = rs + q * k.nzp * J.mgw;
-        const ColPoly2 cp2 = col_poly2(cp, fc.a1);
-        const float2 c2t = make_float2(cp.C2 - fc.h2, cp.C2 - fc.h2);
-        // padded layers (l >= nz) need the mask only below the mesh: for a
-        // station with izs < nz their Z is at least half a layer, so K is
-        // finite there and the zero densities add nothing
-        const unsigned am = __activemask();
-        const int form = (__all_sync(am, cp.rh >= k.rh_t2) ? 1 : 0) |
-                         ((__any_sync(am, ncl || ((k.nz & 7) && izs >= k.nz))) ? 2 : 0);
-        if (MG == 1 || J.mgw == 1) {
-          switch (form) {
-            case 0: far_column<1, false, false>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc); break;
-            case 1: far_column<1, true, false>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc); break;
-            case 2: far_column<1, false, true>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc); break;
-            default: far_column<1, true, true>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc);
-          }
-        } else {
+          const float* col = rs + q * k.nzp * J.mgw;
+          const ColPoly2 cp2 = col_poly2(cp, fc.a1);
+          const float2 c2t = make_float2(cp.C2 - fc.h2, cp.C2 - fc.h2);
+          // padded layers (l >= nz) need the mask only below the mesh: for a
+          // station with izs < nz their Z is at least half a layer, so K is
+          // finite there and the zero densities add nothing
+          const unsigned am = __activemask();
+          const int form = (__all_sync(am, cp.rh >= k.rh_t2) ? 1 : 0) |
+                           ((__any_sync(am, ncl || ((k.nz & 7) && izs >= k.nz))) ? 2 : 0);
           switch (form) {
             case 0: far_column<MG, false, false>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc); break;
             case 1: far_column<MG, true, false>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc); break;
             case 2: far_column<MG, false, true>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc); break;
             default: far_column<MG, true, true>(col, k, cp2, c2t, ez, izs, Lm, elo, espan, ks, kc);
           }
-        }
-        if (++ix == k.nx) {
-          ix = 0;
-          ++iy;
+          if (++ix == k.nx) {
+            ix = 0;
+            ++iy;
+          }
         }
       }
     }
     __syncthreads();
   }
-  if (active) {
+  if (active && one) {
+    J.partial[((size_t)m0 * J.chunks + chunk) * J.ns + s] = acc1.value();
+  } else if (active) {
 #pragma unroll
     for (int md = 0; md < MG; md++)
       if (md < mcnt)

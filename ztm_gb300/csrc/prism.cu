@@ -31,6 +31,7 @@
 
 #include <algorithm>
 
+#include "mesh_far.cuh"
 #include "prism_common.cuh"
 #include "ztm_internal.cuh"
 
@@ -187,263 +188,6 @@ __device__ __forceinline__ float far_pair(float rho, float Z, float rh, float a0
   return fmaf(base, t, base);
 }
 
-// Per-thread station state of the far kernel for one tile of stations.
-struct FarStation {
-  float ex, ey, ez;
-  int ixs, iys, izs;
-  NearBox nb;
-};
-
-// Eight layers l0..l0+7 of one column: adds rho * (far value) to g (two
-// lanes: even and odd layers).  T2: the second-order form for the whole warp.
-// MASK: drop the layers of the station's near region [elo, elo + espan] and
-// the padding layers >= nz (select, not multiply: a NaN there is dropped).
-template <bool T2, bool MASK>
-__device__ __forceinline__ float2 far_group(const float* col, int l0, float fl,
-                                            const float2 (&Zb)[4], float2 zstep,
-                                            const ColPoly2& cp2, float2 c2t, int elo,
-                                            unsigned espan, int nz, float2 g) {
-  const float4 ra = *reinterpret_cast<const float4*>(col + l0);
-  const float4 rb = *reinterpret_cast<const float4*>(col + l0 + 4);
-  const float2 l2 = make_float2(fl, fl);  // fl = l0, carried in float (no conversion)
-  float2 v[4];
-#pragma unroll
-  for (int j = 0; j < 4; j++) {
-    const float2 Z = __ffma2_rn(l2, zstep, Zb[j]);  // Z(l) = (l - izs) dz + ez
-    v[j] = T2 ? far_unit2_t2(Z, cp2, c2t) : far_unit2(Z, cp2);
-  }
-  if (MASK) {
-#pragma unroll
-    for (int j = 0; j < 4; j++) {
-      const int la = l0 + 2 * j, lb = la + 1;
-      if (((unsigned)(la - elo) <= espan) || la >= nz) v[j].x = 0.f;
-      if (((unsigned)(lb - elo) <= espan) || lb >= nz) v[j].y = 0.f;
-    }
-  }
-  g = __ffma2_rn(make_float2(ra.x, ra.y), v[0], g);
-  g = __ffma2_rn(make_float2(ra.z, ra.w), v[1], g);
-  g = __ffma2_rn(make_float2(rb.x, rb.y), v[2], g);
-  return __ffma2_rn(make_float2(rb.z, rb.w), v[3], g);
-}
-
-// All layers of one column: groups [0, lmask) with the near mask, full
-// groups up to nz8 without, a masked tail group if nz is not a multiple of 8.
-// Plain float sums over 32 layers (two lanes of 16), compensated across.
-template <bool T2>
-__device__ __forceinline__ void far_column(const float* col, int lmask, int nz8, int nz,
-                                           const float2 (&Zb)[4], float2 zstep,
-                                           const ColPoly2& cp2, float2 c2t, int elo,
-                                           unsigned espan, Kahan& acc) {
-  float2 g = make_float2(0.f, 0.f);
-  int l0 = 0;
-  float fl = 0.f;
-  for (; l0 < lmask; l0 += 8, fl += 8.f) {
-    g = far_group<T2, true>(col, l0, fl, Zb, zstep, cp2, c2t, elo, espan, nz, g);
-    if ((l0 & 24) == 24) {
-      acc.add(g.x + g.y);
-      g = make_float2(0.f, 0.f);
-    }
-  }
-  // unmasked groups: singly up to a 32-layer boundary, then eight at a time
-  // over whole 64-layer blocks and four at a time over a 32-layer block (one
-  // loop test per block, one compensation per 32 layers), singly after
-  for (; l0 < nz8 && (l0 & 31); l0 += 8, fl += 8.f) {
-    g = far_group<T2, false>(col, l0, fl, Zb, zstep, cp2, c2t, elo, espan, nz, g);
-    if ((l0 & 24) == 24) {
-      acc.add(g.x + g.y);
-      g = make_float2(0.f, 0.f);
-    }
-  }
-  for (; l0 + 64 <= nz8; l0 += 64, fl += 64.f) {
-    g = far_group<T2, false>(col, l0, fl, Zb, zstep, cp2, c2t, elo, espan, nz, g);
-    g = far_group<T2, false>(col, l0 + 8, fl + 8.f, Zb, zstep, cp2, c2t, elo, espan, nz, g);
-    g = far_group<T2, false>(col, l0 + 16, fl + 16.f, Zb, zstep, cp2, c2t, elo, espan, nz, g);
-    g = far_group<T2, false>(col, l0 + 24, fl + 24.f, Zb, zstep, cp2, c2t, elo, espan, nz, g);
-    acc.add(g.x + g.y);
-    g = far_group<T2, false>(col, l0 + 32, fl + 32.f, Zb, zstep, cp2, c2t, elo, espan, nz,
-                             make_float2(0.f, 0.f));
-    g = far_group<T2, false>(col, l0 + 40, fl + 40.f, Zb, zstep, cp2, c2t, elo, espan, nz, g);
-    g = far_group<T2, false>(col, l0 + 48, fl + 48.f, Zb, zstep, cp2, c2t, elo, espan, nz, g);
-    g = far_group<T2, false>(col, l0 + 56, fl + 56.f, Zb, zstep, cp2, c2t, elo, espan, nz, g);
-    acc.add(g.x + g.y);
-    g = make_float2(0.f, 0.f);
-  }
-  for (; l0 + 32 <= nz8; l0 += 32, fl += 32.f) {
-    g = far_group<T2, false>(col, l0, fl, Zb, zstep, cp2, c2t, elo, espan, nz, g);
-    g = far_group<T2, false>(col, l0 + 8, fl + 8.f, Zb, zstep, cp2, c2t, elo, espan, nz, g);
-    g = far_group<T2, false>(col, l0 + 16, fl + 16.f, Zb, zstep, cp2, c2t, elo, espan, nz, g);
-    g = far_group<T2, false>(col, l0 + 24, fl + 24.f, Zb, zstep, cp2, c2t, elo, espan, nz, g);
-    acc.add(g.x + g.y);
-    g = make_float2(0.f, 0.f);
-  }
-  for (; l0 < nz8; l0 += 8, fl += 8.f) {
-    g = far_group<T2, false>(col, l0, fl, Zb, zstep, cp2, c2t, elo, espan, nz, g);
-    if ((l0 & 24) == 24) {
-      acc.add(g.x + g.y);
-      g = make_float2(0.f, 0.f);
-    }
-  }
-  if (nz8 < nz) g = far_group<T2, true>(col, nz8, fl, Zb, zstep, cp2, c2t, elo, espan, nz, g);
-  acc.add(g.x + g.y);
-}
-
-// Two columns A and B, eight layers l0..l0+7, second-order form, no mask:
-// one Z per layer pair serves both columns.
-__device__ __forceinline__ float2 far_group_pair(const float* colA, const float* colB, int l0,
-                                                 float fl, const float2 (&Zb)[4], float2 zstep,
-                                                 const ColPoly2& cpA, float2 c2tA,
-                                                 const ColPoly2& cpB, float2 c2tB, float2 g) {
-  const float4 raA = *reinterpret_cast<const float4*>(colA + l0);
-  const float4 rbA = *reinterpret_cast<const float4*>(colA + l0 + 4);
-  const float4 raB = *reinterpret_cast<const float4*>(colB + l0);
-  const float4 rbB = *reinterpret_cast<const float4*>(colB + l0 + 4);
-  const float2 l2 = make_float2(fl, fl);
-  float2 vA[4], vB[4];
-#pragma unroll
-  for (int j = 0; j < 4; j++) {
-    const float2 Z = __ffma2_rn(l2, zstep, Zb[j]);
-    vA[j] = far_unit2_t2(Z, cpA, c2tA);
-    vB[j] = far_unit2_t2(Z, cpB, c2tB);
-  }
-  g = __ffma2_rn(make_float2(raA.x, raA.y), vA[0], g);
-  g = __ffma2_rn(make_float2(raB.x, raB.y), vB[0], g);
-  g = __ffma2_rn(make_float2(raA.z, raA.w), vA[1], g);
-  g = __ffma2_rn(make_float2(raB.z, raB.w), vB[1], g);
-  g = __ffma2_rn(make_float2(rbA.x, rbA.y), vA[2], g);
-  g = __ffma2_rn(make_float2(rbB.x, rbB.y), vB[2], g);
-  g = __ffma2_rn(make_float2(rbA.z, rbA.w), vA[3], g);
-  return __ffma2_rn(make_float2(rbB.z, rbB.w), vB[3], g);
-}
-
-// All layers of two columns (nz a multiple of 8): plain float sums over 16
-// layers of both (32 terms), compensated across.
-__device__ __forceinline__ void far_column_pair(const float* colA, const float* colB, int nz,
-                                                const float2 (&Zb)[4], float2 zstep,
-                                                const ColPoly2& cpA, float2 c2tA,
-                                                const ColPoly2& cpB, float2 c2tB, Kahan& acc) {
-  int l0 = 0;
-  float fl = 0.f;
-  const float2 z0 = make_float2(0.f, 0.f);
-  for (; l0 + 64 <= nz; l0 += 64, fl += 64.f) {
-#pragma unroll
-    for (int h = 0; h < 4; h++) {
-      float2 g = far_group_pair(colA, colB, l0 + 16 * h, fl + 16.f * h, Zb, zstep, cpA, c2tA,
-                                cpB, c2tB, z0);
-      g = far_group_pair(colA, colB, l0 + 16 * h + 8, fl + 16.f * h + 8.f, Zb, zstep, cpA, c2tA,
-                         cpB, c2tB, g);
-      acc.add(g.x + g.y);
-    }
-  }
-  for (; l0 + 16 <= nz; l0 += 16, fl += 16.f) {
-    float2 g = far_group_pair(colA, colB, l0, fl, Zb, zstep, cpA, c2tA, cpB, c2tB, z0);
-    g = far_group_pair(colA, colB, l0 + 8, fl + 8.f, Zb, zstep, cpA, c2tA, cpB, c2tB, g);
-    acc.add(g.x + g.y);
-  }
-  if (l0 < nz) {
-    const float2 g = far_group_pair(colA, colB, l0, fl, Zb, zstep, cpA, c2tA, cpB, c2tB, z0);
-    acc.add(g.x + g.y);
-  }
-}
-
-// One shared-memory stage (ncol columns starting at column cs) against this
-// thread's station; adds to acc.  Every lane runs the loop (inactive lanes
-// on dummy data) for the warp votes.
-// COUNT: add the (station, prism) slots this thread evaluates to cnt by
-// form: [0] sixth order, [1] second order, [2] second order by column pairs.
-template <bool COUNT>
-__device__ __forceinline__ void far_stage(const FarArgs& a, const MeshConst& k, const FarCoef& fc,
-                                          const FarStation& t, int s, int Lm, const float* rs,
-                                          int cs, int ncol, Kahan& acc, unsigned (&cnt)[3]) {
-  const float2 zstep = make_float2(k.dzn, k.dzn);
-  // Z of layers 2j, 2j+1 of a group at l0 = 0; a group at l0 adds l0 dz
-  float2 Zb[4];
-#pragma unroll
-  for (int j = 0; j < 4; j++)
-    Zb[j] = make_float2(fmaf((float)(2 * j - t.izs), k.dzn, t.ez),
-                        fmaf((float)(2 * j + 1 - t.izs), k.dzn, t.ez));
-  const int nz8 = k.nz & ~7;
-  const int lm8 = min((Lm + 7) & ~7, nz8);
-  int ix = cs % k.nx, iy = cs / k.nx;
-  for (int q = 0; q < ncol; q++) {
-    // two unmasked second-order columns at once where the warp allows it
-    if (nz8 == k.nz && q + 1 < ncol) {
-      int ix1 = ix + 1, iy1 = iy;
-      if (ix1 == k.nx) {
-        ix1 = 0;
-        ++iy1;
-      }
-      const float XA = fmaf((float)(t.ixs - ix), k.dxn, t.ex);
-      const float YA = fmaf((float)(t.iys - iy), k.dyn, t.ey);
-      const float XB = fmaf((float)(t.ixs - ix1), k.dxn, t.ex);
-      const float YB = fmaf((float)(t.iys - iy1), k.dyn, t.ey);
-      const float XA2 = XA * XA, YA2 = YA * YA, rhA = XA2 + YA2;
-      const float XB2 = XB * XB, YB2 = YB * YB, rhB = XB2 + YB2;
-      const bool nclA = ix >= t.nb.x0 && ix <= t.nb.x1 && iy >= t.nb.y0 && iy <= t.nb.y1;
-      const bool nclB = ix1 >= t.nb.x0 && ix1 <= t.nb.x1 && iy1 >= t.nb.y0 && iy1 <= t.nb.y1;
-      const bool unmasked = lm8 == 0 || !__any_sync(0xffffffffu, nclA || nclB);
-      if (unmasked && __all_sync(0xffffffffu, fminf(rhA, rhB) >= k.rh_t2)) {
-        const float cA = fmaf(-fc.a1, rhA, fmaf(XA2, fc.cA, YA2 * fc.cB));
-        const float cB = fmaf(-fc.a1, rhB, fmaf(XB2, fc.cA, YB2 * fc.cB));
-        ColPoly2 cpA, cpB;
-        cpA.rh = make_float2(rhA, rhA);
-        cpB.rh = make_float2(rhB, rhB);
-        cpA.a1 = cpB.a1 = make_float2(fc.a1, fc.a1);
-        cpA.C2 = cpA.C3 = cpA.C4 = cpA.C5 = cpA.C6 = make_float2(0.f, 0.f);
-        cpB.C2 = cpB.C3 = cpB.C4 = cpB.C5 = cpB.C6 = make_float2(0.f, 0.f);
-        far_column_pair(rs + q * k.nzp, rs + (q + 1) * k.nzp, k.nz, Zb, zstep, cpA,
-                        make_float2(cA, cA), cpB, make_float2(cB, cB), acc);
-        if (COUNT) cnt[2] += 2 * k.nz;
-        q++;
-        ix = ix1 + 1;
-        iy = iy1;
-        if (ix == k.nx) {
-          ix = 0;
-          ++iy;
-        }
-        continue;
-      }
-    }
-    const float X = fmaf((float)(t.ixs - ix), k.dxn, t.ex);
-    const float Y = fmaf((float)(t.iys - iy), k.dyn, t.ey);
-    const float X2 = X * X, Y2 = Y * Y, rh = X2 + Y2;
-    const bool ncl = ix >= t.nb.x0 && ix <= t.nb.x1 && iy >= t.nb.y0 && iy <= t.nb.y1;
-    int elo = k.nz;
-    unsigned espan = 0u;
-    if (ncl) {  // the column's near-region layers
-      const short2 iv = a.iv[(size_t)s * k.nslots + near_slot(t.nb, ix, iy)];
-      if (iv.x <= iv.y) {
-        elo = iv.x;
-        espan = (unsigned)(iv.y - iv.x);
-      }
-    }
-    const float* col = rs + q * k.nzp;
-    // a column lies in some lane's near box only near the warp's stations:
-    // test that once per column for the whole warp
-    const int lmask = __any_sync(0xffffffffu, ncl) ? lm8 : 0;
-    // every lane of the warp far enough for the second-order form, which
-    // needs only C2t = a0 - a1 rh of the column polynomial
-    if (__all_sync(0xffffffffu, rh >= k.rh_t2)) {
-      const float c2t = fmaf(-fc.a1, rh, fmaf(X2, fc.cA, Y2 * fc.cB));
-      ColPoly2 cp2;
-      cp2.rh = make_float2(rh, rh);
-      cp2.a1 = make_float2(fc.a1, fc.a1);
-      cp2.C2 = cp2.C3 = cp2.C4 = cp2.C5 = cp2.C6 = make_float2(0.f, 0.f);  // unused by the form
-      far_column<true>(col, lmask, nz8, k.nz, Zb, zstep, cp2, make_float2(c2t, c2t), elo, espan,
-                       acc);
-      if (COUNT) cnt[1] += k.nzp;
-    } else {
-      const ColPoly2 cp2 = col_poly2(col_poly(X, Y, fc), fc.a1);
-      far_column<false>(col, lmask, nz8, k.nz, Zb, zstep, cp2, make_float2(0.f, 0.f), elo, espan,
-                        acc);
-      if (COUNT) cnt[0] += k.nzp;
-    }
-    if (++ix == k.nx) {
-      ix = 0;
-      ++iy;
-    }
-  }
-}
-
 // Persistent kernel of the mixed forward.  The work is tiles x chunks far
 // items (a tile of FAR_TS stations against a chunk of chunk_cols columns) and
 // n_near near items (the double near regions of FAR_NEAR_ST stations, one
@@ -550,7 +294,7 @@ __global__ void __launch_bounds__(FAR_TS, 6) far_kernel(FarArgs a) {
     const int slot = tile * FAR_TS + threadIdx.x;
     const bool active = slot < a.ns;
     const int s = active ? a.perm[slot] : 0;
-    FarStation t = {0.f, 0.f, 0.f, 0, 0, 0, {1, 0, 1, 0, 1, 0}};
+    meshfar::FarStation t = {0.f, 0.f, 0.f, 0, 0, 0, {1, 0, 1, 0, 1, 0}};
     if (active) {
       const float4 fv = a.sf[s];
       const int4 i = a.si[s];
@@ -597,7 +341,8 @@ __global__ void __launch_bounds__(FAR_TS, 6) far_kernel(FarArgs a) {
         int cs;
         const int ncol = stage_cols(f, st, &cs);
         unsigned c3[3] = {0u, 0u, 0u};
-        far_stage<COUNT>(a, k, fc, t, s, Lm, stage + (seq & 1) * stage_floats, cs, ncol, acc, c3);
+        meshfar::far_stage<COUNT>(a.iv, k, fc, t, s, Lm, stage + (seq & 1) * stage_floats, cs,
+                                  ncol, acc, c3);
         if (COUNT && active) {
           cnt[0] += c3[0];
           cnt[1] += c3[1];
