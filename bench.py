@@ -377,11 +377,11 @@ def extras(ctx, mesh, rho, st, d_rho, d_st, gz_mixed, fwd_ms):
         out["accuracy_full_field"] = acc
     sub = np.arange(0, len(st), len(st) // 64)[:64]
     ds = torch.tensor(st[sub], device="cuda")
-    ms64, ref = _median_ms(ctx, lambda: ctx.prism(mesh, d_rho, ds, precision="fp64"), 5)
+    ms64, ref = _median_ms(ctx, lambda: ctx.prism(mesh, d_rho, ds, precision="fp64"), 10)
     r = ref.cpu().numpy()
     m = gz_mixed[sub]
     out["fp64_plain"] = {"value": np_ * len(sub) / (ms64 * 1e-3), "unit": UNIT,
-                         "sample": "%d stations x all prisms, median of 5" % len(sub)}
+                         "sample": "%d stations x all prisms, median of 10" % len(sub)}
     out["accuracy"] = {"normwise_rel_err_vs_fp64": float(np.max(np.abs(m - r)) / np.max(np.abs(r))),
                        "max_station_rel_err": float(np.max(np.abs(m - r) / np.abs(r))),
                        "stations_checked": len(sub), "reference": "the plain FP64 GPU kernel"}
@@ -391,10 +391,10 @@ def extras(ctx, mesh, rho, st, d_rho, d_st, gz_mixed, fwd_ms):
     out["gradient"] = {"value": np_ * len(st) / (msa * 1e-3), "unit": "gradient evals/s",
                        "ms": msa, "what": "d misfit / d rho, all pairs, mixed, median of 10"}
     rs = torch.tensor(np.random.default_rng(0).normal(0, 1, len(sub)), device="cuda")
-    msa64, _ = _median_ms(ctx, lambda: ctx.adjoint(mesh, ds, rs, precision="fp64"), 5)
+    msa64, _ = _median_ms(ctx, lambda: ctx.adjoint(mesh, ds, rs, precision="fp64"), 10)
     out["fp64_plain_adjoint"] = {"value": np_ * len(sub) / (msa64 * 1e-3),
                                  "unit": "gradient evals/s",
-                                 "sample": "%d stations x all prisms, median of 5" % len(sub)}
+                                 "sample": "%d stations x all prisms, median of 10" % len(sub)}
     pairs = np_ * len(st)
     t64 = pairs / out["fp64_plain"]["value"] + pairs / out["fp64_plain_adjoint"]["value"]
     tmx = (fwd_ms + msa) * 1e-3
@@ -443,8 +443,10 @@ def _timed(ctx, fn, reps=1):
 
 
 def other_workloads(ctx):
-    """The other workloads (interface adjoint, line-search batch, interface
-    inversion), once each (not the headline)."""
+    """The other workloads (interface adjoint, line-search batch, LM steps,
+    interface inversion), not the headline: calls under a second timed as the
+    median of 10 replays, the double interface call and the inversions
+    once."""
     import numpy as np
     import torch
     from ztm_gb300 import synth
@@ -457,7 +459,8 @@ def other_workloads(ctx):
     data = ctx.interface(im, dd, dr, ds, precision="fp64")
     ctx.sync()
     data = data + d(rng.normal(0, 0.05, len(st)))
-    ms_m, out_m = _timed(ctx, lambda: ctx.interface_misfit(im, d0, dr, ds, data, precision="mixed"), 3)
+    ms_m, out_m = _median_ms(ctx, lambda: ctx.interface_misfit(im, d0, dr, ds, data,
+                                                             precision="mixed"), 10)
     ms_d, out_d = _timed(ctx, lambda: ctx.interface_misfit(im, d0, dr, ds, data, precision="fp64"))
     pairs = im.nx * im.ny * len(st)
     err = lambda a, b: float((a - b).abs().max() / b.abs().max())
@@ -473,7 +476,7 @@ def other_workloads(ctx):
     djobs = [(m_, d(r_.reshape(r_.shape[0], -1) if r_.ndim == 2 else r_), d(s_)) for m_, r_, s_ in jobs]
     ctx.batch(djobs)  # builds and caches the graph
     ctx.sync()
-    ms_b, outs = _timed(ctx, lambda: ctx.batch(djobs), 2)
+    ms_b, outs = _median_ms(ctx, lambda: ctx.batch(djobs), 10)
     mp = sum(int(r_.shape[0]) * m_.nx * m_.ny * m_.nz * len(s_) for m_, r_, s_ in jobs)
     one = ctx.prism(jobs[0][0], djobs[0][1][5], djobs[0][2], precision="mixed")
     ctx.sync()
@@ -493,8 +496,8 @@ def other_workloads(ctx):
         J = rng.normal(size=(nrows, ncols)) * rng.uniform(0.1, 10.0, ncols)[None, :]
         r_, b_, sg = rng.normal(size=nrows), rng.normal(size=ncols), rng.uniform(0.05, 2.0, ncols)
         dJ, dr_, db_, ds_, ddm = d(J), d(r_), d(b_), d(sg), d(dm)
-        ms, B = _timed(ctx, lambda: ctx.lm_steps(dJ, dr_, db_, ds_, ddm), 3)
-        row = {"gpu_ms": ms, "damping_pairs": 4}
+        ms, B = _median_ms(ctx, lambda: ctx.lm_steps(dJ, dr_, db_, ds_, ddm), 10)
+        row = {"gpu_ms": ms, "damping_pairs": 4, "replays": "median of 10"}
         if ncols == 600 and oracle.ref_lm_available():
             t0 = time.perf_counter()
             Bref, _ = oracle.ref_lm_steps(J, r_, b_, sg, dm)

@@ -35,7 +35,6 @@
 namespace {
 
 constexpr int B_TS = 128;   // threads per block = stations per tile
-constexpr int B_MG = 16;    // models per far item (the default variant's)
 constexpr int B_WARPS = B_TS / 32;
 
 struct BJob {
@@ -971,7 +970,6 @@ void destroy_entry(ZtmGraphEntry& e) {
 // compiler, tensor cores}.  Variants 0-3 run every far item on the CUDA
 // cores; variant 4 runs the far items of multi-model jobs on the tensor cores.
 constexpr int BATCH_VARIANTS[][3] = {{16, 4, 0}, {16, 5, 0}, {8, 6, 0}, {32, 3, 0}, {TC_MG, 4, 1}};
-constexpr int BATCH_TC_VARIANT = 4;
 using BatchFn = void (*)(BArgs);
 BatchFn batch_fn(int v) {
   switch (v) {
