@@ -180,9 +180,9 @@ def run_reference(args, rank):
 def config_dict(n):
     return {"workload": WORKLOAD, "prisms": [256, 256, 64], "cell_m": [1000, 1000, 500],
             "stations": [128, 128], "pairs_per_step": 256 * 256 * 64 * 128 * 128,
-            "precision": "mixed: far pairs float (4th-order expansion, second order beyond 48 "
+            "precision": "mixed: far pairs float (sixth-order expansion, second order beyond 48 "
                          "half-diagonals, compensated sums), near region and per-station sums "
-                         "double", "near_q": 6,
+                         "double", "near_q": 4,
             "l2": "flushed between timed steps (256 MiB write)",
             "parallelism": "replica per GPU" if n > 1 else "single GPU"}
 

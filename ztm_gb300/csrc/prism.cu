@@ -15,11 +15,11 @@
 //               through shared memory, per-chunk partials reduced in a fixed
 //               order.
 //   MIXED       pairs outside a station's near region (every prism whose
-//               centre is >= near_q half-diagonals away) use the 4th-order
-//               far-field expansion in float (second order beyond 48
-//               half-diagonals), two layers per packed instruction and two
-//               neighbouring columns per pass where the warp allows it,
-//               Kahan-summed per thread; the near region is summed in double
+//               centre is >= near_q half-diagonals away, 4 by default) use
+//               the sixth-order far-field expansion in float (second order
+//               beyond 48 half-diagonals), two layers per packed
+//               instruction and two neighbouring columns per pass where the
+//               warp allows it, Kahan-summed per thread; the near region is summed in double
 //               with vertex sharing (one Phi per vertex instead of 8 per
 //               prism); partials and the final per-station sum are double.
 //               Stations are taken in Z order of their home cells.  The
