@@ -44,9 +44,11 @@ enum {
 enum {
   ZTM_PREC_FP64 = 0,  /* plain: every pair in double (closed form / pow) */
   ZTM_PREC_FP32 = 1,  /* every pair in float with compensated sums */
-  ZTM_PREC_MIXED = 2  /* prism modes: far pairs in float (multipole to 4th
-                         order, compensated), near pairs and the final
-                         per-station sums in double */
+  ZTM_PREC_MIXED = 2  /* prism modes: far pairs in float (moment expansion
+                         to sixth order on 3-D meshes, horizontal expansion
+                         to fourth order for interface columns; compensated
+                         sums), near pairs and the final per-station sums in
+                         double */
 };
 
 /* ---- flags ----------------------------------------------------------- */
