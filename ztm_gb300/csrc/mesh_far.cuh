@@ -143,16 +143,17 @@ __device__ __forceinline__ float2 far_group_pair(const float* colA, const float*
   return __ffma2_rn(make_float2(rbB.z, rbB.w), vB[3], g);
 }
 
-// All layers of two columns (nz a multiple of 8): plain float sums over 16
+// Layers 0 .. nl - 1 of two columns (nl a multiple of 8: nz, or the padded
+// nzp where the padding layers' K is finite): plain float sums over 16
 // layers of both (32 terms), compensated across.
-__device__ __forceinline__ void far_column_pair(const float* colA, const float* colB, int nz,
+__device__ __forceinline__ void far_column_pair(const float* colA, const float* colB, int nl,
                                                 const float2 (&Zb)[4], float2 zstep,
                                                 const ColPoly2& cpA, float2 c2tA,
                                                 const ColPoly2& cpB, float2 c2tB, Kahan& acc) {
   int l0 = 0;
   float fl = 0.f;
   const float2 z0 = make_float2(0.f, 0.f);
-  for (; l0 + 64 <= nz; l0 += 64, fl += 64.f) {
+  for (; l0 + 64 <= nl; l0 += 64, fl += 64.f) {
 #pragma unroll
     for (int h = 0; h < 4; h++) {
       float2 g = far_group_pair(colA, colB, l0 + 16 * h, fl + 16.f * h, Zb, zstep, cpA, c2tA,
@@ -162,12 +163,12 @@ __device__ __forceinline__ void far_column_pair(const float* colA, const float* 
       acc.add(g.x + g.y);
     }
   }
-  for (; l0 + 16 <= nz; l0 += 16, fl += 16.f) {
+  for (; l0 + 16 <= nl; l0 += 16, fl += 16.f) {
     float2 g = far_group_pair(colA, colB, l0, fl, Zb, zstep, cpA, c2tA, cpB, c2tB, z0);
     g = far_group_pair(colA, colB, l0 + 8, fl + 8.f, Zb, zstep, cpA, c2tA, cpB, c2tB, g);
     acc.add(g.x + g.y);
   }
-  if (l0 < nz) {
+  if (l0 < nl) {
     const float2 g = far_group_pair(colA, colB, l0, fl, Zb, zstep, cpA, c2tA, cpB, c2tB, z0);
     acc.add(g.x + g.y);
   }
@@ -192,10 +193,15 @@ __device__ __forceinline__ void far_stage(const short2* __restrict__ ivs, const 
                         fmaf((float)(2 * j + 1 - t.izs), k.dzn, t.ez));
   const int nz8 = k.nz & ~7;
   const int lm8 = min((Lm + 7) & ~7, nz8);
+  // column pairs run over all nzp layers unmasked: where nz is not a
+  // multiple of 8 that needs every lane's station above the mesh bottom
+  // (izs < nz), whose Z at a padding layer is then at least half a layer, so
+  // that K there is finite and the zero density adds nothing
+  const bool pairs = nz8 == k.nz || __all_sync(0xffffffffu, t.izs < k.nz);
   int ix = cs % k.nx, iy = cs / k.nx;
   for (int q = 0; q < ncol; q++) {
     // two unmasked second-order columns at once where the warp allows it
-    if (nz8 == k.nz && q + 1 < ncol) {
+    if (pairs && q + 1 < ncol) {
       int ix1 = ix + 1, iy1 = iy;
       if (ix1 == k.nx) {
         ix1 = 0;
@@ -219,9 +225,9 @@ __device__ __forceinline__ void far_stage(const short2* __restrict__ ivs, const 
         cpA.a1 = cpB.a1 = make_float2(fc.a1, fc.a1);
         cpA.C2 = cpA.C3 = cpA.C4 = cpA.C5 = cpA.C6 = make_float2(0.f, 0.f);
         cpB.C2 = cpB.C3 = cpB.C4 = cpB.C5 = cpB.C6 = make_float2(0.f, 0.f);
-        far_column_pair(rs + q * k.nzp, rs + (q + 1) * k.nzp, k.nz, Zb, zstep, cpA,
+        far_column_pair(rs + q * k.nzp, rs + (q + 1) * k.nzp, k.nzp, Zb, zstep, cpA,
                         make_float2(cA, cA), cpB, make_float2(cB, cB), acc);
-        if (COUNT) cnt[2] += 2 * k.nz;
+        if (COUNT) cnt[2] += 2 * k.nzp;
         q++;
         ix = ix1 + 1;
         iy = iy1;
