@@ -183,3 +183,31 @@ def test_form_counts_cover_every_slot(ctx, shape):
     assert counts[0] + counts[1] + counts[2] == len(st) * mesh.nx * mesh.ny * nzp
     assert counts[3] > 0
     assert ctx.form_counts() == (0, 0, 0, 0)  # read clears
+
+
+def test_column_pairs_over_padding_layers(ctx):
+    """nz = 13 (three zero-density padding layers in each 16-layer column):
+    warps whose stations all lie above the mesh bottom take two far columns
+    per pass over all padded layers, a warp with a station below the bottom
+    keeps the masked single-column path; the field matches the oracle and
+    the counters show column pairs."""
+    mesh, rho = small_mesh(120, 24, 13, seed=9)
+    rng = np.random.default_rng(9)
+    n = 95
+    st = np.stack([rng.uniform(mesh.x0, mesh.x0 + 10 * mesh.dx, n),
+                   rng.uniform(mesh.y0, mesh.y0 + mesh.ny * mesh.dy, n),
+                   rng.uniform(mesh.z_top + 10.0, mesh.z_top + 2000.0, n)], axis=1)
+    below = [mesh.x0 + 4.5 * mesh.dx, mesh.y0 + 10.5 * mesh.dy,
+             mesh.z_top - mesh.nz * mesh.dz - 0.5 * mesh.dz]
+    st = np.vstack([st, below])
+    ref = oracle.prism_mesh(mesh, rho, st)
+    ctx.count_forms(True)
+    try:
+        out = ctx.prism(mesh, rho, st, precision="mixed")
+        counts = ctx.form_counts()
+    finally:
+        ctx.count_forms(False)
+    assert np.all(np.isfinite(out))
+    assert rel_err(out, ref) <= TOLMIX
+    assert counts[2] > 0
+    assert counts[0] + counts[1] + counts[2] == len(st) * mesh.nx * mesh.ny * 16
