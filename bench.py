@@ -62,6 +62,16 @@ def dist_env():
             int(os.environ.get("WORLD_SIZE", "1")))
 
 
+def max_over_ranks(dist, x):
+    """The largest x of all ranks (a host float), through the process
+    group's own backend: a device tensor for NCCL, a host tensor for gloo."""
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons during the timed region."""
 
@@ -243,9 +253,7 @@ def run_ours(args, rank, local_rank, world):
     step_ms = [a.elapsed_time(b) for a, b in ev]
     total_s = sum(step_ms) / 1e3
     if dist:
-        t = torch.tensor([total_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s = float(t.item())
+        total_s = max_over_ranks(dist, total_s)
     value = world * pairs * args.steps / total_s
     ms_per_step = 1e3 * total_s / args.steps
     gz = out.cpu().numpy()
@@ -267,12 +275,7 @@ def run_ours(args, rank, local_rank, world):
         t0 = time.perf_counter()
         g_host = ctx.prism(mesh, h_rho, h_st, precision="mixed")
         e2e_t.append(time.perf_counter() - t0)
-    if dist:
-        t = torch.tensor([sum(e2e_t)], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_total = float(t.item())
-    else:
-        e2e_total = sum(e2e_t)
+    e2e_total = max_over_ranks(dist, sum(e2e_t)) if dist else sum(e2e_t)
     e2e = {"value": world * pairs * e2e_steps / e2e_total, "unit": UNIT,
            "h2d_bytes_per_step": int(h_rho.nbytes + h_st.nbytes),
            "d2h_bytes_per_step": int(g_host.nbytes)}
