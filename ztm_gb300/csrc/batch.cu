@@ -5,19 +5,30 @@
 // another (TFM.cpp:165, each FM call running the GPU process of
 // TFM.cpp:90-94).  Here a job is (mesh, stations, nmodels densities); the
 // trial models of a line search are one job with nmodels > 1 and share every
-// pair's geometry: the far-field kernel value of a (station, prism) pair is
-// computed once and applied to a group of up to 8 models (one Kahan sum per
-// model).  Independent regional meshes are further jobs.
+// pair's geometry: the far-field kernel value K of a (station, prism) pair is
+// computed once and applied to every model of a group, so that the far field
+// of the group is a contraction over prisms, sum_p K(s, p) rho_m(p).
+// Independent regional meshes are further jobs.
 //
 // Work items, taken from one global counter by a persistent grid of
-// (resident blocks x SMs), the near items spread evenly among the far ones
-// (the FP64 pipe busy beside the FMA pipe and the tensor cores):
-//   near item  (job, station tile): for each station, Phi at the near-box
-//              vertices in double into shared memory once, then per model
-//              the signed triple difference of that model's density.
-//   far item   (job, station tile, column chunk, model group): the float
-//              far field over the chunk, density staged by 1-D TMA bulk
-//              copies (one per model of the group) on an mbarrier.
+// (resident blocks x SMs), the near items spread evenly over the first half
+// of the queue (the FP64 pipe busy beside the FMA pipe and the tensor cores):
+//   near item  (job, station tile): a warp per station; for one model the
+//              forward's vertex pass (near_station), for several Phi at the
+//              near-box vertices in double once into the warp's slice of a
+//              global scratch, then the unit responses of the near prisms
+//              and per model one multiply-add per near prism.
+//   far item   (job, station tile, column chunk, model group):
+//              - tensor-core variant, multi-model jobs (far_item_tc): 32
+//                models per group; each thread evaluates K for its station,
+//                splits it into TF32 high part and FP32 remainder in its TMEM
+//                lane, and tcgen05 MMAs (A from TMEM, B = the models' split
+//                densities, one 1-D bulk copy per column in the MMA's
+//                shared-memory layout) accumulate the contraction in TMEM;
+//              - CUDA-core variants (far_item_cc): models interleaved in HBM,
+//                one bulk copy per stage, packed FMAs into compensated sums;
+//              - one-model jobs: the mixed forward's column loop
+//                (meshfar::far_stage).
 // Every item bumps its tile's completion counter; the block that completes a
 // tile adds the tile's partials in a fixed order and writes gz, so the launch
 // needs no second kernel and the result is deterministic.
